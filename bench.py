@@ -1,0 +1,356 @@
+#!/usr/bin/env python
+"""Benchmark: simulated years per wall-hour of the quasi-dynamic earthquake
+cycle at 1025 x 1025 (config 1 physics: layered mu, +-5% a-b perturbation,
+8-level multigrid, 1e-9 relative residual).
+
+A "step" is one accepted adaptive-RK43 step: the ARK4(3)6L stages, each an
+elliptic multigrid solve plus the fault stress / Newton / aging-law update,
+retried until the error test passes, then the refresh solve at the new state.
+Warm-up steps start from the steady-sliding initial state (V = Vp); the timed
+steps are the next K steps of the same run.  value = simulated years advanced
+in the timed steps / their device time in hours.
+
+Arms:
+  default           this library on the GPU (mixed precision: FP32 V-cycles in
+                    FP64 refinement); the plain FP64 multigrid is measured too
+  --impl reference  the reference algorithm on the host cores (the CPU
+                    oracle restating odeSolver.cpp / fault.cpp: 6 levels,
+                    V(32,32)), same config, same steps
+
+The L2 cache (129 MB, larger than the 1025^2 working set) is flushed before
+every timed step by writing a 512 MB buffer outside the timed interval.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+YEAR_S = 365.25 * 86400.0
+METRIC = "simulated yr/hr at 1025² (learned+mixed vs plain FP64 MG, 1e-9 rel residual)"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=40)
+    p.add_argument("--warmup", type=int, default=20)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--config", default="config1")
+    p.add_argument("--cpu-sample-s", type=float, default=20.0)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU arm: the reference algorithm through the oracle
+# ---------------------------------------------------------------------------
+def reference_mg_for(cfg):
+    from qdeqcycle_fdm_gb300 import config
+    r = config.reference_mg()
+    r.tol_mode, r.tol = cfg.mg.tol_mode, cfg.mg.tol      # same accuracy target as the GPU arm
+    r.max_cycles = 0
+    return r
+
+
+def run_cpu(prob, warmup, steps, budget_s=None):
+    """Oracle RK43 from t = 0: `warmup` untimed steps, then up to `steps`
+    timed steps (stopping early once budget_s of timed work is spent)."""
+    import oracle
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    mg = reference_mg_for(prob.cfg)
+    sim = oracle.Simulation(prob, mg.n_levels, mg.nu_pre, mg.nu_post, mg.nu_coarse, mg.tol_mode,
+                            mg.tol, mg.max_cycles)
+    sim.start()
+    for _ in range(warmup):
+        sim.step()
+    s0 = sim.state()
+    t0 = time.perf_counter()
+    n = 0
+    while n < steps:
+        sim.step()
+        n += 1
+        if budget_s is not None and time.perf_counter() - t0 > budget_s:
+            break
+    wall = time.perf_counter() - t0
+    s1 = sim.state()
+    yrs = (s1["t"] - s0["t"]) / YEAR_S
+    return {"value": yrs / (wall / 3600.0) if wall > 0 else 0.0, "wall_s": wall, "steps": n,
+            "sim_years": yrs, "threads": threads,
+            "vcycles_per_solve": (s1["vcycles"] - s0["vcycles"]) / max(1, s1["solves"] - s0["solves"]),
+            "schedule": f"{mg.n_levels} levels V({mg.nu_pre},{mg.nu_post}), rel {mg.tol:g}"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from qdeqcycle_fdm_gb300 import config, problem
+    import oracle
+    oracle.build(ref=False)
+    cfg = config.CONFIGS[args.config]()
+    prob = problem.build_problem(cfg, homogenize=lambda ni, nk, mu: oracle.set_medium(ni, nk, mu)[1])
+    r = run_cpu(prob, args.warmup, args.steps)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": r["value"], "unit": "sim_yr/hr",
+        "n_gpus": args.gpus, "steps": r["steps"], "warmup": args.warmup,
+        "ms_per_step": 1e3 * r["wall_s"] / max(1, r["steps"]), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{cfg.name}: {cfg.ni}x{cfg.nk} earthquake cycle, accepted RK43 steps "
+                               f"{args.warmup + 1}..{args.warmup + r['steps']} from steady sliding",
+                   "mg": r["schedule"], "l2": "host run"},
+        "cpu_baseline": {"value": r["value"], "unit": "sim_yr/hr", "cores": r["threads"],
+                         "kind": "port",
+                         "sample": f"{r['steps']} accepted steps after {args.warmup} warm-up steps"},
+        "e2e": {"value": r["value"], "unit": "sim_yr/hr", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "vcycles_per_solve": r["vcycles_per_solve"],
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from qdeqcycle_fdm_gb300 import api, build, config, problem
+    build.build()
+    cfg = config.CONFIGS[args.config]()
+    prob = problem.build_problem(cfg)            # face moduli homogenised on the GPU
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    def timed_run(mg, label):
+        sim = api.Simulation(prob, mg)
+        sim.start()
+        sim.step(args.warmup)
+        stream = torch.cuda.ExternalStream(sim.solver.stream_ptr())
+        s0 = sim.state(with_u=False)
+        ms = 0.0
+        barrier()
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            sim.step(1)
+            e1.record(stream)
+            e1.synchronize()
+            ms += e0.elapsed_time(e1)
+        barrier()
+        s1 = sim.state(with_u=False)
+        return sim, {"ms": ms, "yrs": (s1["t"] - s0["t"]) / YEAR_S,
+                     "launches": s1["kernel_launches"] - s0["kernel_launches"],
+                     "vcycles": s1["vcycles"] - s0["vcycles"], "solves": s1["solves"] - s0["solves"],
+                     "attempts": s1["attempts"] - s0["attempts"], "t_end": s1["t"]}
+
+    def reduce_max(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    clocks = Clocks(local)
+    clocks.start()
+    mixed_cfg = config.MGConfig(**{**cfg.mg.__dict__, "precision": 1})
+    fp64_cfg = config.MGConfig(**{**cfg.mg.__dict__, "precision": 0})
+    sim, head = timed_run(mixed_cfg, "mixed")
+    clk = clocks.stop()
+    sim64, plain = timed_run(fp64_cfg, "fp64")
+    ms_max = reduce_max(head["ms"])
+    value = world * head["yrs"] / (ms_max / 3.6e6)       # replicas: every rank ran the same work
+    plain_value = plain["yrs"] / (reduce_max(plain["ms"]) / 3.6e6)
+
+    # dominant kernel: level-0 smoother sweeps of the headline (FP32) hierarchy
+    stream = torch.cuda.ExternalStream(sim.solver.stream_ptr())
+    nsw = 50
+    sim.solver.smooth(2)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    sim.solver.smooth(nsw)
+    e1.record(stream)
+    e1.synchronize()
+    per_launch_s = e0.elapsed_time(e1) / 1e3 / (2 * nsw)
+    nodes = cfg.ni * cfg.nk
+    algo_bytes = 10.0 * nodes                     # FP32: 20 B/node per red+black sweep, half per colour
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = algo_bytes / per_launch_s / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": None,
+                "kernel": "k_rb<float> level 0 (one colour)",
+                "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"}
+
+    # end to end through the C ABI with host buffers (pinned), one step per call
+    e2e = None
+    if not args.no_e2e:
+        nz, nx = prob.nz, prob.nx
+
+        def pinned(shape):
+            return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+
+        st = sim.solver.rk43_state()
+        hU = pinned((nz, nx))
+        hU[:] = sim.solver.download_u()
+        hv = {k: pinned(nz) for k in ("Slip", "psi", "V", "dpsi", "Ts")}
+        for k in ("Slip", "psi", "V", "dpsi", "Ts"):
+            hv[k][:] = st[k]
+        t_sim, dt, errA, it = st["t"], st["dt"], st["errA"], st["it"]
+        ne2e = min(args.steps, 20)
+        e2e_ms = 0.0
+        t_start = t_sim
+        for _ in range(ne2e):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            a0 = torch.cuda.Event(enable_timing=True)
+            a1 = torch.cuda.Event(enable_timing=True)
+            a0.record(stream)
+            sim.solver.rk43_set_state(hv["Slip"], hv["psi"], hv["V"], hv["dpsi"], t_sim, dt, errA[0],
+                                      errA[1], it)
+            sim.solver.upload_u(hU)
+            sim.solver.rk43_step(1)
+            s2 = sim.solver.rk43_state()
+            hU[:] = sim.solver.download_u()
+            a1.record(stream)
+            a1.synchronize()
+            e2e_ms += a0.elapsed_time(a1)
+            for k in ("Slip", "psi", "V", "dpsi", "Ts"):
+                hv[k][:] = s2[k]
+            t_sim, dt, errA, it = s2["t"], s2["dt"], s2["errA"], s2["it"]
+        e2e_yrs = (t_sim - t_start) / YEAR_S
+        e2e = {"value": world * e2e_yrs / (reduce_max(e2e_ms) / 3.6e6), "unit": "sim_yr/hr",
+               "h2d_bytes_per_step": 8 * (4 * nz + prob.ni * prob.nk),
+               "d2h_bytes_per_step": 8 * (5 * nz + prob.ni * prob.nk), "steps": ne2e}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        r = run_cpu(prob, args.warmup, args.steps, budget_s=args.cpu_sample_s)
+        cpu = {"value": r["value"], "unit": "sim_yr/hr", "cores": r["threads"], "kind": "port",
+               "sample": f"oracle (reference algorithm, {r['schedule']}): {r['steps']} accepted "
+                         f"steps after the same {args.warmup} warm-up steps, {r['wall_s']:.1f}s"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "sim_yr/hr", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
+            "data": "synthetic",
+            "config": {"workload": f"{cfg.name}: {cfg.ni}x{cfg.nk} earthquake cycle, accepted RK43 steps "
+                                   f"{args.warmup + 1}..{args.warmup + args.steps} from steady sliding",
+                       "mg": f"{cfg.mg.n_levels} levels V({cfg.mg.nu_pre},{cfg.mg.nu_post}), "
+                             f"rel {cfg.mg.tol:g}, FP32 cycles in FP64 refinement",
+                       "parallelism": f"replicas x{world}", "l2": "flushed before every timed step"},
+            "sim_years_timed": head["yrs"], "t_end_s": head["t_end"],
+            "vcycles_per_solve": head["vcycles"] / max(1, head["solves"]),
+            "attempts_per_step": head["attempts"] / args.steps,
+            "plain_fp64": {"value": plain_value, "ms_per_step": plain["ms"] / args.steps,
+                           "vcycles_per_solve": plain["vcycles"] / max(1, plain["solves"])},
+            "speedup_vs_plain_fp64": value / world / plain_value if plain_value else None,
+            "gpu_launches": head["launches"],
+            "roofline": roofline, "clocks": clk, "e2e": e2e, "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

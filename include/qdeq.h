@@ -1,0 +1,200 @@
+/*
+ * qdeq.h -- C ABI of the GB300 (sm_103a) quasi-dynamic earthquake-cycle hot
+ * path: the per-stage pipeline of QDEqCycle_FDM's adaptive RK43 loop
+ * (multigrid u-solve, fault shear stress, Newton solve for slip rate, aging
+ * law, RK stage combination / error estimate / step control).
+ *
+ * The reference has no plugin or FFI layer; its interface is the set of C++
+ * free functions in functions.h:11-45, taking struct.h structs by value with
+ * borrowed Real* arrays.  Each entry point below names the reference function
+ * it replaces.  Conventions:
+ *   - plain pointers and sizes only; every array pointer is HOST memory
+ *     unless the name says "device";
+ *   - arrays use the reference's layouts: ghosted fields (U, mu_node) are
+ *     nx*nz doubles indexed i + k*nx with nx = ni+2, nz = nk+2 (struct.h,
+ *     odeSolver.cpp:24-38); fault vectors are nz doubles whose entries
+ *     1..nk are used (Alloc.cpp:3-42); mu_equi is (2nx-1)*(2nz-1) doubles
+ *     (odeSolver.cpp:47,337-589);
+ *   - every call returns a status (QD_OK = 0); qd_last_error() describes the
+ *     last failure of the calling thread.  Nothing calls exit().
+ *   - a solver owns one CUDA stream and all of its device memory; calls on
+ *     one solver are serialised by the caller.  The reference runs one host
+ *     thread on the default stream.
+ */
+#ifndef QDEQ_H
+#define QDEQ_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QDEQ_ABI_VERSION 1
+
+/* status codes */
+#define QD_OK 0
+#define QD_ERR_ARG 1            /* bad argument or size                      */
+#define QD_ERR_CUDA 2           /* CUDA runtime error                        */
+#define QD_ERR_NOMEM 3          /* device allocation failed                  */
+#define QD_ERR_NOT_CONVERGED 4  /* multigrid hit max_cycles above tolerance  */
+#define QD_ERR_NEWTON 5         /* Newton for V gave NaN/no root (the
+                                   reference exit(0)s: fault.cpp:211-225)    */
+#define QD_ERR_STATE 6          /* call out of order (e.g. no fault set up)  */
+
+/* tolerance modes */
+#define QD_TOL_ABS 0            /* ||r||2 <= tol, as odeSolver.cpp:689-705   */
+#define QD_TOL_REL 1            /* ||r||2 <= tol * ||r(u_interior = 0)||2    */
+
+/* precision of the multigrid cycles */
+#define QD_PREC_FP64 0          /* FP64 V-cycles (the drop-in)               */
+#define QD_PREC_MIXED 1         /* FP32 V-cycles inside FP64 iterative
+                                   refinement; FP64 residual and update      */
+
+typedef struct qd_solver qd_solver;
+
+/* Multigrid schedule.  The reference hard-codes n_levels = 6, V(32,32) with
+ * 32 sweeps on the coarsest level, plain red-black Gauss-Seidel and an
+ * absolute 1e-9 residual norm (odeSolver.cpp:2-4,689). */
+typedef struct qd_mg_options {
+    int n_levels;
+    int nu_pre;       /* red+black sweeps before the coarse correction       */
+    int nu_post;      /* ... and after it                                    */
+    int nu_coarse;    /* sweeps on the coarsest level                        */
+    int tol_mode;     /* QD_TOL_ABS or QD_TOL_REL                            */
+    double tol;
+    int max_cycles;   /* V-cycles per solve before QD_ERR_NOT_CONVERGED
+                         (<= 0: no cap, as the reference)                    */
+    int precision;    /* QD_PREC_FP64 or QD_PREC_MIXED                       */
+} qd_mg_options;
+
+/* Time-stepping parameters (PARAMS, struct.h:12-38; SetParams.cpp:14-21). */
+typedef struct qd_rk43_params {
+    double tmax;      /* s */
+    double ini_dt;
+    double mindt;
+    double maxdt;
+    double totTol;
+    int maxNumSteps;
+} qd_rk43_params;
+
+/* Counters of one solver since creation. */
+typedef struct qd_stats {
+    long long solves;        /* elliptic solves (ode_solve calls)            */
+    long long vcycles;       /* V-cycles (FP32 ones in mixed precision)      */
+    long long attempts;      /* RK43 attempts (accepted + rejected)          */
+    long long steps;         /* accepted RK43 steps                          */
+    long long newton_iters;  /* Newton iterations, summed over nodes         */
+    long long kernel_launches; /* kernels this library launched              */
+} qd_stats;
+
+const char *qd_version(void);
+const char *qd_last_error(void);
+/* The reference's schedule: 6 levels, V(32,32), 32 coarse sweeps, absolute
+ * 1e-9, no cap, FP64. */
+void qd_default_options(qd_mg_options *opt);
+
+/* ---------------------------------------------------------------------
+ * Set-up.  Replaces RK43's GPU initialisation (odeSolver.cpp:1365-1425):
+ * level tables, cudaMalloc of the level buffers, H2D of mu_equi.
+ * mu_equi: (2nx-1)*(2nz-1) face moduli (GPa); mu_node: nx*nz node moduli
+ * (only the fault column i = 1 is used, by the stress extraction,
+ * fault.cpp:153).  (ni-1) and (nk-1) must be divisible by 2^(n_levels-1).
+ * ------------------------------------------------------------------- */
+int qd_solver_create(int ni, int nk, double dh, const double *mu_equi,
+                     const double *mu_node, const qd_mg_options *opt,
+                     qd_solver **out);
+int qd_solver_destroy(qd_solver *s);
+int qd_solver_set_options(qd_solver *s, const qd_mg_options *opt);
+int qd_get_stats(qd_solver *s, qd_stats *st);
+/* The solver's CUDA stream (a cudaStream_t), for callers that order their
+ * own work or CUDA events after the solver's. */
+void *qd_solver_stream(qd_solver *s);
+
+/* SetMedium's homogenisation (odeSolver.cpp:337-589) on the GPU: the harmonic
+ * mean of 400 Lagrange-interpolated samples per cell face.  mu_node is the
+ * ghosted nx*nz node modulus with the interior set; writes mu_equi.  Needs
+ * no solver. */
+int qd_set_medium(int ni, int nk, const double *mu_node, double *mu_equi);
+
+/* ---------------------------------------------------------------------
+ * Displacement field.  The device keeps u compact (nk rows x ni columns)
+ * for the whole run; these copy it to and from the reference's ghosted
+ * host array (replacing the pack/unpack of odeSolver.cpp:669-677,707-716
+ * and extend_crew, :612-650).
+ * ------------------------------------------------------------------- */
+int qd_upload_u(qd_solver *s, const double *U);
+int qd_download_u(qd_solver *s, double *U);
+
+/* One elliptic solve on the device-resident u: multigrid() + extend_crew()
+ * (ode_solve, odeSolver.cpp:605-720).  Columns 0 and ni-1 of u are the
+ * Dirichlet data.  cycles / rnorm / r0norm may be NULL. */
+int qd_ode_solve(qd_solver *s, int *cycles, double *rnorm, double *r0norm);
+
+/* ode_solve with the reference's host round trip: U (ghosted, host) in,
+ * solved U with ghosts out. */
+int qd_ode_solve_host(qd_solver *s, double *U, int *cycles, double *rnorm);
+
+/* Individual multigrid steps on the level-0 field, for parity tests:
+ * nsweeps red+black sweeps (smooth(), odeSolver.cpp:741-755); one V-cycle
+ * (vcycle(), :1101-1147); the level-0 residual norm (calcuDelta_dev +
+ * cublasDnrm2, :693-694). */
+int qd_mg_smooth(qd_solver *s, int nsweeps);
+int qd_mg_vcycle(qd_solver *s);
+int qd_mg_residual_norm(qd_solver *s, double *rnorm);
+
+/* ---------------------------------------------------------------------
+ * Fault.  Arrays are nz long (entries 1..nk used).  tau0 (MPa) is added to
+ * the stress the Newton solve balances; pass NULL for the reference's
+ * behaviour (no prestress).  Scalars are RATE_STATE_LAW's f0, V0, L, Vini
+ * (Alloc.cpp:27-31).
+ * ------------------------------------------------------------------- */
+int qd_fault_setup(qd_solver *s, const double *a, const double *b,
+                   const double *eta, const double *Tau_n0,
+                   const double *SlipShift, const double *tau0, double f0,
+                   double V0, double L, double Vini);
+
+/* setBoundary (odeSolver.cpp:1150-1188) on the device u: fault column
+ * u = slip/2, remote column u = Vini (t + ratio dt)/2 + SlipShift. */
+int qd_set_boundary(qd_solver *s, const double *slip, double t_elapsed,
+                    double ratio, double dt);
+
+/* eval_stress_on_fault (fault.cpp:139-164) from the device u: Ts (MPa) and
+ * Tn = Tau_n0.  Either output may be NULL. */
+int qd_eval_stress_on_fault(qd_solver *s, double *Ts, double *Tn);
+
+/* NRsearch (fault.cpp:169-232): slip rate from Ts (+tau0), psi and the
+ * seed in V (overwritten with the result).  One thread per fault node,
+ * Newton in x = asinh(V e^{psi/a} / 2V0) safeguarded by a sign bracket;
+ * from the reference's seed the iterates are the reference's.  iters may
+ * be NULL (else nz ints). */
+int qd_nrsearch(qd_solver *s, const double *Ts, const double *psi, double *V,
+                int *iters);
+
+/* cal_dpsi (odeSolver.cpp:1190-1206): aging law. */
+int qd_cal_dpsi(qd_solver *s, const double *psi, const double *V, double *dpsi);
+
+/* ---------------------------------------------------------------------
+ * RK43 (odeSolver.cpp:1277-1674) with the whole state on the device.
+ * qd_rk43_start runs the pre-loop part (initial solve, stress, Newton,
+ * aging law: :1363,1428-1439) from Slip/psi and the uploaded u;
+ * qd_rk43_step runs nsteps passes of the outer while-loop body
+ * (:1462-1636), stopping early at tmax or maxNumSteps.
+ * ------------------------------------------------------------------- */
+int qd_rk43_start(qd_solver *s, const qd_rk43_params *p, const double *Slip,
+                  const double *psi);
+int qd_rk43_step(qd_solver *s, int nsteps, int *steps_done);
+/* State read-back (any pointer may be NULL): Slip, psi, V (= f1.V_f),
+ * Ts, dpsi (= f1.dpsi). */
+int qd_rk43_get_state(qd_solver *s, double *Slip, double *psi, double *V,
+                      double *Ts, double *dpsi);
+/* Scalars: d[0] = t, d[1] = dt, d[2..3] = errA; it = accepted steps. */
+int qd_rk43_get_scalars(qd_solver *s, double *d4, int *it);
+/* Overwrite the state (checkpoint resume / host-driven stepping): Slip, psi,
+ * V, dpsi are nz arrays (V/dpsi: f1 after the last accepted step). */
+int qd_rk43_set_state(qd_solver *s, const double *Slip, const double *psi,
+                      const double *V, const double *dpsi, double t, double dt,
+                      double errA0, double errA1, int it);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QDEQ_H */

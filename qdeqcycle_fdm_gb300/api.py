@@ -1,0 +1,196 @@
+"""Python mirror of the reference's hot-path interface over the C ABI.
+
+The reference's surface is the C++ free functions of ``functions.h:11-45``.
+Here the same operations are methods of :class:`Solver` (one GB300 solver
+with device-resident state), and :class:`Simulation` runs the reference's
+``RK43`` loop (``odeSolver.cpp:1277-1674``) with the same start/step/state
+shape as the CPU oracle, so parity tests read the same on both sides.
+
+Every call goes through ``libqdeq_gb300.so``; nothing here computes on the
+CPU.  Arrays follow the reference's layouts (ghosted ``(nz, nx)`` fields,
+``nz``-long fault vectors).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import MgOptions, Rk43Params, Stats, check
+from .config import MGConfig
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+def _p(a):
+    if a is None:
+        return None
+    if a.dtype != np.float64 or not a.flags.c_contiguous:
+        raise TypeError("arrays must be C-contiguous float64")
+    return a.ctypes.data_as(_dp)
+
+
+def mg_options(mg: MGConfig) -> MgOptions:
+    return MgOptions(mg.n_levels, mg.nu_pre, mg.nu_post, mg.nu_coarse, mg.tol_mode, mg.tol,
+                     mg.max_cycles, mg.precision)
+
+
+def set_medium(ni: int, nk: int, mu_node: np.ndarray) -> np.ndarray:
+    """SetMedium's homogenisation on the GPU (odeSolver.cpp:337-589)."""
+    L = _lib.load()
+    me = np.zeros((2 * (nk + 2) - 1, 2 * (ni + 2) - 1))
+    check(L.qd_set_medium(ni, nk, _p(np.ascontiguousarray(mu_node, dtype=np.float64)), _p(me)))
+    return me
+
+
+class Solver:
+    """One device-resident solver: multigrid hierarchy + fault state."""
+
+    def __init__(self, ni, nk, dh, mu_equi, mu_node, mg: MGConfig):
+        self.L = _lib.load()
+        self.ni, self.nk, self.nx, self.nz = ni, nk, ni + 2, nk + 2
+        self.h = C.c_void_p()
+        opt = mg_options(mg)
+        check(self.L.qd_solver_create(ni, nk, dh, _p(np.ascontiguousarray(mu_equi)),
+                                      _p(np.ascontiguousarray(mu_node)), C.byref(opt),
+                                      C.byref(self.h)))
+
+    def close(self):
+        if self.h:
+            self.L.qd_solver_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def stream_ptr(self) -> int:
+        return int(self.L.qd_solver_stream(self.h) or 0)
+
+    def set_options(self, mg: MGConfig):
+        opt = mg_options(mg)
+        check(self.L.qd_solver_set_options(self.h, C.byref(opt)))
+
+    def stats(self) -> dict:
+        st = Stats()
+        check(self.L.qd_get_stats(self.h, C.byref(st)))
+        return {f: getattr(st, f) for f, _ in Stats._fields_}
+
+    # -- displacement field ------------------------------------------------
+    def upload_u(self, U):
+        check(self.L.qd_upload_u(self.h, _p(np.ascontiguousarray(U))))
+
+    def download_u(self):
+        U = np.zeros((self.nz, self.nx))
+        check(self.L.qd_download_u(self.h, _p(U)))
+        return U
+
+    def ode_solve(self):
+        """multigrid() + extend_crew() on the device u; (cycles, ||r||, ||r0||)."""
+        cyc = C.c_int(0)
+        rn = C.c_double(0)
+        r0 = C.c_double(0)
+        check(self.L.qd_ode_solve(self.h, C.byref(cyc), C.byref(rn), C.byref(r0)))
+        return cyc.value, rn.value, r0.value
+
+    def ode_solve_host(self, U):
+        """ode_solve with the reference's host round trip (U updated in place)."""
+        cyc = C.c_int(0)
+        rn = C.c_double(0)
+        check(self.L.qd_ode_solve_host(self.h, _p(U), C.byref(cyc), C.byref(rn)))
+        return cyc.value, rn.value
+
+    def smooth(self, nsweeps):
+        check(self.L.qd_mg_smooth(self.h, nsweeps))
+
+    def vcycle(self):
+        check(self.L.qd_mg_vcycle(self.h))
+
+    def residual_norm(self):
+        rn = C.c_double(0)
+        check(self.L.qd_mg_residual_norm(self.h, C.byref(rn)))
+        return rn.value
+
+    # -- fault -------------------------------------------------------------
+    def fault_setup(self, prob, with_tau0=True):
+        check(self.L.qd_fault_setup(self.h, _p(prob.a), _p(prob.b), _p(prob.eta), _p(prob.Tau_n0),
+                                    _p(prob.SlipShift), _p(prob.tau0) if with_tau0 else None,
+                                    prob.f0, prob.V0, prob.L, prob.Vini))
+
+    def set_boundary(self, slip, t, ratio, dt):
+        check(self.L.qd_set_boundary(self.h, _p(np.ascontiguousarray(slip)), t, ratio, dt))
+
+    def eval_stress_on_fault(self):
+        Ts = np.zeros(self.nz)
+        Tn = np.zeros(self.nz)
+        check(self.L.qd_eval_stress_on_fault(self.h, _p(Ts), _p(Tn)))
+        return Ts, Tn
+
+    def nrsearch(self, Ts, psi, V_seed):
+        V = np.array(V_seed, dtype=np.float64, copy=True)
+        iters = np.zeros(self.nz, dtype=np.int32)
+        rc = self.L.qd_nrsearch(self.h, _p(np.ascontiguousarray(Ts)), _p(np.ascontiguousarray(psi)),
+                                _p(V), iters.ctypes.data_as(_ip))
+        return V, iters, rc
+
+    def cal_dpsi(self, psi, V):
+        d = np.zeros(self.nz)
+        check(self.L.qd_cal_dpsi(self.h, _p(np.ascontiguousarray(psi)), _p(np.ascontiguousarray(V)),
+                                 _p(d)))
+        return d
+
+    # -- RK43 --------------------------------------------------------------
+    def rk43_start(self, prob):
+        p = Rk43Params(prob.tmax, prob.ini_dt, prob.mindt, prob.maxdt, prob.totTol,
+                       int(min(prob.maxNumSteps, 2**31 - 1)))
+        check(self.L.qd_rk43_start(self.h, C.byref(p), _p(prob.Slip), _p(prob.psi)))
+
+    def rk43_step(self, n=1):
+        done = C.c_int(0)
+        check(self.L.qd_rk43_step(self.h, n, C.byref(done)))
+        return done.value
+
+    def rk43_state(self):
+        out = {k: np.zeros(self.nz) for k in ("Slip", "psi", "V", "Ts", "dpsi")}
+        check(self.L.qd_rk43_get_state(self.h, _p(out["Slip"]), _p(out["psi"]), _p(out["V"]),
+                                       _p(out["Ts"]), _p(out["dpsi"])))
+        d = np.zeros(4)
+        it = C.c_int(0)
+        check(self.L.qd_rk43_get_scalars(self.h, _p(d), C.byref(it)))
+        out.update(t=d[0], dt=d[1], errA=(d[2], d[3]), it=it.value)
+        return out
+
+    def rk43_set_state(self, Slip, psi, V, dpsi, t, dt, errA0, errA1, it):
+        check(self.L.qd_rk43_set_state(self.h, _p(Slip), _p(psi), _p(V), _p(dpsi), t, dt, errA0,
+                                       errA1, it))
+
+
+class Simulation:
+    """RK43 on the GPU with the oracle's start/step/state interface."""
+
+    def __init__(self, prob, mg: MGConfig, with_tau0=True):
+        self.prob = prob
+        self.solver = Solver(prob.ni, prob.nk, prob.dh, prob.mu_equi, prob.mu_node, mg)
+        self.solver.fault_setup(prob, with_tau0=with_tau0)
+        self.solver.upload_u(prob.U)
+
+    def start(self):
+        self.solver.rk43_start(self.prob)
+        return 0
+
+    def step(self, n=1):
+        return self.solver.rk43_step(n)
+
+    def state(self, with_u=True):
+        st = self.solver.rk43_state()
+        if with_u:
+            st["U"] = self.solver.download_u()
+        st.update(self.solver.stats())
+        return st
+
+    def close(self):
+        self.solver.close()

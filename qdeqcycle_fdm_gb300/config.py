@@ -1,0 +1,116 @@
+"""Named workloads of the quasi-dynamic antiplane earthquake-cycle path.
+
+Each config fixes the grid, the elastic medium, the rate-and-state friction,
+the time-integration tolerances and the multigrid schedule.  Parameters the
+reference hard-codes live in ``SetParams.cpp:3-30`` (time stepping and grid),
+``fault.cpp:85-120`` (friction) and ``odeSolver.cpp:2-4,297-305`` (multigrid,
+medium); here they are data.
+
+Simulated years are 365.25-day years.  (The reference's ``tmax`` counts
+360-day years, ``SetParams.cpp:11-12``.)
+"""
+from __future__ import annotations
+
+import dataclasses
+from dataclasses import dataclass, field
+
+YEAR_S = 365.25 * 86400.0
+
+
+@dataclass
+class MGConfig:
+    n_levels: int = 6          # odeSolver.cpp:3
+    nu_pre: int = 32           # odeSolver.cpp:4 (n_cycles: smooth() repeats)
+    nu_post: int = 32
+    nu_coarse: int = 32
+    tol_mode: int = 0          # 0: absolute ||r||2 (odeSolver.cpp:689); 1: relative
+    tol: float = 1e-9
+    max_cycles: int = 0        # 0 = uncapped, as the reference
+    precision: int = 0         # 0: FP64; 1: FP32 V-cycles inside FP64 refinement
+
+
+@dataclass
+class ProblemConfig:
+    name: str
+    ni: int                    # nodes off-fault (x), GRID.ni
+    nk: int                    # nodes along the fault (depth), GRID.nk
+    domain_m: float = 40e3     # square domain edge
+    mu_profile: str = "uniform"    # "uniform" | "layered"
+    mu_gpa: float = 30.0
+    mu_surface_gpa: float = 20.0   # layered: linear from the surface ...
+    mu_deep_gpa: float = 32.0      # ... to this value at layer_depth_km
+    layer_depth_km: float = 4.0
+    cs_kms: float = 3.3
+    # rate-and-state (aging law); a(z): a_shallow to seis_depth, linear to a_deep
+    a_shallow: float = 0.008
+    a_deep: float = 0.024
+    seis_depth_km: float = 12.0
+    taper_depth_km: float = 16.0
+    b: float = 0.012
+    Dc_m: float = 0.006
+    sigma_n_mpa: float = 40.0
+    f0: float = 0.6
+    V0: float = 1e-6
+    Vp: float = 1e-9
+    amb_perturb: float = 0.0   # uniform +-fraction perturbation of a-b per node
+    seed: int = 12345
+    prestress: bool = True     # tau0 so that V = Vp at t = 0 with u = 0
+    # time stepping (SetParams.cpp:14-17)
+    years: float = 300.0
+    ini_dt: float = 1e-3
+    mindt: float = 1e-5
+    maxdt: float = 1e8
+    totTol: float = 1e-7
+    maxNumSteps: int = 100000000
+    mg: MGConfig = field(default_factory=MGConfig)
+
+    @property
+    def dh(self) -> float:
+        return self.domain_m / (self.nk - 1)
+
+    def replace(self, **kw) -> "ProblemConfig":
+        return dataclasses.replace(self, **kw)
+
+
+def reference_mg() -> MGConfig:
+    """The reference's multigrid: 6 levels, V(32,32), absolute 1e-9."""
+    return MGConfig(6, 32, 32, 32, 0, 1e-9, 0, 0)
+
+
+def config0() -> ProblemConfig:
+    """129x129 FP64, uniform mu = 30 GPa, 5-level V(2,2) to 1e-10 relative."""
+    return ProblemConfig(name="config0_129", ni=129, nk=129, mu_profile="uniform",
+                         years=300.0,
+                         mg=MGConfig(n_levels=5, nu_pre=2, nu_post=2, nu_coarse=32,
+                                     tol_mode=1, tol=1e-10, max_cycles=200))
+
+
+def config1() -> ProblemConfig:
+    """1025x1025 FP64, layered mu 20 -> 32 GPa over 0-4 km, +-5% a-b, 8 levels."""
+    return ProblemConfig(name="config1_1025", ni=1025, nk=1025, mu_profile="layered",
+                         amb_perturb=0.05, years=500.0,
+                         mg=MGConfig(n_levels=8, nu_pre=2, nu_post=2, nu_coarse=32,
+                                     tol_mode=1, tol=1e-9, max_cycles=200))
+
+
+def config1_mixed() -> ProblemConfig:
+    c = config1()
+    c.mg = dataclasses.replace(c.mg, precision=1)
+    c.name = "config1_1025_mixed"
+    return c
+
+
+def small(n: int = 33, **kw) -> ProblemConfig:
+    """A config-0-like problem on an n x n grid (n = 2^m + 1) for tests."""
+    levels = 1
+    m = n - 1
+    while m % 2 == 0 and (m // 2) >= 8:
+        m //= 2
+        levels += 1
+    c = ProblemConfig(name=f"small_{n}", ni=n, nk=n, mu_profile="uniform",
+                      mg=MGConfig(n_levels=levels, nu_pre=2, nu_post=2, nu_coarse=32,
+                                  tol_mode=1, tol=1e-10, max_cycles=200))
+    return c.replace(**kw) if kw else c
+
+
+CONFIGS = {"config0": config0, "config1": config1, "config1_mixed": config1_mixed}

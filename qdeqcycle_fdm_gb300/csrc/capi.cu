@@ -1,0 +1,443 @@
+// capi.cu -- the extern "C" boundary (include/qdeq.h) and the RK43 host
+// driver.  The driver keeps the reference's control flow
+// (odeSolver.cpp:1277-1674) on the host -- attempt loop, step-size control,
+// commit -- and runs every per-node and per-grid-point operation on the
+// device; the only device-to-host traffic per attempt is the error estimate,
+// and per V-cycle the residual norm.
+#include <math.h>
+#include <stdarg.h>
+#include <string.h>
+
+#include <vector>
+
+#include "qdeq_internal.cuh"
+
+namespace qd {
+
+static thread_local char g_err[512] = "";
+
+void set_error(const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+static int check_opts(const qd_mg_options *o) {
+    if (!o || o->n_levels < 1 || o->n_levels > QD_MAXLEV || o->nu_pre < 0 || o->nu_post < 0 ||
+        o->nu_coarse < 0 || (o->tol_mode != QD_TOL_ABS && o->tol_mode != QD_TOL_REL) ||
+        !(o->tol > 0.0) || (o->precision != QD_PREC_FP64 && o->precision != QD_PREC_MIXED)) {
+        set_error("invalid multigrid options");
+        return QD_ERR_ARG;
+    }
+    return QD_OK;
+}
+
+// The step-size controller (computeStepSize, odeSolver.cpp:1241-1271).  A
+// zero in the error history (an accepted step whose two embedded solutions
+// agreed to the last bit) makes the reference's PID branch return mindt or
+// NaN; with a zero there the elementary controller the reference uses for
+// its first steps (:1254-1257) is taken instead.
+static double step_size(int it, double dt, const qd_rk43_params &P, double totErr,
+                        const double errA[2]) {
+    const double ord = 4.0, kappa = 0.9;
+    const double alpha = 0.49 / ord, beta = 0.34 / ord, gamma = 0.1 / ord;
+    const double totTol = P.totTol;
+    double stepRatio;
+    if (it < 4 || errA[0] == 0.0 || errA[1] == 0.0)
+        stepRatio = kappa * pow(totTol / totErr, 1.0 / (1.0 + ord));
+    else
+        stepRatio = kappa * pow(totTol / totErr, alpha) * pow(errA[0] / totTol, beta) *
+                    pow(totTol / errA[1], gamma);
+    double deltaT = stepRatio * dt;
+    deltaT = (dt * 5.0 <= deltaT) ? dt * 5.0 : deltaT;
+    deltaT = (P.maxdt <= deltaT) ? P.maxdt : deltaT;
+    deltaT = (P.mindt >= deltaT) ? P.mindt : deltaT;
+    return deltaT;
+}
+
+static int check_status(qd_solver *s) {
+    QD_CUDA(cudaMemcpyAsync(s->h_status, s->d_status, sizeof(DevStatus), cudaMemcpyDeviceToHost,
+                            s->stream));
+    QD_CUDA(cudaStreamSynchronize(s->stream));
+    if (s->h_status->flags & (ST_NEWTON_NAN | ST_NEWTON_CAP)) {
+        set_error("Newton for slip rate failed at fault node %d (flags %u)", s->h_status->bad_node,
+                  s->h_status->flags);
+        return QD_ERR_NEWTON;
+    }
+    return QD_OK;
+}
+
+static int reset_status(qd_solver *s) {
+    DevStatus z;
+    z.flags = 0;
+    z.bad_node = -1;
+    *s->h_status = z;
+    QD_CUDA(cudaMemcpyAsync(s->d_status, s->h_status, sizeof(DevStatus), cudaMemcpyHostToDevice,
+                            s->stream));
+    return QD_OK;
+}
+
+// one stage: boundary data, elliptic solve, stress/Newton/aging law
+static int stage(qd_solver *s, int st, double ratio) {
+    QD_TRY(launch_stage_boundary(s, st, ratio, nullptr, nullptr));
+    int rc = mg_solve(s, nullptr, nullptr, nullptr);
+    if (rc != QD_OK) return rc;
+    return launch_fault(s, st, 0);
+}
+
+static int rk_start(qd_solver *s) {
+    s->dt = s->P.ini_dt;                                          // :1363
+    QD_TRY(reset_status(s));
+    QD_TRY(stage(s, 1, 0.0));                                     // :1428-1437
+    QD_TRY(check_status(s));
+    s->started = 1;
+    return QD_OK;
+}
+
+// the outer while-loop body, odeSolver.cpp:1464-1636
+static int rk_step(qd_solver *s) {
+    static double c[7], b[7], hb[7], a[7][7];
+    static bool init = false;
+    if (!init) { rk_tableau(c, b, hb, a); init = true; }
+    double totErr = 0.0;
+    s->it = s->it + 1;
+    int attemptCount = 0;
+    while (attemptCount < 100) {
+        attemptCount++;
+        s->attempts++;
+        if (s->t + s->dt > s->P.tmax) s->dt = s->P.tmax - s->t;
+        for (int st = 2; st <= 6; st++) QD_TRY(stage(s, st, c[st]));
+        QD_TRY(launch_error(s));
+        QD_CUDA(cudaMemcpyAsync(s->h_scal + 2, s->d_scal + 2, sizeof(double), cudaMemcpyDeviceToHost,
+                                s->stream));
+        QD_CUDA(cudaStreamSynchronize(s->stream));
+        totErr = s->h_scal[2];
+        if (totErr < s->P.totTol) break;
+        s->dt = step_size(s->it, s->dt, s->P, totErr, s->errA);
+        if (s->P.mindt == s->dt) break;
+    }
+    s->t = s->t + s->dt;
+    QD_TRY(launch_commit(s));
+    QD_TRY(stage(s, 1, 0.0));                                     // :1615-1619
+    const double newDeltaT = (totErr != 0.0) ? step_size(s->it, s->dt, s->P, totErr, s->errA) : s->dt;
+    s->errA[1] = s->errA[0];
+    s->errA[0] = totErr;
+    s->dt = newDeltaT;
+    s->steps++;
+    return check_status(s);
+}
+
+}  // namespace qd
+
+using namespace qd;
+
+extern "C" {
+
+const char *qd_version(void) { return "qdeq-gb300 1 (sm_103a)"; }
+const char *qd_last_error(void) { return g_err; }
+
+void qd_default_options(qd_mg_options *o) {
+    if (!o) return;
+    o->n_levels = 6;
+    o->nu_pre = 32;
+    o->nu_post = 32;
+    o->nu_coarse = 32;
+    o->tol_mode = QD_TOL_ABS;
+    o->tol = 1e-9;
+    o->max_cycles = 0;
+    o->precision = QD_PREC_FP64;
+}
+
+int qd_solver_create(int ni, int nk, double dh, const double *mu_equi, const double *mu_node,
+                     const qd_mg_options *opt, qd_solver **out) {
+    if (!out || !mu_equi || !mu_node || ni < 3 || nk < 3 || !(dh > 0.0)) {
+        set_error("qd_solver_create: bad arguments");
+        return QD_ERR_ARG;
+    }
+    *out = nullptr;
+    QD_TRY(check_opts(opt));
+    qd_solver *s = new qd_solver();
+    memset((void *)s, 0, sizeof(*s));
+    s->ni = ni; s->nk = nk; s->nx = ni + 2; s->nz = nk + 2; s->dh = dh;
+    s->opt = *opt;
+    int rc = QD_OK;
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc(&s->d_scal, 8 * sizeof(double)) != cudaSuccess ||
+        cudaMallocHost(&s->h_scal, 8 * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&s->d_status, sizeof(DevStatus)) != cudaSuccess ||
+        cudaMallocHost(&s->h_status, sizeof(DevStatus)) != cudaSuccess) {
+        set_error("qd_solver_create: CUDA set-up failed: %s", cudaGetErrorString(cudaGetLastError()));
+        qd_solver_destroy(s);
+        return QD_ERR_CUDA;
+    }
+    rc = mg_alloc(s, mu_equi);
+    if (rc == QD_OK) rc = fault_alloc(s);
+    if (rc == QD_OK) {
+        std::vector<double> mu0(s->nz, 0.0);
+        for (int k = 0; k < s->nz; k++) mu0[k] = mu_node[1 + (long)k * s->nx];   // fault.cpp:151-153
+        if (cudaMemcpy(s->F.mu0, mu0.data(), s->nz * sizeof(double), cudaMemcpyHostToDevice) !=
+            cudaSuccess)
+            rc = QD_ERR_CUDA;
+    }
+    if (rc == QD_OK) rc = reset_status(s);
+    if (rc == QD_OK && cudaStreamSynchronize(s->stream) != cudaSuccess) rc = QD_ERR_CUDA;
+    if (rc != QD_OK) {
+        qd_solver_destroy(s);
+        return rc;
+    }
+    *out = s;
+    return QD_OK;
+}
+
+int qd_solver_destroy(qd_solver *s) {
+    if (!s) return QD_OK;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    mg_free(s);
+    fault_free(s);
+    cudaFree(s->d_scal);
+    cudaFreeHost(s->h_scal);
+    cudaFree(s->d_status);
+    cudaFreeHost(s->h_status);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+    return QD_OK;
+}
+
+int qd_solver_set_options(qd_solver *s, const qd_mg_options *opt) {
+    if (!s) return QD_ERR_ARG;
+    QD_TRY(check_opts(opt));
+    if (opt->n_levels != s->opt.n_levels) {
+        set_error("n_levels cannot change after creation");
+        return QD_ERR_ARG;
+    }
+    s->opt = *opt;
+    return QD_OK;
+}
+
+int qd_get_stats(qd_solver *s, qd_stats *st) {
+    if (!s || !st) return QD_ERR_ARG;
+    st->solves = s->solves; st->vcycles = s->vcycles; st->attempts = s->attempts;
+    st->steps = s->steps; st->kernel_launches = s->launches;
+    std::vector<int> it(s->nz);
+    QD_CUDA(cudaMemcpy(it.data(), s->F.iters, s->nz * sizeof(int), cudaMemcpyDeviceToHost));
+    long long sum = 0;
+    for (int v : it) sum += v;
+    st->newton_iters = sum;
+    return QD_OK;
+}
+
+void *qd_solver_stream(qd_solver *s) { return s ? (void *)s->stream : nullptr; }
+
+int qd_set_medium(int ni, int nk, const double *mu_node, double *mu_equi) {
+    return set_medium_gpu(ni, nk, mu_node, mu_equi);
+}
+
+int qd_upload_u(qd_solver *s, const double *U) {
+    if (!s || !U) return QD_ERR_ARG;
+    const LevelDims &d = s->dims[0];
+    // interior of the ghosted array: rows 1..nk, columns 1..ni (:669-677)
+    QD_CUDA(cudaMemcpy2DAsync(s->L64[0].u, d.P * sizeof(double), U + s->nx + 1,
+                              s->nx * sizeof(double), d.K * sizeof(double), d.N,
+                              cudaMemcpyHostToDevice, s->stream));
+    QD_CUDA(cudaStreamSynchronize(s->stream));
+    return QD_OK;
+}
+
+// extend_crew (odeSolver.cpp:612-650) on the host array
+static void extend_crew_host(int ni, int nk, double *U) {
+    const int nx = ni + 2, nz = nk + 2;
+    for (int k = 0; k < nz; k++) {
+        double *row = U + (long)k * nx;
+        row[0] = 2.0 * row[1] - row[2];
+        row[ni + 1] = 2.0 * row[ni] - row[ni - 1];
+    }
+    for (int i = 0; i < nx; i++) {
+        U[i] = U[i + 2L * nx];
+        U[i + (long)(nk + 1) * nx] = U[i + (long)(nk - 1) * nx];
+    }
+}
+
+int qd_download_u(qd_solver *s, double *U) {
+    if (!s || !U) return QD_ERR_ARG;
+    const LevelDims &d = s->dims[0];
+    QD_CUDA(cudaMemcpy2DAsync(U + s->nx + 1, s->nx * sizeof(double), s->L64[0].u,
+                              d.P * sizeof(double), d.K * sizeof(double), d.N,
+                              cudaMemcpyDeviceToHost, s->stream));
+    QD_CUDA(cudaStreamSynchronize(s->stream));
+    extend_crew_host(s->ni, s->nk, U);
+    return QD_OK;
+}
+
+int qd_ode_solve(qd_solver *s, int *cycles, double *rnorm, double *r0norm) {
+    if (!s) return QD_ERR_ARG;
+    return mg_solve(s, cycles, rnorm, r0norm);
+}
+
+int qd_ode_solve_host(qd_solver *s, double *U, int *cycles, double *rnorm) {
+    QD_TRY(qd_upload_u(s, U));
+    int rc = mg_solve(s, cycles, rnorm, nullptr);
+    if (rc != QD_OK && rc != QD_ERR_NOT_CONVERGED) return rc;
+    QD_TRY(qd_download_u(s, U));
+    return rc;
+}
+
+int qd_mg_smooth(qd_solver *s, int nsweeps) {
+    if (!s || nsweeps < 0) return QD_ERR_ARG;
+    return mg_smooth(s, 0, nsweeps);
+}
+
+int qd_mg_vcycle(qd_solver *s) {
+    if (!s) return QD_ERR_ARG;
+    return mg_vcycle(s);
+}
+
+int qd_mg_residual_norm(qd_solver *s, double *rnorm) {
+    if (!s || !rnorm) return QD_ERR_ARG;
+    return mg_residual_norm(s, rnorm);
+}
+
+int qd_fault_setup(qd_solver *s, const double *a, const double *b, const double *eta,
+                   const double *Tau_n0, const double *SlipShift, const double *tau0, double f0,
+                   double V0, double L, double Vini) {
+    if (!s || !a || !b || !eta || !Tau_n0 || !SlipShift) {
+        set_error("qd_fault_setup: null array");
+        return QD_ERR_ARG;
+    }
+    const size_t n = s->nz * sizeof(double);
+    FaultState &F = s->F;
+    QD_CUDA(cudaMemcpy(F.a, a, n, cudaMemcpyHostToDevice));
+    QD_CUDA(cudaMemcpy(F.b, b, n, cudaMemcpyHostToDevice));
+    QD_CUDA(cudaMemcpy(F.eta, eta, n, cudaMemcpyHostToDevice));
+    QD_CUDA(cudaMemcpy(F.Tn0, Tau_n0, n, cudaMemcpyHostToDevice));
+    QD_CUDA(cudaMemcpy(F.SlipShift, SlipShift, n, cudaMemcpyHostToDevice));
+    if (tau0) QD_CUDA(cudaMemcpy(F.tau0, tau0, n, cudaMemcpyHostToDevice));
+    F.have_tau0 = tau0 != nullptr;
+    F.f0 = f0; F.V0 = V0; F.L = L; F.Vini = Vini;
+    s->fault_ready = 1;
+    return QD_OK;
+}
+
+int qd_set_boundary(qd_solver *s, const double *slip, double t_elapsed, double ratio, double dt) {
+    if (!s || !slip) return QD_ERR_ARG;
+    if (!s->fault_ready) { set_error("qd_set_boundary: no fault set up"); return QD_ERR_STATE; }
+    QD_CUDA(cudaMemcpyAsync(s->F.Slip, slip, s->nz * sizeof(double), cudaMemcpyHostToDevice,
+                            s->stream));
+    const double t0 = s->t, dt0 = s->dt;
+    s->t = t_elapsed;
+    s->dt = dt;
+    int rc = launch_stage_boundary(s, 1, ratio, nullptr, nullptr);
+    s->t = t0;
+    s->dt = dt0;
+    QD_TRY(rc);
+    QD_CUDA(cudaStreamSynchronize(s->stream));
+    return QD_OK;
+}
+
+int qd_eval_stress_on_fault(qd_solver *s, double *Ts, double *Tn) {
+    if (!s) return QD_ERR_ARG;
+    if (!s->fault_ready) { set_error("qd_eval_stress_on_fault: no fault set up"); return QD_ERR_STATE; }
+    QD_TRY(launch_stress(s));
+    if (Ts) QD_CUDA(cudaMemcpyAsync(Ts, s->F.Ts, s->nz * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    if (Tn) QD_CUDA(cudaMemcpyAsync(Tn, s->F.Tn, s->nz * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    QD_CUDA(cudaStreamSynchronize(s->stream));
+    return QD_OK;
+}
+
+int qd_nrsearch(qd_solver *s, const double *Ts, const double *psi, double *V, int *iters) {
+    if (!s || !Ts || !psi || !V) return QD_ERR_ARG;
+    if (!s->fault_ready) { set_error("qd_nrsearch: no fault set up"); return QD_ERR_STATE; }
+    const size_t n = s->nz * sizeof(double);
+    // scratch: the stage-6 buffers are free outside qd_rk43_step
+    double *dTs = s->F.kslip[6], *dpsi = s->F.kpsi[6], *dV = s->F.fV[6];
+    QD_CUDA(cudaMemcpyAsync(dTs, Ts, n, cudaMemcpyHostToDevice, s->stream));
+    QD_CUDA(cudaMemcpyAsync(dpsi, psi, n, cudaMemcpyHostToDevice, s->stream));
+    QD_CUDA(cudaMemcpyAsync(dV, V, n, cudaMemcpyHostToDevice, s->stream));
+    int *dit = nullptr;
+    QD_CUDA(cudaMallocAsync(&dit, s->nz * sizeof(int), s->stream));
+    QD_TRY(reset_status(s));
+    QD_TRY(launch_newton(s, dTs, dpsi, dV, dit));
+    QD_CUDA(cudaMemcpyAsync(V, dV, n, cudaMemcpyDeviceToHost, s->stream));
+    if (iters) QD_CUDA(cudaMemcpyAsync(iters, dit, s->nz * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    QD_CUDA(cudaFreeAsync(dit, s->stream));
+    return check_status(s);
+}
+
+int qd_cal_dpsi(qd_solver *s, const double *psi, const double *V, double *dpsi) {
+    if (!s || !psi || !V || !dpsi) return QD_ERR_ARG;
+    if (!s->fault_ready) { set_error("qd_cal_dpsi: no fault set up"); return QD_ERR_STATE; }
+    const size_t n = s->nz * sizeof(double);
+    double *dp = s->F.kpsi[6], *dV = s->F.fV[6], *dd = s->F.fdpsi[6];
+    QD_CUDA(cudaMemcpyAsync(dp, psi, n, cudaMemcpyHostToDevice, s->stream));
+    QD_CUDA(cudaMemcpyAsync(dV, V, n, cudaMemcpyHostToDevice, s->stream));
+    QD_TRY(launch_dpsi(s, dp, dV, dd));
+    QD_CUDA(cudaMemcpyAsync(dpsi, dd, n, cudaMemcpyDeviceToHost, s->stream));
+    QD_CUDA(cudaStreamSynchronize(s->stream));
+    return QD_OK;
+}
+
+int qd_rk43_start(qd_solver *s, const qd_rk43_params *p, const double *Slip, const double *psi) {
+    if (!s || !p || !Slip || !psi) return QD_ERR_ARG;
+    if (!s->fault_ready) { set_error("qd_rk43_start: no fault set up"); return QD_ERR_STATE; }
+    if (p->maxNumSteps == 0) { set_error("max number of steps == 0"); return QD_ERR_ARG; }  // :1357-1361
+    s->P = *p;
+    const size_t n = s->nz * sizeof(double);
+    QD_CUDA(cudaMemcpy(s->F.Slip, Slip, n, cudaMemcpyHostToDevice));
+    QD_CUDA(cudaMemcpy(s->F.psi, psi, n, cudaMemcpyHostToDevice));
+    for (int st = 1; st <= 6; st++) {
+        QD_CUDA(cudaMemset(s->F.fV[st], 0, n));
+        QD_CUDA(cudaMemset(s->F.fdpsi[st], 0, n));
+    }
+    s->t = 0.0;
+    s->it = 0;
+    s->errA[0] = s->errA[1] = 0.0;
+    return rk_start(s);
+}
+
+int qd_rk43_step(qd_solver *s, int nsteps, int *steps_done) {
+    if (!s || nsteps < 0) return QD_ERR_ARG;
+    if (!s->started) { set_error("qd_rk43_step before qd_rk43_start"); return QD_ERR_STATE; }
+    int done = 0;
+    int rc = QD_OK;
+    while (done < nsteps && s->it < s->P.maxNumSteps && s->t < s->P.tmax) {   // :1462
+        rc = rk_step(s);
+        if (rc != QD_OK) break;
+        done++;
+    }
+    if (steps_done) *steps_done = done;
+    return rc;
+}
+
+int qd_rk43_get_state(qd_solver *s, double *Slip, double *psi, double *V, double *Ts, double *dpsi) {
+    if (!s) return QD_ERR_ARG;
+    const size_t n = s->nz * sizeof(double);
+    const double *src[5] = {s->F.Slip, s->F.psi, s->F.fV[1], s->F.Ts, s->F.fdpsi[1]};
+    double *dst[5] = {Slip, psi, V, Ts, dpsi};
+    for (int i = 0; i < 5; i++)
+        if (dst[i]) QD_CUDA(cudaMemcpyAsync(dst[i], src[i], n, cudaMemcpyDeviceToHost, s->stream));
+    QD_CUDA(cudaStreamSynchronize(s->stream));
+    return QD_OK;
+}
+
+int qd_rk43_get_scalars(qd_solver *s, double *d4, int *it) {
+    if (!s) return QD_ERR_ARG;
+    if (d4) { d4[0] = s->t; d4[1] = s->dt; d4[2] = s->errA[0]; d4[3] = s->errA[1]; }
+    if (it) *it = s->it;
+    return QD_OK;
+}
+
+int qd_rk43_set_state(qd_solver *s, const double *Slip, const double *psi, const double *V,
+                      const double *dpsi, double t, double dt, double errA0, double errA1, int it) {
+    if (!s || !Slip || !psi || !V || !dpsi) return QD_ERR_ARG;
+    const size_t n = s->nz * sizeof(double);
+    QD_CUDA(cudaMemcpyAsync(s->F.Slip, Slip, n, cudaMemcpyHostToDevice, s->stream));
+    QD_CUDA(cudaMemcpyAsync(s->F.psi, psi, n, cudaMemcpyHostToDevice, s->stream));
+    QD_CUDA(cudaMemcpyAsync(s->F.fV[1], V, n, cudaMemcpyHostToDevice, s->stream));
+    QD_CUDA(cudaMemcpyAsync(s->F.fdpsi[1], dpsi, n, cudaMemcpyHostToDevice, s->stream));
+    QD_CUDA(cudaStreamSynchronize(s->stream));
+    s->t = t; s->dt = dt; s->errA[0] = errA0; s->errA[1] = errA1; s->it = it;
+    s->started = 1;
+    return QD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,342 @@
+// fault.cu -- fault-node kernels of the RK43 stage pipeline: stage
+// combination + boundary data, shear stress from u, Newton for slip rate,
+// aging law, embedded error estimate and step commit.  One thread per fault
+// node; nodes are independent (fault.cpp:139-232, odeSolver.cpp:1150-1238).
+#include <math.h>
+
+#include "qdeq_internal.cuh"
+
+namespace qd {
+
+// Explicit ARK4(3)6L tableau of the reference's integrator
+// (odeSolver.cpp:1298-1334); published coefficients, kept identical.
+void rk_tableau(double c[7], double b[7], double hb[7], double a[7][7]) {
+    for (int i = 0; i < 7; i++) {
+        c[i] = b[i] = hb[i] = 0.0;
+        for (int j = 0; j < 7; j++) a[i][j] = 0.0;
+    }
+    c[2] = 1. / 2.; c[3] = 83. / 250.; c[4] = 31. / 50.; c[5] = 17. / 20.; c[6] = 1.;
+    b[1] = 82889. / 524892.; b[3] = 15625. / 83664.; b[4] = 69875. / 102672.;
+    b[5] = -2260. / 8211.; b[6] = 1. / 4.;
+    hb[1] = 4586570599. / 29645900160.; hb[3] = 178811875. / 945068544.;
+    hb[4] = 814220225. / 1159782912.; hb[5] = -3700637. / 11593932.; hb[6] = 61727. / 225920.;
+    a[2][1] = 1. / 2.;
+    a[3][1] = 13861. / 62500.; a[3][2] = 6889. / 62500.;
+    a[4][1] = -116923316275. / 2393684061468.; a[4][2] = -2731218467317. / 15368042101831.;
+    a[4][3] = 9408046702089. / 11113171139209.;
+    a[5][1] = -451086348788. / 2902428689909.; a[5][2] = -2682348792572. / 7519795681897.;
+    a[5][3] = 12662868775082. / 11960479115383.; a[5][4] = 3355817975965. / 11060851509271.;
+    a[6][1] = 647845179188. / 3216320057751.; a[6][2] = 73281519250. / 8382639484533.;
+    a[6][3] = 552539513391. / 3454668386233.; a[6][4] = 3354512671639. / 8306763924573.;
+    a[6][5] = 4040. / 17871.;
+}
+
+struct RkCoefs {
+    double c[7], b[7], hb[7], a[7][7];
+};
+__constant__ RkCoefs c_rk;
+static bool g_rk_uploaded = false;
+
+static int upload_tableau(qd_solver *s) {
+    if (g_rk_uploaded) return QD_OK;
+    RkCoefs h;
+    rk_tableau(h.c, h.b, h.hb, h.a);
+    QD_CUDA(cudaMemcpyToSymbol(c_rk, &h, sizeof(h)));
+    g_rk_uploaded = true;
+    (void)s;
+    return QD_OK;
+}
+
+struct FaultArgs {
+    int nk, K, P;
+    double dh;
+    double *u0;  // level-0 displacement (compact, pitched)
+    FaultState F;
+    DevStatus *status;
+};
+
+static FaultArgs fargs(qd_solver *s) {
+    FaultArgs a;
+    a.nk = s->nk; a.K = s->dims[0].K; a.P = s->dims[0].P; a.dh = s->dh;
+    a.u0 = s->L64[0].u; a.F = s->F; a.status = s->d_status;
+    return a;
+}
+
+static inline int nblk(int n, int b) { return (n + b - 1) / b; }
+
+// ---------------------------------------------------------------------------
+// device physics
+// ---------------------------------------------------------------------------
+
+// partial1st + eval_stress_on_fault (fault.cpp:153,162): one-sided SBP-4
+// closure derivative at the fault column, GPa * (m/m) * 1e3 -> MPa.
+__device__ __forceinline__ double fault_stress(const double *urow, double mu, double dh) {
+    const double du = (-24.0 / (17.0 * dh)) * urow[0] + (59.0 / (34.0 * dh)) * urow[1] +
+                      (-4.0 / (17.0 * dh)) * urow[2] + (-3.0 / (34.0 * dh)) * urow[3];
+    return mu * du * 1.0e3;
+}
+
+// NRsearch (fault.cpp:180-228) for one node, safeguarded.  Unknown
+// x = asinh(V e^{psi/a} / 2V0); residual g(x) = A sinh x + fa x - fb with
+// A = 2 eta V0 e^{-psi/a} > 0, fa = a |sigma_n| > 0, so g is increasing and
+// the root lies between 0 and fb/fa.  The iteration is the reference's
+// Newton step and stopping rule; a step that leaves the bracket (or a NaN)
+// is replaced by bisection.  From the reference's seed (x = 0) Newton never
+// leaves the bracket, so the iterates are the reference's.
+__device__ double newton_v(double Ts, double Tn, double tau0, double a, double eta, double psi,
+                           double V0, double Vseed, int *iters, unsigned int *flags) {
+    double x = asinh(0.5 * Vseed / V0 * exp(psi / a));
+    const double fa = a * fabs(Tn);
+    const double fb = Ts + tau0;
+    const double A = 2.0 * eta * V0 * exp(-psi / a);
+    double lo, hi;
+    if (fb >= 0.0) { lo = 0.0; hi = fb / fa; } else { lo = fb / fa; hi = 0.0; }
+    if (!(x >= lo && x <= hi)) x = 0.5 * (lo + hi);
+    const int itmax = 200;
+    int it = 0;
+    bool done = false;
+    while (it < itmax) {
+        const double sh = sinh(x);
+        const double fy = A * sh + fa * x - fb;
+        const double df = A * cosh(x) + fa;
+        double d = -fy / (df + 1e-100);
+        double xn = x + d;
+        if (fy > 0.0) hi = fmin(hi, x); else lo = fmax(lo, x);
+        if (!(xn >= lo && xn <= hi)) {
+            xn = 0.5 * (lo + hi);
+            d = xn - x;
+            *flags |= ST_NEWTON_BRACKET;
+        }
+        const double err = fabs(d) / (fabs(x) + 1e-100);
+        it++;
+        x = xn;
+        if (err < 1e-10) { done = true; break; }
+    }
+    if (!done) *flags |= ST_NEWTON_CAP;
+    *iters = it;
+    double V = 2.0 * V0 * exp(-psi / a);
+    V = V * sinh(x);
+    if (isnan(V)) *flags |= ST_NEWTON_NAN;
+    return V;
+}
+
+// cal_dpsi (odeSolver.cpp:1196-1204)
+__device__ __forceinline__ double aging(double psi, double b, double V, double f0, double V0,
+                                        double L) {
+    const double A = exp((f0 - psi) / b);
+    double d = 0.0;
+    if (!isinf(A) && b > 1e-3) d = (b * V0 / L) * (A - V / V0);
+    return d;
+}
+
+__device__ __forceinline__ void report(DevStatus *st, unsigned int flags, int node) {
+    if (flags & (ST_NEWTON_NAN | ST_NEWTON_CAP)) {
+        atomicOr(&st->flags, flags);
+        atomicCAS(&st->bad_node, -1, node);
+    } else if (flags) {
+        atomicOr(&st->flags, flags);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------
+
+// Stage combination k_s = y + dt sum_j a_sj f_j (odeSolver.cpp:1491-1561),
+// the Newton seed of the stage (f_s.V_f, zeroed by the reference, :1484-1488,
+// :1610) and setBoundary's two Dirichlet columns (:1162-1172).
+// stage 1 copies y (the start and the post-accept refresh, :1430,1606-1614).
+__global__ void k_stage_boundary(FaultArgs A, int stage, double t, double dt, double ratio) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (k > A.nk) return;
+    const FaultState &F = A.F;
+    double ks = F.Slip[k], kp = F.psi[k];
+    if (stage > 1) {
+        ks = ks + c_rk.a[stage][1] * dt * F.fV[1][k];
+        kp = kp + c_rk.a[stage][1] * dt * F.fdpsi[1][k];
+        for (int j = 2; j < stage; j++) {
+            ks = ks + c_rk.a[stage][j] * dt * F.fV[j][k];
+            kp = kp + c_rk.a[stage][j] * dt * F.fdpsi[j][k];
+        }
+        F.fV[stage][k] = 0.0;
+        F.fdpsi[stage][k] = 0.0;
+    }
+    F.kslip[stage][k] = ks;
+    F.kpsi[stage][k] = kp;
+    double *row = A.u0 + (long)(k - 1) * A.P;
+    row[0] = 0.5 * ks;
+    row[A.K - 1] = 0.50 * F.Vini * (t + ratio * dt) + F.SlipShift[k];
+}
+
+// stress -> Newton -> aging law for one stage (odeSolver.cpp:1498-1500)
+__global__ void k_fault_stage(FaultArgs A, int stage) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (k > A.nk) return;
+    const FaultState &F = A.F;
+    const double Ts = fault_stress(A.u0 + (long)(k - 1) * A.P, F.mu0[k], A.dh);
+    const double Tn = F.Tn0[k];
+    F.Ts[k] = Ts;
+    F.Tn[k] = Tn;
+    const double psi = F.kpsi[stage][k];
+    unsigned int flags = 0;
+    int it = 0;
+    const double V = newton_v(Ts, Tn, F.have_tau0 ? F.tau0[k] : 0.0, F.a[k], F.eta[k], psi, F.V0,
+                              F.fV[stage][k], &it, &flags);
+    F.fV[stage][k] = V;
+    F.fdpsi[stage][k] = aging(psi, F.b[k], V, F.f0, F.V0, F.L);
+    F.iters[k] += it;
+    report(A.status, flags, k);
+}
+
+__global__ void k_stress(FaultArgs A) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (k > A.nk) return;
+    A.F.Ts[k] = fault_stress(A.u0 + (long)(k - 1) * A.P, A.F.mu0[k], A.dh);
+    A.F.Tn[k] = A.F.Tn0[k];
+}
+
+__global__ void k_newton(FaultArgs A, const double *Ts, const double *psi, double *V, int *iters) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (k > A.nk) return;
+    const FaultState &F = A.F;
+    unsigned int flags = 0;
+    int it = 0;
+    V[k] = newton_v(Ts[k], F.Tn0[k], F.have_tau0 ? F.tau0[k] : 0.0, F.a[k], F.eta[k], psi[k], F.V0,
+                    V[k], &it, &flags);
+    iters[k] = it;
+    report(A.status, flags, k);
+}
+
+__global__ void k_dpsi(FaultArgs A, const double *psi, const double *V, double *dpsi) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (k > A.nk) return;
+    dpsi[k] = aging(psi[k], A.F.b[k], V[k], A.F.f0, A.F.V0, A.F.L);
+}
+
+// y3 / y4 (odeSolver.cpp:1569-1593) and computeError (:1211-1238); one block.
+__global__ void k_error(FaultArgs A, double dt, double *out) {
+    __shared__ double s1[1024], s2[1024];
+    const FaultState &F = A.F;
+    double e1 = 0.0, e2 = 0.0;
+    for (int k = threadIdx.x + 1; k <= A.nk; k += blockDim.x) {
+        double y3s = F.Slip[k] + c_rk.hb[1] * dt * F.fV[1][k];
+        double y4s = F.Slip[k] + c_rk.b[1] * dt * F.fV[1][k];
+        double y3p = F.psi[k] + c_rk.hb[1] * dt * F.fdpsi[1][k];
+        double y4p = F.psi[k] + c_rk.b[1] * dt * F.fdpsi[1][k];
+        for (int j = 3; j <= 6; j++) {
+            y3s = y3s + c_rk.hb[j] * dt * F.fV[j][k];
+            y3p = y3p + c_rk.hb[j] * dt * F.fdpsi[j][k];
+            y4s = y4s + c_rk.b[j] * dt * F.fV[j][k];
+            y4p = y4p + c_rk.b[j] * dt * F.fdpsi[j][k];
+        }
+        F.y3s[k] = y3s; F.y3p[k] = y3p; F.y4s[k] = y4s; F.y4p[k] = y4p;
+        const double t1 = y3s - y4s, t2 = y3p - y4p;
+        e1 += t1 * t1;
+        e2 += t2 * t2;
+    }
+    s1[threadIdx.x] = e1;
+    s2[threadIdx.x] = e2;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            s1[threadIdx.x] += s1[threadIdx.x + w];
+            s2[threadIdx.x] += s2[threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double sn = sqrt((double)A.nk);
+        *out = sqrt(s1[0]) / (sn * 1.0) + sqrt(s2[0]) / (sn * 1.0);
+    }
+}
+
+// accepted step: y <- y4, f1 zeroed (odeSolver.cpp:1606-1614)
+__global__ void k_commit(FaultArgs A) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (k > A.nk) return;
+    const FaultState &F = A.F;
+    F.Slip[k] = F.y4s[k];
+    F.psi[k] = F.y4p[k];
+    F.fV[1][k] = 0.0;
+    F.fdpsi[1][k] = 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// host wrappers
+// ---------------------------------------------------------------------------
+int fault_alloc(qd_solver *s) {
+    const size_t nz = s->nz;
+    FaultState &F = s->F;
+    double **vecs[] = {&F.mu0, &F.a, &F.b, &F.eta, &F.Tn0, &F.tau0, &F.SlipShift, &F.Slip, &F.psi,
+                       &F.Ts, &F.Tn, &F.y3s, &F.y3p, &F.y4s, &F.y4p};
+    for (double **p : vecs) {
+        if (cudaMalloc(p, nz * sizeof(double)) != cudaSuccess) return QD_ERR_NOMEM;
+        QD_CUDA(cudaMemset(*p, 0, nz * sizeof(double)));
+    }
+    for (int st = 1; st <= 6; st++) {
+        double **pp[] = {&F.kslip[st], &F.kpsi[st], &F.fV[st], &F.fdpsi[st]};
+        for (double **p : pp) {
+            if (cudaMalloc(p, nz * sizeof(double)) != cudaSuccess) return QD_ERR_NOMEM;
+            QD_CUDA(cudaMemset(*p, 0, nz * sizeof(double)));
+        }
+    }
+    if (cudaMalloc(&F.iters, nz * sizeof(int)) != cudaSuccess) return QD_ERR_NOMEM;
+    QD_CUDA(cudaMemset(F.iters, 0, nz * sizeof(int)));
+    return upload_tableau(s);
+}
+
+void fault_free(qd_solver *s) {
+    FaultState &F = s->F;
+    double *vecs[] = {F.mu0, F.a, F.b, F.eta, F.Tn0, F.tau0, F.SlipShift, F.Slip, F.psi,
+                      F.Ts, F.Tn, F.y3s, F.y3p, F.y4s, F.y4p};
+    for (double *p : vecs) cudaFree(p);
+    for (int st = 1; st <= 6; st++) {
+        cudaFree(F.kslip[st]); cudaFree(F.kpsi[st]); cudaFree(F.fV[st]); cudaFree(F.fdpsi[st]);
+    }
+    cudaFree(F.iters);
+    s->F = FaultState();
+}
+
+int launch_stage_boundary(qd_solver *s, int stage, double ratio, const double *, const double *) {
+    k_stage_boundary<<<nblk(s->nk, 128), 128, 0, s->stream>>>(fargs(s), stage, s->t, s->dt, ratio);
+    QD_LAUNCH_CHECK(s);
+    return QD_OK;
+}
+
+int launch_fault(qd_solver *s, int stage, int) {
+    k_fault_stage<<<nblk(s->nk, 128), 128, 0, s->stream>>>(fargs(s), stage);
+    QD_LAUNCH_CHECK(s);
+    return QD_OK;
+}
+
+int launch_error(qd_solver *s) {
+    k_error<<<1, 1024, 0, s->stream>>>(fargs(s), s->dt, s->d_scal + 2);
+    QD_LAUNCH_CHECK(s);
+    return QD_OK;
+}
+
+int launch_commit(qd_solver *s) {
+    k_commit<<<nblk(s->nk, 128), 128, 0, s->stream>>>(fargs(s));
+    QD_LAUNCH_CHECK(s);
+    return QD_OK;
+}
+
+int launch_stress(qd_solver *s) {
+    k_stress<<<nblk(s->nk, 128), 128, 0, s->stream>>>(fargs(s));
+    QD_LAUNCH_CHECK(s);
+    return QD_OK;
+}
+
+int launch_newton(qd_solver *s, const double *Ts, const double *psi, double *V, int *iters) {
+    k_newton<<<nblk(s->nk, 128), 128, 0, s->stream>>>(fargs(s), Ts, psi, V, iters);
+    QD_LAUNCH_CHECK(s);
+    return QD_OK;
+}
+
+int launch_dpsi(qd_solver *s, const double *psi, const double *V, double *dpsi) {
+    k_dpsi<<<nblk(s->nk, 128), 128, 0, s->stream>>>(fargs(s), psi, V, dpsi);
+    QD_LAUNCH_CHECK(s);
+    return QD_OK;
+}
+
+}  // namespace qd

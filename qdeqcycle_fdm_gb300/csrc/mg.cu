@@ -1,0 +1,520 @@
+// mg.cu -- geometric multigrid for  div(mu grad u) = f  on the fault-normal
+// plane, FP64 and FP32, on one GB300.
+//
+// What is solved is exactly the reference's discrete problem
+// (odeSolver.cpp:757-1147):
+//   * 5-point variable-coefficient operator, Dirichlet columns 0 and K-1,
+//     mirrored (Neumann) first and last rows;
+//   * level-0 face moduli from mu_equi's half-grid edges; coarse levels use
+//     the node modulus half-way between coarse nodes (fin_coa indexing,
+//     :823-827), and on coarse levels the mirrored rows take the inner face
+//     twice (:830-847) -- folded here into cz[0] = cz[1], cz[N] = cz[N-1];
+//   * red-black Gauss-Seidel with relaxation 1, red = (j+k) even first;
+//   * full-weighting restriction with mirrored rows (:953-1015) and bilinear
+//     prolongation that skips the last fine row (:1017-1043);
+//   * V-cycle recursion with smoothing only on the coarsest level.
+// The smoother multiplies by a precomputed 1/diag (the reference divides
+// 1/diag on the fly); red-black order makes each colour update independent
+// of thread order, so results are deterministic.
+#include <cstdarg>
+#include <cstring>
+#include <vector>
+
+#include "qdeq_internal.cuh"
+
+namespace qd {
+
+static constexpr int BX = 32, BY = 8;
+
+__host__ __device__ static inline int cdiv(int a, int b) { return (a + b - 1) / b; }
+
+template <typename T>
+struct View {
+    T *u;
+    const T *f;
+    T *r;
+    const T *cx, *cz, *dinv;
+    int N, K, P;
+    T h2, inv_h2;
+};
+
+template <typename T>
+static View<T> make_view(const qd_solver *s, const Level<T> *Ls, int l) {
+    View<T> v;
+    v.u = Ls[l].u; v.f = Ls[l].f; v.r = Ls[l].r;
+    v.cx = Ls[l].cx; v.cz = Ls[l].cz; v.dinv = Ls[l].dinv;
+    v.N = s->dims[l].N; v.K = s->dims[l].K; v.P = s->dims[l].P;
+    v.h2 = (T)s->dims[l].h2; v.inv_h2 = (T)s->dims[l].inv_h2;
+    return v;
+}
+
+// ---------------------------------------------------------------------------
+// reductions (deterministic: fixed block shape, fixed tree)
+// ---------------------------------------------------------------------------
+__device__ static double block_sum(double v) {
+    __shared__ double sh[32];
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int nthr = blockDim.x * blockDim.y;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((tid & 31) == 0) sh[tid >> 5] = v;
+    __syncthreads();
+    if (tid < 32) {
+        v = (tid < (nthr + 31) / 32) ? sh[tid] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    }
+    __syncthreads();
+    return v;  // valid in thread 0
+}
+
+__global__ void k_final_sum(const double *partial, int n, double *out) {
+    double v = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) v += partial[i];
+    v = block_sum(v);
+    if (threadIdx.x == 0) *out = v;
+}
+
+// ---------------------------------------------------------------------------
+// coefficient set-up from the reference's staggered mu_equi
+// ---------------------------------------------------------------------------
+__global__ void k_build_faces(const double *__restrict__ mu, long W, int level, int fc, int N,
+                              int K, int P, double *cx, double *cz) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (k >= K || j > N) return;
+    if (j < N && k < K - 1) {
+        long idx;
+        if (level == 0)
+            idx = ((k + 1) * 2 + 1) + (long)((j + 1) * 2) * W;            // index2, :787
+        else
+            idx = ((k * 2 + 1) * fc / 2 + 1) * 2 + (long)((j * fc + 1) * 2) * W;   // :825
+        cx[(long)j * P + k] = mu[idx];
+    }
+    long idz;
+    if (level == 0) {
+        idz = (k + 1) * 2 + (long)(2 * j + 1) * W;                        // index3 of row j, :788
+    } else {
+        const int jj = (j == 0) ? 1 : (j == N ? N - 1 : j);                // :830-847 quirk
+        idz = (k * fc + 1) * 2 + (long)(((jj * 2 - 1) * fc / 2 + 1) * 2) * W;      // :826
+    }
+    cz[(long)j * P + k] = mu[idz];
+}
+
+__global__ void k_build_dinv(int N, int K, int P, const double *cx, const double *cz,
+                             double *dinv, float *cx32, float *cz32, float *dinv32) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (k >= K || j > N) return;
+    const long c = (long)j * P + k;
+    cz32[c] = (float)cz[c];
+    if (j == N) return;
+    if (k < K - 1) cx32[c] = (float)cx[c];
+    if (k >= 1 && k <= K - 2) {
+        // relax_rbgs / (mu1 + mu2 + mu3 + mu4), same summation order (:794-795)
+        const double d = 1.00 / (((cx[c - 1] + cx[c]) + cz[c]) + cz[c + P]);
+        dinv[c] = d;
+        dinv32[c] = (float)d;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// smoother: one colour of red-black Gauss-Seidel, one thread per node of the
+// colour (the reference launches one thread per node and idles half).
+// ---------------------------------------------------------------------------
+template <typename T, bool HAS_F>
+__global__ void __launch_bounds__(BX * BY) k_rb(View<T> v, int color) {
+    const int kk = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (j >= v.N) return;
+    const int k = 2 * kk + 1 + ((j + 1 + color) & 1);
+    if (k > v.K - 2) return;
+    const long c = (long)j * v.P + k;
+    const long up = (j == 0) ? v.P : -(long)v.P;          // row j-1 (mirrored at j = 0)
+    const long dn = (j == v.N - 1) ? -(long)v.P : v.P;    // row j+1 (mirrored at j = N-1)
+    const T *u = v.u;
+    T acc = v.cx[c - 1] * u[c - 1] + v.cx[c] * u[c + 1] + v.cz[c] * u[c + up] +
+            v.cz[c + v.P] * u[c + dn];
+    if (HAS_F) acc -= v.h2 * v.f[c];
+    v.u[c] = v.dinv[c] * acc;
+}
+
+// residual r = f - A u on interior columns, optional sum of r^2 per block
+template <typename T, bool HAS_F, bool NORM>
+__global__ void __launch_bounds__(BX * BY) k_residual(View<T> v, T *r, double *partial) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    double sq = 0.0;
+    if (j < v.N && k >= 1 && k <= v.K - 2) {
+        const long c = (long)j * v.P + k;
+        const long up = (j == 0) ? v.P : -(long)v.P;
+        const long dn = (j == v.N - 1) ? -(long)v.P : v.P;
+        const T *u = v.u;
+        const T cW = v.cx[c - 1], cE = v.cx[c], cN = v.cz[c], cS = v.cz[c + v.P];
+        const T lap = cW * u[c - 1] + cE * u[c + 1] + cN * u[c + up] + cS * u[c + dn] -
+                      (((cW + cE) + cN) + cS) * u[c];
+        const T res = (HAS_F ? v.f[c] : (T)0) - lap * v.inv_h2;
+        r[c] = res;
+        sq = (double)res * (double)res;
+    }
+    if (NORM) {
+        sq = block_sum(sq);
+        if (threadIdx.x == 0 && threadIdx.y == 0) partial[blockIdx.y * gridDim.x + blockIdx.x] = sq;
+    }
+}
+
+// FP64 residual of the level-0 field, written as the FP32 right-hand side
+// of the correction equation, with its norm (mixed precision).
+__global__ void __launch_bounds__(BX * BY)
+    k_residual64_to32(View<double> v, float *f32, double *partial) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    double sq = 0.0;
+    if (j < v.N && k >= 1 && k <= v.K - 2) {
+        const long c = (long)j * v.P + k;
+        const long up = (j == 0) ? v.P : -(long)v.P;
+        const long dn = (j == v.N - 1) ? -(long)v.P : v.P;
+        const double *u = v.u;
+        const double cW = v.cx[c - 1], cE = v.cx[c], cN = v.cz[c], cS = v.cz[c + v.P];
+        const double lap = cW * u[c - 1] + cE * u[c + 1] + cN * u[c + up] + cS * u[c + dn] -
+                           (((cW + cE) + cN) + cS) * u[c];
+        const double res = (v.f ? v.f[c] : 0.0) - lap * v.inv_h2;
+        f32[c] = (float)res;
+        sq = res * res;
+    }
+    sq = block_sum(sq);
+    if (threadIdx.x == 0 && threadIdx.y == 0) partial[blockIdx.y * gridDim.x + blockIdx.x] = sq;
+}
+
+// u64 += e32 on the interior columns (mixed precision update)
+__global__ void k_correct(double *u, const float *e, int N, int K, int P) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (j >= N || k < 1 || k > K - 2) return;
+    const long c = (long)j * P + k;
+    u[c] += (double)e[c];
+}
+
+// residual norm^2 of the zero-interior guess: only the columns next to the
+// Dirichlet data see a non-zero residual (f = 0 on level 0)
+template <typename T>
+__global__ void k_r0(View<T> v, double *partial) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    double sq = 0.0;
+    if (j < v.N) {
+        const long row = (long)j * v.P;
+        const int K = v.K;
+        if (K - 2 == 1) {
+            const double r = -((double)v.cx[row] * v.u[row] + (double)v.cx[row + 1] * v.u[row + 2]) *
+                             (double)v.inv_h2;
+            sq = r * r;
+        } else if (K - 2 > 1) {
+            const double r1 = -(double)v.cx[row] * (double)v.u[row] * (double)v.inv_h2;
+            const double r2 = -(double)v.cx[row + K - 2] * (double)v.u[row + K - 1] * (double)v.inv_h2;
+            sq = r1 * r1 + r2 * r2;
+        }
+    }
+    sq = block_sum(sq);
+    if (threadIdx.x == 0) partial[blockIdx.x] = sq;
+}
+
+// full-weighting restriction of the fine residual into the coarse rhs, and
+// zero coarse initial guess (restriction_kernel, :953-1015)
+template <typename T>
+__global__ void k_restrict(const T *__restrict__ rf, int Pf, T *fc, T *uc, int Nc, int Kc, int Pc) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (j >= Nc || k < 1 || k > Kc - 2) return;
+    const int rn = (j == 0) ? 2 * j + 1 : 2 * j - 1;
+    const int rs = (j == Nc - 1) ? 2 * j - 1 : 2 * j + 1;
+    const T *c0 = rf + (long)(2 * j) * Pf + 2 * k;
+    const T *cn = rf + (long)rn * Pf + 2 * k;
+    const T *cs = rf + (long)rs * Pf + 2 * k;
+    const T val = (T)0.06250 * ((T)4.0 * c0[0] + (T)2.0 * c0[-1] + (T)2.0 * c0[1] + (T)2.0 * cn[0] +
+                                (T)2.0 * cs[0] + cn[-1] + cn[1] + cs[-1] + cs[1]);
+    const long c = (long)j * Pc + k;
+    fc[c] = val;
+    uc[c] = (T)0;
+}
+
+// bilinear prolongation u_fine += P e_coarse, one thread per fine node;
+// fine rows 0..Nf-2 and columns 1..Kf-2 (prolongate_kernel, :1017-1043)
+template <typename T>
+__global__ void k_prolong(T *uf, int Nf, int Kf, int Pf, const T *__restrict__ ec, int Pc) {
+    const int kf = blockIdx.x * blockDim.x + threadIdx.x;
+    const int jf = blockIdx.y * blockDim.y + threadIdx.y;
+    if (jf >= Nf - 1 || kf < 1 || kf > Kf - 2) return;
+    const int j = jf >> 1, k = kf >> 1;
+    const T *e = ec + (long)j * Pc + k;
+    T add;
+    if (!(jf & 1)) {
+        add = (kf & 1) ? (T)0.5 * (e[0] + e[1]) : e[0];
+    } else {
+        add = (kf & 1) ? (T)0.25 * (e[0] + e[1] + e[Pc] + e[Pc + 1]) : (T)0.5 * (e[0] + e[Pc]);
+    }
+    uf[(long)jf * Pf + kf] += add;
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+template <typename T>
+static T *dalloc(size_t n, int *rc) {
+    T *p = nullptr;
+    if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) {
+        *rc = QD_ERR_NOMEM;
+        return nullptr;
+    }
+    cudaMemset(p, 0, n * sizeof(T));
+    return p;
+}
+
+int mg_alloc(qd_solver *s, const double *mu_equi_host) {
+    const int nl = s->opt.n_levels;
+    if (nl < 1 || nl > QD_MAXLEV) {
+        set_error("n_levels %d out of range 1..%d", nl, QD_MAXLEV);
+        return QD_ERR_ARG;
+    }
+    int N = s->nk, K = s->ni;
+    double h = s->dh;
+    for (int l = 0; l < nl; l++) {
+        if (l > 0) {
+            if ((N - 1) % 2 || (K - 1) % 2) {
+                set_error("grid %dx%d not coarsenable to %d levels", s->nk, s->ni, nl);
+                return QD_ERR_ARG;
+            }
+            N = (N - 1) / 2 + 1;
+            K = (K - 1) / 2 + 1;
+            h *= 2;
+        }
+        if (N < 3 || K < 3) {
+            set_error("level %d has %dx%d nodes (< 3)", l, N, K);
+            return QD_ERR_ARG;
+        }
+        s->dims[l].N = N; s->dims[l].K = K; s->dims[l].P = cdiv(K, 32) * 32;
+        s->dims[l].h2 = h * h;
+        s->dims[l].inv_h2 = 1.0 / (h * h);
+    }
+    s->nlev = nl;
+    int rc = QD_OK;
+    for (int l = 0; l < nl; l++) {
+        const size_t n = (size_t)s->dims[l].N * s->dims[l].P;
+        const size_t nf = (size_t)(s->dims[l].N + 1) * s->dims[l].P;
+        s->L64[l].u = dalloc<double>(n, &rc);
+        s->L64[l].r = dalloc<double>(n, &rc);
+        s->L64[l].f = l > 0 ? dalloc<double>(n, &rc) : nullptr;
+        s->L64[l].cx = dalloc<double>(n, &rc);
+        s->L64[l].cz = dalloc<double>(nf, &rc);
+        s->L64[l].dinv = dalloc<double>(n, &rc);
+        s->L32[l].u = dalloc<float>(n, &rc);
+        s->L32[l].r = dalloc<float>(n, &rc);
+        s->L32[l].f = dalloc<float>(n, &rc);
+        s->L32[l].cx = dalloc<float>(n, &rc);
+        s->L32[l].cz = dalloc<float>(nf, &rc);
+        s->L32[l].dinv = dalloc<float>(n, &rc);
+        if (rc != QD_OK) {
+            set_error("device allocation failed on level %d", l);
+            return rc;
+        }
+    }
+    s->n_partial = cdiv(s->dims[0].K, BX) * cdiv(s->dims[0].N, BY) + 64;
+    s->d_partial = dalloc<double>(s->n_partial, &rc);
+    if (rc != QD_OK) return rc;
+
+    // coefficients from mu_equi
+    const size_t nmu = (size_t)(2 * s->nx - 1) * (2 * s->nz - 1);
+    double *d_mu = dalloc<double>(nmu, &rc);
+    if (rc != QD_OK) return rc;
+    QD_CUDA(cudaMemcpyAsync(d_mu, mu_equi_host, nmu * sizeof(double), cudaMemcpyHostToDevice,
+                            s->stream));
+    const long W = 2L * s->nx - 1;
+    for (int l = 0; l < nl; l++) {
+        const LevelDims &d = s->dims[l];
+        dim3 blk(BX, BY), grd(cdiv(d.K, BX), cdiv(d.N + 1, BY));
+        k_build_faces<<<grd, blk, 0, s->stream>>>(d_mu, W, l, 1 << l, d.N, d.K, d.P, s->L64[l].cx,
+                                                  s->L64[l].cz);
+        QD_LAUNCH_CHECK(s);
+        k_build_dinv<<<grd, blk, 0, s->stream>>>(d.N, d.K, d.P, s->L64[l].cx, s->L64[l].cz,
+                                                 s->L64[l].dinv, s->L32[l].cx, s->L32[l].cz,
+                                                 s->L32[l].dinv);
+        QD_LAUNCH_CHECK(s);
+    }
+    QD_CUDA(cudaStreamSynchronize(s->stream));
+    cudaFree(d_mu);
+    return QD_OK;
+}
+
+void mg_free(qd_solver *s) {
+    for (int l = 0; l < QD_MAXLEV; l++) {
+        cudaFree(s->L64[l].u); cudaFree(s->L64[l].r); cudaFree(s->L64[l].f);
+        cudaFree(s->L64[l].cx); cudaFree(s->L64[l].cz); cudaFree(s->L64[l].dinv);
+        cudaFree(s->L32[l].u); cudaFree(s->L32[l].r); cudaFree(s->L32[l].f);
+        cudaFree(s->L32[l].cx); cudaFree(s->L32[l].cz); cudaFree(s->L32[l].dinv);
+        s->L64[l] = Level<double>();
+        s->L32[l] = Level<float>();
+    }
+    cudaFree(s->d_partial);
+    s->d_partial = nullptr;
+}
+
+template <typename T>
+static int smooth_t(qd_solver *s, Level<T> *Ls, int l, int nsweeps) {
+    View<T> v = make_view(s, Ls, l);
+    dim3 blk(BX, BY), grd(cdiv((v.K - 1) / 2 + 1, BX), cdiv(v.N, BY));
+    for (int it = 0; it < nsweeps; it++) {
+        for (int color = 0; color < 2; color++) {
+            if (v.f)
+                k_rb<T, true><<<grd, blk, 0, s->stream>>>(v, color);
+            else
+                k_rb<T, false><<<grd, blk, 0, s->stream>>>(v, color);
+            QD_LAUNCH_CHECK(s);
+        }
+    }
+    return QD_OK;
+}
+
+template <typename T>
+static int residual_t(qd_solver *s, Level<T> *Ls, int l) {
+    View<T> v = make_view(s, Ls, l);
+    dim3 blk(BX, BY), grd(cdiv(v.K, BX), cdiv(v.N, BY));
+    if (v.f)
+        k_residual<T, true, false><<<grd, blk, 0, s->stream>>>(v, v.r, nullptr);
+    else
+        k_residual<T, false, false><<<grd, blk, 0, s->stream>>>(v, v.r, nullptr);
+    QD_LAUNCH_CHECK(s);
+    return QD_OK;
+}
+
+template <typename T>
+static int restrict_t(qd_solver *s, Level<T> *Ls, int lc) {
+    const LevelDims &f = s->dims[lc - 1], &c = s->dims[lc];
+    dim3 blk(BX, BY), grd(cdiv(c.K, BX), cdiv(c.N, BY));
+    k_restrict<T><<<grd, blk, 0, s->stream>>>(Ls[lc - 1].r, f.P, Ls[lc].f, Ls[lc].u, c.N, c.K, c.P);
+    QD_LAUNCH_CHECK(s);
+    return QD_OK;
+}
+
+template <typename T>
+static int prolong_t(qd_solver *s, Level<T> *Ls, int lc) {
+    const LevelDims &f = s->dims[lc - 1], &c = s->dims[lc];
+    dim3 blk(BX, BY), grd(cdiv(f.K, BX), cdiv(f.N, BY));
+    k_prolong<T><<<grd, blk, 0, s->stream>>>(Ls[lc - 1].u, f.N, f.K, f.P, Ls[lc].u, c.P);
+    QD_LAUNCH_CHECK(s);
+    return QD_OK;
+}
+
+template <typename T>
+static int vcycle_t(qd_solver *s, Level<T> *Ls, int l) {
+    if (l >= s->nlev - 1) return smooth_t(s, Ls, l, s->opt.nu_coarse);
+    QD_TRY(smooth_t(s, Ls, l, s->opt.nu_pre));
+    QD_TRY(residual_t(s, Ls, l));
+    QD_TRY(restrict_t(s, Ls, l + 1));
+    QD_TRY(vcycle_t(s, Ls, l + 1));
+    QD_TRY(prolong_t(s, Ls, l + 1));
+    return smooth_t(s, Ls, l, s->opt.nu_post);
+}
+
+// ||r||^2 of level 0 into d_scal[slot]; for mixed precision also writes the
+// FP32 correction right-hand side.
+static int level0_norm(qd_solver *s, int to32, int slot) {
+    View<double> v = make_view(s, s->L64, 0);
+    dim3 blk(BX, BY), grd(cdiv(v.K, BX), cdiv(v.N, BY));
+    const int nb = grd.x * grd.y;
+    if (to32)
+        k_residual64_to32<<<grd, blk, 0, s->stream>>>(v, s->L32[0].f, s->d_partial);
+    else
+        k_residual<double, false, true><<<grd, blk, 0, s->stream>>>(v, v.r, s->d_partial);
+    QD_LAUNCH_CHECK(s);
+    k_final_sum<<<1, 1024, 0, s->stream>>>(s->d_partial, nb, s->d_scal + slot);
+    QD_LAUNCH_CHECK(s);
+    return QD_OK;
+}
+
+static int r0_norm(qd_solver *s, int slot) {
+    View<double> v = make_view(s, s->L64, 0);
+    const int nb = cdiv(v.N, 256);
+    k_r0<double><<<nb, 256, 0, s->stream>>>(v, s->d_partial);
+    QD_LAUNCH_CHECK(s);
+    k_final_sum<<<1, 1024, 0, s->stream>>>(s->d_partial, nb, s->d_scal + slot);
+    QD_LAUNCH_CHECK(s);
+    return QD_OK;
+}
+
+static int read_scalars(qd_solver *s, int n) {
+    QD_CUDA(cudaMemcpyAsync(s->h_scal, s->d_scal, n * sizeof(double), cudaMemcpyDeviceToHost,
+                            s->stream));
+    QD_CUDA(cudaStreamSynchronize(s->stream));
+    return QD_OK;
+}
+
+// multigrid() (odeSolver.cpp:652-720) on the device-resident u.
+int mg_solve(qd_solver *s, int *cycles, double *rnorm, double *r0norm) {
+    const int mixed = s->opt.precision == QD_PREC_MIXED;
+    const int rel = s->opt.tol_mode == QD_TOL_REL;
+    if (rel) QD_TRY(r0_norm(s, 1));
+    QD_TRY(level0_norm(s, mixed, 0));
+    QD_TRY(read_scalars(s, 2));
+    double r0 = rel ? sqrt(s->h_scal[1]) : 0.0;
+    double thr = rel ? (r0 > 0.0 ? s->opt.tol * r0 : s->opt.tol) : s->opt.tol;
+    double delta = sqrt(s->h_scal[0]);
+    int it = 0;
+    int rc = QD_OK;
+    const LevelDims &d0 = s->dims[0];
+    while (!(delta <= thr)) {
+        if (isnan(delta) || isinf(delta)) {
+            rc = QD_ERR_NOT_CONVERGED;
+            set_error("multigrid: residual norm is %f after %d cycles", delta, it);
+            break;
+        }
+        if (s->opt.max_cycles > 0 && it >= s->opt.max_cycles) {
+            rc = QD_ERR_NOT_CONVERGED;
+            set_error("multigrid: %d cycles, ||r|| = %.3e > %.3e", it, delta, thr);
+            break;
+        }
+        if (mixed) {
+            QD_CUDA(cudaMemsetAsync(s->L32[0].u, 0, sizeof(float) * d0.N * d0.P, s->stream));
+            QD_TRY(vcycle_t<float>(s, s->L32, 0));
+            dim3 blk(BX, BY), grd(cdiv(d0.K, BX), cdiv(d0.N, BY));
+            k_correct<<<grd, blk, 0, s->stream>>>(s->L64[0].u, s->L32[0].u, d0.N, d0.K, d0.P);
+            QD_LAUNCH_CHECK(s);
+        } else {
+            QD_TRY(vcycle_t<double>(s, s->L64, 0));
+        }
+        QD_TRY(level0_norm(s, mixed, 0));
+        QD_TRY(read_scalars(s, 1));
+        delta = sqrt(s->h_scal[0]);
+        it++;
+    }
+    s->solves++;
+    s->vcycles += it;
+    if (cycles) *cycles = it;
+    if (rnorm) *rnorm = delta;
+    if (r0norm) *r0norm = r0;
+    return rc;
+}
+
+// nsweeps red+black sweeps of the level-`level` field of the hierarchy the
+// solver's precision runs its cycles in (FP64 u, or the FP32 correction)
+int mg_smooth(qd_solver *s, int level, int nsweeps) {
+    if (s->opt.precision == QD_PREC_MIXED)
+        QD_TRY(smooth_t<float>(s, s->L32, level, nsweeps));
+    else
+        QD_TRY(smooth_t<double>(s, s->L64, level, nsweeps));
+    QD_CUDA(cudaStreamSynchronize(s->stream));
+    return QD_OK;
+}
+
+int mg_vcycle(qd_solver *s) {
+    QD_TRY(vcycle_t<double>(s, s->L64, 0));
+    QD_CUDA(cudaStreamSynchronize(s->stream));
+    return QD_OK;
+}
+
+int mg_residual_norm(qd_solver *s, double *rnorm) {
+    QD_TRY(level0_norm(s, 0, 0));
+    QD_TRY(read_scalars(s, 1));
+    *rnorm = sqrt(s->h_scal[0]);
+    return QD_OK;
+}
+
+}  // namespace qd

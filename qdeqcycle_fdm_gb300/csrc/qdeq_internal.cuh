@@ -1,0 +1,137 @@
+// qdeq_internal.cuh -- shared definitions of the GB300 hot-path library.
+//
+// Device data layout (one solver, one GPU):
+//   level l of the multigrid hierarchy holds N x K nodes (N rows along the
+//   fault = depth, K columns off-fault), row-major with a row pitch P that
+//   is a multiple of 32 elements, so every row starts on a 256-byte
+//   boundary.  Face moduli are repacked from the reference's staggered
+//   mu_equi into three dense arrays per level:
+//     cx[j*P + k]   face between (j,k) and (j,k+1),   k = 0..K-2
+//     cz[j*P + k]   face between (j-1,k) and (j,k),   j = 0..N (N+1 rows)
+//     dinv[j*P + k] 1 / (cx[k-1] + cx[k] + cz[j] + cz[j+1])
+//   The reference's row quirks are folded into cz (see mg.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include "../../include/qdeq.h"
+
+#define QD_MAXLEV 16
+
+namespace qd {
+
+void set_error(const char *fmt, ...);
+
+#define QD_CUDA(call)                                                              \
+    do {                                                                           \
+        cudaError_t e__ = (call);                                                  \
+        if (e__ != cudaSuccess) {                                                  \
+            ::qd::set_error("%s:%d: %s: %s", __FILE__, __LINE__, #call,            \
+                            cudaGetErrorString(e__));                              \
+            return QD_ERR_CUDA;                                                    \
+        }                                                                          \
+    } while (0)
+
+#define QD_LAUNCH_CHECK(s)                                                         \
+    do {                                                                           \
+        (s)->launches++;                                                           \
+        cudaError_t e__ = cudaPeekAtLastError();                                   \
+        if (e__ != cudaSuccess) {                                                  \
+            ::qd::set_error("%s:%d: launch: %s", __FILE__, __LINE__,               \
+                            cudaGetErrorString(e__));                              \
+            return QD_ERR_CUDA;                                                    \
+        }                                                                          \
+    } while (0)
+
+#define QD_TRY(expr)                                                               \
+    do {                                                                           \
+        int rc__ = (expr);                                                         \
+        if (rc__ != QD_OK) return rc__;                                            \
+    } while (0)
+
+template <typename T>
+struct Level {
+    T *u = nullptr;      // level 0: the solution u; coarse: the error e
+    T *f = nullptr;      // right-hand side (nullptr: identically zero)
+    T *r = nullptr;      // residual scratch
+    T *cx = nullptr, *cz = nullptr, *dinv = nullptr;
+};
+
+struct LevelDims {
+    int N, K, P;
+    double h2, inv_h2;
+};
+
+// Device-side fault / RK43 state (nz-long vectors, entries 1..nk used).
+struct FaultState {
+    double *mu0 = nullptr;  // node modulus at the fault column (fault.cpp:153)
+    double *a = nullptr, *b = nullptr, *eta = nullptr, *Tn0 = nullptr;
+    double *tau0 = nullptr, *SlipShift = nullptr;
+    double *Slip = nullptr, *psi = nullptr, *Ts = nullptr, *Tn = nullptr;
+    double *kslip[7] = {}, *kpsi[7] = {}, *fV[7] = {}, *fdpsi[7] = {};
+    double *y3s = nullptr, *y3p = nullptr, *y4s = nullptr, *y4p = nullptr;
+    int *iters = nullptr;
+    double f0 = 0, V0 = 0, L = 0, Vini = 0;
+    int have_tau0 = 0;
+};
+
+// Status word written by device kernels (bit flags + first bad node).
+struct DevStatus {
+    unsigned int flags;
+    int bad_node;
+};
+enum : unsigned int { ST_NEWTON_NAN = 1u, ST_NEWTON_CAP = 2u, ST_NEWTON_BRACKET = 4u };
+
+}  // namespace qd
+
+struct qd_solver {
+    int ni, nk, nx, nz;
+    double dh;
+    qd_mg_options opt;
+    int nlev;
+    qd::LevelDims dims[QD_MAXLEV];
+    qd::Level<double> L64[QD_MAXLEV];
+    qd::Level<float> L32[QD_MAXLEV];
+    cudaStream_t stream;
+    double *d_partial;     // per-block reduction partials
+    int n_partial;
+    double *d_scal;        // device scalars: [0] ||r||^2, [1] ||r0||^2, [2] totErr
+    double *h_scal;        // pinned mirror
+    qd::DevStatus *d_status;
+    qd::DevStatus *h_status;
+    qd::FaultState F;
+    int fault_ready;
+    // RK43 state (PARAMS)
+    qd_rk43_params P;
+    double t, dt, errA[2];
+    int it;
+    int started;
+    // counters
+    long long solves, vcycles, attempts, steps, newton_iters, launches;
+};
+
+namespace qd {
+// mg.cu
+int mg_alloc(qd_solver *s, const double *mu_equi_host);
+void mg_free(qd_solver *s);
+int mg_solve(qd_solver *s, int *cycles, double *rnorm, double *r0norm);
+int mg_smooth(qd_solver *s, int level, int nsweeps);
+int mg_vcycle(qd_solver *s);
+int mg_residual_norm(qd_solver *s, double *rnorm);
+// fault.cu
+int fault_alloc(qd_solver *s);
+void fault_free(qd_solver *s);
+int launch_stage_boundary(qd_solver *s, int stage, double ratio, const double *slip_dev,
+                          const double *psi_dev);
+int launch_fault(qd_solver *s, int stage, int compute_stress_only);
+int launch_error(qd_solver *s);
+int launch_commit(qd_solver *s);
+int launch_stress(qd_solver *s);
+int launch_newton(qd_solver *s, const double *Ts, const double *psi, double *V, int *iters);
+int launch_dpsi(qd_solver *s, const double *psi, const double *V, double *dpsi);
+void rk_tableau(double c[7], double b[7], double hb[7], double a[7][7]);
+// medium.cu
+int set_medium_gpu(int ni, int nk, const double *mu_node, double *mu_equi);
+}  // namespace qd

@@ -1,0 +1,206 @@
+"""GB300 kernels against the CPU oracle, through the C ABI.
+
+Tolerances (FP64):
+  * single smoother / V-cycle steps: 1e-12 relative to max|u| (the GPU uses
+    fused multiply-adds and a precomputed 1/diag; the oracle rounds every
+    operation as the reference's source reads);
+  * converged solves, stress, slip rate: 1e-10 relative;
+  * after 100 accepted RK43 steps: u, tau, V to 1e-10 and slip, psi to 1e-8
+    relative (the spec parity bar).
+"""
+import numpy as np
+import pytest
+
+import oracle
+from qdeqcycle_fdm_gb300 import api, config, problem
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def oracle_medium(ni, nk, mu):
+    return oracle.set_medium(ni, nk, mu)[1]
+
+
+def make_problem(n=65, **kw):
+    cfg = config.small(n, **kw)
+    return cfg, problem.build_problem(cfg, homogenize=oracle_medium)
+
+
+def random_U(prob, seed=0):
+    rng = np.random.default_rng(seed)
+    U = np.zeros((prob.nz, prob.nx))
+    U[1:-1, 1:-1] = rng.normal(size=(prob.nk, prob.ni)) * 1e-3
+    U[1:-1, 1] = rng.normal(size=prob.nk)          # fault column data
+    U[1:-1, prob.ni] = rng.normal(size=prob.nk)    # remote column data
+    return U
+
+
+def compact(U):
+    return np.ascontiguousarray(U[1:-1, 1:-1])
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _libs(gpu_lib, oracle_lib):
+    return gpu_lib
+
+
+def test_set_medium_gpu_matches_oracle():
+    cfg = config.small(65, mu_profile="layered", layer_depth_km=10.0)
+    nx, nz = cfg.ni + 2, cfg.nk + 2
+    mu_rows = problem.mu_profile(cfg, problem.depth_of_rows(cfg.nk, cfg.dh))
+    mu = np.ascontiguousarray(np.repeat(mu_rows[:, None], nx, axis=1))
+    want = oracle_medium(cfg.ni, cfg.nk, mu)
+    got = api.set_medium(cfg.ni, cfg.nk, mu)
+    assert rel(got, want) < 1e-13
+
+
+@pytest.mark.parametrize("n", [33, 65])
+def test_smoother_matches_oracle(n):
+    cfg, prob = make_problem(n, mu_profile="layered", layer_depth_km=15.0)
+    U = random_U(prob, 1)
+    s = api.Solver(prob.ni, prob.nk, prob.dh, prob.mu_equi, prob.mu_node, cfg.mg)
+    s.upload_u(U)
+    s.smooth(3)
+    got = compact(s.download_u())
+    mg = oracle.Multigrid(prob.ni, prob.nk, prob.dh, prob.mu_equi, cfg.mg.n_levels)
+    u = compact(U).copy()
+    f = np.zeros_like(u)
+    for _ in range(3):
+        mg.rbgs(u, f, 0, 0)
+        mg.rbgs(u, f, 0, 1)
+    assert rel(got, u) < 1e-12
+
+
+@pytest.mark.parametrize("levels", [2, 4, 6])
+def test_vcycle_matches_oracle(levels):
+    cfg, prob = make_problem(129, mu_profile="layered", layer_depth_km=20.0)
+    mg_cfg = config.MGConfig(n_levels=levels, nu_pre=2, nu_post=3, nu_coarse=7)
+    U = random_U(prob, 2)
+    s = api.Solver(prob.ni, prob.nk, prob.dh, prob.mu_equi, prob.mu_node, mg_cfg)
+    s.upload_u(U)
+    s.vcycle()
+    s.vcycle()
+    got = compact(s.download_u())
+    mg = oracle.Multigrid(prob.ni, prob.nk, prob.dh, prob.mu_equi, levels, 2, 3, 7)
+    u = compact(U).copy()
+    f = np.zeros_like(u)
+    mg.vcycle(u, f)
+    mg.vcycle(u, f)
+    assert rel(got, u) < 1e-12
+    r = np.zeros_like(u)
+    mg.residual(r, u, f, 0)
+    assert rel(s.residual_norm(), mg.norm2(r)) < 1e-9
+
+
+def test_reference_schedule_solve_matches_oracle():
+    """The reference's own schedule: 6 levels, V(32,32), absolute 1e-9."""
+    cfg, prob = make_problem(129, mu_profile="layered", layer_depth_km=20.0)
+    ref = config.reference_mg()
+    ref.max_cycles = 1000
+    U = random_U(prob, 3)
+    s = api.Solver(prob.ni, prob.nk, prob.dh, prob.mu_equi, prob.mu_node, ref)
+    Ug = U.copy()
+    cyc, rn = s.ode_solve_host(Ug)
+    mg = oracle.Multigrid(prob.ni, prob.nk, prob.dh, prob.mu_equi, 6, 32, 32, 32)
+    u = compact(U).copy()
+    ocyc, orn, _ = mg.solve(u, tol_mode=0, tol=1e-9, max_cycles=1000)
+    assert cyc == ocyc
+    assert rn <= 1e-9 and orn <= 1e-9
+    Uo = U.copy()
+    Uo[1:-1, 1:-1] = u
+    oracle.extend_crew(prob.ni, prob.nk, Uo)
+    assert rel(Ug, Uo) < 1e-10
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_relative_tolerance_solve(precision):
+    cfg, prob = make_problem(257, mu_profile="layered", layer_depth_km=8.0)
+    mg_cfg = config.MGConfig(n_levels=6, nu_pre=2, nu_post=2, nu_coarse=32, tol_mode=1, tol=1e-10,
+                             max_cycles=100, precision=precision)
+    U = random_U(prob, 4)
+    s = api.Solver(prob.ni, prob.nk, prob.dh, prob.mu_equi, prob.mu_node, mg_cfg)
+    s.upload_u(U)
+    cyc, rn, r0 = s.ode_solve()
+    assert rn <= 1e-10 * r0
+    got = compact(s.download_u())
+    mg = oracle.Multigrid(prob.ni, prob.nk, prob.dh, prob.mu_equi, 6, 2, 2, 32)
+    u = compact(U).copy()
+    ocyc, orn, or0 = mg.solve(u, tol_mode=1, tol=1e-10, max_cycles=100)
+    assert rel(r0, or0) < 1e-12
+    if precision == 0:
+        assert cyc == ocyc
+    # both are within the tolerance of the exact discrete solution
+    assert rel(got, u) < 1e-8
+
+
+def test_fault_functions_match_oracle():
+    cfg, prob = make_problem(65)
+    s = api.Solver(prob.ni, prob.nk, prob.dh, prob.mu_equi, prob.mu_node, cfg.mg)
+    s.fault_setup(prob)
+    U = random_U(prob, 5) * 1e-2
+    s.upload_u(U)
+    Ts, Tn = s.eval_stress_on_fault()
+    oTs, oTn = oracle.eval_stress_on_fault(prob.ni, prob.nk, prob.dh, U, prob.mu_node, prob.Tau_n0)
+    k = slice(1, prob.nk + 1)
+    assert rel(Ts[k], oTs[k]) < 1e-13
+    assert np.array_equal(Tn[k], oTn[k])
+    seed = np.zeros(prob.nz)
+    V, it, rc = s.nrsearch(Ts, prob.psi, seed)
+    assert rc == 0
+    oV, oit, st = oracle.nrsearch(prob.nk, oTs, oTn, prob.a, prob.eta, prob.psi, prob.V0, seed,
+                                  tau0=prob.tau0)
+    assert st == 0
+    assert np.max(np.abs(V[k] - oV[k]) / oV[k]) < 1e-10
+    assert np.array_equal(it[k], oit[k])      # same iterate path from the reference's seed
+    d = s.cal_dpsi(prob.psi, V)
+    od = oracle.cal_dpsi(prob.nk, prob.psi, prob.b, oV, prob.f0, prob.V0, prob.L)
+    assert rel(d[k], od[k]) < 1e-9
+
+
+def test_newton_safeguard_recovers_where_reference_overflows():
+    """fb/fa = 1200: the reference's first step overflows sinh (NaN, exit(0));
+    the bracketed Newton returns the root."""
+    cfg, prob = make_problem(33)
+    p = prob
+    p.a[:] = 0.005
+    p.Tau_n0[:] = -10.0
+    p.eta[:] = 4.0
+    s = api.Solver(p.ni, p.nk, p.dh, p.mu_equi, p.mu_node, cfg.mg)
+    s.fault_setup(p, with_tau0=False)
+    Ts = np.full(p.nz, 60.0)
+    psi = np.full(p.nz, 0.7)
+    V, it, rc = s.nrsearch(Ts, psi, np.zeros(p.nz))
+    assert rc == 0
+    k = slice(1, p.nk + 1)
+    x = np.arcsinh(V[k] / (2 * p.V0) * np.exp(psi[k] / p.a[k]))
+    g = p.eta[k] * V[k] + p.a[k] * 10.0 * x - Ts[k]
+    assert np.all(np.isfinite(V[k])) and np.max(np.abs(g)) < 1e-9 * 60.0
+
+
+def test_rk43_100_steps_match_oracle():
+    cfg, prob = make_problem(33)
+    mg = cfg.mg
+    gpu = api.Simulation(prob, mg)
+    cpu = oracle.Simulation(prob, mg.n_levels, mg.nu_pre, mg.nu_post, mg.nu_coarse, mg.tol_mode,
+                            mg.tol, mg.max_cycles)
+    gpu.start()
+    cpu.start()
+    for _ in range(100):
+        gpu.step()
+        cpu.step()
+    g = gpu.state()
+    c = cpu.state()
+    k = slice(1, prob.nk + 1)
+    assert g["it"] == c["it"] == 100
+    assert rel(g["t"], c["t"]) < 1e-8
+    assert rel(g["Slip"][k], c["Slip"][k]) < 1e-8
+    assert rel(g["psi"][k], c["psi"][k]) < 1e-8
+    assert np.max(np.abs(g["V"][k] - c["V"][k]) / c["V"][k]) < 1e-10
+    assert rel(g["Ts"][k], c["Ts"][k]) < 1e-10
+    assert rel(g["U"], c["U"]) < 1e-10
