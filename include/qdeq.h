@@ -64,6 +64,11 @@ typedef struct qd_mg_options {
     int max_cycles;   /* V-cycles per solve before QD_ERR_NOT_CONVERGED
                          (<= 0: no cap, as the reference)                    */
     int precision;    /* QD_PREC_FP64 or QD_PREC_MIXED                       */
+    int surface_prolong; /* 0: as prolongate_kernel (odeSolver.cpp:1034), the
+                         last row (the free surface) gets no coarse-grid
+                         correction; 1: it gets the coincident coarse row's
+                         correction too (same discrete solution, about 5x
+                         fewer V(2,2) cycles)                                */
 } qd_mg_options;
 
 /* Time-stepping parameters (PARAMS, struct.h:12-38; SetParams.cpp:14-21). */

@@ -230,7 +230,9 @@ void qo_restriction(const qo_mg *m, double *r2, const double *r, double *e2, int
 
 /* prolongate_kernel, odeSolver.cpp:1017-1043.  `level` is the coarse level.
  * Coarse rows 0..Nc-2 and columns 0..Kc-2 only, so the last fine row never
- * receives a correction (:1034). */
+ * receives a correction (:1034).  With m->surface_prolong the last coarse row
+ * also corrects its coincident fine row (the project's option; not in the
+ * reference). */
 void qo_prolongate(const qo_mg *m, double *u, const double *e2, int level) {
     const int Nc = m->N[level], Kc = m->K[level], Kf = m->K[level - 1];
 #define UF(jj, kk) u[(long)(jj) * Kf + (kk)]
@@ -242,6 +244,13 @@ void qo_prolongate(const qo_mg *m, double *u, const double *e2, int level) {
             UF(2 * j, 2 * k + 1) += 0.5 * (EC(j, k) + EC(j, k + 1));
             UF(2 * j + 1, 2 * k) += 0.5 * (EC(j, k) + EC(j + 1, k));
             UF(2 * j + 1, 2 * k + 1) += 0.25 * (EC(j, k) + EC(j, k + 1) + EC(j + 1, k) + EC(j + 1, k + 1));
+        }
+    }
+    if (m->surface_prolong) {
+        const int j = Nc - 1;
+        for (int k = 0; k < Kc - 1; k++) {
+            UF(2 * j, 2 * k) += EC(j, k);
+            UF(2 * j, 2 * k + 1) += 0.5 * (EC(j, k) + EC(j, k + 1));
         }
     }
 #undef UF
@@ -788,6 +797,8 @@ void qo_sim_set_params(qo_sim *s, double tmax, double ini_dt, double mindt,
     s->tmax = tmax; s->ini_dt = ini_dt; s->mindt = mindt; s->maxdt = maxdt;
     s->totTol = totTol; s->maxNumSteps = maxNumSteps;
 }
+
+void qo_sim_set_surface_prolong(qo_sim *s, int v) { s->mg.surface_prolong = v; }
 
 void qo_sim_set_U(qo_sim *s, const double *U) {
     memcpy(s->U, U, (size_t)s->nx * s->nz * sizeof(double));

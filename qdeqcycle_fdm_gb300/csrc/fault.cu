@@ -76,13 +76,22 @@ __device__ __forceinline__ double fault_stress(const double *urow, double mu, do
     return mu * du * 1.0e3;
 }
 
+// log(sinh(y)) for y > 0 without overflow
+__device__ __forceinline__ double log_sinh(double y) {
+    return y > 20.0 ? y - 0.69314718055994531 + log1p(-exp(-2.0 * y)) : log(sinh(y));
+}
+
 // NRsearch (fault.cpp:180-228) for one node, safeguarded.  Unknown
 // x = asinh(V e^{psi/a} / 2V0); residual g(x) = A sinh x + fa x - fb with
 // A = 2 eta V0 e^{-psi/a} > 0, fa = a |sigma_n| > 0, so g is increasing and
-// the root lies between 0 and fb/fa.  The iteration is the reference's
-// Newton step and stopping rule; a step that leaves the bracket (or a NaN)
-// is replaced by bisection.  From the reference's seed (x = 0) Newton never
-// leaves the bracket, so the iterates are the reference's.
+// the root lies in the bracket between 0 and fb/fa.
+// Phase 1 is the reference's Newton step and stopping rule; from the
+// reference's seed (x = 0) its iterates never leave the bracket, so they are
+// the reference's.  If a step leaves the bracket or overflows (the reference
+// then produces NaN and exits), phase 2 takes over: Newton on
+// G(y) = ln(A sinh y) - ln(|fb| - fa y), y = |x|, which is nearly linear
+// where sinh is exponential, with bisection whenever a step leaves the
+// shrinking bracket.
 __device__ double newton_v(double Ts, double Tn, double tau0, double a, double eta, double psi,
                            double V0, double Vseed, int *iters, unsigned int *flags) {
     double x = asinh(0.5 * Vseed / V0 * exp(psi / a));
@@ -94,23 +103,48 @@ __device__ double newton_v(double Ts, double Tn, double tau0, double a, double e
     if (!(x >= lo && x <= hi)) x = 0.5 * (lo + hi);
     const int itmax = 200;
     int it = 0;
-    bool done = false;
+    bool done = false, phase2 = false;
     while (it < itmax) {
-        const double sh = sinh(x);
-        const double fy = A * sh + fa * x - fb;
+        const double fy = A * sinh(x) + fa * x - fb;
         const double df = A * cosh(x) + fa;
-        double d = -fy / (df + 1e-100);
-        double xn = x + d;
-        if (fy > 0.0) hi = fmin(hi, x); else lo = fmax(lo, x);
-        if (!(xn >= lo && xn <= hi)) {
-            xn = 0.5 * (lo + hi);
-            d = xn - x;
+        const double d = -fy / (df + 1e-100);
+        const double xn = x + d;
+        if (!isnan(fy)) {
+            if (fy > 0.0) hi = fmin(hi, x); else lo = fmax(lo, x);
+        }
+        if (!(xn >= lo && xn <= hi) || isinf(fy) || isnan(fy)) {
+            phase2 = true;
             *flags |= ST_NEWTON_BRACKET;
+            break;
         }
         const double err = fabs(d) / (fabs(x) + 1e-100);
         it++;
         x = xn;
         if (err < 1e-10) { done = true; break; }
+    }
+    if (phase2) {
+        const double sg = fb >= 0.0 ? 1.0 : -1.0, afb = fabs(fb);
+        double ylo = sg > 0.0 ? lo : -hi, yhi = sg > 0.0 ? hi : -lo;
+        double y = fmin(fmax(sg * x, ylo), yhi);
+        const double lnA = log(A);
+        while (it < itmax) {
+            double yn;
+            const double rem = afb - fa * y;
+            if (y > 0.0 && rem > 0.0) {
+                const double G = lnA + log_sinh(y) - log(rem);
+                const double dG = 1.0 / tanh(y) + fa / rem;
+                if (G > 0.0) yhi = fmin(yhi, y); else ylo = fmax(ylo, y);
+                yn = y - G / dG;
+            } else {
+                yn = -1.0;   // outside the domain: bisect
+            }
+            if (!(yn > ylo && yn < yhi)) yn = 0.5 * (ylo + yhi);
+            const double err = fabs(yn - y) / (fabs(y) + 1e-100);
+            it++;
+            y = yn;
+            if (err < 1e-10) { done = true; break; }
+        }
+        x = sg * y;
     }
     if (!done) *flags |= ST_NEWTON_CAP;
     *iters = it;

@@ -238,12 +238,14 @@ __global__ void k_restrict(const T *__restrict__ rf, int Pf, T *fc, T *uc, int N
 }
 
 // bilinear prolongation u_fine += P e_coarse, one thread per fine node;
-// fine rows 0..Nf-2 and columns 1..Kf-2 (prolongate_kernel, :1017-1043)
+// fine rows 0..Nf-2 (0..Nf-1 with surface_prolong) and columns 1..Kf-2
+// (prolongate_kernel, :1017-1043)
 template <typename T>
-__global__ void k_prolong(T *uf, int Nf, int Kf, int Pf, const T *__restrict__ ec, int Pc) {
+__global__ void k_prolong(T *uf, int Nf, int Kf, int Pf, const T *__restrict__ ec, int Pc,
+                          int surface) {
     const int kf = blockIdx.x * blockDim.x + threadIdx.x;
     const int jf = blockIdx.y * blockDim.y + threadIdx.y;
-    if (jf >= Nf - 1 || kf < 1 || kf > Kf - 2) return;
+    if (jf >= Nf - 1 + surface || kf < 1 || kf > Kf - 2) return;
     const int j = jf >> 1, k = kf >> 1;
     const T *e = ec + (long)j * Pc + k;
     T add;
@@ -398,7 +400,8 @@ template <typename T>
 static int prolong_t(qd_solver *s, Level<T> *Ls, int lc) {
     const LevelDims &f = s->dims[lc - 1], &c = s->dims[lc];
     dim3 blk(BX, BY), grd(cdiv(f.K, BX), cdiv(f.N, BY));
-    k_prolong<T><<<grd, blk, 0, s->stream>>>(Ls[lc - 1].u, f.N, f.K, f.P, Ls[lc].u, c.P);
+    k_prolong<T><<<grd, blk, 0, s->stream>>>(Ls[lc - 1].u, f.N, f.K, f.P, Ls[lc].u, c.P,
+                                             s->opt.surface_prolong);
     QD_LAUNCH_CHECK(s);
     return QD_OK;
 }
