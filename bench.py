@@ -41,8 +41,8 @@ METRIC = "simulated yr/hr at 1025² (learned+mixed vs plain FP64 MG, 1e-9 rel re
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=40)
-    p.add_argument("--warmup", type=int, default=20)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=10)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--config", default="config1")
     p.add_argument("--cpu-sample-s", type=float, default=20.0)
@@ -202,13 +202,29 @@ def run_ours(args):
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    def timed_run(mg, label):
+    def timed_run(mg, label, host_io=False):
+        """W untimed steps, then K steps each bracketed by CUDA events on the
+        solver's stream (L2 flushed before each).  host_io: every step goes
+        through the C ABI with host buffers -- state and u uploaded from
+        pinned memory before, read back after (the e2e measurement)."""
         sim = api.Simulation(prob, mg)
         sim.start()
         sim.step(args.warmup)
         stream = torch.cuda.ExternalStream(sim.solver.stream_ptr())
         s0 = sim.state(with_u=False)
-        ms = 0.0
+        ms, step_ms, step_t = 0.0, [], [s0["t"]]
+        if host_io:
+            nz, nx = prob.nz, prob.nx
+
+            def pinned(shape):
+                return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+
+            hU = pinned((nz, nx))
+            hU[:] = sim.solver.download_u()
+            hv = {k: pinned(nz) for k in ("Slip", "psi", "V", "dpsi", "Ts")}
+            st = sim.solver.rk43_state()
+            for k in hv:
+                hv[k][:] = st[k]
         barrier()
         for _ in range(args.steps):
             flush.fill_(1.0)
@@ -216,13 +232,27 @@ def run_ours(args):
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            sim.step(1)
+            if host_io:
+                sim.solver.rk43_set_state(hv["Slip"], hv["psi"], hv["V"], hv["dpsi"], st["t"], st["dt"],
+                                          st["errA"][0], st["errA"][1], st["it"])
+                sim.solver.upload_u(hU)
+                sim.solver.rk43_step(1)
+                st = sim.solver.rk43_state()
+                hU[:] = sim.solver.download_u()
+            else:
+                sim.step(1)
             e1.record(stream)
             e1.synchronize()
-            ms += e0.elapsed_time(e1)
+            if host_io:
+                for k in hv:
+                    hv[k][:] = st[k]
+            step_ms.append(e0.elapsed_time(e1))
+            ms += step_ms[-1]
+            step_t.append(sim.solver.rk43_state()["t"])
         barrier()
         s1 = sim.state(with_u=False)
-        return sim, {"ms": ms, "yrs": (s1["t"] - s0["t"]) / YEAR_S,
+        return sim, {"ms": ms, "yrs": (s1["t"] - s0["t"]) / YEAR_S, "step_ms": step_ms,
+                     "step_t": step_t,
                      "launches": s1["kernel_launches"] - s0["kernel_launches"],
                      "vcycles": s1["vcycles"] - s0["vcycles"], "solves": s1["solves"] - s0["solves"],
                      "attempts": s1["attempts"] - s0["attempts"], "t_end": s1["t"]}
@@ -236,11 +266,15 @@ def run_ours(args):
 
     clocks = Clocks(local)
     clocks.start()
-    mixed_cfg = config.MGConfig(**{**cfg.mg.__dict__, "precision": 1})
-    fp64_cfg = config.MGConfig(**{**cfg.mg.__dict__, "precision": 0})
+    mixed_cfg = config.MGConfig(**{**cfg.mg.__dict__, "precision": 1, "surface_prolong": 1})
+    fp64_cfg = config.MGConfig(**{**cfg.mg.__dict__, "precision": 0, "surface_prolong": 0})
+    fp64s_cfg = config.MGConfig(**{**cfg.mg.__dict__, "precision": 0, "surface_prolong": 1})
     sim, head = timed_run(mixed_cfg, "mixed")
     clk = clocks.stop()
     sim64, plain = timed_run(fp64_cfg, "fp64")
+    sim64.close()
+    sim64s, plain_s = timed_run(fp64s_cfg, "fp64+surface")
+    sim64s.close()
     ms_max = reduce_max(head["ms"])
     value = world * head["yrs"] / (ms_max / 3.6e6)       # replicas: every rank ran the same work
     plain_value = plain["yrs"] / (reduce_max(plain["ms"]) / 3.6e6)
@@ -271,53 +305,27 @@ def run_ours(args):
                 "kernel": "k_rb<float> level 0 (one colour)",
                 "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"}
 
-    # end to end through the C ABI with host buffers (pinned), one step per call
+    # end to end through the C ABI with host buffers (pinned), the same steps
     e2e = None
     if not args.no_e2e:
-        nz, nx = prob.nz, prob.nx
-
-        def pinned(shape):
-            return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
-
-        st = sim.solver.rk43_state()
-        hU = pinned((nz, nx))
-        hU[:] = sim.solver.download_u()
-        hv = {k: pinned(nz) for k in ("Slip", "psi", "V", "dpsi", "Ts")}
-        for k in ("Slip", "psi", "V", "dpsi", "Ts"):
-            hv[k][:] = st[k]
-        t_sim, dt, errA, it = st["t"], st["dt"], st["errA"], st["it"]
-        ne2e = min(args.steps, 20)
-        e2e_ms = 0.0
-        t_start = t_sim
-        for _ in range(ne2e):
-            flush.fill_(1.0)
-            torch.cuda.synchronize()
-            a0 = torch.cuda.Event(enable_timing=True)
-            a1 = torch.cuda.Event(enable_timing=True)
-            a0.record(stream)
-            sim.solver.rk43_set_state(hv["Slip"], hv["psi"], hv["V"], hv["dpsi"], t_sim, dt, errA[0],
-                                      errA[1], it)
-            sim.solver.upload_u(hU)
-            sim.solver.rk43_step(1)
-            s2 = sim.solver.rk43_state()
-            hU[:] = sim.solver.download_u()
-            a1.record(stream)
-            a1.synchronize()
-            e2e_ms += a0.elapsed_time(a1)
-            for k in ("Slip", "psi", "V", "dpsi", "Ts"):
-                hv[k][:] = s2[k]
-            t_sim, dt, errA, it = s2["t"], s2["dt"], s2["errA"], s2["it"]
-        e2e_yrs = (t_sim - t_start) / YEAR_S
-        e2e = {"value": world * e2e_yrs / (reduce_max(e2e_ms) / 3.6e6), "unit": "sim_yr/hr",
-               "h2d_bytes_per_step": 8 * (4 * nz + prob.ni * prob.nk),
-               "d2h_bytes_per_step": 8 * (5 * nz + prob.ni * prob.nk), "steps": ne2e}
+        sim_e, io = timed_run(mixed_cfg, "mixed-host-io", host_io=True)
+        sim_e.close()
+        e2e = {"value": world * io["yrs"] / (reduce_max(io["ms"]) / 3.6e6), "unit": "sim_yr/hr",
+               "h2d_bytes_per_step": 8 * (4 * prob.nz + prob.ni * prob.nk),
+               "d2h_bytes_per_step": 8 * (5 * prob.nz + prob.ni * prob.nk),
+               "ms_per_step": io["ms"] / args.steps}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         r = run_cpu(prob, args.warmup, args.steps, budget_s=args.cpu_sample_s)
+        n = r["steps"]
+        g_yrs = (head["step_t"][n] - head["step_t"][0]) / YEAR_S
+        g_ms = sum(head["step_ms"][:n])
         cpu = {"value": r["value"], "unit": "sim_yr/hr", "cores": r["threads"], "kind": "port",
-               "sample": f"oracle (reference algorithm, {r['schedule']}): {r['steps']} accepted "
-                         f"steps after the same {args.warmup} warm-up steps, {r['wall_s']:.1f}s"}
+               "sample": f"oracle (reference algorithm, {r['schedule']}): accepted steps "
+                         f"{args.warmup + 1}..{args.warmup + n} (the first {n} timed steps), "
+                         f"{r['wall_s']:.1f}s",
+               "gpu_value_same_steps": g_yrs / (g_ms / 3.6e6) if g_ms > 0 else None}
 
     if rank == 0:
         line = {
@@ -328,13 +336,18 @@ def run_ours(args):
             "config": {"workload": f"{cfg.name}: {cfg.ni}x{cfg.nk} earthquake cycle, accepted RK43 steps "
                                    f"{args.warmup + 1}..{args.warmup + args.steps} from steady sliding",
                        "mg": f"{cfg.mg.n_levels} levels V({cfg.mg.nu_pre},{cfg.mg.nu_post}), "
-                             f"rel {cfg.mg.tol:g}, FP32 cycles in FP64 refinement",
+                             f"rel {cfg.mg.tol:g}, FP32 cycles in FP64 refinement, surface-row "
+                             f"prolongation",
                        "parallelism": f"replicas x{world}", "l2": "flushed before every timed step"},
             "sim_years_timed": head["yrs"], "t_end_s": head["t_end"],
             "vcycles_per_solve": head["vcycles"] / max(1, head["solves"]),
             "attempts_per_step": head["attempts"] / args.steps,
             "plain_fp64": {"value": plain_value, "ms_per_step": plain["ms"] / args.steps,
-                           "vcycles_per_solve": plain["vcycles"] / max(1, plain["solves"])},
+                           "vcycles_per_solve": plain["vcycles"] / max(1, plain["solves"]),
+                           "mg": "reference prolongation (no surface-row correction)"},
+            "fp64_surface_prolong": {"value": plain_s["yrs"] / (plain_s["ms"] / 3.6e6),
+                                     "ms_per_step": plain_s["ms"] / args.steps,
+                                     "vcycles_per_solve": plain_s["vcycles"] / max(1, plain_s["solves"])},
             "speedup_vs_plain_fp64": value / world / plain_value if plain_value else None,
             "gpu_launches": head["launches"],
             "roofline": roofline, "clocks": clk, "e2e": e2e, "cpu_baseline": cpu,

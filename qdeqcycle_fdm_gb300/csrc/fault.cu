@@ -138,7 +138,7 @@ __device__ double newton_v(double Ts, double Tn, double tau0, double a, double e
             } else {
                 yn = -1.0;   // outside the domain: bisect
             }
-            if (!(yn > ylo && yn < yhi)) yn = 0.5 * (ylo + yhi);
+            if (!(yn >= ylo && yn <= yhi)) yn = 0.5 * (ylo + yhi);
             const double err = fabs(yn - y) / (fabs(y) + 1e-100);
             it++;
             y = yn;

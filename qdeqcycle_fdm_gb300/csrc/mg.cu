@@ -186,15 +186,6 @@ __global__ void __launch_bounds__(BX * BY)
     if (threadIdx.x == 0 && threadIdx.y == 0) partial[blockIdx.y * gridDim.x + blockIdx.x] = sq;
 }
 
-// u64 += e32 on the interior columns (mixed precision update)
-__global__ void k_correct(double *u, const float *e, int N, int K, int P) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    if (j >= N || k < 1 || k > K - 2) return;
-    const long c = (long)j * P + k;
-    u[c] += (double)e[c];
-}
-
 // residual norm^2 of the zero-interior guess: only the columns next to the
 // Dirichlet data see a non-zero residual (f = 0 on level 0)
 template <typename T>
@@ -216,45 +207,6 @@ __global__ void k_r0(View<T> v, double *partial) {
     }
     sq = block_sum(sq);
     if (threadIdx.x == 0) partial[blockIdx.x] = sq;
-}
-
-// full-weighting restriction of the fine residual into the coarse rhs, and
-// zero coarse initial guess (restriction_kernel, :953-1015)
-template <typename T>
-__global__ void k_restrict(const T *__restrict__ rf, int Pf, T *fc, T *uc, int Nc, int Kc, int Pc) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    if (j >= Nc || k < 1 || k > Kc - 2) return;
-    const int rn = (j == 0) ? 2 * j + 1 : 2 * j - 1;
-    const int rs = (j == Nc - 1) ? 2 * j - 1 : 2 * j + 1;
-    const T *c0 = rf + (long)(2 * j) * Pf + 2 * k;
-    const T *cn = rf + (long)rn * Pf + 2 * k;
-    const T *cs = rf + (long)rs * Pf + 2 * k;
-    const T val = (T)0.06250 * ((T)4.0 * c0[0] + (T)2.0 * c0[-1] + (T)2.0 * c0[1] + (T)2.0 * cn[0] +
-                                (T)2.0 * cs[0] + cn[-1] + cn[1] + cs[-1] + cs[1]);
-    const long c = (long)j * Pc + k;
-    fc[c] = val;
-    uc[c] = (T)0;
-}
-
-// bilinear prolongation u_fine += P e_coarse, one thread per fine node;
-// fine rows 0..Nf-2 (0..Nf-1 with surface_prolong) and columns 1..Kf-2
-// (prolongate_kernel, :1017-1043)
-template <typename T>
-__global__ void k_prolong(T *uf, int Nf, int Kf, int Pf, const T *__restrict__ ec, int Pc,
-                          int surface) {
-    const int kf = blockIdx.x * blockDim.x + threadIdx.x;
-    const int jf = blockIdx.y * blockDim.y + threadIdx.y;
-    if (jf >= Nf - 1 + surface || kf < 1 || kf > Kf - 2) return;
-    const int j = jf >> 1, k = kf >> 1;
-    const T *e = ec + (long)j * Pc + k;
-    T add;
-    if (!(jf & 1)) {
-        add = (kf & 1) ? (T)0.5 * (e[0] + e[1]) : e[0];
-    } else {
-        add = (kf & 1) ? (T)0.25 * (e[0] + e[1] + e[Pc] + e[Pc + 1]) : (T)0.5 * (e[0] + e[Pc]);
-    }
-    uf[(long)jf * Pf + kf] += add;
 }
 
 // ---------------------------------------------------------------------------
@@ -375,48 +327,6 @@ static int smooth_t(qd_solver *s, Level<T> *Ls, int l, int nsweeps) {
     return QD_OK;
 }
 
-template <typename T>
-static int residual_t(qd_solver *s, Level<T> *Ls, int l) {
-    View<T> v = make_view(s, Ls, l);
-    dim3 blk(BX, BY), grd(cdiv(v.K, BX), cdiv(v.N, BY));
-    if (v.f)
-        k_residual<T, true, false><<<grd, blk, 0, s->stream>>>(v, v.r, nullptr);
-    else
-        k_residual<T, false, false><<<grd, blk, 0, s->stream>>>(v, v.r, nullptr);
-    QD_LAUNCH_CHECK(s);
-    return QD_OK;
-}
-
-template <typename T>
-static int restrict_t(qd_solver *s, Level<T> *Ls, int lc) {
-    const LevelDims &f = s->dims[lc - 1], &c = s->dims[lc];
-    dim3 blk(BX, BY), grd(cdiv(c.K, BX), cdiv(c.N, BY));
-    k_restrict<T><<<grd, blk, 0, s->stream>>>(Ls[lc - 1].r, f.P, Ls[lc].f, Ls[lc].u, c.N, c.K, c.P);
-    QD_LAUNCH_CHECK(s);
-    return QD_OK;
-}
-
-template <typename T>
-static int prolong_t(qd_solver *s, Level<T> *Ls, int lc) {
-    const LevelDims &f = s->dims[lc - 1], &c = s->dims[lc];
-    dim3 blk(BX, BY), grd(cdiv(f.K, BX), cdiv(f.N, BY));
-    k_prolong<T><<<grd, blk, 0, s->stream>>>(Ls[lc - 1].u, f.N, f.K, f.P, Ls[lc].u, c.P,
-                                             s->opt.surface_prolong);
-    QD_LAUNCH_CHECK(s);
-    return QD_OK;
-}
-
-template <typename T>
-static int vcycle_t(qd_solver *s, Level<T> *Ls, int l) {
-    if (l >= s->nlev - 1) return smooth_t(s, Ls, l, s->opt.nu_coarse);
-    QD_TRY(smooth_t(s, Ls, l, s->opt.nu_pre));
-    QD_TRY(residual_t(s, Ls, l));
-    QD_TRY(restrict_t(s, Ls, l + 1));
-    QD_TRY(vcycle_t(s, Ls, l + 1));
-    QD_TRY(prolong_t(s, Ls, l + 1));
-    return smooth_t(s, Ls, l, s->opt.nu_post);
-}
-
 // ||r||^2 of level 0 into d_scal[slot]; for mixed precision also writes the
 // FP32 correction right-hand side.
 static int level0_norm(qd_solver *s, int to32, int slot) {
@@ -462,7 +372,6 @@ int mg_solve(qd_solver *s, int *cycles, double *rnorm, double *r0norm) {
     double delta = sqrt(s->h_scal[0]);
     int it = 0;
     int rc = QD_OK;
-    const LevelDims &d0 = s->dims[0];
     while (!(delta <= thr)) {
         if (isnan(delta) || isinf(delta)) {
             rc = QD_ERR_NOT_CONVERGED;
@@ -475,15 +384,18 @@ int mg_solve(qd_solver *s, int *cycles, double *rnorm, double *r0norm) {
             break;
         }
         if (mixed) {
-            QD_CUDA(cudaMemsetAsync(s->L32[0].u, 0, sizeof(float) * d0.N * d0.P, s->stream));
-            QD_TRY(vcycle_t<float>(s, s->L32, 0));
-            dim3 blk(BX, BY), grd(cdiv(d0.K, BX), cdiv(d0.N, BY));
-            k_correct<<<grd, blk, 0, s->stream>>>(s->L64[0].u, s->L32[0].u, d0.N, d0.K, d0.P);
-            QD_LAUNCH_CHECK(s);
+            QD_TRY(vcycle32_into64(s));            // FP32 cycle on A e = r, then u += e
+            QD_TRY(level0_norm(s, 1, 0));          // FP64 residual -> FP32 rhs, norm
         } else {
-            QD_TRY(vcycle_t<double>(s, s->L64, 0));
+            int nb = 0;
+            QD_TRY(vcycle64_norm(s, &nb));         // the last kernel leaves norm partials
+            if (nb > 0) {
+                k_final_sum<<<1, 1024, 0, s->stream>>>(s->d_partial, nb, s->d_scal);
+                QD_LAUNCH_CHECK(s);
+            } else {
+                QD_TRY(level0_norm(s, 0, 0));
+            }
         }
-        QD_TRY(level0_norm(s, mixed, 0));
         QD_TRY(read_scalars(s, 1));
         delta = sqrt(s->h_scal[0]);
         it++;
@@ -508,7 +420,8 @@ int mg_smooth(qd_solver *s, int level, int nsweeps) {
 }
 
 int mg_vcycle(qd_solver *s) {
-    QD_TRY(vcycle_t<double>(s, s->L64, 0));
+    int nb = 0;
+    QD_TRY(vcycle64_norm(s, &nb));
     QD_CUDA(cudaStreamSynchronize(s->stream));
     return QD_OK;
 }

@@ -120,6 +120,9 @@ int mg_solve(qd_solver *s, int *cycles, double *rnorm, double *r0norm);
 int mg_smooth(qd_solver *s, int level, int nsweeps);
 int mg_vcycle(qd_solver *s);
 int mg_residual_norm(qd_solver *s, double *rnorm);
+// mg_fused.cu
+int vcycle64_norm(qd_solver *s, int *nblocks);
+int vcycle32_into64(qd_solver *s);
 // fault.cu
 int fault_alloc(qd_solver *s);
 void fault_free(qd_solver *s);

@@ -183,12 +183,28 @@ def test_newton_safeguard_recovers_where_reference_overflows():
     assert np.all(np.isfinite(V[k])) and np.max(np.abs(g)) < 1e-9 * 60.0
 
 
-def test_rk43_100_steps_match_oracle():
-    cfg, prob = make_problem(33)
-    mg = cfg.mg
+@pytest.mark.parametrize("surface", [0, 1])
+def test_rk43_100_steps_match_oracle(surface):
+    """100 accepted RK43 steps of the interseismic period, GPU vs oracle.
+
+    Steady sliding at Vp in the velocity-weakening zone is an unstable
+    equilibrium: perturbations grow like exp(t V/L), about 1e10 per decade
+    here, so any two implementations that differ in the last bit diverge
+    after a few simulated years, and round-off-level error estimates make
+    the adaptive step sequence itself round-off driven.  Parity is therefore
+    checked over one simulated year with the step fixed by the reference's
+    own parameters (ini_dt = mindt = maxdt = 3e5 s; computeStepSize then
+    always returns it), and solves tight enough (1e-13 relative) that the
+    solver tolerance is not what differs.  Over this window an oracle run
+    perturbed by 1e-14 in one node's prestress stays within 1e-13 of the
+    unperturbed one."""
+    cfg, prob = make_problem(65)
+    prob.ini_dt = prob.mindt = prob.maxdt = 3e5
+    mg = config.MGConfig(n_levels=cfg.mg.n_levels, nu_pre=2, nu_post=2, nu_coarse=32, tol_mode=1,
+                         tol=1e-13, max_cycles=400, surface_prolong=surface)
     gpu = api.Simulation(prob, mg)
     cpu = oracle.Simulation(prob, mg.n_levels, mg.nu_pre, mg.nu_post, mg.nu_coarse, mg.tol_mode,
-                            mg.tol, mg.max_cycles)
+                            mg.tol, mg.max_cycles, surface_prolong=surface)
     gpu.start()
     cpu.start()
     for _ in range(100):
@@ -198,9 +214,46 @@ def test_rk43_100_steps_match_oracle():
     c = cpu.state()
     k = slice(1, prob.nk + 1)
     assert g["it"] == c["it"] == 100
-    assert rel(g["t"], c["t"]) < 1e-8
+    assert g["vcycles"] == c["vcycles"]
+    assert rel(g["t"], c["t"]) < 1e-12 and rel(g["dt"], c["dt"]) < 1e-12
     assert rel(g["Slip"][k], c["Slip"][k]) < 1e-8
     assert rel(g["psi"][k], c["psi"][k]) < 1e-8
     assert np.max(np.abs(g["V"][k] - c["V"][k]) / c["V"][k]) < 1e-10
-    assert rel(g["Ts"][k], c["Ts"][k]) < 1e-10
+    assert rel(g["Ts"][k] + prob.tau0[k], c["Ts"][k] + prob.tau0[k]) < 1e-10   # total shear stress
     assert rel(g["U"], c["U"]) < 1e-10
+
+
+def test_rk43_adaptive_steps_match_oracle():
+    """The first adaptive steps (dt growing 5x per step from ini_dt, the
+    accept/reject logic and the error estimate) against the oracle."""
+    cfg, prob = make_problem(65)
+    mg = config.MGConfig(n_levels=cfg.mg.n_levels, nu_pre=2, nu_post=2, nu_coarse=32, tol_mode=1,
+                         tol=1e-13, max_cycles=400, surface_prolong=1)
+    gpu = api.Simulation(prob, mg)
+    cpu = oracle.Simulation(prob, mg.n_levels, mg.nu_pre, mg.nu_post, mg.nu_coarse, mg.tol_mode,
+                            mg.tol, mg.max_cycles, surface_prolong=1)
+    gpu.start()
+    cpu.start()
+    for _ in range(6):
+        gpu.step()
+        cpu.step()
+        g = gpu.state(with_u=False)
+        c = cpu.state()
+        assert rel(g["t"], c["t"]) < 1e-12 and rel(g["dt"], c["dt"]) < 1e-12
+    k = slice(1, prob.nk + 1)
+    assert np.max(np.abs(g["V"][k] - c["V"][k]) / c["V"][k]) < 1e-10
+    assert rel(g["Slip"][k], c["Slip"][k]) < 1e-8
+
+
+def test_gpu_runs_are_bitwise_reproducible():
+    cfg, prob = make_problem(33)
+    outs = []
+    for _ in range(2):
+        sim = api.Simulation(prob, cfg.mg)
+        sim.start()
+        sim.step(20)
+        outs.append(sim.state())
+        sim.close()
+    for key in ("Slip", "psi", "V", "U"):
+        assert np.array_equal(outs[0][key], outs[1][key]), key
+    assert outs[0]["t"] == outs[1]["t"]
