@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libqdeq_gb300.so")
-SOURCES = ["capi.cu", "mg.cu", "mg_fused.cu", "fault.cu", "medium.cu"]
+SOURCES = ["capi.cu", "mg.cu", "mg_fused.cu", "fault.cu", "medium.cu", "dropin.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr"]
@@ -42,7 +42,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
     jobs = []
     for src in SOURCES:
         sp = os.path.join(CSRC, src)
-        obj = os.path.join(OUT_DIR, src.replace(".cu", ".o"))
+        obj = os.path.join(OUT_DIR, os.path.splitext(src)[0] + ".o")
         objs.append(obj)
         if force or _stale([sp] + headers, obj):
             cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *extra_flags, "-c", sp, "-o", obj]
