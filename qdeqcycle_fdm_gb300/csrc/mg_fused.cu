@@ -252,9 +252,16 @@ template <typename K>
 static int set_smem(K kernel, size_t bytes) {
     static size_t done = 0;   // one per kernel instantiation
     if (bytes <= done) return QD_OK;
-    QD_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_limit()));
+    cudaFuncAttributes fa;
+    QD_CUDA(cudaFuncGetAttributes(&fa, kernel));
+    const size_t cap = smem_limit() - fa.sharedSizeBytes;   // static + dynamic <= opt-in limit
+    if (bytes > cap) {
+        set_error("kernel needs %zu B of dynamic shared memory, %zu available", bytes, cap);
+        return QD_ERR_ARG;
+    }
+    QD_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap));
     QD_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
-    done = smem_limit();
+    done = cap;
     return QD_OK;
 }
 

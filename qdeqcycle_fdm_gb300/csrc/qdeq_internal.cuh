@@ -28,6 +28,7 @@ void set_error(const char *fmt, ...);
     do {                                                                           \
         cudaError_t e__ = (call);                                                  \
         if (e__ != cudaSuccess) {                                                  \
+            (void)cudaGetLastError(); /* clear a non-sticky error for later calls */ \
             ::qd::set_error("%s:%d: %s: %s", __FILE__, __LINE__, #call,            \
                             cudaGetErrorString(e__));                              \
             return QD_ERR_CUDA;                                                    \
