@@ -92,10 +92,11 @@ __device__ void tv_halfsweep(const TV<T> &g, int color) {
         const int c = j * g.K + k, cc = j * g.CP + k;
         const int up = (j == 0) ? g.K : -g.K;
         const int dn = (j == g.N - 1) ? -g.K : g.K;
-        T acc = __ldg(g.cx + cc - 1) * g.u[c - 1] + __ldg(g.cx + cc) * g.u[c + 1] +
-                __ldg(g.cz + cc) * g.u[c + up] + __ldg(g.cz + cc + g.CP) * g.u[c + dn];
+        // the moduli may live in shared or in global memory: generic loads
+        T acc = g.cx[cc - 1] * g.u[c - 1] + g.cx[cc] * g.u[c + 1] + g.cz[cc] * g.u[c + up] +
+                g.cz[cc + g.CP] * g.u[c + dn];
         acc -= g.h2 * g.f[c];
-        g.u[c] = __ldg(g.dinv + cc) * acc;
+        g.u[c] = g.dinv[cc] * acc;
     }
 }
 
@@ -175,8 +176,7 @@ __global__ void __launch_bounds__(NT_TAIL) k_tail(TailArgs<T> a) {
             const int cc = j * g.CP + k;
             const int up = (j == 0) ? g.K : -g.K;
             const int dn = (j == g.N - 1) ? -g.K : g.K;
-            const T cW = __ldg(g.cx + cc - 1), cE = __ldg(g.cx + cc), cN = __ldg(g.cz + cc),
-                    cS = __ldg(g.cz + cc + g.CP);
+            const T cW = g.cx[cc - 1], cE = g.cx[cc], cN = g.cz[cc], cS = g.cz[cc + g.CP];
             const T lap = cW * g.u[i - 1] + cE * g.u[i + 1] + cN * g.u[i + up] + cS * g.u[i + dn] -
                           (((cW + cE) + cN) + cS) * g.u[i];
             g.r[i] = g.f[i] - lap * g.inv_h2;
