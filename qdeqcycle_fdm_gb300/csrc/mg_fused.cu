@@ -20,6 +20,9 @@
 // never reads u (the reference zeroes e2 in restriction_kernel and then
 // reads it back).
 #include <algorithm>
+#include <mutex>
+#include <utility>
+#include <vector>
 
 #include "qdeq_internal.cuh"
 
@@ -250,7 +253,14 @@ static size_t smem_limit() {
 // raise a kernel's dynamic shared-memory limit once, to the device maximum
 template <typename K>
 static int set_smem(K kernel, size_t bytes) {
-    static size_t done = 0;   // one per kernel instantiation
+    // kernels already raised, keyed by their address (kernels of one
+    // signature share K, so a per-type static would not do)
+    static std::vector<std::pair<const void *, size_t>> raised;
+    static std::mutex mtx;
+    std::lock_guard<std::mutex> lock(mtx);
+    size_t done = 0;
+    for (const auto &e : raised)
+        if (e.first == (const void *)kernel) done = e.second;
     if (bytes <= done) return QD_OK;
     cudaFuncAttributes fa;
     QD_CUDA(cudaFuncGetAttributes(&fa, kernel));
@@ -261,7 +271,7 @@ static int set_smem(K kernel, size_t bytes) {
     }
     QD_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap));
     QD_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
-    done = cap;
+    raised.emplace_back((const void *)kernel, cap);
     return QD_OK;
 }
 
