@@ -146,6 +146,27 @@ int qd_mg_smooth(qd_solver *s, int nsweeps);
 int qd_mg_vcycle(qd_solver *s);
 int qd_mg_residual_norm(qd_solver *s, double *rnorm);
 
+/* The level-0 residual norm ||0 - A u||2 that qd_mg_residual_norm returns,
+ * for a caller that cannot allocate device memory: a host framework that
+ * owns every device byte (its own allocator, or a budget fixed at start-up),
+ * or code where a cudaMalloc would synchronise the device in the middle of
+ * its own work.  It needs no solver and allocates nothing: u (nk rows x ni
+ * columns), cx and cz (the face moduli of a solver's level 0 -- cx[j][k]
+ * between columns k and k+1, cz[j][k] for j = 0..nk between rows j-1 and j)
+ * are DEVICE arrays the caller owns, with a row pitch of `pitch` doubles;
+ * dh is the grid spacing; the work runs on `stream` (a cudaStream_t; NULL
+ * for the default stream) and *rnorm (host) receives the norm.
+ * The block partial sums live in a file-scope device array of 69,633
+ * doubles (544 KB) that every GPU using this library keeps until the
+ * process exits; grids beyond 4097 x 4097 nodes are rejected with
+ * QD_ERR_ARG.  The first call on each device looks up that array's device
+ * address, so make it before any stream capture.  All calls share the
+ * array: calls that overlap on the GPU (two streams, two host threads)
+ * race and must be serialised by the caller.  This entry point has no
+ * counterpart in the reference. */
+int qd_residual_norm_noalloc(const double *u, const double *cx, const double *cz, int nk, int ni,
+                             int pitch, double dh, void *stream, double *rnorm);
+
 /* ---------------------------------------------------------------------
  * Fault.  Arrays are nz long (entries 1..nk used).  tau0 (MPa) is added to
  * the stress the Newton solve balances; pass NULL for the reference's
