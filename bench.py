@@ -186,12 +186,10 @@ def run_ours(args):
     import numpy as np
     import torch
 
-    rank, world, local = dist_env()
+    from qdeqcycle_fdm_gb300 import api, build, config, problem, replicas
+    rank, world, local = replicas.env()
     torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-    from qdeqcycle_fdm_gb300 import api, build, config, problem
+    replicas.init("nccl")          # replicas only: the data path has no collective
     build.build()
     cfg = config.CONFIGS[args.config]()
     prob = problem.build_problem(cfg)            # face moduli homogenised on the GPU
@@ -257,12 +255,12 @@ def run_ours(args):
                      "vcycles": s1["vcycles"] - s0["vcycles"], "solves": s1["solves"] - s0["solves"],
                      "attempts": s1["attempts"] - s0["attempts"], "t_end": s1["t"]}
 
+    def job_value(run):
+        """whole-job simulated yr/hr: years of all replicas / slowest rank's hours"""
+        return replicas.aggregate(run["yrs"], run["ms"] / 3.6e6, device="cuda")[2]
+
     def reduce_max(x):
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
+        return replicas.aggregate(0.0, x, device="cuda")[1]
 
     clocks = Clocks(local)
     clocks.start()
@@ -276,7 +274,7 @@ def run_ours(args):
     sim64s, plain_s = timed_run(fp64s_cfg, "fp64+surface")
     sim64s.close()
     ms_max = reduce_max(head["ms"])
-    value = world * head["yrs"] / (ms_max / 3.6e6)       # replicas: every rank ran the same work
+    value = job_value(head)
     plain_value = plain["yrs"] / (reduce_max(plain["ms"]) / 3.6e6)
 
     # dominant kernel: level-0 smoother sweeps of the headline (FP32) hierarchy
@@ -310,7 +308,7 @@ def run_ours(args):
     if not args.no_e2e:
         sim_e, io = timed_run(mixed_cfg, "mixed-host-io", host_io=True)
         sim_e.close()
-        e2e = {"value": world * io["yrs"] / (reduce_max(io["ms"]) / 3.6e6), "unit": "sim_yr/hr",
+        e2e = {"value": job_value(io), "unit": "sim_yr/hr",
                "h2d_bytes_per_step": 8 * (4 * prob.nz + prob.ni * prob.nk),
                "d2h_bytes_per_step": 8 * (5 * prob.nz + prob.ni * prob.nk),
                "ms_per_step": io["ms"] / args.steps}
