@@ -264,9 +264,11 @@ def run_ours(args):
 
     clocks = Clocks(local)
     clocks.start()
-    mixed_cfg = config.MGConfig(**{**cfg.mg.__dict__, "precision": 1, "surface_prolong": 1})
+    mixed_cfg = config.MGConfig(**{**cfg.mg.__dict__, "precision": 1, "surface_prolong": 1,
+                                   "coarse_solve": 1})
     fp64_cfg = config.MGConfig(**{**cfg.mg.__dict__, "precision": 0, "surface_prolong": 0})
-    fp64s_cfg = config.MGConfig(**{**cfg.mg.__dict__, "precision": 0, "surface_prolong": 1})
+    fp64s_cfg = config.MGConfig(**{**cfg.mg.__dict__, "precision": 0, "surface_prolong": 1,
+                                   "coarse_solve": 1})
     sim, head = timed_run(mixed_cfg, "mixed")
     clk = clocks.stop()
     sim64, plain = timed_run(fp64_cfg, "fp64")
@@ -334,7 +336,7 @@ def run_ours(args):
             "config": {"workload": f"{cfg.name}: {cfg.ni}x{cfg.nk} earthquake cycle, accepted RK43 steps "
                                    f"{args.warmup + 1}..{args.warmup + args.steps} from steady sliding",
                        "mg": f"{cfg.mg.n_levels} levels V({cfg.mg.nu_pre},{cfg.mg.nu_post}), "
-                             f"rel {cfg.mg.tol:g}, FP32 cycles in FP64 refinement, surface-row "
+                             f"rel {cfg.mg.tol:g}, FP32 cycles in FP64 refinement, exact coarsest solve, surface-row "
                              f"prolongation",
                        "parallelism": f"replicas x{world}", "l2": "flushed before every timed step"},
             "sim_years_timed": head["yrs"], "t_end_s": head["t_end"],

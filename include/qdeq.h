@@ -69,6 +69,10 @@ typedef struct qd_mg_options {
                          correction; 1: it gets the coincident coarse row's
                          correction too (same discrete solution, about 5x
                          fewer V(2,2) cycles)                                */
+    int coarse_solve;    /* 0: nu_coarse red+black sweeps on the coarsest level,
+                         as vcycle() (odeSolver.cpp:1103-1107); 1: exact
+                         solve there with a dense inverse built at set-up
+                         (coarsest level of at most 1024 unknowns)           */
 } qd_mg_options;
 
 /* Time-stepping parameters (PARAMS, struct.h:12-38; SetParams.cpp:14-21). */

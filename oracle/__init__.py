@@ -63,6 +63,7 @@ def lib():
         L.qo_sim_set_params.argtypes = [C.c_void_p] + [C.c_double] * 5 + [C.c_int]
         L.qo_sim_set_U.argtypes = [C.c_void_p, _dp]
         L.qo_sim_set_surface_prolong.argtypes = [C.c_void_p, C.c_int]
+        L.qo_sim_set_coarse_solve.argtypes = [C.c_void_p, C.c_int]
         L.qo_sim_start.argtypes = [C.c_void_p]
         L.qo_sim_step.argtypes = [C.c_void_p]
         L.qo_sim_get.argtypes = [C.c_void_p] + [_dp] * 6
@@ -119,14 +120,15 @@ class _QoMg(C.Structure):
                 ("nu_coarse", C.c_int), ("N", C.c_int * 16), ("K", C.c_int * 16),
                 ("fc", C.c_int * 16), ("DH", C.c_double * 16), ("nx", C.c_int),
                 ("mu", _dp), ("res", _dp * 16), ("res2", _dp * 16), ("err2", _dp * 16),
-                ("delta", _dp), ("rowsum", _dp), ("surface_prolong", C.c_int)]
+                ("delta", _dp), ("rowsum", _dp), ("surface_prolong", C.c_int),
+                ("coarse_solve", C.c_int)]
 
 
 class Multigrid:
     """The reference's multigrid (odeSolver.cpp:652-1147) on the CPU."""
 
     def __init__(self, ni, nk, dh, mu_equi, n_levels=6, nu_pre=32, nu_post=32, nu_coarse=32,
-                 surface_prolong=0):
+                 surface_prolong=0, coarse_solve=0):
         L = lib()
         self._mu = np.ascontiguousarray(mu_equi, dtype=np.float64)
         self.m = _QoMg()
@@ -135,6 +137,7 @@ class Multigrid:
         if rc != 0:
             raise ValueError("bad multigrid configuration")
         self.m.surface_prolong = int(surface_prolong)
+        self.m.coarse_solve = int(coarse_solve)
         self.ni, self.nk = ni, nk
         self.shapes = [(self.m.N[l], self.m.K[l]) for l in range(n_levels)]
 
@@ -243,7 +246,7 @@ class Simulation:
     """The reference's RK43 loop (odeSolver.cpp:1277-1674) on the CPU."""
 
     def __init__(self, prob, n_levels=6, nu_pre=32, nu_post=32, nu_coarse=32, tol_mode=0,
-                 tol=1e-9, max_cycles=0, surface_prolong=0):
+                 tol=1e-9, max_cycles=0, surface_prolong=0, coarse_solve=0):
         L = lib()
         self.prob = prob
         self.ni, self.nk = prob.ni, prob.nk
@@ -259,6 +262,7 @@ class Simulation:
                             prob.totTol, int(prob.maxNumSteps))
         L.qo_sim_set_U(self.h, _p(np.ascontiguousarray(prob.U)))
         L.qo_sim_set_surface_prolong(self.h, int(surface_prolong))
+        L.qo_sim_set_coarse_solve(self.h, int(coarse_solve))
 
     def __del__(self):
         try:

@@ -265,10 +265,63 @@ void qo_smooth(const qo_mg *m, double *u, const double *f, int level, int nsweep
     }
 }
 
+/* The project's exact coarsest-level solve (not in the reference): the
+ * equations the smoother relaxes at `level`, with the same face moduli,
+ * mirrored rows and row quirks as qo_rbgs, solved by Gaussian elimination
+ * with partial pivoting on the interior unknowns. */
+static void qo_coarse_solve(const qo_mg *m, double *u, const double *f, int level) {
+    const int N = m->N[level], K = m->K[level], KI = K - 2, n = N * KI;
+    const double DH2 = m->DH[level] * m->DH[level];
+    const double *mu = m->mu;
+    double *A = (double *)calloc((size_t)n * (n + 1), sizeof(double));
+#define AA(r, c) A[(size_t)(r) * (n + 1) + (c)]
+    for (int j = 0; j < N; j++)
+        for (int k = 1; k <= KI; k++) {
+            long i1, i2, i3, i4;
+            mu_index(m, level, j, k, &i1, &i2, &i3, &i4);
+            double mN, mS;
+            if (j == 0) { mN = (level == 0) ? mu[i3] : mu[i4]; mS = mu[i4]; }
+            else if (j == N - 1) { mN = mu[i3]; mS = (level == 0) ? mu[i4] : mu[i3]; }
+            else { mN = mu[i3]; mS = mu[i4]; }
+            const int row = j * KI + (k - 1);
+            const int jn = (j == 0) ? 1 : j - 1, js = (j == N - 1) ? N - 2 : j + 1;
+            AA(row, row) -= (mu[i1] + mu[i2] + mN + mS) / DH2;
+            if (k - 1 >= 1) AA(row, row - 1) += mu[i1] / DH2;
+            if (k + 1 <= KI) AA(row, row + 1) += mu[i2] / DH2;
+            AA(row, jn * KI + (k - 1)) += mN / DH2;
+            AA(row, js * KI + (k - 1)) += mS / DH2;
+            AA(row, n) = f[(long)j * K + k];
+        }
+    for (int c = 0; c < n; c++) {
+        int p = c;
+        for (int r = c + 1; r < n; r++)
+            if (fabs(AA(r, c)) > fabs(AA(p, c))) p = r;
+        if (p != c)
+            for (int q = 0; q <= n; q++) { const double t = AA(p, q); AA(p, q) = AA(c, q); AA(c, q) = t; }
+        for (int r = c + 1; r < n; r++) {
+            const double fr = AA(r, c) / AA(c, c);
+            if (fr == 0.0) continue;
+            for (int q = c; q <= n; q++) AA(r, q) -= fr * AA(c, q);
+        }
+    }
+    for (int r = n - 1; r >= 0; r--) {
+        double s = AA(r, n);
+        for (int q = r + 1; q < n; q++) s -= AA(r, q) * AA(q, n);
+        AA(r, n) = s / AA(r, r);
+    }
+    for (int j = 0; j < N; j++)
+        for (int k = 1; k <= KI; k++) u[(long)j * K + k] = AA(j * KI + (k - 1), n);
+#undef AA
+    free(A);
+}
+
 /* vcycle(), odeSolver.cpp:1101-1147. */
 void qo_vcycle(qo_mg *m, double *u, const double *f, int level) {
     if (level >= m->n_levels - 1) {
-        qo_smooth(m, u, f, level, m->nu_coarse);
+        if (m->coarse_solve)
+            qo_coarse_solve(m, u, f, level);
+        else
+            qo_smooth(m, u, f, level, m->nu_coarse);
         return;
     }
     double *r = m->res[level], *r2 = m->res2[level], *e2 = m->err2[level];
@@ -799,6 +852,7 @@ void qo_sim_set_params(qo_sim *s, double tmax, double ini_dt, double mindt,
 }
 
 void qo_sim_set_surface_prolong(qo_sim *s, int v) { s->mg.surface_prolong = v; }
+void qo_sim_set_coarse_solve(qo_sim *s, int v) { s->mg.coarse_solve = v; }
 
 void qo_sim_set_U(qo_sim *s, const double *U) {
     memcpy(s->U, U, (size_t)s->nx * s->nz * sizeof(double));

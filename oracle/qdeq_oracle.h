@@ -38,6 +38,7 @@ typedef struct qo_mg {
     double *delta;          /* level-0 residual buffer (delta_res)            */
     double *rowsum;         /* per-row partial sums for a deterministic norm  */
     int surface_prolong;    /* 1: also correct the last row (see qo_prolongate) */
+    int coarse_solve;       /* 1: exact solve on the coarsest level (qo_coarse_solve) */
 } qo_mg;
 
 int  qo_mg_init(qo_mg *m, int ni, int nk, double dh, const double *mu_equi,
@@ -119,6 +120,7 @@ void qo_sim_set_params(qo_sim *s, double tmax, double ini_dt, double mindt,
                        double maxdt, double totTol, int maxNumSteps);
 void qo_sim_set_U(qo_sim *s, const double *U);       /* ghosted nx*nz */
 void qo_sim_set_surface_prolong(qo_sim *s, int v);
+void qo_sim_set_coarse_solve(qo_sim *s, int v);
 /* The pre-loop part of RK43 (odeSolver.cpp:1363, 1428-1439). */
 int  qo_sim_start(qo_sim *s);
 /* One pass of the outer while-loop body (odeSolver.cpp:1462-1636). */

@@ -57,7 +57,8 @@ EXPORTS = [
 class MgOptions(C.Structure):
     _fields_ = [("n_levels", C.c_int), ("nu_pre", C.c_int), ("nu_post", C.c_int),
                 ("nu_coarse", C.c_int), ("tol_mode", C.c_int), ("tol", C.c_double),
-                ("max_cycles", C.c_int), ("precision", C.c_int), ("surface_prolong", C.c_int)]
+                ("max_cycles", C.c_int), ("precision", C.c_int), ("surface_prolong", C.c_int),
+                ("coarse_solve", C.c_int)]
 
 
 class Rk43Params(C.Structure):

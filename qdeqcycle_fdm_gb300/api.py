@@ -34,7 +34,7 @@ def _p(a):
 
 def mg_options(mg: MGConfig) -> MgOptions:
     return MgOptions(mg.n_levels, mg.nu_pre, mg.nu_post, mg.nu_coarse, mg.tol_mode, mg.tol,
-                     mg.max_cycles, mg.precision, mg.surface_prolong)
+                     mg.max_cycles, mg.precision, mg.surface_prolong, mg.coarse_solve)
 
 
 def set_medium(ni: int, nk: int, mu_node: np.ndarray) -> np.ndarray:

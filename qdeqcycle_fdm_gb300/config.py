@@ -28,6 +28,7 @@ class MGConfig:
     max_cycles: int = 0        # 0 = uncapped, as the reference
     precision: int = 0         # 0: FP64; 1: FP32 V-cycles inside FP64 refinement
     surface_prolong: int = 0   # 1: coarse correction also on the free-surface row
+    coarse_solve: int = 0      # 1: exact (dense) solve on the coarsest level
 
 
 @dataclass

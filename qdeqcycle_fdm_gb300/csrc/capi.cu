@@ -27,7 +27,8 @@ static int check_opts(const qd_mg_options *o) {
     if (!o || o->n_levels < 1 || o->n_levels > QD_MAXLEV || o->nu_pre < 0 || o->nu_post < 0 ||
         o->nu_coarse < 0 || (o->tol_mode != QD_TOL_ABS && o->tol_mode != QD_TOL_REL) ||
         !(o->tol > 0.0) || (o->precision != QD_PREC_FP64 && o->precision != QD_PREC_MIXED) ||
-        (o->surface_prolong != 0 && o->surface_prolong != 1)) {
+        (o->surface_prolong != 0 && o->surface_prolong != 1) ||
+        (o->coarse_solve != 0 && o->coarse_solve != 1)) {
         set_error("invalid multigrid options");
         return QD_ERR_ARG;
     }
@@ -149,6 +150,7 @@ void qd_default_options(qd_mg_options *o) {
     o->max_cycles = 0;
     o->precision = QD_PREC_FP64;
     o->surface_prolong = 0;
+    o->coarse_solve = 0;
 }
 
 int qd_solver_create(int ni, int nk, double dh, const double *mu_equi, const double *mu_node,

@@ -16,6 +16,8 @@
 // The smoother multiplies by a precomputed 1/diag (the reference divides
 // 1/diag on the fly); red-black order makes each colour update independent
 // of thread order, so results are deterministic.
+#include <algorithm>
+#include <cmath>
 #include <cstdarg>
 #include <cstring>
 #include <vector>
@@ -295,6 +297,74 @@ int mg_alloc(qd_solver *s, const double *mu_equi_host) {
     }
     QD_CUDA(cudaStreamSynchronize(s->stream));
     cudaFree(d_mu);
+    return build_coarse_inverse(s);
+}
+
+// Dense inverse of the coarsest level's operator, for the exact coarse solve
+// (qd_mg_options.coarse_solve).  Row (j,k) of A holds the equation the
+// smoother relaxes, (sum_nb c_nb e_nb - diag e) / h^2 = f, over the interior
+// columns with the mirrored rows and zero Dirichlet columns; Gauss-Jordan
+// with partial pivoting in FP64 on the host, once.
+int build_coarse_inverse(qd_solver *s) {
+    const int l = s->nlev - 1;
+    const LevelDims &d = s->dims[l];
+    const int N = d.N, K = d.K, P = d.P, n = N * (K - 2);
+    s->n_cint = 0;
+    if (s->nlev < 2 || n > 1024) return QD_OK;   // coarse_solve then rejected by the solve
+    std::vector<double> cx((size_t)N * P), cz((size_t)(N + 1) * P);
+    QD_CUDA(cudaMemcpy(cx.data(), s->L64[l].cx, cx.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    QD_CUDA(cudaMemcpy(cz.data(), s->L64[l].cz, cz.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    auto id = [K](int j, int k) { return j * (K - 2) + (k - 1); };
+    const double ih2 = 1.0 / d.h2;
+    std::vector<double> A((size_t)n * n, 0.0), B((size_t)n * n, 0.0);
+    for (int j = 0; j < N; j++)
+        for (int k = 1; k <= K - 2; k++) {
+            const long c = (long)j * P + k;
+            const double cW = cx[c - 1], cE = cx[c], cN = cz[c], cS = cz[c + P];
+            const long row = (long)id(j, k) * n;
+            A[row + id(j, k)] -= (((cW + cE) + cN) + cS) * ih2;
+            if (k - 1 >= 1) A[row + id(j, k - 1)] += cW * ih2;
+            if (k + 1 <= K - 2) A[row + id(j, k + 1)] += cE * ih2;
+            const int jn = (j == 0) ? 1 : j - 1, js = (j == N - 1) ? N - 2 : j + 1;
+            A[row + id(jn, k)] += cN * ih2;
+            A[row + id(js, k)] += cS * ih2;
+        }
+    for (int i = 0; i < n; i++) B[(long)i * n + i] = 1.0;
+    for (int c = 0; c < n; c++) {
+        int p = c;
+        for (int r = c + 1; r < n; r++)
+            if (fabs(A[(long)r * n + c]) > fabs(A[(long)p * n + c])) p = r;
+        if (A[(long)p * n + c] == 0.0) {
+            set_error("coarsest-level operator is singular");
+            return QD_ERR_ARG;
+        }
+        if (p != c)
+            for (int m = 0; m < n; m++) {
+                std::swap(A[(long)p * n + m], A[(long)c * n + m]);
+                std::swap(B[(long)p * n + m], B[(long)c * n + m]);
+            }
+        const double inv = 1.0 / A[(long)c * n + c];
+        for (int m = 0; m < n; m++) {
+            A[(long)c * n + m] *= inv;
+            B[(long)c * n + m] *= inv;
+        }
+        for (int r = 0; r < n; r++) {
+            if (r == c) continue;
+            const double f = A[(long)r * n + c];
+            if (f == 0.0) continue;
+            for (int m = 0; m < n; m++) {
+                A[(long)r * n + m] -= f * A[(long)c * n + m];
+                B[(long)r * n + m] -= f * B[(long)c * n + m];
+            }
+        }
+    }
+    std::vector<float> B32(B.size());
+    for (size_t i = 0; i < B.size(); i++) B32[i] = (float)B[i];
+    QD_CUDA(cudaMalloc(&s->d_ainv64, B.size() * sizeof(double)));
+    QD_CUDA(cudaMalloc(&s->d_ainv32, B.size() * sizeof(float)));
+    QD_CUDA(cudaMemcpy(s->d_ainv64, B.data(), B.size() * sizeof(double), cudaMemcpyHostToDevice));
+    QD_CUDA(cudaMemcpy(s->d_ainv32, B32.data(), B32.size() * sizeof(float), cudaMemcpyHostToDevice));
+    s->n_cint = n;
     return QD_OK;
 }
 
@@ -308,6 +378,10 @@ void mg_free(qd_solver *s) {
         s->L32[l] = Level<float>();
     }
     cudaFree(s->d_partial);
+    cudaFree(s->d_ainv64);
+    cudaFree(s->d_ainv32);
+    s->d_ainv64 = nullptr;
+    s->d_ainv32 = nullptr;
     s->d_partial = nullptr;
 }
 

@@ -68,11 +68,13 @@ namespace qd {
 // ---------------------------------------------------------------------------
 struct TailLevels {
     int l0, nlev, nu_pre, nu_post, nu_coarse, surface, coef_smem;
+    int coarse_solve, nint;   // exact coarsest solve with the dense inverse ainv
 };
 
 template <typename T>
 struct TailArgs {
     LvArgs<T> L[QD_MAXLEV];
+    const T *ainv;
     TailLevels p;
 };
 
@@ -169,7 +171,22 @@ __global__ void __launch_bounds__(NT_TAIL) k_tail(TailArgs<T> a) {
         for (int i = threadIdx.x; i < g.N * g.K; i += blockDim.x) g.u[i] = (T)0;
         __syncthreads();
         if (l == p.nlev - 1) {
-            tv_smooth(g, p.nu_coarse);
+            if (p.coarse_solve) {
+                // e = A^-1 f over the interior nodes, one row per thread
+                const int KI = g.K - 2;
+                for (int i = threadIdx.x; i < p.nint; i += blockDim.x) {
+                    const T *row = a.ainv + (long)i * p.nint;
+                    T acc = (T)0;
+                    int m = 0;
+                    for (int jm = 0; jm < g.N; jm++)
+                        for (int km = 1; km <= KI; km++, m++) acc += row[m] * g.f[jm * g.K + km];
+                    const int j = i / KI, k = i - j * KI + 1;
+                    g.u[j * g.K + k] = acc;
+                }
+                __syncthreads();
+            } else {
+                tv_smooth(g, p.nu_coarse);
+            }
             break;
         }
         tv_smooth(g, p.nu_pre);
@@ -371,6 +388,13 @@ static int vcycle_fused(qd_solver *s, Level<T> *Ls, int zero0, int *nblocks) {
         for (int l = 0; l < nl; l++) ta.L[l] = lv(s, Ls, l);
         ta.p.l0 = lt; ta.p.nlev = nl; ta.p.nu_pre = s->opt.nu_pre; ta.p.nu_post = s->opt.nu_post;
         ta.p.nu_coarse = s->opt.nu_coarse; ta.p.surface = s->opt.surface_prolong;
+        ta.p.coarse_solve = s->opt.coarse_solve;
+        ta.p.nint = s->n_cint;
+        ta.ainv = sizeof(T) == 8 ? (const T *)s->d_ainv64 : (const T *)s->d_ainv32;
+        if (ta.p.coarse_solve && (s->n_cint == 0 || !ta.ainv)) {
+            set_error("coarse_solve needs a coarsest level of at most 1024 unknowns");
+            return QD_ERR_ARG;
+        }
         ta.p.coef_smem = tail_smem_bytes<T>(s, lt, 1) <= smem_limit();
         const size_t smem = tail_smem_bytes<T>(s, lt, ta.p.coef_smem);
         if (smem > smem_limit()) {
@@ -381,6 +405,10 @@ static int vcycle_fused(qd_solver *s, Level<T> *Ls, int zero0, int *nblocks) {
         k_tail<T><<<1, NT_TAIL, smem, s->stream>>>(ta);
         QD_LAUNCH_CHECK(s);
     } else {
+        if (s->opt.coarse_solve) {
+            set_error("coarse_solve needs the coarsest level in the single-CTA tail (<= 65 rows)");
+            return QD_ERR_ARG;
+        }
         QD_TRY(smooth_passes<T>(s, Ls, nl - 1, s->opt.nu_coarse, 1));
     }
     // ascend

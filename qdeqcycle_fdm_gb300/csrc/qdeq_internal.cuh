@@ -97,6 +97,9 @@ struct qd_solver {
     qd::Level<float> L32[QD_MAXLEV];
     cudaStream_t stream;
     double *d_partial;     // per-block reduction partials
+    double *d_ainv64;      // dense inverse of the coarsest-level operator (or null)
+    float *d_ainv32;
+    int n_cint;            // its order: coarsest N * (K-2) interior unknowns
     int n_partial;
     double *d_scal;        // device scalars: [0] ||r||^2, [1] ||r0||^2, [2] totErr
     double *h_scal;        // pinned mirror
@@ -121,6 +124,7 @@ int mg_solve(qd_solver *s, int *cycles, double *rnorm, double *r0norm);
 int mg_smooth(qd_solver *s, int level, int nsweeps);
 int mg_vcycle(qd_solver *s);
 int mg_residual_norm(qd_solver *s, double *rnorm);
+int build_coarse_inverse(qd_solver *s);
 // mg_fused.cu
 int vcycle64_norm(qd_solver *s, int *nblocks);
 int vcycle32_into64(qd_solver *s);

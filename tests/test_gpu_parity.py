@@ -98,6 +98,43 @@ def test_vcycle_matches_oracle(levels):
     assert rel(s.residual_norm(), mg.norm2(r)) < 1e-9
 
 
+@pytest.mark.parametrize("surface", [0, 1])
+def test_vcycle_exact_coarse_solve_matches_oracle(surface):
+    cfg, prob = make_problem(129, mu_profile="layered", layer_depth_km=20.0)
+    mg_cfg = config.MGConfig(n_levels=5, nu_pre=2, nu_post=2, nu_coarse=0, surface_prolong=surface,
+                             coarse_solve=1)
+    U = random_U(prob, 7)
+    s = api.Solver(prob.ni, prob.nk, prob.dh, prob.mu_equi, prob.mu_node, mg_cfg)
+    s.upload_u(U)
+    s.vcycle()
+    s.vcycle()
+    got = compact(s.download_u())
+    mg = oracle.Multigrid(prob.ni, prob.nk, prob.dh, prob.mu_equi, 5, 2, 2, 0, surface_prolong=surface,
+                          coarse_solve=1)
+    u = compact(U).copy()
+    f = np.zeros_like(u)
+    mg.vcycle(u, f)
+    mg.vcycle(u, f)
+    assert rel(got, u) < 1e-11
+
+
+def test_mixed_solve_with_exact_coarse_solve():
+    cfg, prob = make_problem(257, mu_profile="layered", layer_depth_km=8.0)
+    base = dict(n_levels=6, nu_pre=2, nu_post=2, nu_coarse=32, tol_mode=1, tol=1e-10, max_cycles=100,
+                surface_prolong=1)
+    U = random_U(prob, 8)
+    res = {}
+    for prec, cs in ((0, 0), (1, 1)):
+        s = api.Solver(prob.ni, prob.nk, prob.dh, prob.mu_equi, prob.mu_node,
+                       config.MGConfig(**base, precision=prec, coarse_solve=cs))
+        s.upload_u(U)
+        cyc, rn, r0 = s.ode_solve()
+        assert rn <= 1e-10 * r0
+        res[(prec, cs)] = (cyc, compact(s.download_u()))
+    assert res[(1, 1)][0] <= res[(0, 0)][0]
+    assert rel(res[(1, 1)][1], res[(0, 0)][1]) < 1e-8
+
+
 def test_reference_schedule_solve_matches_oracle():
     """The reference's own schedule: 6 levels, V(32,32), absolute 1e-9."""
     cfg, prob = make_problem(129, mu_profile="layered", layer_depth_km=20.0)
