@@ -48,6 +48,8 @@ def parse():
     p.add_argument("--cpu-sample-s", type=float, default=20.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--headline-only", action="store_true",
+                   help="time only the headline solver (no FP64 comparison, e2e or CPU runs)")
     return p.parse_args()
 
 
@@ -271,13 +273,18 @@ def run_ours(args):
                                    "coarse_solve": 1})
     sim, head = timed_run(mixed_cfg, "mixed")
     clk = clocks.stop()
-    sim64, plain = timed_run(fp64_cfg, "fp64")
-    sim64.close()
-    sim64s, plain_s = timed_run(fp64s_cfg, "fp64+surface")
-    sim64s.close()
     ms_max = reduce_max(head["ms"])
     value = job_value(head)
-    plain_value = plain["yrs"] / (reduce_max(plain["ms"]) / 3.6e6)
+    if args.headline_only:
+        args.no_e2e = args.no_cpu_baseline = True
+        plain = plain_s = {"yrs": 0.0, "ms": float("nan"), "vcycles": 0, "solves": 0}
+        plain_value = None
+    else:
+        sim64, plain = timed_run(fp64_cfg, "fp64")
+        sim64.close()
+        sim64s, plain_s = timed_run(fp64s_cfg, "fp64+surface")
+        sim64s.close()
+        plain_value = plain["yrs"] / (reduce_max(plain["ms"]) / 3.6e6)
 
     # dominant kernel: level-0 smoother sweeps of the headline (FP32) hierarchy
     stream = torch.cuda.ExternalStream(sim.solver.stream_ptr())

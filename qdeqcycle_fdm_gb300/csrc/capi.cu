@@ -58,10 +58,25 @@ static double step_size(int it, double dt, const qd_rk43_params &P, double totEr
     return deltaT;
 }
 
+// Multigrid failures the device recorded since the flag was last cleared
+static int solve_flag_error(const SolveState &st) {
+    if (st.flag & 1) {
+        set_error("multigrid: residual norm is not finite (%d cycles)", st.cycles);
+        return QD_ERR_NOT_CONVERGED;
+    }
+    if (st.flag & 2) {
+        set_error("multigrid: cycle cap reached, ||r|| = %.3e > %.3e", st.delta, st.thr);
+        return QD_ERR_NOT_CONVERGED;
+    }
+    return QD_OK;
+}
+
 static int check_status(qd_solver *s) {
     QD_CUDA(cudaMemcpyAsync(s->h_status, s->d_status, sizeof(DevStatus), cudaMemcpyDeviceToHost,
                             s->stream));
-    QD_CUDA(cudaStreamSynchronize(s->stream));
+    SolveState st;
+    QD_TRY(solve_state_read(s, &st));   // synchronises the stream
+    QD_TRY(solve_flag_error(st));
     if (s->h_status->flags & (ST_NEWTON_NAN | ST_NEWTON_CAP)) {
         set_error("Newton for slip rate failed at fault node %d (flags %u)", s->h_status->bad_node,
                   s->h_status->flags);
@@ -80,17 +95,18 @@ static int reset_status(qd_solver *s) {
     return QD_OK;
 }
 
-// one stage: boundary data, elliptic solve, stress/Newton/aging law
+// one stage: boundary data, elliptic solve, stress/Newton/aging law, all
+// enqueued on the solver's stream without waiting
 static int stage(qd_solver *s, int st, double ratio) {
     QD_TRY(launch_stage_boundary(s, st, ratio, nullptr, nullptr));
-    int rc = mg_solve(s, nullptr, nullptr, nullptr);
-    if (rc != QD_OK) return rc;
+    QD_TRY(mg_solve_async(s));
     return launch_fault(s, st, 0);
 }
 
 static int rk_start(qd_solver *s) {
     s->dt = s->P.ini_dt;                                          // :1363
     QD_TRY(reset_status(s));
+    QD_TRY(solve_state_clear_flag(s));
     QD_TRY(stage(s, 1, 0.0));                                     // :1428-1437
     QD_TRY(check_status(s));
     s->started = 1;
@@ -104,6 +120,7 @@ static int rk_step(qd_solver *s) {
     if (!init) { rk_tableau(c, b, hb, a); init = true; }
     double totErr = 0.0;
     s->it = s->it + 1;
+    QD_TRY(solve_state_clear_flag(s));
     int attemptCount = 0;
     while (attemptCount < 100) {
         attemptCount++;
@@ -113,7 +130,9 @@ static int rk_step(qd_solver *s) {
         QD_TRY(launch_error(s));
         QD_CUDA(cudaMemcpyAsync(s->h_scal + 2, s->d_scal + 2, sizeof(double), cudaMemcpyDeviceToHost,
                                 s->stream));
-        QD_CUDA(cudaStreamSynchronize(s->stream));
+        SolveState sst;
+        QD_TRY(solve_state_read(s, &sst));                        // the attempt's one sync
+        QD_TRY(solve_flag_error(sst));
         totErr = s->h_scal[2];
         if (totErr < s->P.totTol) break;
         s->dt = step_size(s->it, s->dt, s->P, totErr, s->errA);
@@ -170,7 +189,10 @@ int qd_solver_create(int ni, int nk, double dh, const double *mu_equi, const dou
         cudaMalloc(&s->d_scal, 8 * sizeof(double)) != cudaSuccess ||
         cudaMallocHost(&s->h_scal, 8 * sizeof(double)) != cudaSuccess ||
         cudaMalloc(&s->d_status, sizeof(DevStatus)) != cudaSuccess ||
-        cudaMallocHost(&s->h_status, sizeof(DevStatus)) != cudaSuccess) {
+        cudaMallocHost(&s->h_status, sizeof(DevStatus)) != cudaSuccess ||
+        cudaMalloc(&s->d_solve, sizeof(SolveState)) != cudaSuccess ||
+        cudaMemset(s->d_solve, 0, sizeof(SolveState)) != cudaSuccess ||
+        cudaMallocHost(&s->h_solve, sizeof(SolveState)) != cudaSuccess) {
         set_error("qd_solver_create: CUDA set-up failed: %s", cudaGetErrorString(cudaGetLastError()));
         qd_solver_destroy(s);
         return QD_ERR_CUDA;
@@ -199,6 +221,9 @@ int qd_solver_destroy(qd_solver *s) {
     if (s->stream) cudaStreamSynchronize(s->stream);
     mg_free(s);
     fault_free(s);
+    solve_graph_free(s);
+    cudaFree(s->d_solve);
+    cudaFreeHost(s->h_solve);
     cudaFree(s->d_scal);
     cudaFreeHost(s->h_scal);
     cudaFree(s->d_status);
@@ -221,8 +246,12 @@ int qd_solver_set_options(qd_solver *s, const qd_mg_options *opt) {
 
 int qd_get_stats(qd_solver *s, qd_stats *st) {
     if (!s || !st) return QD_ERR_ARG;
-    st->solves = s->solves; st->vcycles = s->vcycles; st->attempts = s->attempts;
-    st->steps = s->steps; st->kernel_launches = s->launches;
+    SolveState ss;
+    QD_TRY(solve_state_read(s, &ss));
+    st->solves = (long long)ss.total_solves; st->vcycles = (long long)ss.total_cycles;
+    st->attempts = s->attempts;
+    // host-issued kernels plus the kernels the solve graphs ran on the device
+    st->steps = s->steps; st->kernel_launches = s->launches + (long long)ss.kernels;
     std::vector<int> it(s->nz);
     QD_CUDA(cudaMemcpy(it.data(), s->F.iters, s->nz * sizeof(int), cudaMemcpyDeviceToHost));
     long long sum = 0;

@@ -104,7 +104,7 @@ __global__ void k_build_faces(const double *__restrict__ mu, long W, int level, 
 }
 
 __global__ void k_build_dinv(int N, int K, int P, const double *cx, const double *cz,
-                             double *dinv, float *cx32, float *cz32, float *dinv32) {
+                             double *dinv, float *cx32, float *cz32, float *dinv32, double *diag) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (k >= K || j > N) return;
@@ -114,9 +114,11 @@ __global__ void k_build_dinv(int N, int K, int P, const double *cx, const double
     if (k < K - 1) cx32[c] = (float)cx[c];
     if (k >= 1 && k <= K - 2) {
         // relax_rbgs / (mu1 + mu2 + mu3 + mu4), same summation order (:794-795)
-        const double d = 1.00 / (((cx[c - 1] + cx[c]) + cz[c]) + cz[c + P]);
+        const double sum = ((cx[c - 1] + cx[c]) + cz[c]) + cz[c + P];
+        const double d = 1.00 / sum;
         dinv[c] = d;
         dinv32[c] = (float)d;
+        if (diag) diag[c] = sum;
     }
 }
 
@@ -166,26 +168,66 @@ __global__ void __launch_bounds__(BX * BY) k_residual(View<T> v, T *r, double *p
 }
 
 // FP64 residual of the level-0 field, written as the FP32 right-hand side
-// of the correction equation, with its norm (mixed precision).
+// of the correction equation, and ||r||^2 into *out (mixed precision).
+//
+// GB300 issues about two FP64 instructions per SM clock, which bounds this
+// kernel, so it spends few of them per node: the stored diagonal replaces
+// three additions; without a right-hand side the 1/h^2 scale is applied in
+// FP32 after the conversion and once to the final sum; each thread
+// accumulates RES_RPT rows before the block reduction.  The last block to
+// finish adds the per-block partials in a fixed order (the sum is
+// deterministic) and re-arms the counter for the next launch.
+static constexpr int RES_RPT = 4;
+
+template <bool HAS_F>
 __global__ void __launch_bounds__(BX * BY)
-    k_residual64_to32(View<double> v, float *f32, double *partial) {
+    k_residual64_to32(View<double> v, const double *__restrict__ diag, float *f32, double *partial,
+                      unsigned *count, double *out) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int j0 = blockIdx.y * (BY * RES_RPT) + threadIdx.y;
+    const float nih2 = -(float)v.inv_h2;
     double sq = 0.0;
-    if (j < v.N && k >= 1 && k <= v.K - 2) {
-        const long c = (long)j * v.P + k;
-        const long up = (j == 0) ? v.P : -(long)v.P;
-        const long dn = (j == v.N - 1) ? -(long)v.P : v.P;
-        const double *u = v.u;
-        const double cW = v.cx[c - 1], cE = v.cx[c], cN = v.cz[c], cS = v.cz[c + v.P];
-        const double lap = cW * u[c - 1] + cE * u[c + 1] + cN * u[c + up] + cS * u[c + dn] -
-                           (((cW + cE) + cN) + cS) * u[c];
-        const double res = (v.f ? v.f[c] : 0.0) - lap * v.inv_h2;
-        f32[c] = (float)res;
-        sq = res * res;
+    if (k >= 1 && k <= v.K - 2) {
+        const double *__restrict__ u = v.u;
+#pragma unroll
+        for (int i = 0; i < RES_RPT; i++) {
+            const int j = j0 + i * BY;
+            if (j < v.N) {
+                const long c = (long)j * v.P + k;
+                const long up = (j == 0) ? v.P : -(long)v.P;
+                const long dn = (j == v.N - 1) ? -(long)v.P : v.P;
+                const double lap = v.cx[c - 1] * u[c - 1] + v.cx[c] * u[c + 1] + v.cz[c] * u[c + up] +
+                                   v.cz[c + v.P] * u[c + dn] - diag[c] * u[c];
+                if (HAS_F) {
+                    const double res = v.f[c] - lap * v.inv_h2;
+                    f32[c] = (float)res;
+                    sq = fma(res, res, sq);
+                } else {
+                    f32[c] = (float)lap * nih2;
+                    sq = fma(lap, lap, sq);
+                }
+            }
+        }
     }
     sq = block_sum(sq);
-    if (threadIdx.x == 0 && threadIdx.y == 0) partial[blockIdx.y * gridDim.x + blockIdx.x] = sq;
+    __shared__ bool last;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const unsigned nblk = gridDim.x * gridDim.y;
+    if (tid == 0) {
+        partial[blockIdx.y * gridDim.x + blockIdx.x] = sq;
+        __threadfence();
+        last = atomicAdd(count, 1u) == nblk - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double t = 0.0;
+    for (unsigned i = tid; i < nblk; i += blockDim.x * blockDim.y) t += __ldcg(partial + i);
+    t = block_sum(t);
+    if (tid == 0) {
+        *out = HAS_F ? t : t * (v.inv_h2 * v.inv_h2);
+        *count = 0;
+    }
 }
 
 // residual norm^2 of the zero-interior guess: only the columns next to the
@@ -262,6 +304,7 @@ int mg_alloc(qd_solver *s, const double *mu_equi_host) {
         s->L64[l].cx = dalloc<double>(n, &rc);
         s->L64[l].cz = dalloc<double>(nf, &rc);
         s->L64[l].dinv = dalloc<double>(n, &rc);
+        s->L64[l].diag = l == 0 ? dalloc<double>(n, &rc) : nullptr;
         s->L32[l].u = dalloc<float>(n, &rc);
         s->L32[l].r = dalloc<float>(n, &rc);
         s->L32[l].f = dalloc<float>(n, &rc);
@@ -275,7 +318,9 @@ int mg_alloc(qd_solver *s, const double *mu_equi_host) {
     }
     s->n_partial = cdiv(s->dims[0].K, BX) * cdiv(s->dims[0].N, BY) + 64;
     s->d_partial = dalloc<double>(s->n_partial, &rc);
+    s->d_count = dalloc<unsigned>(1, &rc);
     if (rc != QD_OK) return rc;
+    QD_CUDA(cudaMemsetAsync(s->d_count, 0, sizeof(unsigned), s->stream));
 
     // coefficients from mu_equi
     const size_t nmu = (size_t)(2 * s->nx - 1) * (2 * s->nz - 1);
@@ -292,7 +337,7 @@ int mg_alloc(qd_solver *s, const double *mu_equi_host) {
         QD_LAUNCH_CHECK(s);
         k_build_dinv<<<grd, blk, 0, s->stream>>>(d.N, d.K, d.P, s->L64[l].cx, s->L64[l].cz,
                                                  s->L64[l].dinv, s->L32[l].cx, s->L32[l].cz,
-                                                 s->L32[l].dinv);
+                                                 s->L32[l].dinv, s->L64[l].diag);
         QD_LAUNCH_CHECK(s);
     }
     QD_CUDA(cudaStreamSynchronize(s->stream));
@@ -372,14 +417,18 @@ void mg_free(qd_solver *s) {
     for (int l = 0; l < QD_MAXLEV; l++) {
         cudaFree(s->L64[l].u); cudaFree(s->L64[l].r); cudaFree(s->L64[l].f);
         cudaFree(s->L64[l].cx); cudaFree(s->L64[l].cz); cudaFree(s->L64[l].dinv);
+        cudaFree(s->L64[l].diag);
         cudaFree(s->L32[l].u); cudaFree(s->L32[l].r); cudaFree(s->L32[l].f);
         cudaFree(s->L32[l].cx); cudaFree(s->L32[l].cz); cudaFree(s->L32[l].dinv);
         s->L64[l] = Level<double>();
         s->L32[l] = Level<float>();
     }
     cudaFree(s->d_partial);
+    cudaFree(s->d_count);
+    s->d_count = nullptr;
     cudaFree(s->d_ainv64);
     cudaFree(s->d_ainv32);
+    tma_cache_free(s);
     s->d_ainv64 = nullptr;
     s->d_ainv32 = nullptr;
     s->d_partial = nullptr;
@@ -403,21 +452,31 @@ static int smooth_t(qd_solver *s, Level<T> *Ls, int l, int nsweeps) {
 
 // ||r||^2 of level 0 into d_scal[slot]; for mixed precision also writes the
 // FP32 correction right-hand side.
-static int level0_norm(qd_solver *s, int to32, int slot) {
+int level0_norm(qd_solver *s, int to32, int slot) {
     View<double> v = make_view(s, s->L64, 0);
+    if (to32) {
+        dim3 blk(BX, BY), grd(cdiv(v.K, BX), cdiv(v.N, BY * RES_RPT));
+        if (v.f)
+            k_residual64_to32<true><<<grd, blk, 0, s->stream>>>(v, s->L64[0].diag, s->L32[0].f,
+                                                                 s->d_partial, s->d_count,
+                                                                 s->d_scal + slot);
+        else
+            k_residual64_to32<false><<<grd, blk, 0, s->stream>>>(v, s->L64[0].diag, s->L32[0].f,
+                                                                  s->d_partial, s->d_count,
+                                                                  s->d_scal + slot);
+        QD_LAUNCH_CHECK(s);
+        return QD_OK;
+    }
     dim3 blk(BX, BY), grd(cdiv(v.K, BX), cdiv(v.N, BY));
     const int nb = grd.x * grd.y;
-    if (to32)
-        k_residual64_to32<<<grd, blk, 0, s->stream>>>(v, s->L32[0].f, s->d_partial);
-    else
-        k_residual<double, false, true><<<grd, blk, 0, s->stream>>>(v, v.r, s->d_partial);
+    k_residual<double, false, true><<<grd, blk, 0, s->stream>>>(v, v.r, s->d_partial);
     QD_LAUNCH_CHECK(s);
     k_final_sum<<<1, 1024, 0, s->stream>>>(s->d_partial, nb, s->d_scal + slot);
     QD_LAUNCH_CHECK(s);
     return QD_OK;
 }
 
-static int r0_norm(qd_solver *s, int slot) {
+int r0_norm(qd_solver *s, int slot) {
     View<double> v = make_view(s, s->L64, 0);
     const int nb = cdiv(v.N, 256);
     k_r0<double><<<nb, 256, 0, s->stream>>>(v, s->d_partial);
@@ -432,54 +491,6 @@ static int read_scalars(qd_solver *s, int n) {
                             s->stream));
     QD_CUDA(cudaStreamSynchronize(s->stream));
     return QD_OK;
-}
-
-// multigrid() (odeSolver.cpp:652-720) on the device-resident u.
-int mg_solve(qd_solver *s, int *cycles, double *rnorm, double *r0norm) {
-    const int mixed = s->opt.precision == QD_PREC_MIXED;
-    const int rel = s->opt.tol_mode == QD_TOL_REL;
-    if (rel) QD_TRY(r0_norm(s, 1));
-    QD_TRY(level0_norm(s, mixed, 0));
-    QD_TRY(read_scalars(s, 2));
-    double r0 = rel ? sqrt(s->h_scal[1]) : 0.0;
-    double thr = rel ? (r0 > 0.0 ? s->opt.tol * r0 : s->opt.tol) : s->opt.tol;
-    double delta = sqrt(s->h_scal[0]);
-    int it = 0;
-    int rc = QD_OK;
-    while (!(delta <= thr)) {
-        if (isnan(delta) || isinf(delta)) {
-            rc = QD_ERR_NOT_CONVERGED;
-            set_error("multigrid: residual norm is %f after %d cycles", delta, it);
-            break;
-        }
-        if (s->opt.max_cycles > 0 && it >= s->opt.max_cycles) {
-            rc = QD_ERR_NOT_CONVERGED;
-            set_error("multigrid: %d cycles, ||r|| = %.3e > %.3e", it, delta, thr);
-            break;
-        }
-        if (mixed) {
-            QD_TRY(vcycle32_into64(s));            // FP32 cycle on A e = r, then u += e
-            QD_TRY(level0_norm(s, 1, 0));          // FP64 residual -> FP32 rhs, norm
-        } else {
-            int nb = 0;
-            QD_TRY(vcycle64_norm(s, &nb));         // the last kernel leaves norm partials
-            if (nb > 0) {
-                k_final_sum<<<1, 1024, 0, s->stream>>>(s->d_partial, nb, s->d_scal);
-                QD_LAUNCH_CHECK(s);
-            } else {
-                QD_TRY(level0_norm(s, 0, 0));
-            }
-        }
-        QD_TRY(read_scalars(s, 1));
-        delta = sqrt(s->h_scal[0]);
-        it++;
-    }
-    s->solves++;
-    s->vcycles += it;
-    if (cycles) *cycles = it;
-    if (rnorm) *rnorm = delta;
-    if (r0norm) *r0norm = r0;
-    return rc;
 }
 
 // nsweeps red+black sweeps of the level-`level` field of the hierarchy the

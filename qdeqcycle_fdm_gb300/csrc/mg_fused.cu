@@ -20,6 +20,7 @@
 // never reads u (the reference zeroes e2 in restriction_kernel and then
 // reads it back).
 #include <algorithm>
+#include <cstring>
 #include <mutex>
 #include <utility>
 #include <vector>
@@ -86,22 +87,21 @@ struct TV {                       // one tail level as the kernel sees it
     T h2, inv_h2;
 };
 
+// one colour, warp per row and lane per node of that colour (a tail level
+// has at most 65 columns, so one pass of a warp covers a row)
 template <typename T>
 __device__ void tv_halfsweep(const TV<T> &g, int color) {
-    const int HC = (g.K - 1) / 2;  // colour-compacted interior columns per row
-    const int n = g.N * HC;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const int j = i / HC, m = i - j * HC;
-        const int k = 2 * m + 1 + ((j + 1 + color) & 1);
-        if (k > g.K - 2) continue;
-        const int c = j * g.K + k, cc = j * g.CP + k;
+    for (int j = TWARP; j < g.N; j += TNWARP) {
         const int up = (j == 0) ? g.K : -g.K;
         const int dn = (j == g.N - 1) ? -g.K : g.K;
-        // the moduli may live in shared or in global memory: generic loads
-        T acc = g.cx[cc - 1] * g.u[c - 1] + g.cx[cc] * g.u[c + 1] + g.cz[cc] * g.u[c + up] +
-                g.cz[cc + g.CP] * g.u[c + dn];
-        acc -= g.h2 * g.f[c];
-        g.u[c] = g.dinv[cc] * acc;
+        for (int k = 1 + ((j + 1 + color) & 1) + 2 * TLANE; k <= g.K - 2; k += 64) {
+            const int c = j * g.K + k, cc = j * g.CP + k;
+            // the moduli may live in shared or in global memory: generic loads
+            T acc = g.cx[cc - 1] * g.u[c - 1] + g.cx[cc] * g.u[c + 1] + g.cz[cc] * g.u[c + up] +
+                    g.cz[cc + g.CP] * g.u[c + dn];
+            acc -= g.h2 * g.f[c];
+            g.u[c] = g.dinv[cc] * acc;
+        }
     }
 }
 
@@ -127,7 +127,7 @@ static size_t tail_smem_bytes(const qd_solver *s, int l0, int coef_smem) {
 
 template <typename T>
 __global__ void __launch_bounds__(NT_TAIL) k_tail(TailArgs<T> a) {
-    extern __shared__ __align__(16) unsigned char smem[];
+    extern __shared__ __align__(128) unsigned char smem[];
     const TailLevels &p = a.p;
     __shared__ TV<T> V[QD_MAXLEV];   // per-level views, read by every thread
     T *ptr = reinterpret_cast<T *>(smem);
@@ -143,15 +143,16 @@ __global__ void __launch_bounds__(NT_TAIL) k_tail(TailArgs<T> a) {
             T *cx = ptr; ptr += n;
             T *cz = ptr; ptr += n + g.K;
             T *dv = ptr; ptr += n;
-            for (int i = threadIdx.x; i < n; i += blockDim.x) {
-                const int j = i / g.K, k = i - j * g.K;
-                cx[i] = g.cx[(long)j * g.P + k];
-                dv[i] = g.dinv[(long)j * g.P + k];
-            }
-            for (int i = threadIdx.x; i < n + g.K; i += blockDim.x) {
-                const int j = i / g.K, k = i - j * g.K;
-                cz[i] = g.cz[(long)j * g.P + k];
-            }
+            for (int j = TWARP; j <= g.N; j += TNWARP)
+                for (int k = TLANE; k < g.K; k += 32) {
+                    const long gi = (long)j * g.P + k;
+                    const int i = j * g.K + k;
+                    cz[i] = g.cz[gi];
+                    if (j < g.N) {
+                        cx[i] = g.cx[gi];
+                        dv[i] = g.dinv[gi];
+                    }
+                }
             v.cx = cx; v.cz = cz; v.dinv = dv; v.CP = g.K;
         } else {
             v.cx = g.cx; v.cz = g.cz; v.dinv = g.dinv; v.CP = g.P;
@@ -161,10 +162,8 @@ __global__ void __launch_bounds__(NT_TAIL) k_tail(TailArgs<T> a) {
     __syncthreads();
     {   // right-hand side of the first tail level
         const LvArgs<T> &g = a.L[p.l0];
-        for (int i = threadIdx.x; i < g.N * g.K; i += blockDim.x) {
-            const int j = i / g.K, k = i - j * g.K;
-            V[p.l0].f[i] = g.f[(long)j * g.P + k];
-        }
+        for (int j = TWARP; j < g.N; j += TNWARP)
+            for (int k = TLANE; k < g.K; k += 32) V[p.l0].f[j * g.K + k] = g.f[(long)j * g.P + k];
     }
     for (int l = p.l0; l < p.nlev; l++) {
         const TV<T> &g = V[l];
@@ -190,55 +189,57 @@ __global__ void __launch_bounds__(NT_TAIL) k_tail(TailArgs<T> a) {
             break;
         }
         tv_smooth(g, p.nu_pre);
-        for (int i = threadIdx.x; i < g.N * g.K; i += blockDim.x) {
-            const int j = i / g.K, k = i - j * g.K;
-            if (k < 1 || k > g.K - 2) continue;
-            const int cc = j * g.CP + k;
+        for (int j = TWARP; j < g.N; j += TNWARP) {
             const int up = (j == 0) ? g.K : -g.K;
             const int dn = (j == g.N - 1) ? -g.K : g.K;
-            const T cW = g.cx[cc - 1], cE = g.cx[cc], cN = g.cz[cc], cS = g.cz[cc + g.CP];
-            const T lap = cW * g.u[i - 1] + cE * g.u[i + 1] + cN * g.u[i + up] + cS * g.u[i + dn] -
-                          (((cW + cE) + cN) + cS) * g.u[i];
-            g.r[i] = g.f[i] - lap * g.inv_h2;
+            for (int k = 1 + TLANE; k <= g.K - 2; k += 32) {
+                const int i = j * g.K + k, cc = j * g.CP + k;
+                const T cW = g.cx[cc - 1], cE = g.cx[cc], cN = g.cz[cc], cS = g.cz[cc + g.CP];
+                const T lap = cW * g.u[i - 1] + cE * g.u[i + 1] + cN * g.u[i + up] + cS * g.u[i + dn] -
+                              (((cW + cE) + cN) + cS) * g.u[i];
+                g.r[i] = g.f[i] - lap * g.inv_h2;
+            }
         }
         __syncthreads();
         const TV<T> &cl = V[l + 1];
-        for (int i = threadIdx.x; i < cl.N * cl.K; i += blockDim.x) {
-            const int j = i / cl.K, k = i - j * cl.K;
-            if (k < 1 || k > cl.K - 2) continue;
+        for (int j = TWARP; j < cl.N; j += TNWARP) {
             const int rn = (j == 0) ? 2 * j + 1 : 2 * j - 1;
             const int rs = (j == cl.N - 1) ? 2 * j - 1 : 2 * j + 1;
-            const T *c0 = g.r + (2 * j) * g.K + 2 * k;
-            const T *cn = g.r + rn * g.K + 2 * k;
-            const T *cs = g.r + rs * g.K + 2 * k;
-            cl.f[i] = (T)0.06250 * ((T)4.0 * c0[0] + (T)2.0 * c0[-1] + (T)2.0 * c0[1] + (T)2.0 * cn[0] +
-                                    (T)2.0 * cs[0] + cn[-1] + cn[1] + cs[-1] + cs[1]);
+            for (int k = 1 + TLANE; k <= cl.K - 2; k += 32) {
+                const T *c0 = g.r + (2 * j) * g.K + 2 * k;
+                const T *cn = g.r + rn * g.K + 2 * k;
+                const T *cs = g.r + rs * g.K + 2 * k;
+                cl.f[j * cl.K + k] = (T)0.06250 * ((T)4.0 * c0[0] + (T)2.0 * c0[-1] + (T)2.0 * c0[1] +
+                                                   (T)2.0 * cn[0] + (T)2.0 * cs[0] + cn[-1] + cn[1] +
+                                                   cs[-1] + cs[1]);
+            }
         }
         __syncthreads();
     }
     for (int l = p.nlev - 2; l >= p.l0; l--) {
         const TV<T> &g = V[l];
         const TV<T> &cl = V[l + 1];
-        for (int i = threadIdx.x; i < g.N * g.K; i += blockDim.x) {
-            const int jf = i / g.K, kf = i - jf * g.K;
-            if (jf >= g.N - 1 + p.surface || kf < 1 || kf > g.K - 2) continue;
-            const T *e = cl.u + (jf >> 1) * cl.K + (kf >> 1);
-            T add;
-            if (!(jf & 1))
-                add = (kf & 1) ? (T)0.5 * (e[0] + e[1]) : e[0];
-            else
-                add = (kf & 1) ? (T)0.25 * (e[0] + e[1] + e[cl.K] + e[cl.K + 1]) : (T)0.5 * (e[0] + e[cl.K]);
-            g.u[i] += add;
+        const int jmax = g.N - 1 + p.surface;
+        for (int jf = TWARP; jf < jmax; jf += TNWARP) {
+            const T *er = cl.u + (jf >> 1) * cl.K;
+            for (int kf = 1 + TLANE; kf <= g.K - 2; kf += 32) {
+                const T *e = er + (kf >> 1);
+                T add;
+                if (!(jf & 1))
+                    add = (kf & 1) ? (T)0.5 * (e[0] + e[1]) : e[0];
+                else
+                    add = (kf & 1) ? (T)0.25 * (e[0] + e[1] + e[cl.K] + e[cl.K + 1])
+                                   : (T)0.5 * (e[0] + e[cl.K]);
+                g.u[jf * g.K + kf] += add;
+            }
         }
         __syncthreads();
         tv_smooth(g, p.nu_post);
     }
     {   // the first tail level's correction, for k_up of the level above
         const LvArgs<T> &g = a.L[p.l0];
-        for (int i = threadIdx.x; i < g.N * g.K; i += blockDim.x) {
-            const int j = i / g.K, k = i - j * g.K;
-            g.u[(long)j * g.P + k] = V[p.l0].u[i];
-        }
+        for (int j = TWARP; j < g.N; j += TNWARP)
+            for (int k = TLANE; k < g.K; k += 32) g.u[(long)j * g.P + k] = V[p.l0].u[j * g.K + k];
     }
 }
 
@@ -292,23 +293,64 @@ static int set_smem(K kernel, size_t bytes) {
     return QD_OK;
 }
 
+// tensor maps of a level's arrays for a W x BH box, cached per solver
+struct TmaCache {
+    struct Entry {
+        int level, fp64, W, BH;
+        TileMaps maps;
+    };
+    std::vector<Entry> v;
+};
+
+template <typename T>
+static int tile_maps(qd_solver *s, Level<T> *Ls, int l, int W, int BH, const TileMaps **out) {
+    if (!s->tma_cache) s->tma_cache = new TmaCache();
+    TmaCache *tc = static_cast<TmaCache *>(s->tma_cache);
+    const int fp64 = sizeof(T) == 8;
+    for (const auto &e : tc->v)
+        if (e.level == l && e.fp64 == fp64 && e.W == W && e.BH == BH) {
+            *out = &e.maps;
+            return QD_OK;
+        }
+    TmaCache::Entry e;
+    memset(&e, 0, sizeof(e));
+    e.level = l; e.fp64 = fp64; e.W = W; e.BH = BH;
+    e.maps.W = W; e.maps.BH = BH;
+    const LevelDims &d = s->dims[l];
+    QD_TRY(make_tensor_map_2d(&e.maps.u, Ls[l].u, fp64, d.K, d.N, d.P, W, BH));
+    QD_TRY(make_tensor_map_2d(&e.maps.cx, Ls[l].cx, fp64, d.K, d.N, d.P, W, BH));
+    QD_TRY(make_tensor_map_2d(&e.maps.cz, Ls[l].cz, fp64, d.K, d.N + 1, d.P, W, BH + 1));
+    if (Ls[l].f) QD_TRY(make_tensor_map_2d(&e.maps.f, Ls[l].f, fp64, d.K, d.N, d.P, W, BH));
+    if (fp64) QD_TRY(make_tensor_map_2d(&e.maps.dv, Ls[l].dinv, fp64, d.K, d.N, d.P, W, BH));
+    tc->v.push_back(e);
+    *out = &tc->v.back().maps;
+    return QD_OK;
+}
+
+static int round_up(int x, int a) { return (x + a - 1) / a * a; }
+
 template <typename T>
 static int launch_down(qd_solver *s, Level<T> *Ls, int l, int S, int zero_u) {
     const LvArgs<T> g = lv(s, Ls, l), c = lv(s, Ls, l + 1);
     int TE = tile_edge<T>(g.N);
     int CH = TE / 2, CW = (sizeof(T) == 4 ? TE : 2 * TE) / 2;
     const int ntj = std::max(1, (c.N - 1) / CH), ntk = std::max(1, (c.K - 1) / CW);
-    // largest tile: the last one absorbs the remainder
+    // largest tile: the last one absorbs the remainder; the box covers it
+    // plus the column rounding of the aligned origin
     const int maxCH = c.N - (ntj - 1) * CH, maxCW = c.K - (ntk - 1) * CW;
-    const int LR = std::min(g.N, 2 * maxCH + 2 * S + 3), LC = std::min(g.K, 2 * maxCW + 2 * S + 3);
+    const int A = TileCfg<T>::kAlign;
+    const int BH = 2 * maxCH + 2 * S + 3, W = round_up(2 * maxCW + 2 * S + 3 + A - 1, A);
     const bool has_f = (g.f != nullptr) || sizeof(T) == 4;
-    const size_t smem = sizeof(T) * tile_elems<T>(LR, LC, has_f);
-    if (smem > smem_limit()) {
-        set_error("k_down tile %dx%d needs %zu B of shared memory", LR, LC, smem);
+    const size_t smem = tile_bytes<T>(BH, W, has_f) + kSmemSlack;
+    if (BH > 256 || W > 256 || smem > smem_limit()) {
+        set_error("k_down tile %dx%d (%zu B of shared memory) exceeds the TMA box or smem", BH, W, smem);
         return QD_ERR_ARG;
     }
+    const TileMaps *maps = nullptr;
+    QD_TRY(tile_maps<T>(s, Ls, l, W, BH, &maps));
     QD_TRY(set_smem(k_down<T>, smem));
-    k_down<T><<<dim3(ntk, ntj), NT, smem, s->stream>>>(g, c, CH, CW, ntj, ntk, S, zero_u);
+    k_down<T><<<dim3(ntk, ntj), NT, smem, s->stream>>>(g, c, *maps, CH, CW, ntj, ntk, S, zero_u,
+                                                       &s->d_status->flags);
     QD_LAUNCH_CHECK(s);
     return QD_OK;
 }
@@ -323,24 +365,76 @@ static int launch_up(qd_solver *s, Level<T> *Ls, int l, int S, int prolong, int 
     const int ntj = std::max(1, (g.N - 1) / TH), ntk = std::max(1, (g.K - 1) / TW);
     const int maxTH = g.N - (ntj - 1) * TH, maxTW = g.K - (ntk - 1) * TW;
     const int R1 = MODE == 1 ? 1 : 0;
-    const int LR = std::min(g.N, maxTH + 2 * (S + R1)), LC = std::min(g.K, maxTW + 2 * (S + R1));
-    size_t smem = sizeof(T) * tile_elems<T>(LR, LC, g.f != nullptr);
-    if (prolong) smem += sizeof(T) * (size_t)(LR / 2 + 2) * (LC / 2 + 2);
-    if (smem > smem_limit()) {
-        set_error("k_up tile %dx%d needs %zu B of shared memory", LR, LC, smem);
+    const int A = TileCfg<T>::kAlign;
+    const int BH = maxTH + 2 * (S + R1), W = round_up(maxTW + 2 * (S + R1) + A - 1, A);
+    size_t smem = tile_bytes<T>(BH, W, g.f != nullptr);
+    if (prolong) smem += sizeof(T) * (size_t)(BH / 2 + 2) * (W / 2 + 2);
+    smem += kSmemSlack;
+    if (BH > 256 || W > 256 || smem > smem_limit()) {
+        set_error("k_up tile %dx%d (%zu B of shared memory) exceeds the TMA box or smem", BH, W, smem);
         return QD_ERR_ARG;
     }
     if (MODE == 1 && ntj * ntk > s->n_partial) {
         set_error("too many tiles for the partial-sum buffer");
         return QD_ERR_ARG;
     }
+    const TileMaps *maps = nullptr;
+    QD_TRY(tile_maps<T>(s, Ls, l, W, BH, &maps));
     QD_TRY(set_smem(k_up<T, MODE>, smem));
-    k_up<T, MODE><<<dim3(ntk, ntj), NT, smem, s->stream>>>(g, c, TH, TW, ntj, ntk, S, prolong,
+    k_up<T, MODE><<<dim3(ntk, ntj), NT, smem, s->stream>>>(g, c, *maps, TH, TW, ntj, ntk, S, prolong,
                                                          s->opt.surface_prolong, zero_u, s->d_partial,
-                                                         u64, P64);
+                                                         u64, P64, &s->d_status->flags);
     QD_LAUNCH_CHECK(s);
     if (nblocks) *nblocks = ntj * ntk;
     return QD_OK;
+}
+
+// host side of tma.cuh: cuTensorMapEncodeTiled through the runtime's
+// driver entry point (no link against libcuda)
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+int make_tensor_map_2d(CUtensorMap *map, const void *base, bool fp64, int width, int height,
+                       int pitch, int box_w, int box_h) {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        QD_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                                 &q));
+        if (!p || q != cudaDriverEntryPointSuccess) {
+            set_error("cuTensorMapEncodeTiled is not available from the driver");
+            return QD_ERR_CUDA;
+        }
+        fn = (EncodeTiledFn)p;
+    }
+    const size_t esz = fp64 ? 8 : 4;
+    if (!base || ((uintptr_t)base & 15) || (pitch * esz) % 16 || (box_w * esz) % 16 || box_w < 1 ||
+        box_w > 256 || box_h < 1 || box_h > 256 || width < 1 || height < 1) {
+        set_error("tensor map %dx%d pitch %d box %dx%d violates the TMA rules", width, height, pitch,
+                  box_w, box_h);
+        return QD_ERR_ARG;
+    }
+    const cuuint64_t dims[2] = {(cuuint64_t)width, (cuuint64_t)height};
+    const cuuint64_t strides[1] = {(cuuint64_t)pitch * esz};
+    const cuuint32_t box[2] = {(cuuint32_t)box_w, (cuuint32_t)box_h};
+    const cuuint32_t es[2] = {1, 1};
+    const CUresult r = fn(map, fp64 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+                          const_cast<void *>(base), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+        return QD_ERR_CUDA;
+    }
+    return QD_OK;
+}
+
+void tma_cache_free(qd_solver *s) {
+    delete static_cast<TmaCache *>(s->tma_cache);
+    s->tma_cache = nullptr;
 }
 
 // nsweeps red+black sweeps on level l as tile passes of at most SMAX

@@ -1,0 +1,267 @@
+// mg_graph.cu -- multigrid() (odeSolver.cpp:652-720) as one CUDA graph.
+//
+// The reference reads the residual norm back to the host after every
+// V-cycle (a blocking cublasDnrm2, :694,700).  Here the whole solve is one
+// graph launch:
+//
+//   prologue   [||r0|| for the relative tolerance] -> ||r|| of the guess
+//              -> k_solve_begin: threshold, first "continue?" decision
+//   WHILE      body: one V-cycle -> ||r|| -> k_solve_check: next decision
+//
+// The loop condition is a graph conditional handle that the check kernels
+// set on the device (cudaGraphSetConditional), so no host round trip
+// happens inside a solve.  The loop stops when ||r|| <= threshold, when the
+// cycle cap is reached or when the norm is not finite; the last two leave a
+// flag the host reads with the next result it fetches.  The graph is built
+// from the same launch code as an eager V-cycle (stream capture into the
+// loop body) and rebuilt when the multigrid options change.
+#include <math.h>
+#include <stdlib.h>
+
+#include <vector>
+
+#include "qdeq_internal.cuh"
+
+namespace qd {
+
+// declared in mg.cu
+int level0_norm(qd_solver *s, int to32, int slot);
+int r0_norm(qd_solver *s, int slot);
+__global__ void k_final_sum(const double *partial, int n, double *out);
+
+struct SolveGraph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    qd_mg_options opt;
+};
+
+// n_kernels: kernels of the prologue, this one included; in_graph: set the
+// loop condition (otherwise the host reads st->go)
+__global__ void k_solve_begin(cudaGraphConditionalHandle h, const double *scal, SolveState *st,
+                              int rel, double tol, int n_kernels, int in_graph) {
+    const double r0 = rel ? sqrt(scal[1]) : 0.0;
+    const double thr = rel ? (r0 > 0.0 ? tol * r0 : tol) : tol;
+    const double delta = sqrt(scal[0]);
+    st->r0 = r0;
+    st->thr = thr;
+    st->delta = delta;
+    st->cycles = 0;
+    st->total_solves++;
+    st->kernels += (unsigned long long)n_kernels;
+    int go = !(delta <= thr);
+    if (go && !isfinite(delta)) {
+        st->flag |= 1;
+        go = 0;
+    }
+    st->go = go;
+    if (in_graph) cudaGraphSetConditional(h, go ? 1u : 0u);
+}
+
+// n_kernels: kernels of one loop iteration, this one included
+__global__ void k_solve_check(cudaGraphConditionalHandle h, const double *scal, SolveState *st,
+                              int max_cycles, int n_kernels, int in_graph) {
+    const double delta = sqrt(scal[0]);
+    st->delta = delta;
+    st->cycles++;
+    st->total_cycles++;
+    st->kernels += (unsigned long long)n_kernels;
+    int go = !(delta <= st->thr);
+    if (go && !isfinite(delta)) {
+        st->flag |= 1;
+        go = 0;
+    }
+    if (go && max_cycles > 0 && st->cycles >= max_cycles) {
+        st->flag |= 2;
+        go = 0;
+    }
+    st->go = go;
+    if (in_graph) cudaGraphSetConditional(h, go ? 1u : 0u);
+}
+
+static bool same_opts(const qd_mg_options &a, const qd_mg_options &b) {
+    return a.n_levels == b.n_levels && a.nu_pre == b.nu_pre && a.nu_post == b.nu_post &&
+           a.nu_coarse == b.nu_coarse && a.tol_mode == b.tol_mode && a.tol == b.tol &&
+           a.max_cycles == b.max_cycles && a.precision == b.precision &&
+           a.surface_prolong == b.surface_prolong && a.coarse_solve == b.coarse_solve;
+}
+
+void solve_graph_free(qd_solver *s) {
+    SolveGraph *g = static_cast<SolveGraph *>(s->solve_graph);
+    if (!g) return;
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    delete g;
+    s->solve_graph = nullptr;
+}
+
+// the body of one loop iteration: a V-cycle and the norm of the new residual
+static int capture_cycle(qd_solver *s) {
+    if (s->opt.precision == QD_PREC_MIXED) {
+        QD_TRY(vcycle32_into64(s));          // FP32 cycle on A e = r, then u += e
+        QD_TRY(level0_norm(s, 1, 0));        // FP64 residual -> FP32 rhs, norm
+    } else {
+        int nb = 0;
+        QD_TRY(vcycle64_norm(s, &nb));       // the last kernel leaves norm partials
+        if (nb > 0) {
+            k_final_sum<<<1, 1024, 0, s->stream>>>(s->d_partial, nb, s->d_scal);
+            QD_LAUNCH_CHECK(s);
+        } else {
+            QD_TRY(level0_norm(s, 0, 0));
+        }
+    }
+    return QD_OK;
+}
+
+static int end_capture(qd_solver *s, cudaGraph_t *g, int rc) {
+    cudaGraph_t out = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(s->stream, &out);
+    if (rc != QD_OK) return rc;
+    QD_CUDA(e);
+    if (g) *g = out;
+    return QD_OK;
+}
+
+static int build(qd_solver *s, SolveGraph *sg) {
+    const int rel = s->opt.tol_mode == QD_TOL_REL;
+    QD_CUDA(cudaGraphCreate(&sg->graph, 0));
+    cudaGraphConditionalHandle h;
+    QD_CUDA(cudaGraphConditionalHandleCreate(&h, sg->graph, 0, cudaGraphCondAssignDefault));
+    // prologue, captured into the top-level graph
+    // captured launches are counted on the device each time they run, so the
+    // host counter is restored after each capture
+    const long long launches0 = s->launches;
+    QD_CUDA(cudaStreamBeginCaptureToGraph(s->stream, sg->graph, nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeRelaxed));
+    int rc = QD_OK;
+    if (rel) rc = r0_norm(s, 1);
+    if (rc == QD_OK) rc = level0_norm(s, s->opt.precision == QD_PREC_MIXED, 0);
+    if (rc == QD_OK) {
+        const int n = (int)(s->launches - launches0) + 1;
+        k_solve_begin<<<1, 1, 0, s->stream>>>(h, s->d_scal, s->d_solve, rel, s->opt.tol, n, 1);
+        if (cudaPeekAtLastError() != cudaSuccess) rc = QD_ERR_CUDA;
+    }
+    s->launches = launches0;
+    QD_TRY(end_capture(s, nullptr, rc));
+    // the prologue is a chain: its one leaf is the loop's dependency
+    size_t n = 0;
+    QD_CUDA(cudaGraphGetNodes(sg->graph, nullptr, &n));
+    std::vector<cudaGraphNode_t> nodes(n);
+    QD_CUDA(cudaGraphGetNodes(sg->graph, nodes.data(), &n));
+    cudaGraphNode_t leaf = nullptr;
+    for (auto nd : nodes) {
+        size_t nout = 0;
+        QD_CUDA(cudaGraphNodeGetDependentNodes(nd, nullptr, nullptr, &nout));
+        if (nout == 0) leaf = nd;
+    }
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t loop;
+    QD_CUDA(cudaGraphAddNode(&loop, sg->graph, leaf ? &leaf : nullptr, nullptr, leaf ? 1 : 0, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    QD_CUDA(cudaStreamBeginCaptureToGraph(s->stream, body, nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeRelaxed));
+    rc = capture_cycle(s);
+    if (rc == QD_OK) {
+        const int n = (int)(s->launches - launches0) + 1;
+        k_solve_check<<<1, 1, 0, s->stream>>>(h, s->d_scal, s->d_solve, s->opt.max_cycles, n, 1);
+        if (cudaPeekAtLastError() != cudaSuccess) rc = QD_ERR_CUDA;
+    }
+    s->launches = launches0;
+    QD_TRY(end_capture(s, nullptr, rc));
+    QD_CUDA(cudaGraphInstantiate(&sg->exec, sg->graph, 0));
+    sg->opt = s->opt;
+    return QD_OK;
+}
+
+// The same solve with the loop on the host: every kernel is an ordinary
+// stream launch and the host reads the decision after each cycle.  Chosen
+// by QDEQ_EAGER_SOLVE=1, for per-kernel profilers that do not descend into
+// conditional graph nodes; the kernels and their order are the graph's.
+static bool eager_solve() {
+    static const bool on = [] {
+        const char *e = getenv("QDEQ_EAGER_SOLVE");
+        return e && e[0] == '1';
+    }();
+    return on;
+}
+
+static int solve_eager(qd_solver *s) {
+    const int rel = s->opt.tol_mode == QD_TOL_REL;
+    const long long launches0 = s->launches;
+    if (rel) QD_TRY(r0_norm(s, 1));
+    QD_TRY(level0_norm(s, s->opt.precision == QD_PREC_MIXED, 0));
+    k_solve_begin<<<1, 1, 0, s->stream>>>(0, s->d_scal, s->d_solve, rel, s->opt.tol,
+                                          (int)(s->launches - launches0) + 1, 0);
+    QD_LAUNCH_CHECK(s);
+    s->launches = launches0;       // counted on the device, as in the graph
+    for (;;) {
+        SolveState st;
+        QD_TRY(solve_state_read(s, &st));
+        if (!st.go) return QD_OK;
+        QD_TRY(capture_cycle(s));
+        k_solve_check<<<1, 1, 0, s->stream>>>(0, s->d_scal, s->d_solve, s->opt.max_cycles,
+                                              (int)(s->launches - launches0) + 1, 0);
+        QD_LAUNCH_CHECK(s);
+        s->launches = launches0;
+    }
+}
+
+// Enqueue one solve on the solver's stream (no host synchronisation).
+int mg_solve_async(qd_solver *s) {
+    if (eager_solve()) return solve_eager(s);
+    SolveGraph *sg = static_cast<SolveGraph *>(s->solve_graph);
+    if (sg && !same_opts(sg->opt, s->opt)) {
+        solve_graph_free(s);
+        sg = nullptr;
+    }
+    if (!sg) {
+        sg = new SolveGraph();
+        s->solve_graph = sg;
+        const int rc = build(s, sg);
+        if (rc != QD_OK) {
+            solve_graph_free(s);
+            return rc;
+        }
+    }
+    QD_CUDA(cudaGraphLaunch(sg->exec, s->stream));
+    return QD_OK;
+}
+
+// Fetch the solve state (synchronises the stream).
+int solve_state_read(qd_solver *s, SolveState *out) {
+    QD_CUDA(cudaMemcpyAsync(s->h_solve, s->d_solve, sizeof(SolveState), cudaMemcpyDeviceToHost,
+                            s->stream));
+    QD_CUDA(cudaStreamSynchronize(s->stream));
+    *out = *s->h_solve;
+    return QD_OK;
+}
+
+int solve_state_clear_flag(qd_solver *s) {
+    QD_CUDA(cudaMemsetAsync(&s->d_solve->flag, 0, sizeof(int), s->stream));
+    return QD_OK;
+}
+
+// multigrid(): one solve, then its outcome
+int mg_solve(qd_solver *s, int *cycles, double *rnorm, double *r0norm) {
+    QD_TRY(solve_state_clear_flag(s));
+    QD_TRY(mg_solve_async(s));
+    SolveState st;
+    QD_TRY(solve_state_read(s, &st));
+    if (cycles) *cycles = st.cycles;
+    if (rnorm) *rnorm = st.delta;
+    if (r0norm) *r0norm = st.r0;
+    if (st.flag & 1) {
+        set_error("multigrid: residual norm is %f after %d cycles", st.delta, st.cycles);
+        return QD_ERR_NOT_CONVERGED;
+    }
+    if (st.flag & 2) {
+        set_error("multigrid: %d cycles, ||r|| = %.3e > %.3e", st.cycles, st.delta, st.thr);
+        return QD_ERR_NOT_CONVERGED;
+    }
+    return QD_OK;
+}
+
+}  // namespace qd

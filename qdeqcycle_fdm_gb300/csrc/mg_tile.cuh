@@ -1,17 +1,21 @@
 // mg_tile.cuh -- shared-memory tile kernels of the fused V-cycle (included by
 // mg_fused.cu).
 //
-// A CTA of NT threads stages one tile (core + halo) of u, the face moduli and
-// f.  Loops over the tile are warp-per-row, lane-per-column, so rows and
-// columns come straight from the thread index.  One colour of red-black
-// Gauss-Seidel per half-sweep; a node is updated only where its four
-// neighbours lie in the tile, and the halo is as wide as the number of
+// A CTA of NT threads stages one tile (core + halo) of u, the face moduli
+// and f with TMA 2-D bulk loads (tma.cuh): one thread issues the copies for
+// all arrays against one mbarrier.  The tile origin column is rounded down to
+// a 16-byte boundary and every array is a box of BH x W elements with row
+// pitch W.  Loops over the tile are warp-per-row, lane-per-column.  One colour
+// of red-black Gauss-Seidel per half-sweep; a node is updated only where its
+// four neighbours lie in the tile, and the halo is as wide as the number of
 // half-sweeps, so the core ends exact.
 //
 // FP64 tiles stage 1/diag (a double division costs ~30 instructions on
 // GB300's FP64 pipe); FP32 tiles recompute it with a correctly rounded
 // reciprocal, which frees shared memory for two CTAs per SM.
 #pragma once
+
+#include "tma.cuh"
 
 namespace qd {
 
@@ -22,58 +26,92 @@ namespace qd {
 template <typename T>
 struct TileCfg {
     static constexpr bool kDinv = sizeof(T) == 8;
+    static constexpr int kAlign = 16 / (int)sizeof(T);   // elements per 16 bytes
 };
 
 __device__ __forceinline__ float recip(float x) { return __frcp_rn(x); }
 __device__ __forceinline__ double recip(double x) { return 1.0 / x; }
 
+// tensor maps of one level's arrays, boxes of W x BH (cz: W x BH+1)
+struct TileMaps {
+    CUtensorMap u, f, cx, cz, dv;
+    int W, BH;
+};
+
 template <typename T>
 struct STile {
     T *u, *f, *cx, *cz, *dv;
-    int jL0, kL0, LR, LC;
+    int jL0, kL0;    // global row / column of smem (0,0); kL0 is 16-byte aligned
+    int LR, LC;      // rows / columns of the tile that lie inside the grid
+    int W;           // smem row pitch (the TMA box width)
 };
 
-// layout: u | cx | cz (LR+1 rows) | f (if has_f) | dv (FP64 only)
+__host__ __device__ inline size_t pad128(size_t bytes) { return (bytes + 127) & ~(size_t)127; }
+
+// TMA destinations must be 128-byte aligned in the shared window; the
+// dynamic allocation carries 128 spare bytes so the base can be rounded up
+static constexpr size_t kSmemSlack = 128;
+__device__ __forceinline__ unsigned char *align_smem128(unsigned char *p) {
+    return p + ((128u - (smem_u32(p) & 127u)) & 127u);
+}
+
+// layout: u | cx | cz (BH+1 rows) | f (if has_f) | dv (FP64 only), each
+// 128-byte aligned
 template <typename T>
-__device__ __forceinline__ STile<T> carve(unsigned char *raw, int jL0, int kL0, int LR, int LC,
-                                          bool has_f) {
+__host__ __device__ inline size_t tile_bytes(int BH, int W, bool has_f) {
+    const size_t a = pad128(sizeof(T) * (size_t)BH * W), cz = pad128(sizeof(T) * (size_t)(BH + 1) * W);
+    return 2 * a + cz + (has_f ? a : 0) + (TileCfg<T>::kDinv ? a : 0);
+}
+
+template <typename T>
+__device__ __forceinline__ STile<T> carve(unsigned char *raw, int jL0, int kL0, int LR, int LC, int BH,
+                                          int W, bool has_f) {
     STile<T> t;
-    t.jL0 = jL0; t.kL0 = kL0; t.LR = LR; t.LC = LC;
-    const int n = LR * LC;
-    T *p = reinterpret_cast<T *>(raw);
-    t.u = p; p += n;
-    t.cx = p; p += n;
-    t.cz = p; p += n + LC;
-    t.f = has_f ? p : nullptr;
-    if (has_f) p += n;
-    t.dv = TileCfg<T>::kDinv ? p : nullptr;
+    t.jL0 = jL0; t.kL0 = kL0; t.LR = LR; t.LC = LC; t.W = W;
+    const size_t a = pad128(sizeof(T) * (size_t)BH * W), cz = pad128(sizeof(T) * (size_t)(BH + 1) * W);
+    unsigned char *p = raw;
+    t.u = reinterpret_cast<T *>(p); p += a;
+    t.cx = reinterpret_cast<T *>(p); p += a;
+    t.cz = reinterpret_cast<T *>(p); p += cz;
+    t.f = has_f ? reinterpret_cast<T *>(p) : nullptr;
+    if (has_f) p += a;
+    t.dv = TileCfg<T>::kDinv ? reinterpret_cast<T *>(p) : nullptr;
     return t;
 }
 
+// Stage the tile.  u is zero-filled instead of loaded when zero_u; f is
+// zero-filled when the level has no right-hand side but the kernel keeps an
+// array for it.  Returns false (in every thread) if the copies did not land.
 template <typename T>
-__host__ __device__ inline size_t tile_elems(int LR, int LC, bool has_f) {
-    const size_t n = (size_t)LR * LC;
-    return n * (3 + (has_f ? 1 : 0) + (TileCfg<T>::kDinv ? 1 : 0)) + LC;
-}
-
-// stage the tile; f is zero-filled when the level has no right-hand side
-// but the kernel wants the array (to hold the residual)
-template <typename T>
-__device__ void tile_load(const LvArgs<T> &g, STile<T> &t, bool zero_u) {
-    for (int r = TWARP; r < t.LR; r += TNWARP) {
-        const long gr = (long)(t.jL0 + r) * g.P + t.kL0;
-        const int sr = r * t.LC;
-        for (int c = TLANE; c < t.LC; c += 32) {
-            t.u[sr + c] = zero_u ? (T)0 : g.u[gr + c];
-            t.cx[sr + c] = g.cx[gr + c];
-            if (t.f) t.f[sr + c] = g.f ? g.f[gr + c] : (T)0;
-            if (TileCfg<T>::kDinv) t.dv[sr + c] = g.dinv[gr + c];
-        }
+__device__ bool tile_load(const LvArgs<T> &g, const TileMaps &m, STile<T> &t, bool zero_u,
+                          uint64_t *bar, unsigned *status) {
+    const int BH = m.BH, W = m.W;
+    const bool load_f = t.f && g.f;
+    if (threadIdx.x == 0) mbar_init(bar, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        // every box lands in full (rows past the grid arrive as zeros), so the
+        // transaction count is the sum of the box sizes
+        const unsigned a = (unsigned)(sizeof(T) * BH * W);
+        unsigned bytes = a + (unsigned)(sizeof(T) * (BH + 1) * W);   // cx, cz
+        if (!zero_u) bytes += a;
+        if (load_f) bytes += a;
+        if (TileCfg<T>::kDinv) bytes += a;
+        mbar_expect_tx(bar, bytes);
+        if (!zero_u) tma_load_2d(t.u, &m.u, t.kL0, t.jL0, bar);
+        tma_load_2d(t.cx, &m.cx, t.kL0, t.jL0, bar);
+        tma_load_2d(t.cz, &m.cz, t.kL0, t.jL0, bar);
+        if (load_f) tma_load_2d(t.f, &m.f, t.kL0, t.jL0, bar);
+        if (TileCfg<T>::kDinv) tma_load_2d(t.dv, &m.dv, t.kL0, t.jL0, bar);
     }
-    for (int r = TWARP; r <= t.LR; r += TNWARP) {
-        const long gr = (long)(t.jL0 + r) * g.P + t.kL0;
-        for (int c = TLANE; c < t.LC; c += 32) t.cz[r * t.LC + c] = g.cz[gr + c];
-    }
+    const int n = BH * W;
+    if (zero_u)
+        for (int i = threadIdx.x; i < n; i += blockDim.x) t.u[i] = (T)0;
+    if (t.f && !g.f)
+        for (int i = threadIdx.x; i < n; i += blockDim.x) t.f[i] = (T)0;
+    const bool ok = mbar_wait(bar, 0);
+    if (!ok && status) atomicOr(status, 1u);
+    return __syncthreads_and(ok) != 0;
 }
 
 // one colour over the tile
@@ -86,11 +124,11 @@ __device__ void tile_halfsweep(const LvArgs<T> &g, const STile<T> &t, int color)
         const int rs = (j == g.N - 1) ? r - 1 : r + 1;
         if (rn < 0 || rn >= t.LR || rs < 0 || rs >= t.LR) continue;
         const int p = (color + j + t.kL0) & 1;
-        const int sr = r * t.LC, sn = rn * t.LC, ss = rs * t.LC;
+        const int sr = r * t.W, sn = rn * t.W, ss = rs * t.W;
         for (int c = p + 2 * TLANE; c <= cmax; c += 64) {
             if (c < 1) continue;
             const int idx = sr + c;
-            const T cW = t.cx[idx - 1], cE = t.cx[idx], cN = t.cz[idx], cS = t.cz[idx + t.LC];
+            const T cW = t.cx[idx - 1], cE = t.cx[idx], cN = t.cz[idx], cS = t.cz[idx + t.W];
             T acc = cW * t.u[idx - 1] + cE * t.u[idx + 1] + cN * t.u[sn + c] + cS * t.u[ss + c];
             if (t.f) acc -= g.h2 * t.f[idx];
             const T d = TileCfg<T>::kDinv ? t.dv[idx] : recip(((cW + cE) + cN) + cS);
@@ -104,9 +142,9 @@ template <typename T>
 __device__ __forceinline__ T tile_residual(const LvArgs<T> &g, const STile<T> &t, int r, int c, int j) {
     const int rn = (j == 0) ? r + 1 : r - 1;
     const int rs = (j == g.N - 1) ? r - 1 : r + 1;
-    const int idx = r * t.LC + c;
-    const T cW = t.cx[idx - 1], cE = t.cx[idx], cN = t.cz[idx], cS = t.cz[idx + t.LC];
-    const T lap = cW * t.u[idx - 1] + cE * t.u[idx + 1] + cN * t.u[rn * t.LC + c] + cS * t.u[rs * t.LC + c] -
+    const int idx = r * t.W + c;
+    const T cW = t.cx[idx - 1], cE = t.cx[idx], cN = t.cz[idx], cS = t.cz[idx + t.W];
+    const T lap = cW * t.u[idx - 1] + cE * t.u[idx + 1] + cN * t.u[rn * t.W + c] + cS * t.u[rs * t.W + c] -
                   (((cW + cE) + cN) + cS) * t.u[idx];
     return (t.f ? t.f[idx] : (T)0) - lap * g.inv_h2;
 }
@@ -131,32 +169,35 @@ __device__ static double block_sum_1d(double v) {
 // ---------------------------------------------------------------------------
 template <typename T>
 __global__ void __launch_bounds__(NT, 2)
-    k_down(LvArgs<T> g, LvArgs<T> c, int CH, int CW, int ntj, int ntk, int S, int zero_u) {
-    extern __shared__ __align__(16) unsigned char smem[];
+    k_down(LvArgs<T> g, LvArgs<T> c, const __grid_constant__ TileMaps maps, int CH, int CW, int ntj,
+           int ntk, int S, int zero_u, unsigned *status) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t bar;
+    unsigned char *smem = align_smem128(smem_raw);
     const int tj = blockIdx.y, tk = blockIdx.x;
     const int cj0 = tj * CH, cj1 = (tj == ntj - 1) ? c.N : cj0 + CH;
     const int ck0 = tk * CW, ck1 = (tk == ntk - 1) ? c.K : ck0 + CW;
-    const int jL0 = max(0, 2 * cj0 - 2 - S), jL1 = min(g.N, 2 * cj1 + S + 1);
-    const int kL0 = max(0, 2 * ck0 - 2 - S), kL1 = min(g.K, 2 * ck1 + S + 1);
+    const int jL0 = max(0, 2 * cj0 - 2 - S);
+    const int kL0 = max(0, 2 * ck0 - 2 - S) & ~(TileCfg<T>::kAlign - 1);
+    const int LR = min(maps.BH, g.N - jL0), LC = min(maps.W, g.K - kL0);
     // the residual goes into f (FP32 levels and FP64 coarse levels all have
     // one) or, on the FP64 level 0 with its zero right-hand side, into dv
     const bool has_f = (g.f != nullptr) || !TileCfg<T>::kDinv;
-    STile<T> t = carve<T>(smem, jL0, kL0, jL1 - jL0, kL1 - kL0, has_f);
-    tile_load(g, t, zero_u != 0);
-    __syncthreads();
+    STile<T> t = carve<T>(smem, jL0, kL0, LR, LC, maps.BH, maps.W, has_f);
+    if (!tile_load(g, maps, t, zero_u != 0, &bar, status)) return;
     for (int s = 0; s < S; s++) {
         tile_halfsweep(g, t, s & 1);
         __syncthreads();
     }
     T *res = t.f ? t.f : t.dv;
-    {   // residual on fine rows 2cj0-1 .. 2cj1-1, columns 2ck0-1 .. 2ck1-1
+    {   // residual on fine rows 2cj0-1 .. 2cj1-1, columns 2ck0-1 .. 2ck1-1; a
+        // node's residual reads f only at that node, so overwriting f in place
+        // is race-free; u and the moduli are only read here
         const int ja = max(0, 2 * cj0 - 1), jb = min(g.N - 1, 2 * cj1 - 1);
         const int ka = max(1, 2 * ck0 - 1), kb = min(g.K - 2, 2 * ck1 - 1);
-        // a node's residual reads f only at that node, so overwriting f in
-        // place is race-free; u and the moduli are only read here
         for (int j = ja + TWARP; j <= jb; j += TNWARP)
             for (int k = ka + TLANE; k <= kb; k += 32)
-                res[(j - jL0) * t.LC + (k - kL0)] = tile_residual(g, t, j - jL0, k - kL0, j);
+                res[(j - jL0) * t.W + (k - kL0)] = tile_residual(g, t, j - jL0, k - kL0, j);
     }
     __syncthreads();
     {   // restriction onto owned coarse nodes (restriction_kernel, :953-1015)
@@ -164,9 +205,9 @@ __global__ void __launch_bounds__(NT, 2)
         for (int j = cj0 + TWARP; j < cj1; j += TNWARP) {
             const int rn = (j == 0) ? 2 * j + 1 : 2 * j - 1;
             const int rs = (j == c.N - 1) ? 2 * j - 1 : 2 * j + 1;
-            const T *R0 = res + (2 * j - jL0) * t.LC - kL0;
-            const T *RN = res + (rn - jL0) * t.LC - kL0;
-            const T *RS = res + (rs - jL0) * t.LC - kL0;
+            const T *R0 = res + (2 * j - jL0) * t.W - kL0;
+            const T *RN = res + (rn - jL0) * t.W - kL0;
+            const T *RS = res + (rs - jL0) * t.W - kL0;
             for (int k = ka + TLANE; k <= kb; k += 32) {
                 const int f = 2 * k;
                 const T val = (T)0.06250 * ((T)4.0 * R0[f] + (T)2.0 * R0[f - 1] + (T)2.0 * R0[f + 1] +
@@ -180,7 +221,7 @@ __global__ void __launch_bounds__(NT, 2)
         const int ja = 2 * cj0, jb = min(g.N, 2 * cj1);
         const int ka = max(1, 2 * ck0), kb = min(g.K - 1, 2 * ck1);
         for (int j = ja + TWARP; j < jb; j += TNWARP) {
-            const T *ur = t.u + (j - jL0) * t.LC - kL0;
+            const T *ur = t.u + (j - jL0) * t.W - kL0;
             T *gr = g.u + (long)j * g.P;
             for (int k = ka + TLANE; k < kb; k += 32) gr[k] = ur[k];
         }
@@ -195,24 +236,32 @@ __global__ void __launch_bounds__(NT, 2)
 // ---------------------------------------------------------------------------
 template <typename T, int MODE>
 __global__ void __launch_bounds__(NT, 2)
-    k_up(LvArgs<T> g, LvArgs<T> c, int TH, int TW, int ntj, int ntk, int S, int prolong,
-         int surface, int zero_u, double *partial, double *u64, int P64) {
-    extern __shared__ __align__(16) unsigned char smem[];
+    k_up(LvArgs<T> g, LvArgs<T> c, const __grid_constant__ TileMaps maps, int TH, int TW, int ntj,
+         int ntk, int S, int prolong, int surface, int zero_u, double *partial, double *u64, int P64,
+         unsigned *status) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t bar;
+    unsigned char *smem = align_smem128(smem_raw);
     const int tj = blockIdx.y, tk = blockIdx.x;
     const int j0 = tj * TH, j1 = (tj == ntj - 1) ? g.N : j0 + TH;
     const int k0 = tk * TW, k1 = (tk == ntk - 1) ? g.K : k0 + TW;
     const int R1 = (MODE == 1) ? 1 : 0;
-    const int jL0 = max(0, j0 - S - R1), jL1 = min(g.N, j1 + S + R1);
-    const int kL0 = max(0, k0 - S - R1), kL1 = min(g.K, k1 + S + R1);
-    const int LR = jL1 - jL0, LC = kL1 - kL0;
-    STile<T> t = carve<T>(smem, jL0, kL0, LR, LC, g.f != nullptr);
-    tile_load(g, t, zero_u != 0);
+    const int jL0 = max(0, j0 - S - R1);
+    const int kL0 = max(0, k0 - S - R1) & ~(TileCfg<T>::kAlign - 1);
+    const int LR = min(maps.BH, g.N - jL0), LC = min(maps.W, g.K - kL0);
+    STile<T> t = carve<T>(smem, jL0, kL0, LR, LC, maps.BH, maps.W, g.f != nullptr);
+    const bool ok = tile_load(g, maps, t, zero_u != 0, &bar, status);
+    if (!ok) {
+        if (MODE == 1 && threadIdx.x == 0) partial[blockIdx.y * gridDim.x + blockIdx.x] = 0.0;
+        return;
+    }
     if (prolong) {
         // coarse block covering the tile, staged after the tile arrays
+        const int jL1 = jL0 + LR, kL1 = kL0 + LC;
         const int cjA = jL0 >> 1, cjB = min(c.N - 1, ((jL1 - 1) >> 1) + 1);
         const int ckA = kL0 >> 1, ckB = min(c.K - 1, ((kL1 - 1) >> 1) + 1);
         const int EW = ckB - ckA + 1;
-        T *E = reinterpret_cast<T *>(smem) + tile_elems<T>(LR, LC, g.f != nullptr);
+        T *E = reinterpret_cast<T *>(smem + tile_bytes<T>(maps.BH, maps.W, g.f != nullptr));
         for (int r = TWARP; r <= cjB - cjA; r += TNWARP)
             for (int cc = TLANE; cc < EW; cc += 32) E[r * EW + cc] = c.u[(long)(cjA + r) * c.P + ckA + cc];
         __syncthreads();
@@ -230,11 +279,11 @@ __global__ void __launch_bounds__(NT, 2)
                     add = (k & 1) ? (T)0.5 * (e[0] + e[1]) : e[0];
                 else
                     add = (k & 1) ? (T)0.25 * (e[0] + e[1] + e[EW] + e[EW + 1]) : (T)0.5 * (e[0] + e[EW]);
-                t.u[r * LC + cc] += add;
+                t.u[r * t.W + cc] += add;
             }
         }
+        __syncthreads();
     }
-    __syncthreads();
     for (int s = 0; s < S; s++) {
         tile_halfsweep(g, t, s & 1);
         __syncthreads();
@@ -250,9 +299,9 @@ __global__ void __launch_bounds__(NT, 2)
                 sq += rv * rv;
             }
             if (MODE == 2)
-                u64[(long)j * P64 + k] += (double)t.u[r * LC + cc];
+                u64[(long)j * P64 + k] += (double)t.u[r * t.W + cc];
             else
-                g.u[(long)j * g.P + k] = t.u[r * LC + cc];
+                g.u[(long)j * g.P + k] = t.u[r * t.W + cc];
         }
     }
     if (MODE == 1) {

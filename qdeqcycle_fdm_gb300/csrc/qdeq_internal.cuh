@@ -58,6 +58,7 @@ struct Level {
     T *f = nullptr;      // right-hand side (nullptr: identically zero)
     T *r = nullptr;      // residual scratch
     T *cx = nullptr, *cz = nullptr, *dinv = nullptr;
+    T *diag = nullptr;   // level 0 of the FP64 hierarchy only: cx[k-1]+cx[k]+cz[j]+cz[j+1]
 };
 
 struct LevelDims {
@@ -84,6 +85,18 @@ struct DevStatus {
     int bad_node;
 };
 enum : unsigned int { ST_NEWTON_NAN = 1u, ST_NEWTON_CAP = 2u, ST_NEWTON_BRACKET = 4u };
+// set by a multigrid tile kernel whose TMA staging did not complete
+static constexpr unsigned int ST_TMA_TIMEOUT = 1u;
+
+// state of the device-driven multigrid loop (mg_graph.cu)
+struct SolveState {
+    double thr, delta, r0;
+    int cycles;                           // V-cycles of the last solve
+    int flag;                             // 1: non-finite norm, 2: cycle cap (sticky)
+    int go;                               // the last "run another cycle" decision
+    unsigned long long total_cycles, total_solves;
+    unsigned long long kernels;           // kernels the solve graphs ran
+};
 
 }  // namespace qd
 
@@ -97,9 +110,13 @@ struct qd_solver {
     qd::Level<float> L32[QD_MAXLEV];
     cudaStream_t stream;
     double *d_partial;     // per-block reduction partials
+    unsigned *d_count;     // blocks done, for reductions finished by their last block
     double *d_ainv64;      // dense inverse of the coarsest-level operator (or null)
     float *d_ainv32;
     int n_cint;            // its order: coarsest N * (K-2) interior unknowns
+    void *tma_cache;       // tensor maps of the tile kernels (mg_fused.cu)
+    void *solve_graph;     // the instantiated multigrid graph (mg_graph.cu)
+    qd::SolveState *d_solve, *h_solve;
     int n_partial;
     double *d_scal;        // device scalars: [0] ||r||^2, [1] ||r0||^2, [2] totErr
     double *h_scal;        // pinned mirror
@@ -128,6 +145,12 @@ int build_coarse_inverse(qd_solver *s);
 // mg_fused.cu
 int vcycle64_norm(qd_solver *s, int *nblocks);
 int vcycle32_into64(qd_solver *s);
+void tma_cache_free(qd_solver *s);
+// mg_graph.cu
+int mg_solve_async(qd_solver *s);
+int solve_state_read(qd_solver *s, SolveState *out);
+int solve_state_clear_flag(qd_solver *s);
+void solve_graph_free(qd_solver *s);
 // fault.cu
 int fault_alloc(qd_solver *s);
 void fault_free(qd_solver *s);
