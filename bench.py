@@ -35,6 +35,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 YEAR_S = 365.25 * 86400.0
+# DRAM bytes (read + write) per launch of the V-cycle kernels at 1025^2,
+# from one ncu capture of the headline solver (profiles/vcycle_kernels_1025.md)
+TRAFFIC = {"up0": 26.86e6, "down0": 13.02e6, "residual": 33.74e6}
 METRIC = "simulated yr/hr at 1025² (learned+mixed vs plain FP64 MG, 1e-9 rel residual)"
 
 
@@ -286,31 +289,46 @@ def run_ours(args):
         sim64s.close()
         plain_value = plain["yrs"] / (reduce_max(plain["ms"]) / 3.6e6)
 
-    # dominant kernel: level-0 smoother sweeps of the headline (FP32) hierarchy
-    stream = torch.cuda.ExternalStream(sim.solver.stream_ptr())
-    nsw = 50
-    sim.solver.smooth(2)
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    sim.solver.smooth(nsw)
-    e1.record(stream)
-    e1.synchronize()
-    per_launch_s = e0.elapsed_time(e1) / 1e3 / (2 * nsw)
-    nodes = cfg.ni * cfg.nk
-    algo_bytes = 10.0 * nodes                     # FP32: 20 B/node per red+black sweep, half per colour
+    # Roofline of the V-cycle's kernels.  Inside a solve they run in a CUDA
+    # graph, so each is timed by qd_mg_time_kernel: REPS back-to-back
+    # launches on the solver's stream between two CUDA events, on the
+    # headline solver's own state after the timed run.  Algorithmic bytes
+    # per launch are the unfused algorithm's traffic (FP32 hierarchy):
+    #   down0    2 red+black sweeps x 20 B + residual/restriction 16 B per
+    #            level-0 node, + 4 B per level-1 node
+    #   up0      prolongation 8 B + 2 sweeps x 20 B + u64 += e 16 B per
+    #            level-0 node, + 4 B per level-1 node
+    #   residual FP64 u, cx, cz, diag read + FP32 rhs written: 36 B per node
+    # The dominant kernel (largest time per V-cycle) is the roofline entry.
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except (OSError, ValueError):
         pass
     peak = peaks.get("hbm_gbs", 6800.0)
-    achieved = algo_bytes / per_launch_s / 1e9
+    n0 = cfg.ni * cfg.nk
+    n1 = ((cfg.ni - 1) // 2 + 1) * ((cfg.nk - 1) // 2 + 1)
+    algo = {"up0": 64.0 * n0 + 4.0 * n1, "down0": 56.0 * n0 + 4.0 * n1, "residual": 36.0 * n0}
+    names = {"up0": "k_up<float,2> level 0 (prolongation + 2 sweeps + u64 += e)",
+             "down0": "k_down<float> level 0 (2 sweeps + residual + restriction)",
+             "residual": "k_residual64_to32 (FP64 residual -> FP32 rhs + norm)",
+             "tail": "k_tail<float> (levels <= 65 rows, one CTA)"}
+    REPS = 50
+    kern = {}
+    for k in ("up0", "down0", "residual", "tail"):
+        sim.solver.time_kernel(k, 3)                      # warm-up launches
+        us = sim.solver.time_kernel(k, REPS)
+        kern[k] = {"us": us, "kernel": names[k]}
+        if k in algo:
+            kern[k]["algo_bytes"] = algo[k]
+            kern[k]["achieved_gbs"] = algo[k] / (us * 1e-6) / 1e9
+    dom = max(algo, key=lambda k: kern[k]["us"])
+    achieved = kern[dom]["achieved_gbs"]
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": None,
-                "kernel": "k_rb<float> level 0 (one colour)",
-                "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"}
+                "frac": achieved / peak, "traffic": TRAFFIC.get(dom),
+                "kernel": names[dom], "us_per_launch": kern[dom]["us"], "reps": REPS,
+                "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+                "vcycle_kernels": kern}
 
     # end to end through the C ABI with host buffers (pinned), the same steps
     e2e = None

@@ -150,6 +150,25 @@ int qd_mg_smooth(qd_solver *s, int nsweeps);
 int qd_mg_vcycle(qd_solver *s);
 int qd_mg_residual_norm(qd_solver *s, double *rnorm);
 
+/* Per-launch device time of one kernel of the V-cycle that the solver's
+ * precision runs (inside a solve they run in a CUDA graph, out of reach of
+ * per-kernel events): the kernel is launched `reps` times back to back on
+ * the solver's stream between two CUDA events and *us receives the mean
+ * microseconds per launch.  The launches change the solver's state (they
+ * smooth, restrict and add corrections), so use it after a run, for
+ * roofline measurements.  No counterpart in the reference. */
+#define QD_KERNEL_DOWN0    0   /* level-0 pre-smoothing + residual + restriction tile kernel */
+#define QD_KERNEL_UP0      1   /* level-0 prolongation + post-smoothing tile kernel (final pass) */
+#define QD_KERNEL_RESIDUAL 2   /* FP64 level-0 residual -> FP32 right-hand side + norm (mixed) */
+#define QD_KERNEL_TAIL     3   /* single-CTA coarse tail */
+int qd_mg_time_kernel(qd_solver *s, int kernel, int reps, double *us);
+
+/* The binary64 -> binary32 rounding (to nearest, ties to even) that the
+ * mixed-precision residual kernel performs on the device's integer pipes,
+ * applied to n host values (a device round trip), so that tests can hold it
+ * to IEEE conversion on the host.  No counterpart in the reference. */
+int qd_convert_f64_to_f32(const double *in, float *out, int n);
+
 /* The level-0 residual norm ||0 - A u||2 that qd_mg_residual_norm returns,
  * for a caller that cannot allocate device memory: a host framework that
  * owns every device byte (its own allocator, or a budget fixed at start-up),

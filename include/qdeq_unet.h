@@ -1,0 +1,63 @@
+/* qdeq_unet.h -- the learned warm start of the GB300 hot path.
+ *
+ * A 4-level U-Net (16/32/64/128 channels, 3x3 convolutions, BF16 weights and
+ * activations, FP32 accumulation on the 5th-generation tensor cores) that
+ * predicts the change a stage's multigrid solve will make to the
+ * displacement field u, from the field the solve starts at and the stage's
+ * change of the Dirichlet data on the fault and far columns.  The multigrid
+ * always iterates from the predicted field to the same residual tolerance,
+ * so the prediction only changes the V-cycle count, never the result's
+ * tolerance.  The reference has no counterpart to anything in this header.
+ *
+ * Parameters are flat FP32 arrays: for each of the 15 convolutions in order
+ * (encoder 8, decoder 6, head 1), weights [9 taps][cout][cin] (tap = 3*(dy+1)
+ * + (dx+1)) followed by the bias [cout].  The first layer has cin = 16 (four
+ * input channels used), the head cout = 16 (channel 0 used).
+ * Host inputs are planar float arrays over the nk x ni level-0 grid:
+ * x = [4][nk][ni] input channels, target / y = [nk][ni].
+ */
+#ifndef QDEQ_UNET_H
+#define QDEQ_UNET_H
+
+#include "qdeq.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct qd_unet qd_unet;
+
+/* A network for an nk x ni grid ((nk-1) and (ni-1) divisible by 8), with
+ * seeded He-normal weights (the head and the unused input channels start at
+ * zero, so a fresh network predicts no change). */
+int qd_unet_create(int nk, int ni, unsigned long long seed, qd_unet **out);
+void qd_unet_destroy(qd_unet *u);
+long long qd_unet_num_params(const qd_unet *u);
+int qd_unet_get_params(qd_unet *u, float *host);
+int qd_unet_set_params(qd_unet *u, const float *host);
+
+/* y = network(x), on the host arrays (device round trip) */
+int qd_unet_forward_host(qd_unet *u, const float *x, float *y);
+
+/* loss = mean over the grid of (y - target)^2 and its gradient with respect
+ * to every parameter (grads: num_params floats, may be NULL) */
+int qd_unet_loss_grad_host(qd_unet *u, const float *x, const float *target, float *loss, float *grads);
+
+/* one Adam step (beta 0.9 / 0.999) with learning rate lr on (x, target) */
+int qd_unet_train_step_host(qd_unet *u, const float *x, const float *target, float lr, float *loss);
+
+/* Attach the network to a solver of the same grid: mode 1 trains online
+ * (one Adam step per stage solve on the change the solve made, the solve
+ * itself starting from the unmodified field), mode 2 predicts (the solve
+ * starts from u + prediction), mode 0 detaches.  While attached the
+ * network runs on the solver's stream; destroying the solver detaches it. */
+int qd_solver_warm_start(qd_solver *s, qd_unet *u, int mode, float lr);
+
+/* training steps taken, and the loss of the last step */
+int qd_unet_stats(qd_unet *u, long long *train_steps, float *last_loss);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -37,6 +37,8 @@ EXPORTS = [
     ("qd_mg_smooth", C.c_int, [C.c_void_p, C.c_int]),
     ("qd_mg_vcycle", C.c_int, [C.c_void_p]),
     ("qd_mg_residual_norm", C.c_int, [C.c_void_p, _dp]),
+    ("qd_mg_time_kernel", C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp]),
+    ("qd_convert_f64_to_f32", C.c_int, [_dp, C.POINTER(C.c_float), C.c_int]),
     ("qd_residual_norm_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                            C.c_int, C.c_double, C.c_void_p, _dp]),
     ("qd_fault_setup", C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp, C.c_double,

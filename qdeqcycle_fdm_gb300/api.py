@@ -115,6 +115,15 @@ class Solver:
         check(self.L.qd_mg_residual_norm(self.h, C.byref(rn)))
         return rn.value
 
+    KERNELS = {"down0": 0, "up0": 1, "residual": 2, "tail": 3}
+
+    def time_kernel(self, name, reps=50):
+        """Mean device microseconds per launch of one V-cycle kernel
+        (qd_mg_time_kernel); perturbs the solver state."""
+        us = C.c_double(0)
+        check(self.L.qd_mg_time_kernel(self.h, self.KERNELS[name], reps, C.byref(us)))
+        return us.value
+
     # -- fault -------------------------------------------------------------
     def fault_setup(self, prob, with_tau0=True):
         check(self.L.qd_fault_setup(self.h, _p(prob.a), _p(prob.b), _p(prob.eta), _p(prob.Tau_n0),

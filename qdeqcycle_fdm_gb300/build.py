@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libqdeq_gb300.so")
-SOURCES = ["capi.cu", "mg.cu", "mg_fused.cu", "fault.cu", "medium.cu", "dropin.cpp", "noalloc.cu", "mg_graph.cu"]
+SOURCES = ["capi.cu", "mg.cu", "mg_fused.cu", "fault.cu", "medium.cu", "dropin.cpp", "noalloc.cu", "mg_graph.cu", "unet.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr"]
@@ -37,7 +37,8 @@ def _stale(src_paths, target) -> bool:
 def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
     os.makedirs(OUT_DIR, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
-    headers.append(os.path.join(os.path.dirname(HERE), "include", "qdeq.h"))
+    for h in ("qdeq.h", "qdeq_unet.h"):
+        headers.append(os.path.join(os.path.dirname(HERE), "include", h))
     objs = []
     jobs = []
     for src in SOURCES:

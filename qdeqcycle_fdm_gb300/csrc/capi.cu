@@ -77,6 +77,11 @@ static int check_status(qd_solver *s) {
     SolveState st;
     QD_TRY(solve_state_read(s, &st));   // synchronises the stream
     QD_TRY(solve_flag_error(st));
+    if (s->h_status->flags & ST_TMA_TIMEOUT) {
+        set_error("a multigrid kernel's shared-memory staging did not complete (flags %u)",
+                  s->h_status->flags);
+        return QD_ERR_CUDA;
+    }
     if (s->h_status->flags & (ST_NEWTON_NAN | ST_NEWTON_CAP)) {
         set_error("Newton for slip rate failed at fault node %d (flags %u)", s->h_status->bad_node,
                   s->h_status->flags);
@@ -98,8 +103,11 @@ static int reset_status(qd_solver *s) {
 // one stage: boundary data, elliptic solve, stress/Newton/aging law, all
 // enqueued on the solver's stream without waiting
 static int stage(qd_solver *s, int st, double ratio) {
+    QD_TRY(warm_start_before_boundary(s));     // no-ops without an attached network
     QD_TRY(launch_stage_boundary(s, st, ratio, nullptr, nullptr));
+    QD_TRY(warm_start_after_boundary(s));
     QD_TRY(mg_solve_async(s));
+    QD_TRY(warm_start_after_solve(s));
     return launch_fault(s, st, 0);
 }
 
@@ -219,6 +227,7 @@ int qd_solver_create(int ni, int nk, double dh, const double *mu_equi, const dou
 int qd_solver_destroy(qd_solver *s) {
     if (!s) return QD_OK;
     if (s->stream) cudaStreamSynchronize(s->stream);
+    warm_start_detach(s);            // the network outlives the solver
     mg_free(s);
     fault_free(s);
     solve_graph_free(s);
@@ -328,6 +337,27 @@ int qd_mg_vcycle(qd_solver *s) {
 int qd_mg_residual_norm(qd_solver *s, double *rnorm) {
     if (!s || !rnorm) return QD_ERR_ARG;
     return mg_residual_norm(s, rnorm);
+}
+
+int qd_convert_f64_to_f32(const double *in, float *out, int n) {
+    if (!in || !out || n < 0) {
+        set_error("qd_convert_f64_to_f32: bad arguments");
+        return QD_ERR_ARG;
+    }
+    if (n == 0) return QD_OK;
+    return convert_f64_f32(in, out, n);
+}
+
+int qd_mg_time_kernel(qd_solver *s, int kernel, int reps, double *us) {
+    if (!s || !us) {
+        set_error("qd_mg_time_kernel: bad arguments");
+        return QD_ERR_ARG;
+    }
+    if (kernel == QD_KERNEL_RESIDUAL && s->opt.precision != QD_PREC_MIXED) {
+        set_error("qd_mg_time_kernel: the FP64-to-FP32 residual runs only in mixed precision");
+        return QD_ERR_ARG;
+    }
+    return time_kernel(s, kernel, reps, us);
 }
 
 int qd_fault_setup(qd_solver *s, const double *a, const double *b, const double *eta,

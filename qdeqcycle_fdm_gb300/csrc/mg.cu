@@ -171,10 +171,13 @@ __global__ void __launch_bounds__(BX * BY) k_residual(View<T> v, T *r, double *p
 // of the correction equation, and ||r||^2 into *out (mixed precision).
 //
 // GB300 issues about two FP64 instructions per SM clock, which bounds this
-// kernel, so it spends few of them per node: the stored diagonal replaces
+// kernel, so it spends five of them per node: the stored diagonal replaces
 // three additions; without a right-hand side the 1/h^2 scale is applied in
-// FP32 after the conversion and once to the final sum; each thread
-// accumulates RES_RPT rows before the block reduction.  The last block to
+// FP32 after the conversion; the FP64 -> FP32 conversion runs on the
+// integer pipes (d2f_rne); the norm sums the squares of the FP32 residual
+// the correction equation receives, in FP32 over a warp (128 nodes) and in
+// FP64 above that -- a relative error near 1e-7 in the norm, which only the
+// stopping test reads.  The last block to
 // finish adds the per-block partials in a fixed order (the sum is
 // deterministic) and re-arms the counter for the next launch.
 static constexpr int RES_RPT = 4;
@@ -186,7 +189,7 @@ __global__ void __launch_bounds__(BX * BY)
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j0 = blockIdx.y * (BY * RES_RPT) + threadIdx.y;
     const float nih2 = -(float)v.inv_h2;
-    double sq = 0.0;
+    float sq = 0.f;   // squares of the FP32 residual, summed in FP32 within a warp
     if (k >= 1 && k <= v.K - 2) {
         const double *__restrict__ u = v.u;
 #pragma unroll
@@ -198,23 +201,24 @@ __global__ void __launch_bounds__(BX * BY)
                 const long dn = (j == v.N - 1) ? -(long)v.P : v.P;
                 const double lap = v.cx[c - 1] * u[c - 1] + v.cx[c] * u[c + 1] + v.cz[c] * u[c + up] +
                                    v.cz[c + v.P] * u[c + dn] - diag[c] * u[c];
-                if (HAS_F) {
-                    const double res = v.f[c] - lap * v.inv_h2;
-                    f32[c] = (float)res;
-                    sq = fma(res, res, sq);
-                } else {
-                    f32[c] = (float)lap * nih2;
-                    sq = fma(lap, lap, sq);
-                }
+                const float r = HAS_F ? d2f_rne(v.f[c] - lap * v.inv_h2) : d2f_rne(lap) * nih2;
+                f32[c] = r;
+                sq = fmaf(r, r, sq);
             }
         }
     }
-    sq = block_sum(sq);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
+    __shared__ double wsum[BX * BY / 32];
     __shared__ bool last;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    if ((tid & 31) == 0) wsum[tid >> 5] = (double)sq;
+    __syncthreads();
     const unsigned nblk = gridDim.x * gridDim.y;
     if (tid == 0) {
-        partial[blockIdx.y * gridDim.x + blockIdx.x] = sq;
+        double b = 0.0;
+        for (int w = 0; w < BX * BY / 32; w++) b += wsum[w];
+        partial[blockIdx.y * gridDim.x + blockIdx.x] = b;
         __threadfence();
         last = atomicAdd(count, 1u) == nblk - 1;
     }
@@ -225,7 +229,7 @@ __global__ void __launch_bounds__(BX * BY)
     for (unsigned i = tid; i < nblk; i += blockDim.x * blockDim.y) t += __ldcg(partial + i);
     t = block_sum(t);
     if (tid == 0) {
-        *out = HAS_F ? t : t * (v.inv_h2 * v.inv_h2);
+        *out = t;
         *count = 0;
     }
 }
@@ -342,7 +346,8 @@ int mg_alloc(qd_solver *s, const double *mu_equi_host) {
     }
     QD_CUDA(cudaStreamSynchronize(s->stream));
     cudaFree(d_mu);
-    return build_coarse_inverse(s);
+    QD_TRY(build_coarse_inverse(s));
+    return tail_image_build(s);
 }
 
 // Dense inverse of the coarsest level's operator, for the exact coarse solve
@@ -429,6 +434,7 @@ void mg_free(qd_solver *s) {
     cudaFree(s->d_ainv64);
     cudaFree(s->d_ainv32);
     tma_cache_free(s);
+    tail_image_free(s);
     s->d_ainv64 = nullptr;
     s->d_ainv32 = nullptr;
     s->d_partial = nullptr;
@@ -516,6 +522,35 @@ int mg_residual_norm(qd_solver *s, double *rnorm) {
     QD_TRY(read_scalars(s, 1));
     *rnorm = sqrt(s->h_scal[0]);
     return QD_OK;
+}
+
+__global__ void k_d2f(const double *in, float *out, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = d2f_rne(in[i]);
+}
+
+// d2f_rne over a host array (a device round trip), for its test
+int convert_f64_f32(const double *in, float *out, int n) {
+    double *din = nullptr;
+    float *dout = nullptr;
+    int rc = QD_OK;
+    if (cudaMalloc(&din, sizeof(double) * (size_t)n) != cudaSuccess ||
+        cudaMalloc(&dout, sizeof(float) * (size_t)n) != cudaSuccess ||
+        cudaMemcpy(din, in, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice) != cudaSuccess) {
+        rc = QD_ERR_CUDA;
+    } else {
+        k_d2f<<<cdiv(n, 256), 256>>>(din, dout, n);
+        if (cudaGetLastError() != cudaSuccess ||
+            cudaMemcpy(out, dout, sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost) != cudaSuccess)
+            rc = QD_ERR_CUDA;
+    }
+    if (rc != QD_OK) {
+        (void)cudaGetLastError();
+        set_error("convert_f64_f32: CUDA failure");
+    }
+    cudaFree(din);
+    cudaFree(dout);
+    return rc;
 }
 
 }  // namespace qd

@@ -62,28 +62,63 @@ namespace qd {
 
 // ---------------------------------------------------------------------------
 // k_tail: levels l0 .. nlev-1 of the V-cycle in one CTA, with the levels'
-// u, f and r in shared memory (and, when they fit, the face moduli too;
-// otherwise those are read through the read-only cache).  Level l0's
-// correction starts from zero; its f comes from k_down of level l0-1 and its
-// u goes back to global memory for k_up of level l0-1.
+// u, f and r in shared memory.  Their face moduli and the dense coarsest
+// inverse never change, so they are packed once, at set-up, into one
+// contiguous image in global memory laid out as the kernel uses them (row
+// pitch K).  The kernel stages the longest prefix of the image that fits in
+// shared memory with bulk asynchronous copies on one mbarrier, while its
+// threads load f and clear u; arrays past the prefix are read in place.
+// The image starts with the inverse and then holds the levels from the
+// coarsest up, so the most-read arrays are the staged ones.  Level l0's
+// correction starts from zero; its f comes from k_down of level l0-1 and
+// its u goes back to global memory for k_up of level l0-1.
 // ---------------------------------------------------------------------------
 struct TailLevels {
-    int l0, nlev, nu_pre, nu_post, nu_coarse, surface, coef_smem;
-    int coarse_solve, nint;   // exact coarsest solve with the dense inverse ainv
+    int l0, nlev, nu_pre, nu_post, nu_coarse, surface;
+    int coarse_solve, nint;        // exact coarsest solve with the dense inverse
+    int img_smem;                  // bytes of the image prefix staged in shared memory
+    int work_off;                  // byte offset of the u/f/r arrays in shared memory
+    int coef_off[QD_MAXLEV];       // element offset of level l's cx in the image (cz, dinv follow)
+    int ainv_off;                  // element offset of the inverse (-1: none)
 };
 
 template <typename T>
 struct TailArgs {
     LvArgs<T> L[QD_MAXLEV];
-    const T *ainv;
+    const T *img;                  // the packed image in global memory
+    unsigned *status;
     TailLevels p;
 };
+
+// element counts of a level's arrays in the image, each padded to 16 bytes
+template <typename T>
+__host__ __device__ inline int img_pad(long n) {
+    const int a = 16 / (int)sizeof(T);
+    return (int)((n + a - 1) / a * a);
+}
+
+// layout of the image: [inverse] then, for l = nlev-1 down to l0, cx | cz | dinv
+template <typename T>
+static size_t tail_layout(const qd_solver *s, int l0, TailLevels *p) {
+    long off = 0;
+    p->ainv_off = -1;
+    if (s->n_cint > 0) {
+        p->ainv_off = 0;
+        off += img_pad<T>((long)s->n_cint * s->n_cint);
+    }
+    for (int l = s->nlev - 1; l >= l0; l--) {
+        const long N = s->dims[l].N, K = s->dims[l].K;
+        p->coef_off[l] = (int)off;
+        off += img_pad<T>(N * K) + img_pad<T>((N + 1) * K) + img_pad<T>(N * K);
+    }
+    return (size_t)off * sizeof(T);
+}
 
 template <typename T>
 struct TV {                       // one tail level as the kernel sees it
     T *u, *f, *r;                 // shared memory, row pitch K
-    const T *cx, *cz, *dinv;      // shared (pitch K) or global (pitch P)
-    int N, K, CP;
+    const T *cx, *cz, *dinv;      // shared or global (the image), row pitch K
+    int N, K;
     T h2, inv_h2;
 };
 
@@ -95,12 +130,12 @@ __device__ void tv_halfsweep(const TV<T> &g, int color) {
         const int up = (j == 0) ? g.K : -g.K;
         const int dn = (j == g.N - 1) ? -g.K : g.K;
         for (int k = 1 + ((j + 1 + color) & 1) + 2 * TLANE; k <= g.K - 2; k += 64) {
-            const int c = j * g.K + k, cc = j * g.CP + k;
+            const int c = j * g.K + k;
             // the moduli may live in shared or in global memory: generic loads
-            T acc = g.cx[cc - 1] * g.u[c - 1] + g.cx[cc] * g.u[c + 1] + g.cz[cc] * g.u[c + up] +
-                    g.cz[cc + g.CP] * g.u[c + dn];
+            T acc = g.cx[c - 1] * g.u[c - 1] + g.cx[c] * g.u[c + 1] + g.cz[c] * g.u[c + up] +
+                    g.cz[c + g.K] * g.u[c + dn];
             acc -= g.h2 * g.f[c];
-            g.u[c] = g.dinv[cc] * acc;
+            g.u[c] = g.dinv[c] * acc;
         }
     }
 }
@@ -116,71 +151,97 @@ __device__ void tv_smooth(const TV<T> &g, int nsweeps) {
 }
 
 template <typename T>
-static size_t tail_smem_bytes(const qd_solver *s, int l0, int coef_smem) {
+static size_t tail_work_bytes(const qd_solver *s, int l0) {
     size_t n = 0;
-    for (int l = l0; l < s->nlev; l++) {
-        const size_t nk = (size_t)s->dims[l].N * s->dims[l].K;
-        n += 3 * nk + (coef_smem ? 3 * nk + s->dims[l].K : 0);
-    }
+    for (int l = l0; l < s->nlev; l++) n += 3 * (size_t)s->dims[l].N * s->dims[l].K;
     return n * sizeof(T);
+}
+
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned bytes, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
 }
 
 template <typename T>
 __global__ void __launch_bounds__(NT_TAIL) k_tail(TailArgs<T> a) {
-    extern __shared__ __align__(128) unsigned char smem[];
-    const TailLevels &p = a.p;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t bar;
     __shared__ TV<T> V[QD_MAXLEV];   // per-level views, read by every thread
-    T *ptr = reinterpret_cast<T *>(smem);
-    for (int l = p.l0; l < p.nlev; l++) {
-        const LvArgs<T> &g = a.L[l];
-        TV<T> v;
-        const int n = g.N * g.K;
-        v.N = g.N; v.K = g.K; v.h2 = g.h2; v.inv_h2 = g.inv_h2;
-        v.u = ptr; ptr += n;
-        v.f = ptr; ptr += n;
-        v.r = ptr; ptr += n;
-        if (p.coef_smem) {
-            T *cx = ptr; ptr += n;
-            T *cz = ptr; ptr += n + g.K;
-            T *dv = ptr; ptr += n;
-            for (int j = TWARP; j <= g.N; j += TNWARP)
-                for (int k = TLANE; k < g.K; k += 32) {
-                    const long gi = (long)j * g.P + k;
-                    const int i = j * g.K + k;
-                    cz[i] = g.cz[gi];
-                    if (j < g.N) {
-                        cx[i] = g.cx[gi];
-                        dv[i] = g.dinv[gi];
-                    }
-                }
-            v.cx = cx; v.cz = cz; v.dinv = dv; v.CP = g.K;
-        } else {
-            v.cx = g.cx; v.cz = g.cz; v.dinv = g.dinv; v.CP = g.P;
+    __shared__ const T *ainv;
+    unsigned char *smem = align_smem128(smem_raw);
+    const TailLevels &p = a.p;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        if (p.img_smem > 0) {
+            mbar_expect_tx(&bar, (unsigned)p.img_smem);
+            const int CH = 32768;
+            for (int off = 0; off < p.img_smem; off += CH)
+                bulk_load(smem + off, reinterpret_cast<const unsigned char *>(a.img) + off,
+                          (unsigned)min(CH, p.img_smem - off), &bar);
         }
-        if (threadIdx.x == 0) V[l] = v;
+        // an array is read from shared memory when it lies inside the prefix
+        const T *simg = reinterpret_cast<const T *>(smem);
+        const long staged = p.img_smem / (long)sizeof(T);
+        auto pick = [&](long off, long n) { return off + n <= staged ? simg + off : a.img + off; };
+        T *w = reinterpret_cast<T *>(smem + p.work_off);
+        for (int l = p.l0; l < p.nlev; l++) {
+            const LvArgs<T> &g = a.L[l];
+            const long N = g.N, K = g.K, n = N * K;
+            TV<T> v;
+            v.N = g.N; v.K = g.K; v.h2 = g.h2; v.inv_h2 = g.inv_h2;
+            v.u = w; w += n;
+            v.f = w; w += n;
+            v.r = w; w += n;
+            const long ox = p.coef_off[l], oz = ox + img_pad<T>(n), od = oz + img_pad<T>(n + K);
+            v.cx = pick(ox, n);
+            v.cz = pick(oz, n + K);
+            v.dinv = pick(od, n);
+            V[l] = v;
+        }
+        ainv = p.ainv_off >= 0 ? pick(p.ainv_off, (long)p.nint * p.nint) : nullptr;
     }
     __syncthreads();
-    {   // right-hand side of the first tail level
+    {   // right-hand side of the first tail level; every correction starts at zero
         const LvArgs<T> &g = a.L[p.l0];
+        const T *__restrict__ gf = g.f;
+        T *sf = V[p.l0].f;
         for (int j = TWARP; j < g.N; j += TNWARP)
-            for (int k = TLANE; k < g.K; k += 32) V[p.l0].f[j * g.K + k] = g.f[(long)j * g.P + k];
+            for (int k = TLANE; k < g.K; k += 32) sf[j * g.K + k] = __ldg(gf + (long)j * g.P + k);
+        for (int l = p.l0; l < p.nlev; l++) {
+            const TV<T> v = V[l];
+            for (int i = threadIdx.x; i < v.N * v.K; i += blockDim.x) v.u[i] = (T)0;
+        }
+    }
+    bool ok = true;
+    if (p.img_smem > 0) ok = mbar_wait(&bar, 0);
+    if (!__syncthreads_and(ok)) {
+        if (threadIdx.x == 0 && a.status) atomicOr(a.status, ST_TMA_TIMEOUT);
+        return;
     }
     for (int l = p.l0; l < p.nlev; l++) {
-        const TV<T> &g = V[l];
-        for (int i = threadIdx.x; i < g.N * g.K; i += blockDim.x) g.u[i] = (T)0;
-        __syncthreads();
+        const TV<T> g = V[l];   // by value: stores through g.u cannot clobber it
         if (l == p.nlev - 1) {
             if (p.coarse_solve) {
-                // e = A^-1 f over the interior nodes, one row per thread
+                // e = A^-1 f over the interior nodes: a warp per row of the
+                // inverse, lanes along the row, then a butterfly sum
                 const int KI = g.K - 2;
-                for (int i = threadIdx.x; i < p.nint; i += blockDim.x) {
-                    const T *row = a.ainv + (long)i * p.nint;
+                const T *ai = ainv;
+                for (int i = TWARP; i < p.nint; i += TNWARP) {
+                    const T *row = ai + (long)i * p.nint;
                     T acc = (T)0;
-                    int m = 0;
-                    for (int jm = 0; jm < g.N; jm++)
-                        for (int km = 1; km <= KI; km++, m++) acc += row[m] * g.f[jm * g.K + km];
-                    const int j = i / KI, k = i - j * KI + 1;
-                    g.u[j * g.K + k] = acc;
+                    for (int m = TLANE; m < p.nint; m += 32) {
+                        const int jm = m / KI, km = m - jm * KI + 1;
+                        acc += row[m] * g.f[jm * g.K + km];
+                    }
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                    if (TLANE == 0) {
+                        const int j = i / KI, k = i - j * KI + 1;
+                        g.u[j * g.K + k] = acc;
+                    }
                 }
                 __syncthreads();
             } else {
@@ -193,15 +254,15 @@ __global__ void __launch_bounds__(NT_TAIL) k_tail(TailArgs<T> a) {
             const int up = (j == 0) ? g.K : -g.K;
             const int dn = (j == g.N - 1) ? -g.K : g.K;
             for (int k = 1 + TLANE; k <= g.K - 2; k += 32) {
-                const int i = j * g.K + k, cc = j * g.CP + k;
-                const T cW = g.cx[cc - 1], cE = g.cx[cc], cN = g.cz[cc], cS = g.cz[cc + g.CP];
+                const int i = j * g.K + k;
+                const T cW = g.cx[i - 1], cE = g.cx[i], cN = g.cz[i], cS = g.cz[i + g.K];
                 const T lap = cW * g.u[i - 1] + cE * g.u[i + 1] + cN * g.u[i + up] + cS * g.u[i + dn] -
                               (((cW + cE) + cN) + cS) * g.u[i];
                 g.r[i] = g.f[i] - lap * g.inv_h2;
             }
         }
         __syncthreads();
-        const TV<T> &cl = V[l + 1];
+        const TV<T> cl = V[l + 1];
         for (int j = TWARP; j < cl.N; j += TNWARP) {
             const int rn = (j == 0) ? 2 * j + 1 : 2 * j - 1;
             const int rs = (j == cl.N - 1) ? 2 * j - 1 : 2 * j + 1;
@@ -217,8 +278,8 @@ __global__ void __launch_bounds__(NT_TAIL) k_tail(TailArgs<T> a) {
         __syncthreads();
     }
     for (int l = p.nlev - 2; l >= p.l0; l--) {
-        const TV<T> &g = V[l];
-        const TV<T> &cl = V[l + 1];
+        const TV<T> g = V[l];
+        const TV<T> cl = V[l + 1];
         const int jmax = g.N - 1 + p.surface;
         for (int jf = TWARP; jf < jmax; jf += TNWARP) {
             const T *er = cl.u + (jf >> 1) * cl.K;
@@ -238,8 +299,9 @@ __global__ void __launch_bounds__(NT_TAIL) k_tail(TailArgs<T> a) {
     }
     {   // the first tail level's correction, for k_up of the level above
         const LvArgs<T> &g = a.L[p.l0];
+        const T *su = V[p.l0].u;
         for (int j = TWARP; j < g.N; j += TNWARP)
-            for (int k = TLANE; k < g.K; k += 32) g.u[(long)j * g.P + k] = V[p.l0].u[j * g.K + k];
+            for (int k = TLANE; k < g.K; k += 32) g.u[(long)j * g.P + k] = su[j * g.K + k];
     }
 }
 
@@ -248,13 +310,6 @@ __global__ void __launch_bounds__(NT_TAIL) k_tail(TailArgs<T> a) {
 // ---------------------------------------------------------------------------
 static int cdivi(int a, int b) { return (a + b - 1) / b; }
 
-// fine-tile edge for level dims (N rows): aim for >= ~150 CTAs, cap by smem
-template <typename T>
-static int tile_edge(int N) {
-    int t = sizeof(T) == 4 ? 64 : 32;
-    while (t > 16 && cdivi(N - 1, t) * cdivi(N - 1, t) < 144) t /= 2;
-    return t;
-}
 
 static size_t g_smem_limit = 0;
 
@@ -321,7 +376,7 @@ static int tile_maps(qd_solver *s, Level<T> *Ls, int l, int W, int BH, const Til
     QD_TRY(make_tensor_map_2d(&e.maps.cx, Ls[l].cx, fp64, d.K, d.N, d.P, W, BH));
     QD_TRY(make_tensor_map_2d(&e.maps.cz, Ls[l].cz, fp64, d.K, d.N + 1, d.P, W, BH + 1));
     if (Ls[l].f) QD_TRY(make_tensor_map_2d(&e.maps.f, Ls[l].f, fp64, d.K, d.N, d.P, W, BH));
-    if (fp64) QD_TRY(make_tensor_map_2d(&e.maps.dv, Ls[l].dinv, fp64, d.K, d.N, d.P, W, BH));
+    QD_TRY(make_tensor_map_2d(&e.maps.dv, Ls[l].dinv, fp64, d.K, d.N, d.P, W, BH));
     tc->v.push_back(e);
     *out = &tc->v.back().maps;
     return QD_OK;
@@ -329,19 +384,116 @@ static int tile_maps(qd_solver *s, Level<T> *Ls, int l, int W, int BH, const Til
 
 static int round_up(int x, int a) { return (x + a - 1) / a * a; }
 
+// Tile geometry.  A warp updates one row of a tile per pass, a lane every
+// other node, so a box 64 columns wide keeps all 32 lanes busy in one pass
+// per row; tile widths are chosen for W <= 64 and tile heights for about a
+// full wave of CTAs at two CTAs per SM.
+struct TileGeom {
+    int ntj, ntk;     // tiles along rows / columns
+    int BH, W;        // the staged box (largest over the tiles)
+    int TH, TW;       // core rows / columns (fine nodes for k_up, coarse for k_down)
+    size_t smem;
+};
+
+static constexpr int kBoxW = 64;       // k_up boxes: one pass of 32 lanes per row
+static constexpr int kDownBoxW = 64;   // k_down boxes (80 measured slower at 1025^2: 24.1 vs 22.6 us)
+static constexpr int kWaveCtas = 150;
+
+static size_t two_cta_smem() { return std::min<size_t>(smem_limit(), 112 * 1024); }
+
+// k_up / smoother tiles on an N x K level with halo H: rows in blocks of TH
+// (the last absorbs the remainder), columns in blocks of TW (the last is
+// the short one).  Must match the tile bounds k_up computes.
+static TileGeom up_geom(int N, int K, int TH, int TW, int H, int A) {
+    TileGeom t{};
+    t.TH = TH; t.TW = TW;
+    t.ntj = std::max(1, (N - 1) / TH);
+    t.ntk = std::max(1, cdivi(K - 1, TW));
+    for (int tj = 0; tj < t.ntj; tj++) {
+        const int j0 = tj * TH, j1 = (tj == t.ntj - 1) ? N : j0 + TH;
+        t.BH = std::max(t.BH, std::min(N, j1 + H) - std::max(0, j0 - H));
+    }
+    for (int tk = 0; tk < t.ntk; tk++) {
+        const int k0 = tk * TW, k1 = (tk == t.ntk - 1) ? K : k0 + TW;
+        t.W = std::max(t.W, std::min(K, k1 + H) - (std::max(0, k0 - H) & ~(A - 1)));
+    }
+    t.W = round_up(t.W, A);
+    return t;
+}
+
+// k_down tiles: coarse rows / columns in blocks of CH / CW over the coarse
+// Nc x Kc level; the fine box spans rows 2cj0-2-S .. 2cj1+S.  Must match
+// the tile bounds k_down computes.
+static TileGeom down_geom(int Nc, int Kc, int N, int K, int CH, int CW, int S, int A) {
+    TileGeom t{};
+    t.TH = CH; t.TW = CW;
+    t.ntj = std::max(1, (Nc - 1) / CH);
+    t.ntk = std::max(1, cdivi(Kc - 1, CW));
+    for (int tj = 0; tj < t.ntj; tj++) {
+        const int c0 = tj * CH, c1 = (tj == t.ntj - 1) ? Nc : c0 + CH;
+        t.BH = std::max(t.BH, std::min(N, 2 * c1 + S + 1) - std::max(0, 2 * c0 - 2 - S));
+    }
+    for (int tk = 0; tk < t.ntk; tk++) {
+        const int c0 = tk * CW, c1 = (tk == t.ntk - 1) ? Kc : c0 + CW;
+        t.W = std::max(t.W, std::min(K, 2 * c1 + S + 1) - (std::max(0, 2 * c0 - 2 - S) & ~(A - 1)));
+    }
+    t.W = round_up(t.W, A);
+    return t;
+}
+
+template <typename T>
+static size_t up_smem(const TileGeom &t, bool has_f, bool prolong) {
+    size_t b = tile_bytes<T>(t.BH, t.W, has_f) + kSmemSlack;
+    if (prolong) b += sizeof(T) * (size_t)(t.BH / 2 + 2) * (t.W / 2 + 2);
+    return b;
+}
+
+// widest TW with W <= kBoxW, then the tallest TH that fits two CTAs per SM
+// and still gives about a wave of CTAs
+template <typename T>
+static TileGeom pick_up(int N, int K, int H, bool has_f, bool prolong) {
+    const int A = TileCfg<T>::kAlign;
+    int tw = std::max(A, (kBoxW - 2 * H) / A * A);
+    while (tw > A && up_geom(N, K, 8, tw, H, A).W > kBoxW) tw -= A;
+    TileGeom best{};
+    bool found = false;
+    for (int th = 64; th >= 8; th /= 2) {
+        TileGeom t = up_geom(N, K, th, tw, H, A);
+        t.smem = up_smem<T>(t, has_f, prolong);
+        if (t.smem > two_cta_smem() && th > 8) continue;
+        best = t;
+        found = true;
+        if (t.ntj * t.ntk >= kWaveCtas) break;
+    }
+    if (!found) best = up_geom(N, K, 8, tw, H, A);
+    best.smem = up_smem<T>(best, has_f, prolong);
+    return best;
+}
+
+template <typename T>
+static TileGeom pick_down(int Nc, int Kc, int N, int K, int S, bool has_f) {
+    const int A = TileCfg<T>::kAlign;
+    int cw = std::max(2, (kDownBoxW - 2 * S - 3) / 2);
+    while (cw > 2 && down_geom(Nc, Kc, N, K, 8, cw, S, A).W > kDownBoxW) cw--;
+    TileGeom best{};
+    for (int ch = 32; ch >= 4; ch /= 2) {
+        TileGeom t = down_geom(Nc, Kc, N, K, ch, cw, S, A);
+        t.smem = tile_bytes<T>(t.BH, t.W, has_f) + kSmemSlack;
+        best = t;
+        if (t.smem > two_cta_smem() && ch > 4) continue;
+        if (t.ntj * t.ntk >= kWaveCtas) break;
+    }
+    return best;
+}
+
 template <typename T>
 static int launch_down(qd_solver *s, Level<T> *Ls, int l, int S, int zero_u) {
     const LvArgs<T> g = lv(s, Ls, l), c = lv(s, Ls, l + 1);
-    int TE = tile_edge<T>(g.N);
-    int CH = TE / 2, CW = (sizeof(T) == 4 ? TE : 2 * TE) / 2;
-    const int ntj = std::max(1, (c.N - 1) / CH), ntk = std::max(1, (c.K - 1) / CW);
-    // largest tile: the last one absorbs the remainder; the box covers it
-    // plus the column rounding of the aligned origin
-    const int maxCH = c.N - (ntj - 1) * CH, maxCW = c.K - (ntk - 1) * CW;
-    const int A = TileCfg<T>::kAlign;
-    const int BH = 2 * maxCH + 2 * S + 3, W = round_up(2 * maxCW + 2 * S + 3 + A - 1, A);
-    const bool has_f = (g.f != nullptr) || sizeof(T) == 4;
-    const size_t smem = tile_bytes<T>(BH, W, has_f) + kSmemSlack;
+    // the residual goes into f, or into the dinv slot on the FP64 level 0
+    const bool has_f = g.f != nullptr;
+    const TileGeom t = pick_down<T>(c.N, c.K, g.N, g.K, S, has_f);
+    const int BH = t.BH, W = t.W, CH = t.TH, CW = t.TW, ntj = t.ntj, ntk = t.ntk;
+    const size_t smem = t.smem;
     if (BH > 256 || W > 256 || smem > smem_limit()) {
         set_error("k_down tile %dx%d (%zu B of shared memory) exceeds the TMA box or smem", BH, W, smem);
         return QD_ERR_ARG;
@@ -360,16 +512,10 @@ static int launch_up(qd_solver *s, Level<T> *Ls, int l, int S, int prolong, int 
                      double *u64 = nullptr, int P64 = 0, int *nblocks = nullptr) {
     const LvArgs<T> g = lv(s, Ls, l);
     const LvArgs<T> c = (l + 1 < s->nlev) ? lv(s, Ls, l + 1) : g;
-    const int TE = tile_edge<T>(g.N);
-    const int TH = TE, TW = sizeof(T) == 4 ? TE : 2 * TE;
-    const int ntj = std::max(1, (g.N - 1) / TH), ntk = std::max(1, (g.K - 1) / TW);
-    const int maxTH = g.N - (ntj - 1) * TH, maxTW = g.K - (ntk - 1) * TW;
     const int R1 = MODE == 1 ? 1 : 0;
-    const int A = TileCfg<T>::kAlign;
-    const int BH = maxTH + 2 * (S + R1), W = round_up(maxTW + 2 * (S + R1) + A - 1, A);
-    size_t smem = tile_bytes<T>(BH, W, g.f != nullptr);
-    if (prolong) smem += sizeof(T) * (size_t)(BH / 2 + 2) * (W / 2 + 2);
-    smem += kSmemSlack;
+    const TileGeom t = pick_up<T>(g.N, g.K, S + R1, g.f != nullptr, prolong != 0);
+    const int BH = t.BH, W = t.W, TH = t.TH, TW = t.TW, ntj = t.ntj, ntk = t.ntk;
+    const size_t smem = t.smem;
     if (BH > 256 || W > 256 || smem > smem_limit()) {
         set_error("k_up tile %dx%d (%zu B of shared memory) exceeds the TMA box or smem", BH, W, smem);
         return QD_ERR_ARG;
@@ -396,8 +542,8 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t
                                   const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
-int make_tensor_map_2d(CUtensorMap *map, const void *base, bool fp64, int width, int height,
-                       int pitch, int box_w, int box_h) {
+int encode_tiled_2d(CUtensorMap *map, const void *base, int dtype, int esz, long width, long height,
+                    long pitch_bytes, int box_w, int box_h, int swizzle) {
     static EncodeTiledFn fn = nullptr;
     if (!fn) {
         void *p = nullptr;
@@ -410,26 +556,35 @@ int make_tensor_map_2d(CUtensorMap *map, const void *base, bool fp64, int width,
         }
         fn = (EncodeTiledFn)p;
     }
-    const size_t esz = fp64 ? 8 : 4;
-    if (!base || ((uintptr_t)base & 15) || (pitch * esz) % 16 || (box_w * esz) % 16 || box_w < 1 ||
-        box_w > 256 || box_h < 1 || box_h > 256 || width < 1 || height < 1) {
-        set_error("tensor map %dx%d pitch %d box %dx%d violates the TMA rules", width, height, pitch,
-                  box_w, box_h);
+    const int sw_bytes = swizzle == CU_TENSOR_MAP_SWIZZLE_128B ? 128
+                         : swizzle == CU_TENSOR_MAP_SWIZZLE_64B ? 64
+                         : swizzle == CU_TENSOR_MAP_SWIZZLE_32B ? 32 : 0;
+    if (!base || ((uintptr_t)base & 15) || pitch_bytes % 16 || ((long)box_w * esz) % 16 || box_w < 1 ||
+        box_w > 256 || box_h < 1 || box_h > 256 || width < 1 || height < 1 ||
+        (sw_bytes && (long)box_w * esz > sw_bytes)) {
+        set_error("tensor map %ldx%ld pitch %ld B box %dx%d violates the TMA rules", width, height,
+                  pitch_bytes, box_w, box_h);
         return QD_ERR_ARG;
     }
     const cuuint64_t dims[2] = {(cuuint64_t)width, (cuuint64_t)height};
-    const cuuint64_t strides[1] = {(cuuint64_t)pitch * esz};
+    const cuuint64_t strides[1] = {(cuuint64_t)pitch_bytes};
     const cuuint32_t box[2] = {(cuuint32_t)box_w, (cuuint32_t)box_h};
     const cuuint32_t es[2] = {1, 1};
-    const CUresult r = fn(map, fp64 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
-                          const_cast<void *>(base), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    const CUresult r = fn(map, (CUtensorMapDataType)dtype, 2, const_cast<void *>(base), dims, strides, box,
+                          es, CU_TENSOR_MAP_INTERLEAVE_NONE, (CUtensorMapSwizzle)swizzle,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
         set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
         return QD_ERR_CUDA;
     }
     return QD_OK;
+}
+
+int make_tensor_map_2d(CUtensorMap *map, const void *base, bool fp64, int width, int height,
+                       int pitch, int box_w, int box_h) {
+    const int esz = fp64 ? 8 : 4;
+    return encode_tiled_2d(map, base, fp64 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                           esz, width, height, (long)pitch * esz, box_w, box_h, CU_TENSOR_MAP_SWIZZLE_NONE);
 }
 
 void tma_cache_free(qd_solver *s) {
@@ -461,6 +616,44 @@ static int first_tail_level(const qd_solver *s) {
     return lt;
 }
 
+// the single-CTA coarse tail from level lt down
+template <typename T>
+static int launch_tail(qd_solver *s, Level<T> *Ls, int lt) {
+    const int nl = s->nlev;
+    TailArgs<T> ta;
+    for (int l = 0; l < nl; l++) ta.L[l] = lv(s, Ls, l);
+    ta.p.l0 = lt; ta.p.nlev = nl; ta.p.nu_pre = s->opt.nu_pre; ta.p.nu_post = s->opt.nu_post;
+    ta.p.nu_coarse = s->opt.nu_coarse; ta.p.surface = s->opt.surface_prolong;
+    ta.p.coarse_solve = s->opt.coarse_solve;
+    ta.p.nint = s->n_cint;
+    ta.img = static_cast<const T *>(s->d_tail_img[sizeof(T) == 8]);
+    ta.status = &s->d_status->flags;
+    if (!ta.img || s->tail_l0 != lt) {
+        set_error("coarse tail image missing");
+        return QD_ERR_ARG;
+    }
+    const size_t img = tail_layout<T>(s, lt, &ta.p);
+    if (ta.p.coarse_solve && ta.p.ainv_off < 0) {
+        set_error("coarse_solve needs a coarsest level of at most 1024 unknowns");
+        return QD_ERR_ARG;
+    }
+    // the work arrays always live in shared memory; the image prefix
+    // takes what is left (static shared memory and alignment kept aside)
+    const size_t budget = smem_limit() - 4096, work = tail_work_bytes<T>(s, lt);
+    if (work > budget) {
+        set_error("coarse tail needs %zu B of shared memory", work);
+        return QD_ERR_ARG;
+    }
+    const size_t prefix = std::min(img, (budget - work) / 128 * 128);
+    ta.p.img_smem = (int)prefix;
+    ta.p.work_off = (int)prefix;
+    const size_t smem = prefix + work + kSmemSlack;
+    QD_TRY(set_smem(k_tail<T>, smem));
+    k_tail<T><<<1, NT_TAIL, smem, s->stream>>>(ta);
+    QD_LAUNCH_CHECK(s);
+    return QD_OK;
+}
+
 // One V-cycle on hierarchy Ls.  zero0: level 0 starts from a zero guess.
 // MODE of level 0's k_up: 1 = plain (with residual norm), 2 = add into u64.
 template <typename T, int MODE0>
@@ -478,26 +671,7 @@ static int vcycle_fused(qd_solver *s, Level<T> *Ls, int zero0, int *nblocks) {
     }
     // coarse tail (or the coarsest level on its own)
     if (lt < nl) {
-        TailArgs<T> ta;
-        for (int l = 0; l < nl; l++) ta.L[l] = lv(s, Ls, l);
-        ta.p.l0 = lt; ta.p.nlev = nl; ta.p.nu_pre = s->opt.nu_pre; ta.p.nu_post = s->opt.nu_post;
-        ta.p.nu_coarse = s->opt.nu_coarse; ta.p.surface = s->opt.surface_prolong;
-        ta.p.coarse_solve = s->opt.coarse_solve;
-        ta.p.nint = s->n_cint;
-        ta.ainv = sizeof(T) == 8 ? (const T *)s->d_ainv64 : (const T *)s->d_ainv32;
-        if (ta.p.coarse_solve && (s->n_cint == 0 || !ta.ainv)) {
-            set_error("coarse_solve needs a coarsest level of at most 1024 unknowns");
-            return QD_ERR_ARG;
-        }
-        ta.p.coef_smem = tail_smem_bytes<T>(s, lt, 1) <= smem_limit();
-        const size_t smem = tail_smem_bytes<T>(s, lt, ta.p.coef_smem);
-        if (smem > smem_limit()) {
-            set_error("coarse tail needs %zu B of shared memory", smem);
-            return QD_ERR_ARG;
-        }
-        QD_TRY(set_smem(k_tail<T>, smem));
-        k_tail<T><<<1, NT_TAIL, smem, s->stream>>>(ta);
-        QD_LAUNCH_CHECK(s);
+        QD_TRY(launch_tail<T>(s, Ls, lt));
     } else {
         if (s->opt.coarse_solve) {
             set_error("coarse_solve needs the coarsest level in the single-CTA tail (<= 65 rows)");
@@ -536,5 +710,112 @@ static int vcycle_fused(qd_solver *s, Level<T> *Ls, int zero0, int *nblocks) {
 int vcycle64_norm(qd_solver *s, int *nblocks) { return vcycle_fused<double, 1>(s, s->L64, 0, nblocks); }
 
 int vcycle32_into64(qd_solver *s) { return vcycle_fused<float, 2>(s, s->L32, 1, nullptr); }
+
+// One kernel of the V-cycle the solver's precision runs, launched `reps`
+// times back to back on the solver's stream between two events: the
+// per-launch time of a kernel that otherwise runs inside the solve graph.
+// The launches change the solver's state (they smooth, restrict and add
+// corrections), so this is for measurements after a run.
+template <typename T, int MODE_UP>
+static int time_kernel_t(qd_solver *s, Level<T> *Ls, int which, int reps) {
+    const int S = std::min(2 * s->opt.nu_pre, SMAX), S1 = std::min(2 * s->opt.nu_post, SMAX);
+    for (int i = 0; i < reps; i++) {
+        switch (which) {
+            case QD_KERNEL_DOWN0:
+                QD_TRY(launch_down<T>(s, Ls, 0, S, 0));
+                break;
+            case QD_KERNEL_UP0: {
+                int nb = 0;
+                QD_TRY((launch_up<T, MODE_UP>(s, Ls, 0, S1, 1, 0, s->L64[0].u, s->dims[0].P, &nb)));
+                break;
+            }
+            case QD_KERNEL_TAIL:
+                if (s->tail_l0 >= s->nlev) {
+                    set_error("this hierarchy has no coarse tail");
+                    return QD_ERR_ARG;
+                }
+                QD_TRY(launch_tail<T>(s, Ls, s->tail_l0));
+                break;
+            default:
+                set_error("unknown kernel id %d", which);
+                return QD_ERR_ARG;
+        }
+    }
+    return QD_OK;
+}
+
+int time_kernel(qd_solver *s, int which, int reps, double *us) {
+    if (s->nlev < 2 || reps < 1) {
+        set_error("time_kernel needs two levels and reps >= 1");
+        return QD_ERR_ARG;
+    }
+    cudaEvent_t e0, e1;
+    QD_CUDA(cudaEventCreate(&e0));
+    QD_CUDA(cudaEventCreate(&e1));
+    int rc = QD_OK;
+    if (cudaEventRecord(e0, s->stream) != cudaSuccess) rc = QD_ERR_CUDA;
+    if (rc == QD_OK) {
+        if (which == QD_KERNEL_RESIDUAL)
+            for (int i = 0; i < reps && rc == QD_OK; i++) rc = level0_norm(s, 1, 0);
+        else if (s->opt.precision == QD_PREC_MIXED)
+            rc = time_kernel_t<float, 2>(s, s->L32, which, reps);
+        else
+            rc = time_kernel_t<double, 1>(s, s->L64, which, reps);
+    }
+    float ms = 0.f;
+    if (rc == QD_OK && (cudaEventRecord(e1, s->stream) != cudaSuccess ||
+                        cudaEventSynchronize(e1) != cudaSuccess ||
+                        cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)) {
+        set_error("time_kernel: event timing failed");
+        rc = QD_ERR_CUDA;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc == QD_OK) *us = 1e3 * ms / reps;
+    return rc;
+}
+
+// pack one hierarchy's tail moduli (and the coarsest inverse) into its image
+template <typename T>
+static int build_image(qd_solver *s, const Level<T> *Ls, const T *ainv, void **out) {
+    const int lt = s->tail_l0;
+    TailLevels p;
+    const size_t bytes = tail_layout<T>(s, lt, &p);
+    T *img = nullptr;
+    QD_CUDA(cudaMalloc(&img, bytes));
+    *out = img;
+    QD_CUDA(cudaMemsetAsync(img, 0, bytes, s->stream));
+    if (p.ainv_off >= 0 && ainv)
+        QD_CUDA(cudaMemcpyAsync(img + p.ainv_off, ainv, sizeof(T) * (size_t)s->n_cint * s->n_cint,
+                                cudaMemcpyDeviceToDevice, s->stream));
+    for (int l = lt; l < s->nlev; l++) {
+        const LevelDims &d = s->dims[l];
+        const long n = (long)d.N * d.K;
+        T *cx = img + p.coef_off[l], *cz = cx + img_pad<T>(n), *dv = cz + img_pad<T>(n + d.K);
+        const size_t w = sizeof(T) * d.K, sp = sizeof(T) * d.P;
+        QD_CUDA(cudaMemcpy2DAsync(cx, w, Ls[l].cx, sp, w, d.N, cudaMemcpyDeviceToDevice, s->stream));
+        QD_CUDA(cudaMemcpy2DAsync(cz, w, Ls[l].cz, sp, w, d.N + 1, cudaMemcpyDeviceToDevice, s->stream));
+        QD_CUDA(cudaMemcpy2DAsync(dv, w, Ls[l].dinv, sp, w, d.N, cudaMemcpyDeviceToDevice, s->stream));
+    }
+    return QD_OK;
+}
+
+// Set-up of the coarse-tail images, once the moduli and the coarsest
+// inverse exist (end of mg_alloc).
+int tail_image_build(qd_solver *s) {
+    s->tail_l0 = first_tail_level<float>(s);
+    if (s->tail_l0 >= s->nlev) return QD_OK;
+    QD_TRY(build_image<float>(s, s->L32, s->d_ainv32, &s->d_tail_img[0]));
+    QD_TRY(build_image<double>(s, s->L64, s->d_ainv64, &s->d_tail_img[1]));
+    QD_CUDA(cudaStreamSynchronize(s->stream));
+    return QD_OK;
+}
+
+void tail_image_free(qd_solver *s) {
+    for (int i = 0; i < 2; i++) {
+        cudaFree(s->d_tail_img[i]);
+        s->d_tail_img[i] = nullptr;
+    }
+}
 
 }  // namespace qd

@@ -25,8 +25,6 @@
 namespace qd {
 
 // declared in mg.cu
-int level0_norm(qd_solver *s, int to32, int slot);
-int r0_norm(qd_solver *s, int slot);
 __global__ void k_final_sum(const double *partial, int n, double *out);
 
 struct SolveGraph {

@@ -10,9 +10,9 @@
 // four neighbours lie in the tile, and the halo is as wide as the number of
 // half-sweeps, so the core ends exact.
 //
-// FP64 tiles stage 1/diag (a double division costs ~30 instructions on
-// GB300's FP64 pipe); FP32 tiles recompute it with a correctly rounded
-// reciprocal, which frees shared memory for two CTAs per SM.
+// Tiles stage 1/diag with the other arrays: a division (or a correctly
+// rounded reciprocal) per update costs more issue slots than one more
+// shared-memory load, and the boxes are sized so two CTAs still fit per SM.
 #pragma once
 
 #include "tma.cuh"
@@ -25,12 +25,9 @@ namespace qd {
 
 template <typename T>
 struct TileCfg {
-    static constexpr bool kDinv = sizeof(T) == 8;
+    static constexpr bool kDinv = true;                  // 1/diag staged (dv array)
     static constexpr int kAlign = 16 / (int)sizeof(T);   // elements per 16 bytes
 };
-
-__device__ __forceinline__ float recip(float x) { return __frcp_rn(x); }
-__device__ __forceinline__ double recip(double x) { return 1.0 / x; }
 
 // tensor maps of one level's arrays, boxes of W x BH (cz: W x BH+1)
 struct TileMaps {
@@ -79,12 +76,14 @@ __device__ __forceinline__ STile<T> carve(unsigned char *raw, int jL0, int kL0, 
     return t;
 }
 
-// Stage the tile.  u is zero-filled instead of loaded when zero_u; f is
-// zero-filled when the level has no right-hand side but the kernel keeps an
-// array for it.  Returns false (in every thread) if the copies did not land.
+// Stage the tile: tile_issue starts the copies, tile_wait waits for them
+// (the threads may do independent work in between).  u is zero-filled
+// instead of loaded when zero_u; f is zero-filled when the level has no
+// right-hand side but the kernel keeps an array for it.  tile_wait returns
+// false (in every thread) if the copies did not land.
 template <typename T>
-__device__ bool tile_load(const LvArgs<T> &g, const TileMaps &m, STile<T> &t, bool zero_u,
-                          uint64_t *bar, unsigned *status) {
+__device__ void tile_issue(const LvArgs<T> &g, const TileMaps &m, STile<T> &t, bool zero_u,
+                           uint64_t *bar) {
     const int BH = m.BH, W = m.W;
     const bool load_f = t.f && g.f;
     if (threadIdx.x == 0) mbar_init(bar, 1);
@@ -109,9 +108,19 @@ __device__ bool tile_load(const LvArgs<T> &g, const TileMaps &m, STile<T> &t, bo
         for (int i = threadIdx.x; i < n; i += blockDim.x) t.u[i] = (T)0;
     if (t.f && !g.f)
         for (int i = threadIdx.x; i < n; i += blockDim.x) t.f[i] = (T)0;
+}
+
+__device__ __forceinline__ bool tile_wait(uint64_t *bar, unsigned *status) {
     const bool ok = mbar_wait(bar, 0);
-    if (!ok && status) atomicOr(status, 1u);
+    if (!ok && status) atomicOr(status, ST_TMA_TIMEOUT);
     return __syncthreads_and(ok) != 0;
+}
+
+template <typename T>
+__device__ bool tile_load(const LvArgs<T> &g, const TileMaps &m, STile<T> &t, bool zero_u,
+                          uint64_t *bar, unsigned *status) {
+    tile_issue(g, m, t, zero_u, bar);
+    return tile_wait(bar, status);
 }
 
 // one colour over the tile
@@ -131,8 +140,7 @@ __device__ void tile_halfsweep(const LvArgs<T> &g, const STile<T> &t, int color)
             const T cW = t.cx[idx - 1], cE = t.cx[idx], cN = t.cz[idx], cS = t.cz[idx + t.W];
             T acc = cW * t.u[idx - 1] + cE * t.u[idx + 1] + cN * t.u[sn + c] + cS * t.u[ss + c];
             if (t.f) acc -= g.h2 * t.f[idx];
-            const T d = TileCfg<T>::kDinv ? t.dv[idx] : recip(((cW + cE) + cN) + cS);
-            t.u[idx] = d * acc;
+            t.u[idx] = t.dv[idx] * acc;
         }
     }
 }
@@ -182,7 +190,7 @@ __global__ void __launch_bounds__(NT, 2)
     const int LR = min(maps.BH, g.N - jL0), LC = min(maps.W, g.K - kL0);
     // the residual goes into f (FP32 levels and FP64 coarse levels all have
     // one) or, on the FP64 level 0 with its zero right-hand side, into dv
-    const bool has_f = (g.f != nullptr) || !TileCfg<T>::kDinv;
+    const bool has_f = g.f != nullptr;
     STile<T> t = carve<T>(smem, jL0, kL0, LR, LC, maps.BH, maps.W, has_f);
     if (!tile_load(g, maps, t, zero_u != 0, &bar, status)) return;
     for (int s = 0; s < S; s++) {
@@ -250,21 +258,22 @@ __global__ void __launch_bounds__(NT, 2)
     const int kL0 = max(0, k0 - S - R1) & ~(TileCfg<T>::kAlign - 1);
     const int LR = min(maps.BH, g.N - jL0), LC = min(maps.W, g.K - kL0);
     STile<T> t = carve<T>(smem, jL0, kL0, LR, LC, maps.BH, maps.W, g.f != nullptr);
-    const bool ok = tile_load(g, maps, t, zero_u != 0, &bar, status);
+    tile_issue(g, maps, t, zero_u != 0, &bar);
+    // coarse block covering the tile, gathered while the tile copies fly
+    const int jL1 = jL0 + LR, kL1 = kL0 + LC;
+    const int cjA = jL0 >> 1, cjB = min(c.N - 1, ((jL1 - 1) >> 1) + 1);
+    const int ckA = kL0 >> 1, ckB = min(c.K - 1, ((kL1 - 1) >> 1) + 1);
+    const int EW = ckB - ckA + 1;
+    T *E = reinterpret_cast<T *>(smem + tile_bytes<T>(maps.BH, maps.W, g.f != nullptr));
+    if (prolong)
+        for (int r = TWARP; r <= cjB - cjA; r += TNWARP)
+            for (int cc = TLANE; cc < EW; cc += 32) E[r * EW + cc] = c.u[(long)(cjA + r) * c.P + ckA + cc];
+    const bool ok = tile_wait(&bar, status);
     if (!ok) {
         if (MODE == 1 && threadIdx.x == 0) partial[blockIdx.y * gridDim.x + blockIdx.x] = 0.0;
         return;
     }
     if (prolong) {
-        // coarse block covering the tile, staged after the tile arrays
-        const int jL1 = jL0 + LR, kL1 = kL0 + LC;
-        const int cjA = jL0 >> 1, cjB = min(c.N - 1, ((jL1 - 1) >> 1) + 1);
-        const int ckA = kL0 >> 1, ckB = min(c.K - 1, ((kL1 - 1) >> 1) + 1);
-        const int EW = ckB - ckA + 1;
-        T *E = reinterpret_cast<T *>(smem + tile_bytes<T>(maps.BH, maps.W, g.f != nullptr));
-        for (int r = TWARP; r <= cjB - cjA; r += TNWARP)
-            for (int cc = TLANE; cc < EW; cc += 32) E[r * EW + cc] = c.u[(long)(cjA + r) * c.P + ckA + cc];
-        __syncthreads();
         // u += P e (prolongate_kernel, :1034-1040)
         for (int r = TWARP; r < LR; r += TNWARP) {
             const int j = jL0 + r;
@@ -289,6 +298,35 @@ __global__ void __launch_bounds__(NT, 2)
         __syncthreads();
     }
     const int ka = max(1, k0), kb = min(g.K - 2, k1 - 1);
+    if (MODE == 2) {
+        // u64 += e: the loads of two rows x two columns go out before any
+        // store, so each warp waits on memory once per four nodes
+        for (int jb = j0 + TWARP; jb < j1; jb += 2 * TNWARP) {
+            double a[2][2];
+#pragma unroll
+            for (int q = 0; q < 2; q++)
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const int j = jb + q * TNWARP, k = ka + TLANE + 32 * h;
+                    a[q][h] = (j < j1 && k <= kb) ? __ldcg(u64 + (long)j * P64 + k) : 0.0;
+                }
+#pragma unroll
+            for (int q = 0; q < 2; q++)
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const int j = jb + q * TNWARP, k = ka + TLANE + 32 * h;
+                    if (j < j1 && k <= kb)
+                        u64[(long)j * P64 + k] = a[q][h] + (double)t.u[(j - jL0) * t.W + (k - kL0)];
+                }
+            for (int q = 0; q < 2; q++) {   // columns past 64 (wide tiles only)
+                const int j = jb + q * TNWARP;
+                if (j >= j1) break;
+                for (int k = ka + TLANE + 64; k <= kb; k += 32)
+                    u64[(long)j * P64 + k] += (double)t.u[(j - jL0) * t.W + (k - kL0)];
+            }
+        }
+        return;
+    }
     double sq = 0.0;
     for (int j = j0 + TWARP; j < j1; j += TNWARP) {
         const int r = j - jL0;

@@ -86,7 +86,7 @@ struct DevStatus {
 };
 enum : unsigned int { ST_NEWTON_NAN = 1u, ST_NEWTON_CAP = 2u, ST_NEWTON_BRACKET = 4u };
 // set by a multigrid tile kernel whose TMA staging did not complete
-static constexpr unsigned int ST_TMA_TIMEOUT = 1u;
+static constexpr unsigned int ST_TMA_TIMEOUT = 8u;
 
 // state of the device-driven multigrid loop (mg_graph.cu)
 struct SolveState {
@@ -97,6 +97,40 @@ struct SolveState {
     unsigned long long total_cycles, total_solves;
     unsigned long long kernels;           // kernels the solve graphs ran
 };
+
+// binary64 -> binary32 with round-to-nearest-even, on the integer pipes.
+// GB300's FP64 pipe also executes the hardware F2F conversion, and that pipe
+// bounds the mixed-precision residual kernel; this routine follows the IEEE
+// 754 definition directly: keep the top 23 of the 52 fraction bits, round on
+// the 29 dropped bits (ties to even) and let a carry out of the fraction
+// bump the exponent (which also rounds the largest values to infinity as
+// RNE requires).  Results below the normal binary32 range round the full
+// 53-bit significand to a multiple of 2^-149 the same way (a carry reaches
+// the smallest normal); |x| >= 2^128 gives infinity; NaN stays NaN.  No
+// FP64 instruction is involved.
+__device__ __forceinline__ float d2f_rne(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned hi = (unsigned)(b >> 32), sign = hi & 0x80000000u;
+    const int ex = (int)((hi >> 20) & 0x7FFu);
+    const unsigned long long frac = b & 0xFFFFFFFFFFFFFull;
+    if (ex == 0x7FF) return __uint_as_float(sign | 0x7F800000u | (frac ? 0x00400000u : 0u));
+    const int e = ex - 1023 + 127;
+    if (e >= 255) return __uint_as_float(sign | 0x7F800000u);
+    if (e >= 1) {
+        unsigned q = (unsigned)(frac >> 29);
+        const unsigned rem = (unsigned)(frac & 0x1FFFFFFFull), half = 0x10000000u;
+        q += (rem > half || (rem == half && (q & 1u))) ? 1u : 0u;
+        return __uint_as_float((sign | ((unsigned)e << 23)) + q);
+    }
+    // binary32 subnormal range: units of 2^-149 are m >> (30 - e)
+    const int shift = 30 - e;
+    if (ex == 0 || shift >= 54) return __uint_as_float(sign);
+    const unsigned long long m = frac | (1ull << 52);
+    const unsigned long long rem = m & ((1ull << shift) - 1), half = 1ull << (shift - 1);
+    unsigned q = (unsigned)(m >> shift);
+    q += (rem > half || (rem == half && (q & 1u))) ? 1u : 0u;
+    return __uint_as_float(sign | q);
+}
 
 }  // namespace qd
 
@@ -115,6 +149,9 @@ struct qd_solver {
     float *d_ainv32;
     int n_cint;            // its order: coarsest N * (K-2) interior unknowns
     void *tma_cache;       // tensor maps of the tile kernels (mg_fused.cu)
+    void *d_tail_img[2];   // coarse-tail coefficient images, FP32 [0] and FP64 [1]
+    void *unet;            // attached warm-start network (unet.cu), or null
+    int tail_l0;           // first level of the coarse tail
     void *solve_graph;     // the instantiated multigrid graph (mg_graph.cu)
     qd::SolveState *d_solve, *h_solve;
     int n_partial;
@@ -146,6 +183,13 @@ int build_coarse_inverse(qd_solver *s);
 int vcycle64_norm(qd_solver *s, int *nblocks);
 int vcycle32_into64(qd_solver *s);
 void tma_cache_free(qd_solver *s);
+int tail_image_build(qd_solver *s);
+int time_kernel(qd_solver *s, int which, int reps, double *us);
+// mg.cu: level-0 norms into d_scal[slot] (to32: FP64 residual -> FP32 rhs)
+int level0_norm(qd_solver *s, int to32, int slot);
+int convert_f64_f32(const double *in, float *out, int n);
+int r0_norm(qd_solver *s, int slot);
+void tail_image_free(qd_solver *s);
 // mg_graph.cu
 int mg_solve_async(qd_solver *s);
 int solve_state_read(qd_solver *s, SolveState *out);
@@ -165,4 +209,9 @@ int launch_dpsi(qd_solver *s, const double *psi, const double *V, double *dpsi);
 void rk_tableau(double c[7], double b[7], double hb[7], double a[7][7]);
 // medium.cu
 int set_medium_gpu(int ni, int nk, const double *mu_node, double *mu_equi);
+// unet.cu: the learned warm start around a stage solve
+int warm_start_before_boundary(qd_solver *s);
+int warm_start_after_boundary(qd_solver *s);
+int warm_start_after_solve(qd_solver *s);
+void warm_start_detach(qd_solver *s);
 }  // namespace qd

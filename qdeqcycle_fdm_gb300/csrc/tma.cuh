@@ -71,5 +71,9 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, i
 // elements apart, `height` rows) with a box of box_w x box_h elements
 int make_tensor_map_2d(CUtensorMap *map, const void *base, bool fp64, int width, int height,
                        int pitch, int box_w, int box_h);
+// general form: dtype a CUtensorMapDataType, esz its bytes, swizzle a
+// CUtensorMapSwizzle (the box row must fit the swizzle span)
+int encode_tiled_2d(CUtensorMap *map, const void *base, int dtype, int esz, long width, long height,
+                    long pitch_bytes, int box_w, int box_h, int swizzle);
 
 }  // namespace qd

@@ -1,0 +1,264 @@
+// unet_conv.cuh -- 3x3 convolutions of the warm-start U-Net on tcgen05.
+//
+// Activations are BF16, NHWC, on a padded grid: H+2 rows of Wp >= W+2
+// pixels (Wp a multiple of 8), the border pixels held at zero, flattened to
+// P = (H+2)*Wp pixel rows of C channels.  With that layout a 3x3 tap (dy,dx)
+// is a shift of the pixel index by dy*Wp + dx, so
+//
+//   out[p, n] = sum_t sum_c in[p + shift_t, c] * W[t][n][c]
+//
+// is nine accumulated GEMMs whose A operand is the activation tile shifted
+// by whole pixel rows -- the TMA box origin moves along the outer (pixel)
+// coordinate, which needs no alignment, and out-of-range rows arrive as
+// zeros.  No im2col buffer exists.
+//
+// k_conv_fwd: one CTA per 128 output pixels, N = Cout accumulator columns
+//   in tensor memory.  K steps = 9 taps x (Cin / KB) channel blocks of
+//   KB = min(Cin, 64) channels (rows of 32, 64 or 128 bytes, matching
+//   swizzle).  Warp 0 lane 0 streams A/B tiles with TMA through a STAGES-deep
+//   ring of mbarriers, warp 1 lane 0 issues the MMAs, warp 2 owns the tensor
+//   memory, and all four warps run the epilogue (bias, ReLU, gradient mask,
+//   border zeroing, BF16 or FP32 store).  The same kernel computes the data
+//   gradient of a convolution, with the tap order reversed and the weights
+//   transposed per tap.
+// k_conv_wgrad: dW[t][co][ci] = sum_p dY[p, co] * X[p + shift_t, ci] with
+//   pixel-contiguous (planar) copies of dY and X: M = Cout rows (padded to
+//   128 by the TMA zero fill), N = Cin, K = a chunk of pixels; one CTA per
+//   (chunk, tap) adds its partial product into dW with FP32 atomics.
+//   The X copies are pre-shifted by dx in {-1, 0, 1}, so the remaining tap
+//   shift dy*Wp is a multiple of 8 pixels (16 bytes): a legal TMA x origin.
+//
+// Every wait is bounded; a wait that gives up records ST_UNET_TIMEOUT in the
+// status word and the kernel winds down without further waits on copies it
+// never issued.
+#pragma once
+
+#include "tc.cuh"
+
+namespace qd {
+
+static constexpr unsigned ST_UNET_TIMEOUT = 16u;
+static constexpr int CONV_STAGES = 4;
+static constexpr int CONV_THREADS = 128;
+
+struct ConvArgs {
+    int Cin, Cout, KB;        // channels; channel block per K step
+    int Wp, H, W, P;          // padded grid: P = (H+2)*Wp pixels, interior 1..H x 1..W
+    int relu;                 // apply ReLU
+    const float *bias;        // Cout (nullable)
+    __nv_bfloat16 *out;       // NHWC Cout (or null when out_f32 is set)
+    float *out_f32;           // channel 0 only, P floats (nullable)
+    const __nv_bfloat16 *mask;  // multiply by (mask > 0), NHWC Cout (nullable)
+    int tap_reverse;          // data-gradient mode: tap t reads shift of tap 8-t
+    unsigned *status;
+};
+
+__device__ __forceinline__ int tap_shift(int t, int Wp) { return (t / 3 - 1) * Wp + (t % 3 - 1); }
+
+__device__ __forceinline__ bool interior_pixel(int p, const ConvArgs &a) {
+    const int r = p / a.Wp, c = p - r * a.Wp;
+    return r >= 1 && r <= a.H && c >= 1 && c <= a.W;
+}
+
+template <int KB, int COUT>
+__global__ void __launch_bounds__(CONV_THREADS) k_conv_fwd(const __grid_constant__ CUtensorMap ta,
+                                                           const __grid_constant__ CUtensorMap tb,
+                                                           ConvArgs a) {
+    constexpr int ROWB = KB * 2;                        // bytes per operand row
+    constexpr int ABYTES = 128 * ROWB, BBYTES = COUT * ROWB;
+    constexpr int STAGE = ((ABYTES + BBYTES) + 1023) / 1024 * 1024;
+    constexpr uint32_t TCOLS = COUT <= 32 ? 32 : (COUT <= 64 ? 64 : (COUT <= 128 ? 128 : 256));
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t full[CONV_STAGES], empty[CONV_STAGES], done;
+    __shared__ uint32_t tmem_base;
+    unsigned char *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = blockIdx.x * 128;
+    const int nkb = a.Cin / KB, nsteps = 9 * nkb;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < CONV_STAGES; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(&done, 1);
+    }
+    if (warp == 2) tmem_alloc(&tmem_base, TCOLS);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base;
+
+    if (warp == 0 && lane == 0) {
+        // producer
+        for (int s = 0; s < nsteps; s++) {
+            const int st = s % CONV_STAGES;
+            if (s >= CONV_STAGES && !mbar_wait(&empty[st], ((s / CONV_STAGES) - 1) & 1)) {
+                atomicOr(a.status, ST_UNET_TIMEOUT);
+                break;
+            }
+            const int t = s / nkb, kb = s - t * nkb;
+            const int ts = a.tap_reverse ? 8 - t : t;
+            unsigned char *sa = smem + st * STAGE, *sb = sa + ABYTES;
+            mbar_expect_tx(&full[st], ABYTES + BBYTES);
+            tma_load_2d(sa, &ta, kb * KB, m0 + tap_shift(ts, a.Wp), &full[st]);
+            tma_load_2d(sb, &tb, kb * KB, t * COUT, &full[st]);
+        }
+    } else if (warp == 1 && lane == 0) {
+        // MMA issuer
+        constexpr uint32_t idesc = idesc_bf16_f32(COUT);
+        bool ok = true;
+        for (int s = 0; s < nsteps && ok; s++) {
+            const int st = s % CONV_STAGES;
+            if (!mbar_wait(&full[st], (s / CONV_STAGES) & 1)) {
+                atomicOr(a.status, ST_UNET_TIMEOUT);
+                ok = false;
+                break;
+            }
+            tc_fence_after();
+            const uint32_t sa = smem_u32(smem + st * STAGE), sb = sa + ABYTES;
+#pragma unroll
+            for (int k = 0; k < KB / 16; k++)
+                mma_bf16(tmem, smem_desc(sa + 32 * k, ROWB), smem_desc(sb + 32 * k, ROWB), idesc,
+                         (s > 0 || k > 0) ? 1u : 0u);
+            mma_commit(&empty[st]);
+        }
+        mma_commit(&done);
+    }
+    __syncwarp();
+    // epilogue: thread (warp, lane) owns pixel m0 + 32*warp + lane
+    const bool ok = mbar_wait(&done, 0);
+    if (!ok && threadIdx.x == 0) atomicOr(a.status, ST_UNET_TIMEOUT);
+    tc_fence_after();
+    const int p = m0 + 32 * warp + lane;
+    const bool in = p < a.P && interior_pixel(p, a);
+#pragma unroll
+    for (int n0 = 0; n0 < COUT; n0 += 8) {
+        float v[8];
+        tmem_ld8(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)n0, v);
+        if (p >= a.P || !ok) continue;
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            float x = v[i] + (a.bias ? a.bias[n0 + i] : 0.f);
+            if (a.relu) x = fmaxf(x, 0.f);
+            v[i] = x;
+        }
+        if (a.mask && in) {
+            const uint4 mk = *reinterpret_cast<const uint4 *>(a.mask + (size_t)p * COUT + n0);
+            const __nv_bfloat16 *mv = reinterpret_cast<const __nv_bfloat16 *>(&mk);
+#pragma unroll
+            for (int i = 0; i < 8; i++)
+                if (!(__bfloat162float(mv[i]) > 0.f)) v[i] = 0.f;
+        }
+        if (!in) {
+#pragma unroll
+            for (int i = 0; i < 8; i++) v[i] = 0.f;
+        }
+        if (a.out_f32) {
+            if (n0 == 0) a.out_f32[p] = v[0];
+        } else {
+            uint4 o;
+            __nv_bfloat162 *ov = reinterpret_cast<__nv_bfloat162 *>(&o);
+#pragma unroll
+            for (int i = 0; i < 4; i++) ov[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+            *reinterpret_cast<uint4 *>(a.out + (size_t)p * COUT + n0) = o;
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 2) tmem_free(tmem, TCOLS);
+}
+
+struct WgradArgs {
+    int Cin, Cout, Wp, P;
+    int chunk;                // pixels per CTA (a multiple of 64)
+    float *dW;                // [9][Cout][Cin] FP32, accumulated
+    unsigned *status;
+};
+
+// B operands: X pre-shifted by dx = -1, 0, +1 (planar, Cin rows of P pixels)
+struct WgradMaps {
+    CUtensorMap dy;           // planar dY: Cout rows of P pixels, box 64 x 128
+    CUtensorMap x[3];         // planar X shifted by dx, box 64 x Cin
+};
+
+template <int CIN>
+__global__ void __launch_bounds__(CONV_THREADS) k_conv_wgrad(const __grid_constant__ WgradMaps maps,
+                                                             WgradArgs a) {
+    constexpr int ROWB = 128;                            // 64 pixels of BF16
+    constexpr int ABYTES = 128 * ROWB, BBYTES = CIN * ROWB;
+    constexpr int STAGE = ((ABYTES + BBYTES) + 1023) / 1024 * 1024;
+    constexpr uint32_t TCOLS = CIN <= 32 ? 32 : (CIN <= 64 ? 64 : (CIN <= 128 ? 128 : 256));
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t full[CONV_STAGES], empty[CONV_STAGES], done;
+    __shared__ uint32_t tmem_base;
+    unsigned char *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int t = blockIdx.y, dy = t / 3 - 1, dx = t % 3 - 1;
+    const int p0 = blockIdx.x * a.chunk;
+    const int nsteps = min(a.chunk, a.P - p0 + 63) / 64;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < CONV_STAGES; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(&done, 1);
+    }
+    if (warp == 2) tmem_alloc(&tmem_base, TCOLS);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base;
+
+    if (warp == 0 && lane == 0) {
+        for (int s = 0; s < nsteps; s++) {
+            const int st = s % CONV_STAGES;
+            if (s >= CONV_STAGES && !mbar_wait(&empty[st], ((s / CONV_STAGES) - 1) & 1)) {
+                atomicOr(a.status, ST_UNET_TIMEOUT);
+                break;
+            }
+            unsigned char *sa = smem + st * STAGE, *sb = sa + ABYTES;
+            const int px = p0 + 64 * s;
+            mbar_expect_tx(&full[st], ABYTES + BBYTES);
+            tma_load_2d(sa, &maps.dy, px, 0, &full[st]);
+            tma_load_2d(sb, &maps.x[dx + 1], px + dy * a.Wp, 0, &full[st]);
+        }
+    } else if (warp == 1 && lane == 0) {
+        constexpr uint32_t idesc = idesc_bf16_f32(CIN);
+        for (int s = 0; s < nsteps; s++) {
+            const int st = s % CONV_STAGES;
+            if (!mbar_wait(&full[st], (s / CONV_STAGES) & 1)) {
+                atomicOr(a.status, ST_UNET_TIMEOUT);
+                break;
+            }
+            tc_fence_after();
+            const uint32_t sa = smem_u32(smem + st * STAGE), sb = sa + ABYTES;
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                mma_bf16(tmem, smem_desc(sa + 32 * k, ROWB), smem_desc(sb + 32 * k, ROWB), idesc,
+                         (s > 0 || k > 0) ? 1u : 0u);
+            mma_commit(&empty[st]);
+        }
+        mma_commit(&done);
+    }
+    __syncwarp();
+    const bool ok = mbar_wait(&done, 0) && nsteps > 0;
+    if (!ok && nsteps > 0 && threadIdx.x == 0) atomicOr(a.status, ST_UNET_TIMEOUT);
+    tc_fence_after();
+    const int co = 32 * warp + lane;
+#pragma unroll
+    for (int n0 = 0; n0 < CIN; n0 += 8) {
+        float v[8];
+        tmem_ld8(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)n0, v);
+        if (!ok || co >= a.Cout) continue;
+        float *dst = a.dW + ((size_t)t * a.Cout + co) * a.Cin + n0;
+#pragma unroll
+        for (int i = 0; i < 8; i++) atomicAdd(dst + i, v[i]);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 2) tmem_free(tmem, TCOLS);
+}
+
+}  // namespace qd

@@ -296,3 +296,38 @@ def test_gpu_runs_are_bitwise_reproducible():
     for key in ("Slip", "psi", "V", "U"):
         assert np.array_equal(outs[0][key], outs[1][key]), key
     assert outs[0]["t"] == outs[1]["t"]
+
+
+def test_f64_to_f32_rounding_matches_ieee():
+    """The residual kernel's integer-pipe FP64 -> FP32 rounding (d2f_rne)
+    equals IEEE round-to-nearest-even (numpy's cast) bit for bit: random
+    values over the whole binary32 exponent range, exact ties with even and
+    odd kept fractions, the overflow boundary, subnormal results, zeros,
+    infinities and NaN."""
+    import ctypes as C
+    from qdeqcycle_fdm_gb300 import _lib
+    rng = np.random.default_rng(7)
+    x = [rng.uniform(-1, 1, 20000) * 10.0 ** rng.uniform(-46, 39, 20000)]
+    # ties: fraction bits below the kept 23 are exactly one half
+    frac = rng.integers(0, 1 << 23, 4000, dtype=np.uint64) << np.uint64(29)
+    tie = frac | np.uint64(1 << 28)
+    exp = rng.integers(1023 - 126, 1023 + 127, 4000).astype(np.uint64) << np.uint64(52)
+    x.append((tie | exp).view(np.float64))
+    x.append(((tie + np.uint64(1)) | exp).view(np.float64))   # just above a tie
+    x.append(((tie - np.uint64(1)) | exp).view(np.float64))   # just below a tie
+    fmax = float(np.finfo(np.float32).max)
+    x.append(np.array([fmax, np.nextafter(fmax, np.inf), fmax * (1 + 2.0 ** -25), fmax * (1 + 2.0 ** -24),
+                       2.0 ** -126, 2.0 ** -127, 2.0 ** -149, 2.0 ** -150, 2.0 ** -151, 1e-300,
+                       0.0, -0.0, np.inf, -np.inf, np.nan, 1.0, -1.0, 1.0 + 2.0 ** -24,
+                       1.0 + 3 * 2.0 ** -24]))
+    x = np.ascontiguousarray(np.concatenate(x))
+    out = np.empty(x.size, dtype=np.float32)
+    L = _lib.load()
+    rc = L.qd_convert_f64_to_f32(x.ctypes.data_as(C.POINTER(C.c_double)),
+                                 out.ctypes.data_as(C.POINTER(C.c_float)), x.size)
+    assert rc == 0, L.qd_last_error().decode()
+    with np.errstate(over="ignore"):
+        ref = x.astype(np.float32)
+    nan = np.isnan(ref)
+    assert np.array_equal(np.isnan(out), nan)
+    assert np.array_equal(out[~nan].view(np.uint32), ref[~nan].view(np.uint32))
