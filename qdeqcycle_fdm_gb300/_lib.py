@@ -13,6 +13,7 @@ from .build import LIB
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
+_fp = C.POINTER(C.c_float)
 
 QD_OK, QD_ERR_ARG, QD_ERR_CUDA, QD_ERR_NOMEM, QD_ERR_NOT_CONVERGED, QD_ERR_NEWTON, QD_ERR_STATE = range(7)
 QD_TOL_ABS, QD_TOL_REL = 0, 1
@@ -38,7 +39,7 @@ EXPORTS = [
     ("qd_mg_vcycle", C.c_int, [C.c_void_p]),
     ("qd_mg_residual_norm", C.c_int, [C.c_void_p, _dp]),
     ("qd_mg_time_kernel", C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp]),
-    ("qd_convert_f64_to_f32", C.c_int, [_dp, C.POINTER(C.c_float), C.c_int]),
+    ("qd_convert_f64_to_f32", C.c_int, [_dp, _fp, C.c_int]),
     ("qd_residual_norm_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                            C.c_int, C.c_double, C.c_void_p, _dp]),
     ("qd_fault_setup", C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp, C.c_double,
@@ -53,6 +54,17 @@ EXPORTS = [
     ("qd_rk43_get_scalars", C.c_int, [C.c_void_p, _dp, _ip]),
     ("qd_rk43_set_state", C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp, C.c_double, C.c_double,
                                     C.c_double, C.c_double, C.c_int]),
+    # include/qdeq_unet.h
+    ("qd_unet_create", C.c_int, [C.c_int, C.c_int, C.c_ulonglong, C.POINTER(C.c_void_p)]),
+    ("qd_unet_destroy", None, [C.c_void_p]),
+    ("qd_unet_num_params", C.c_longlong, [C.c_void_p]),
+    ("qd_unet_get_params", C.c_int, [C.c_void_p, _fp]),
+    ("qd_unet_set_params", C.c_int, [C.c_void_p, _fp]),
+    ("qd_unet_forward_host", C.c_int, [C.c_void_p, _fp, _fp]),
+    ("qd_unet_loss_grad_host", C.c_int, [C.c_void_p, _fp, _fp, _fp, _fp]),
+    ("qd_unet_train_step_host", C.c_int, [C.c_void_p, _fp, _fp, C.c_float, _fp]),
+    ("qd_solver_warm_start", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_float]),
+    ("qd_unet_stats", C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), _fp]),
 ]
 
 

@@ -712,8 +712,7 @@ static int unet_build(qd_unet *u, unsigned long long seed) {
             for (int co = 0; co < Ly.cout; co++)
                 for (int ci = 0; ci < Ly.cin; ci++) {
                     double v = rnd_normal(&st) * sd;
-                    if (ci >= cin_real || (head && co > 0)) v = 0.0;
-                    if (head) v *= 0.1;
+                    if (ci >= cin_real || head) v = 0.0;   // a fresh net predicts no change
                     w[((size_t)t * Ly.cout + co) * Ly.cin + ci] = (float)v;
                 }
         QD_CUDA(cudaMemcpy(Ly.w32, w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice));

@@ -1,0 +1,86 @@
+"""The learned warm start (``include/qdeq_unet.h``): a BF16 U-Net that
+predicts the change a stage solve makes to u, trained online on the
+multigrid's own solutions with the library's tensor-core kernels.
+
+Host arrays follow the header: inputs ``x`` are float32 [4, nk, ni],
+targets and outputs float32 [nk, ni], parameters a flat float32 vector.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._lib import check, load
+
+MODE_OFF, MODE_TRAIN, MODE_PREDICT = 0, 1, 2
+
+
+def _f(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class UNet:
+    def __init__(self, nk: int, ni: int, seed: int = 1):
+        self.L = load()
+        self.nk, self.ni = nk, ni
+        h = C.c_void_p()
+        check(self.L.qd_unet_create(nk, ni, seed, C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.L.qd_unet_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def num_params(self) -> int:
+        return int(self.L.qd_unet_num_params(self.h))
+
+    def get_params(self) -> np.ndarray:
+        out = np.empty(self.num_params, dtype=np.float32)
+        check(self.L.qd_unet_get_params(self.h, _f(out)))
+        return out
+
+    def set_params(self, theta) -> None:
+        t = np.ascontiguousarray(theta, dtype=np.float32)
+        assert t.size == self.num_params
+        check(self.L.qd_unet_set_params(self.h, _f(t)))
+
+    def forward(self, x) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.empty((self.nk, self.ni), dtype=np.float32)
+        check(self.L.qd_unet_forward_host(self.h, _f(x), _f(y)))
+        return y
+
+    def loss_grad(self, x, target):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(target, dtype=np.float32)
+        loss = C.c_float(0)
+        g = np.empty(self.num_params, dtype=np.float32)
+        check(self.L.qd_unet_loss_grad_host(self.h, _f(x), _f(t), C.byref(loss), _f(g)))
+        return float(loss.value), g
+
+    def train_step(self, x, target, lr: float = 1e-3) -> float:
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(target, dtype=np.float32)
+        loss = C.c_float(0)
+        check(self.L.qd_unet_train_step_host(self.h, _f(x), _f(t), lr, C.byref(loss)))
+        return float(loss.value)
+
+    def attach(self, solver, mode: int, lr: float = 1e-3) -> None:
+        """Couple to an ``api.Solver`` of the same grid (MODE_TRAIN,
+        MODE_PREDICT or MODE_OFF)."""
+        check(self.L.qd_solver_warm_start(solver.h, self.h if mode else None, mode, lr))
+
+    def stats(self):
+        n = C.c_longlong(0)
+        loss = C.c_float(0)
+        check(self.L.qd_unet_stats(self.h, C.byref(n), C.byref(loss)))
+        return int(n.value), float(loss.value)

@@ -1,5 +1,5 @@
 """The C-ABI library builds for sm_103a here, loads without a GPU, and
-exports every entry point include/qdeq.h declares."""
+exports every entry point include/qdeq.h and include/qdeq_unet.h declare."""
 import os
 import re
 
@@ -17,6 +17,7 @@ def declared(header):
 def test_library_exports_every_declared_symbol(gpu_lib):
     names = declared("qdeq.h")
     assert len(names) >= 20
+    names += declared("qdeq_unet.h")
     missing = [n for n in names if not hasattr(gpu_lib, n)]
     assert not missing, missing
 
@@ -25,6 +26,7 @@ def test_python_bindings_cover_header():
     from qdeqcycle_fdm_gb300 import _lib
     bound = {n for n, _, _ in _lib.EXPORTS}
     assert set(declared("qdeq.h")) <= bound
+    assert set(declared("qdeq_unet.h")) <= bound
 
 
 def test_version_and_defaults(gpu_lib):

@@ -1,0 +1,137 @@
+"""The warm-start U-Net's tensor-core kernels against the CPU oracle
+(oracle/unet_oracle.py, BF16 rounding emulated at the points where the GPU
+stores BF16), and the network coupled to the solver.
+
+Tolerances: the GPU accumulates in FP32 in a different order than the
+oracle's float64 sums, so a BF16 rounding occasionally lands one unit apart
+and the difference grows through the 15 layers; outputs are held to 3e-2
+relative (max-norm), the loss to 2e-2, every layer's gradient to a cosine
+of 0.995 with the oracle's and 5e-2 relative in norm.
+"""
+import numpy as np
+import pytest
+
+from oracle import unet_oracle as uo
+from qdeqcycle_fdm_gb300 import warmstart
+
+pytestmark = pytest.mark.gpu
+
+N = 33
+
+
+def rel(a, b):
+    return float(np.max(np.abs(np.asarray(a) - np.asarray(b))) / max(np.max(np.abs(b)), 1e-30))
+
+
+def random_theta(seed):
+    rng = np.random.default_rng(seed)
+    parts = []
+    for ci, co, _ in uo.layer_shapes():
+        w = rng.normal(size=(9, co, ci)) * np.sqrt(2.0 / (9 * ci))
+        b = rng.normal(size=co) * 0.05
+        parts.append((w, b))
+    return uo.pack(parts).astype(np.float32)
+
+
+@pytest.fixture(scope="module")
+def net():
+    u = warmstart.UNet(N, N, seed=3)
+    yield u
+    u.close()
+
+
+def test_fresh_network_predicts_zero(net):
+    x = np.random.default_rng(0).normal(size=(4, N, N)).astype(np.float32)
+    assert np.all(net.forward(x) == 0.0)
+    assert net.num_params == uo.num_params()
+
+
+def test_forward_matches_oracle(net):
+    theta = random_theta(1)
+    net.set_params(theta)
+    assert np.array_equal(net.get_params(), theta)
+    x = np.random.default_rng(2).normal(size=(4, N, N)).astype(np.float32)
+    y = net.forward(x)
+    yo = uo.UNet(theta, bf16_mode=True).forward(np.moveaxis(x, 0, -1))
+    assert np.all(np.isfinite(y))
+    assert rel(y, yo) < 3e-2, rel(y, yo)
+
+
+def test_loss_and_gradients_match_oracle(net):
+    theta = random_theta(4)
+    net.set_params(theta)
+    rng = np.random.default_rng(5)
+    x = rng.normal(size=(4, N, N)).astype(np.float32)
+    target = rng.normal(size=(N, N)).astype(np.float32)
+    loss, g = net.loss_grad(x, target)
+    lo, _, go = uo.UNet(theta, bf16_mode=True).loss_grad(np.moveaxis(x, 0, -1), target)
+    assert abs(loss - lo) <= 2e-2 * lo, (loss, lo)
+    off = 0
+    for i, (ci, co, _) in enumerate(uo.layer_shapes()):
+        n = 9 * co * ci + co
+        a, b = g[off:off + n].astype(np.float64), go[off:off + n]
+        off += n
+        nb = np.linalg.norm(b)
+        if nb == 0:
+            assert np.linalg.norm(a) == 0
+            continue
+        cos = float(a @ b / (np.linalg.norm(a) * nb))
+        assert cos > 0.995, (i, cos)
+        assert np.linalg.norm(a - b) <= 5e-2 * nb, (i, np.linalg.norm(a - b) / nb)
+
+
+def test_adam_training_reduces_the_loss(net):
+    theta = random_theta(6) * 0.5
+    net.set_params(theta)
+    rng = np.random.default_rng(7)
+    x = rng.normal(size=(4, N, N)).astype(np.float32)
+    yy, xx = np.mgrid[0:N, 0:N] / (N - 1)
+    target = (np.sin(3 * yy) * np.exp(-2 * xx)).astype(np.float32)
+    losses = [net.train_step(x, target, 3e-3) for _ in range(80)]
+    assert np.all(np.isfinite(losses))
+    assert losses[-1] < 0.2 * losses[0], (losses[0], losses[-1])
+
+
+def test_warm_start_coupled_to_the_solver():
+    """Online training for T accepted steps, then prediction for K steps, on
+    a 65 x 65 problem with the mixed-precision solver.  The multigrid still
+    iterates to its tolerance from the predicted field, so the run follows
+    the plain run (the states agree to the solver tolerance's effect); the
+    V-cycles per solve of both runs are reported."""
+    import dataclasses
+    from qdeqcycle_fdm_gb300 import api, config, problem
+    cfg = config.small(65)
+    mg = dataclasses.replace(cfg.mg, precision=1, surface_prolong=1, coarse_solve=1, tol=1e-9)
+    prob = problem.build_problem(cfg)
+    T, K = 60, 30
+
+    def cycles(a, b):
+        return (b["vcycles"] - a["vcycles"]) / max(1, b["solves"] - a["solves"])
+
+    plain = api.Simulation(prob, mg)
+    plain.start()
+    plain.step(T)
+    p0 = plain.state(with_u=False)
+    plain.step(K)
+    p1 = plain.state(with_u=False)
+    plain.close()
+
+    net = warmstart.UNet(65, 65, seed=1)
+    sim = api.Simulation(prob, mg)
+    net.attach(sim.solver, warmstart.MODE_TRAIN, 1e-3)
+    sim.start()
+    sim.step(T)
+    w0 = sim.state(with_u=False)
+    steps, loss = net.stats()
+    net.attach(sim.solver, warmstart.MODE_PREDICT)
+    sim.step(K)
+    w1 = sim.state(with_u=False)
+    sim.close()
+    net.close()
+    c_plain, c_ws = cycles(p0, p1), cycles(w0, w1)
+    print(f"\nwarm start: {steps} training steps, last loss {loss:.3e}; "
+          f"V-cycles per solve {c_ws:.3f} (plain {c_plain:.3f})")
+    assert steps == w0["solves"] and np.isfinite(loss)
+    for k in ("Slip", "psi"):
+        assert rel(w1[k], p1[k]) < 1e-5, (k, rel(w1[k], p1[k]))
+    assert abs(w1["t"] - p1["t"]) <= 1e-6 * p1["t"]
