@@ -6,13 +6,17 @@ cycle at 1025 x 1025 (config 1 physics: layered mu, +-5% a-b perturbation,
 A "step" is one accepted adaptive-RK43 step: the ARK4(3)6L stages, each an
 elliptic multigrid solve plus the fault stress / Newton / aging-law update,
 retried until the error test passes, then the refresh solve at the new state.
-Warm-up steps start from the steady-sliding initial state (V = Vp); the timed
-steps are the next K steps of the same run.  value = simulated years advanced
-in the timed steps / their device time in hours.
+Every GPU run starts from the steady-sliding initial state (V = Vp), takes T
+untimed steps (--train-steps; the learned run trains its U-Net online on every
+stage solve of these steps), W untimed warm-up steps, and times the next K
+steps.  value = simulated years advanced in the timed steps / their device
+time in hours.
 
 Arms:
-  default           this library on the GPU (mixed precision: FP32 V-cycles in
-                    FP64 refinement); the plain FP64 multigrid is measured too
+  default           this library on the GPU: the learned warm start with FP32
+                    V-cycles in FP64 refinement (the headline); the same
+                    solver without the network, and the plain FP64 multigrid,
+                    are measured on the same steps
   --impl reference  the reference algorithm on the host cores (the CPU
                     oracle restating odeSolver.cpp / fault.cpp: 6 levels,
                     V(32,32)), same config, same steps
@@ -53,6 +57,11 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--headline-only", action="store_true",
                    help="time only the headline solver (no FP64 comparison, e2e or CPU runs)")
+    p.add_argument("--train-steps", type=int, default=100,
+                   help="untimed steps before the warm-up (the learned run trains online on them)")
+    p.add_argument("--no-learned", action="store_true", help="headline without the learned warm start")
+    p.add_argument("--lr", type=float, default=1e-3)
+    p.add_argument("--seed", type=int, default=1)
     return p.parse_args()
 
 
@@ -188,10 +197,9 @@ def run_reference(args):
 # GPU arm
 # ---------------------------------------------------------------------------
 def run_ours(args):
-    import numpy as np
     import torch
 
-    from qdeqcycle_fdm_gb300 import api, build, config, problem, replicas
+    from qdeqcycle_fdm_gb300 import api, build, config, problem, replicas, warmstart
     rank, world, local = replicas.env()
     torch.cuda.set_device(local)
     replicas.init("nccl")          # replicas only: the data path has no collective
@@ -199,23 +207,35 @@ def run_ours(args):
     cfg = config.CONFIGS[args.config]()
     prob = problem.build_problem(cfg)            # face moduli homogenised on the GPU
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    T = args.train_steps
 
     def barrier():
         if world > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    def timed_run(mg, label, host_io=False):
-        """W untimed steps, then K steps each bracketed by CUDA events on the
-        solver's stream (L2 flushed before each).  host_io: every step goes
+    def timed_run(mg, host_io=False, learned=False):
+        """T untimed steps from steady sliding (the learned run trains its
+        network online on every stage solve of these steps, then predicts),
+        W untimed warm-up steps, then K steps each bracketed by CUDA events on
+        the solver's stream (L2 flushed before each).  host_io: every step goes
         through the C ABI with host buffers -- state and u uploaded from
         pinned memory before, read back after (the e2e measurement)."""
         sim = api.Simulation(prob, mg)
+        net, info = None, {}
+        if learned:
+            net = warmstart.UNet(prob.nk, prob.ni, seed=args.seed)
+            net.attach(sim.solver, warmstart.MODE_TRAIN, args.lr)
         sim.start()
+        sim.step(T)
+        if learned:
+            n, loss = net.stats()
+            info = {"train_samples": n, "last_loss": loss}
+            net.attach(sim.solver, warmstart.MODE_PREDICT)
         sim.step(args.warmup)
         stream = torch.cuda.ExternalStream(sim.solver.stream_ptr())
         s0 = sim.state(with_u=False)
-        ms, step_ms, step_t = 0.0, [], [s0["t"]]
+        ms, step_ms = 0.0, []
         if host_io:
             nz, nx = prob.nz, prob.nx
 
@@ -251,14 +271,13 @@ def run_ours(args):
                     hv[k][:] = st[k]
             step_ms.append(e0.elapsed_time(e1))
             ms += step_ms[-1]
-            step_t.append(sim.solver.rk43_state()["t"])
         barrier()
         s1 = sim.state(with_u=False)
-        return sim, {"ms": ms, "yrs": (s1["t"] - s0["t"]) / YEAR_S, "step_ms": step_ms,
-                     "step_t": step_t,
-                     "launches": s1["kernel_launches"] - s0["kernel_launches"],
-                     "vcycles": s1["vcycles"] - s0["vcycles"], "solves": s1["solves"] - s0["solves"],
-                     "attempts": s1["attempts"] - s0["attempts"], "t_end": s1["t"]}
+        return sim, net, {"ms": ms, "yrs": (s1["t"] - s0["t"]) / YEAR_S, "step_ms": step_ms,
+                          "t0": s0["t"], "t_end": s1["t"],
+                          "launches": s1["kernel_launches"] - s0["kernel_launches"],
+                          "vcycles": s1["vcycles"] - s0["vcycles"], "solves": s1["solves"] - s0["solves"],
+                          "attempts": s1["attempts"] - s0["attempts"], **info}
 
     def job_value(run):
         """whole-job simulated yr/hr: years of all replicas / slowest rank's hours"""
@@ -267,44 +286,63 @@ def run_ours(args):
     def reduce_max(x):
         return replicas.aggregate(0.0, x, device="cuda")[1]
 
-    clocks = Clocks(local)
-    clocks.start()
+    def summary(run):
+        return {"value": job_value(run), "ms_per_step": reduce_max(run["ms"]) / args.steps,
+                "vcycles_per_solve": run["vcycles"] / max(1, run["solves"]),
+                "sim_years_timed": run["yrs"]}
+
     mixed_cfg = config.MGConfig(**{**cfg.mg.__dict__, "precision": 1, "surface_prolong": 1,
                                    "coarse_solve": 1})
     fp64_cfg = config.MGConfig(**{**cfg.mg.__dict__, "precision": 0, "surface_prolong": 0})
     fp64s_cfg = config.MGConfig(**{**cfg.mg.__dict__, "precision": 0, "surface_prolong": 1,
                                    "coarse_solve": 1})
-    sim, head = timed_run(mixed_cfg, "mixed")
+    learned = not args.no_learned
+    peaks = _peaks()
+    clocks = Clocks(local)
+    clocks.start()
+    sim, net, head = timed_run(mixed_cfg, learned=learned)
     clk = clocks.stop()
     ms_max = reduce_max(head["ms"])
     value = job_value(head)
+    extra = {}
+    if learned:
+        simm, _, mixed = timed_run(mixed_cfg)
+        simm.close()
+        extra["mixed_no_learned"] = summary(mixed)
+        us_f, fl_f = net.time("forward", 10)
+        us_t, fl_t = net.time("train", 5)
+        bf = peaks.get("bf16_tflops", 1900.0)
+        extra["warm_start"] = {
+            "network": "U-Net 4 levels 16/32/64/128 ch, 3x3 conv, BF16 in / FP32 accumulate (tcgen05)",
+            "train_steps": T, "train_samples": head.get("train_samples"), "last_loss": head.get("last_loss"),
+            "lr": args.lr,
+            "inference_us": us_f, "inference_tflops": fl_f / (us_f * 1e-6) / 1e12,
+            "train_step_us": us_t, "train_tflops": fl_t / (us_t * 1e-6) / 1e12,
+            "tensor_peak_tflops": bf, "inference_frac_of_peak": fl_f / (us_f * 1e-6) / 1e12 / bf}
     if args.headline_only:
         args.no_e2e = args.no_cpu_baseline = True
-        plain = plain_s = {"yrs": 0.0, "ms": float("nan"), "vcycles": 0, "solves": 0}
+        plain = plain_s = None
         plain_value = None
     else:
-        sim64, plain = timed_run(fp64_cfg, "fp64")
+        sim64, _, plain = timed_run(fp64_cfg)
         sim64.close()
-        sim64s, plain_s = timed_run(fp64s_cfg, "fp64+surface")
+        sim64s, _, plain_s = timed_run(fp64s_cfg)
         sim64s.close()
         plain_value = plain["yrs"] / (reduce_max(plain["ms"]) / 3.6e6)
 
-    # Roofline of the V-cycle's kernels.  Inside a solve they run in a CUDA
-    # graph, so each is timed by qd_mg_time_kernel: REPS back-to-back
-    # launches on the solver's stream between two CUDA events, on the
-    # headline solver's own state after the timed run.  Algorithmic bytes
-    # per launch are the unfused algorithm's traffic (FP32 hierarchy):
+    # Roofline of the V-cycle's kernels (the headline solver's hierarchy).
+    # Inside a solve they run in a CUDA graph, so each is timed by
+    # qd_mg_time_kernel: REPS back-to-back launches on the solver's stream
+    # between two CUDA events, on the solver's own state after the timed run.
+    # Algorithmic bytes per launch are the unfused algorithm's traffic:
     #   down0    2 red+black sweeps x 20 B + residual/restriction 16 B per
     #            level-0 node, + 4 B per level-1 node
     #   up0      prolongation 8 B + 2 sweeps x 20 B + u64 += e 16 B per
     #            level-0 node, + 4 B per level-1 node
     #   residual FP64 u, cx, cz, diag read + FP32 rhs written: 36 B per node
     # The dominant kernel (largest time per V-cycle) is the roofline entry.
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except (OSError, ValueError):
-        pass
+    if net is not None:
+        net.attach(sim.solver, warmstart.MODE_OFF)
     peak = peaks.get("hbm_gbs", 6800.0)
     n0 = cfg.ni * cfg.nk
     n1 = ((cfg.ni - 1) // 2 + 1) * ((cfg.nk - 1) // 2 + 1)
@@ -333,8 +371,10 @@ def run_ours(args):
     # end to end through the C ABI with host buffers (pinned), the same steps
     e2e = None
     if not args.no_e2e:
-        sim_e, io = timed_run(mixed_cfg, "mixed-host-io", host_io=True)
+        sim_e, net_e, io = timed_run(mixed_cfg, host_io=True, learned=learned)
         sim_e.close()
+        if net_e is not None:
+            net_e.close()
         e2e = {"value": job_value(io), "unit": "sim_yr/hr",
                "h2d_bytes_per_step": 8 * (4 * prob.nz + prob.ni * prob.nk),
                "d2h_bytes_per_step": 8 * (5 * prob.nz + prob.ni * prob.nk),
@@ -343,44 +383,52 @@ def run_ours(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         r = run_cpu(prob, args.warmup, args.steps, budget_s=args.cpu_sample_s)
-        n = r["steps"]
-        g_yrs = (head["step_t"][n] - head["step_t"][0]) / YEAR_S
-        g_ms = sum(head["step_ms"][:n])
         cpu = {"value": r["value"], "unit": "sim_yr/hr", "cores": r["threads"], "kind": "port",
                "sample": f"oracle (reference algorithm, {r['schedule']}): accepted steps "
-                         f"{args.warmup + 1}..{args.warmup + n} (the first {n} timed steps), "
-                         f"{r['wall_s']:.1f}s",
-               "gpu_value_same_steps": g_yrs / (g_ms / 3.6e6) if g_ms > 0 else None}
+                         f"{args.warmup + 1}..{args.warmup + r['steps']} from steady sliding, "
+                         f"{r['wall_s']:.1f}s"}
 
     if rank == 0:
+        mode = ("learned warm start + FP32 cycles in FP64 refinement" if learned
+                else "FP32 cycles in FP64 refinement")
         line = {
             "metric": METRIC, "value": value, "unit": "sim_yr/hr", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
-            "data": "synthetic",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64+f32+bf16" if learned else "f64+f32", "data": "synthetic",
             "config": {"workload": f"{cfg.name}: {cfg.ni}x{cfg.nk} earthquake cycle, accepted RK43 steps "
-                                   f"{args.warmup + 1}..{args.warmup + args.steps} from steady sliding",
+                                   f"{T + args.warmup + 1}..{T + args.warmup + args.steps} from steady "
+                                   f"sliding",
                        "mg": f"{cfg.mg.n_levels} levels V({cfg.mg.nu_pre},{cfg.mg.nu_post}), "
-                             f"rel {cfg.mg.tol:g}, FP32 cycles in FP64 refinement, exact coarsest solve, surface-row "
-                             f"prolongation",
+                             f"rel {cfg.mg.tol:g}, {mode}, exact coarsest solve, surface-row prolongation",
                        "parallelism": f"replicas x{world}", "l2": "flushed before every timed step"},
-            "sim_years_timed": head["yrs"], "t_end_s": head["t_end"],
+            "sim_years_timed": head["yrs"], "t_start_s": head["t0"], "t_end_s": head["t_end"],
             "vcycles_per_solve": head["vcycles"] / max(1, head["solves"]),
             "attempts_per_step": head["attempts"] / args.steps,
-            "plain_fp64": {"value": plain_value, "ms_per_step": plain["ms"] / args.steps,
-                           "vcycles_per_solve": plain["vcycles"] / max(1, plain["solves"]),
-                           "mg": "reference prolongation (no surface-row correction)"},
-            "fp64_surface_prolong": {"value": plain_s["yrs"] / (plain_s["ms"] / 3.6e6),
-                                     "ms_per_step": plain_s["ms"] / args.steps,
-                                     "vcycles_per_solve": plain_s["vcycles"] / max(1, plain_s["solves"])},
+            **extra,
+            "plain_fp64": None if plain is None else {
+                "value": plain_value, "ms_per_step": plain["ms"] / args.steps,
+                "vcycles_per_solve": plain["vcycles"] / max(1, plain["solves"]),
+                "mg": "reference prolongation (no surface-row correction)"},
+            "fp64_surface_prolong": None if plain_s is None else summary(plain_s),
             "speedup_vs_plain_fp64": value / world / plain_value if plain_value else None,
             "gpu_launches": head["launches"],
             "roofline": roofline, "clocks": clk, "e2e": e2e, "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)
+    if net is not None:
+        net.close()
+    sim.close()
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def _peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return {}
 
 
 def main():

@@ -65,6 +65,7 @@ EXPORTS = [
     ("qd_unet_train_step_host", C.c_int, [C.c_void_p, _fp, _fp, C.c_float, _fp]),
     ("qd_solver_warm_start", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_float]),
     ("qd_unet_stats", C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), _fp]),
+    ("qd_unet_time", C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp]),
 ]
 
 

@@ -982,6 +982,31 @@ int qd_solver_warm_start(qd_solver *s, qd_unet *u, int mode, float lr) {
     return QD_OK;
 }
 
+int qd_unet_time(qd_unet *u, int what, int reps, double *us, double *flops) {
+    if (!u || (what != 0 && what != 1) || reps < 1 || !us) return QD_ERR_ARG;
+    double f = 0.0;
+    for (const auto &Ly : u->L) {
+        const UGrid &g = u->g[Ly.lvl];
+        const double conv = 2.0 * 9.0 * Ly.cin * Ly.cout * (double)g.H * g.W;
+        f += conv * (what ? (Ly.gin ? 3.0 : 2.0) : 1.0);
+    }
+    if (flops) *flops = f;
+    cudaEvent_t e0, e1;
+    QD_CUDA(cudaEventCreate(&e0));
+    QD_CUDA(cudaEventCreate(&e1));
+    int rc = cudaEventRecord(e0, u->stream) == cudaSuccess ? QD_OK : QD_ERR_CUDA;
+    for (int i = 0; i < reps && rc == QD_OK; i++) rc = what ? loss_and_grad(u) : forward(u);
+    float ms = 0.f;
+    if (rc == QD_OK && (cudaEventRecord(e1, u->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                        cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
+        rc = QD_ERR_CUDA;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc == QD_OK) rc = check_unet_status(u);
+    if (rc == QD_OK) *us = 1e3 * ms / reps;
+    return rc;
+}
+
 int qd_unet_stats(qd_unet *u, long long *train_steps, float *last_loss) {
     if (!u) return QD_ERR_ARG;
     if (train_steps) *train_steps = u->steps;

@@ -79,6 +79,13 @@ class UNet:
         MODE_PREDICT or MODE_OFF)."""
         check(self.L.qd_solver_warm_start(solver.h, self.h if mode else None, mode, lr))
 
+    def time(self, what: str = "forward", reps: int = 10):
+        """(microseconds per run, tensor-core FLOPs per run) of one inference
+        ("forward") or one training step without the update ("train")."""
+        us, fl = C.c_double(0), C.c_double(0)
+        check(self.L.qd_unet_time(self.h, 0 if what == "forward" else 1, reps, C.byref(us), C.byref(fl)))
+        return us.value, fl.value
+
     def stats(self):
         n = C.c_longlong(0)
         loss = C.c_float(0)
