@@ -6,10 +6,12 @@ cycle at 1025 x 1025 (config 1 physics: layered mu, +-5% a-b perturbation,
 A "step" is one accepted adaptive-RK43 step: the ARK4(3)6L stages, each an
 elliptic multigrid solve plus the fault stress / Newton / aging-law update,
 retried until the error test passes, then the refresh solve at the new state.
-Every GPU run starts from the steady-sliding initial state (V = Vp), takes T
-untimed steps (--train-steps; the learned run trains its U-Net online on every
-stage solve of these steps), W untimed warm-up steps, and times the next K
-steps.  value = simulated years advanced in the timed steps / their device
+Every GPU run starts from the steady-sliding initial state (V = Vp), takes W
+untimed warm-up steps and times the next K steps.  The learned warm start's
+U-Net is first trained online for T accepted steps (--train-steps) on a
+separate instance of the workload (another seed of the a-b perturbation),
+one Adam step per stage solve; the timed run then starts every stage solve
+from the network's prediction.  value = simulated years advanced in the timed steps / their device
 time in hours.
 
 Arms:
@@ -58,7 +60,7 @@ def parse():
     p.add_argument("--headline-only", action="store_true",
                    help="time only the headline solver (no FP64 comparison, e2e or CPU runs)")
     p.add_argument("--train-steps", type=int, default=100,
-                   help="untimed steps before the warm-up (the learned run trains online on them)")
+                   help="accepted steps of online training on a separate instance of the workload")
     p.add_argument("--no-learned", action="store_true", help="headline without the learned warm start")
     p.add_argument("--lr", type=float, default=1e-3)
     p.add_argument("--seed", type=int, default=1)
@@ -214,24 +216,35 @@ def run_ours(args):
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    def timed_run(mg, host_io=False, learned=False):
-        """T untimed steps from steady sliding (the learned run trains its
-        network online on every stage solve of these steps, then predicts),
-        W untimed warm-up steps, then K steps each bracketed by CUDA events on
-        the solver's stream (L2 flushed before each).  host_io: every step goes
-        through the C ABI with host buffers -- state and u uploaded from
-        pinned memory before, read back after (the e2e measurement)."""
+    def train_network(mg):
+        """Online training on a separate instance of the workload (the same
+        physics with another seed of the a-b perturbation): T accepted steps
+        from steady sliding, one Adam step per stage solve.  The timed runs
+        then use the network on the benchmark instance, whose states it has
+        not seen."""
+        tcfg = cfg.replace(seed=cfg.seed + 1)
+        tprob = problem.build_problem(tcfg)
+        tsim = api.Simulation(tprob, mg)
+        net = warmstart.UNet(tprob.nk, tprob.ni, seed=args.seed)
+        net.attach(tsim.solver, warmstart.MODE_TRAIN, args.lr)
+        tsim.start()
+        tsim.step(T)
+        n, loss = net.stats()
+        net.attach(tsim.solver, warmstart.MODE_OFF)
+        tsim.close()
+        return net, {"train_samples": n, "last_loss": loss, "train_instance_seed": tcfg.seed}
+
+    def timed_run(mg, host_io=False, net=None):
+        """W untimed warm-up steps from steady sliding, then K steps each
+        bracketed by CUDA events on the solver's stream (L2 flushed before
+        each); with `net` the solve of every stage starts from the network's
+        prediction.  host_io: every step goes through the C ABI with host
+        buffers -- state and u uploaded from pinned memory before, read back
+        after (the e2e measurement)."""
         sim = api.Simulation(prob, mg)
-        net, info = None, {}
-        if learned:
-            net = warmstart.UNet(prob.nk, prob.ni, seed=args.seed)
-            net.attach(sim.solver, warmstart.MODE_TRAIN, args.lr)
-        sim.start()
-        sim.step(T)
-        if learned:
-            n, loss = net.stats()
-            info = {"train_samples": n, "last_loss": loss}
+        if net is not None:
             net.attach(sim.solver, warmstart.MODE_PREDICT)
+        sim.start()
         sim.step(args.warmup)
         stream = torch.cuda.ExternalStream(sim.solver.stream_ptr())
         s0 = sim.state(with_u=False)
@@ -273,11 +286,13 @@ def run_ours(args):
             ms += step_ms[-1]
         barrier()
         s1 = sim.state(with_u=False)
-        return sim, net, {"ms": ms, "yrs": (s1["t"] - s0["t"]) / YEAR_S, "step_ms": step_ms,
-                          "t0": s0["t"], "t_end": s1["t"],
-                          "launches": s1["kernel_launches"] - s0["kernel_launches"],
-                          "vcycles": s1["vcycles"] - s0["vcycles"], "solves": s1["solves"] - s0["solves"],
-                          "attempts": s1["attempts"] - s0["attempts"], **info}
+        if net is not None:
+            net.attach(sim.solver, warmstart.MODE_OFF)
+        return sim, {"ms": ms, "yrs": (s1["t"] - s0["t"]) / YEAR_S, "step_ms": step_ms,
+                     "t0": s0["t"], "t_end": s1["t"],
+                     "launches": s1["kernel_launches"] - s0["kernel_launches"],
+                     "vcycles": s1["vcycles"] - s0["vcycles"], "solves": s1["solves"] - s0["solves"],
+                     "attempts": s1["attempts"] - s0["attempts"]}
 
     def job_value(run):
         """whole-job simulated yr/hr: years of all replicas / slowest rank's hours"""
@@ -298,15 +313,16 @@ def run_ours(args):
                                    "coarse_solve": 1})
     learned = not args.no_learned
     peaks = _peaks()
+    net, tinfo = train_network(mixed_cfg) if learned else (None, {})
     clocks = Clocks(local)
     clocks.start()
-    sim, net, head = timed_run(mixed_cfg, learned=learned)
+    sim, head = timed_run(mixed_cfg, net=net)
     clk = clocks.stop()
     ms_max = reduce_max(head["ms"])
     value = job_value(head)
     extra = {}
     if learned:
-        simm, _, mixed = timed_run(mixed_cfg)
+        simm, mixed = timed_run(mixed_cfg)
         simm.close()
         extra["mixed_no_learned"] = summary(mixed)
         us_f, fl_f = net.time("forward", 10)
@@ -314,8 +330,7 @@ def run_ours(args):
         bf = peaks.get("bf16_tflops", 1900.0)
         extra["warm_start"] = {
             "network": "U-Net 4 levels 16/32/64/128 ch, 3x3 conv, BF16 in / FP32 accumulate (tcgen05)",
-            "train_steps": T, "train_samples": head.get("train_samples"), "last_loss": head.get("last_loss"),
-            "lr": args.lr,
+            "train_steps": T, **tinfo, "lr": args.lr,
             "inference_us": us_f, "inference_tflops": fl_f / (us_f * 1e-6) / 1e12,
             "train_step_us": us_t, "train_tflops": fl_t / (us_t * 1e-6) / 1e12,
             "tensor_peak_tflops": bf, "inference_frac_of_peak": fl_f / (us_f * 1e-6) / 1e12 / bf}
@@ -324,9 +339,9 @@ def run_ours(args):
         plain = plain_s = None
         plain_value = None
     else:
-        sim64, _, plain = timed_run(fp64_cfg)
+        sim64, plain = timed_run(fp64_cfg)
         sim64.close()
-        sim64s, _, plain_s = timed_run(fp64s_cfg)
+        sim64s, plain_s = timed_run(fp64s_cfg)
         sim64s.close()
         plain_value = plain["yrs"] / (reduce_max(plain["ms"]) / 3.6e6)
 
@@ -341,8 +356,6 @@ def run_ours(args):
     #            level-0 node, + 4 B per level-1 node
     #   residual FP64 u, cx, cz, diag read + FP32 rhs written: 36 B per node
     # The dominant kernel (largest time per V-cycle) is the roofline entry.
-    if net is not None:
-        net.attach(sim.solver, warmstart.MODE_OFF)
     peak = peaks.get("hbm_gbs", 6800.0)
     n0 = cfg.ni * cfg.nk
     n1 = ((cfg.ni - 1) // 2 + 1) * ((cfg.nk - 1) // 2 + 1)
@@ -371,10 +384,8 @@ def run_ours(args):
     # end to end through the C ABI with host buffers (pinned), the same steps
     e2e = None
     if not args.no_e2e:
-        sim_e, net_e, io = timed_run(mixed_cfg, host_io=True, learned=learned)
+        sim_e, io = timed_run(mixed_cfg, host_io=True, net=net)
         sim_e.close()
-        if net_e is not None:
-            net_e.close()
         e2e = {"value": job_value(io), "unit": "sim_yr/hr",
                "h2d_bytes_per_step": 8 * (4 * prob.nz + prob.ni * prob.nk),
                "d2h_bytes_per_step": 8 * (5 * prob.nz + prob.ni * prob.nk),
@@ -397,8 +408,7 @@ def run_ours(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64+f32+bf16" if learned else "f64+f32", "data": "synthetic",
             "config": {"workload": f"{cfg.name}: {cfg.ni}x{cfg.nk} earthquake cycle, accepted RK43 steps "
-                                   f"{T + args.warmup + 1}..{T + args.warmup + args.steps} from steady "
-                                   f"sliding",
+                                   f"{args.warmup + 1}..{args.warmup + args.steps} from steady sliding",
                        "mg": f"{cfg.mg.n_levels} levels V({cfg.mg.nu_pre},{cfg.mg.nu_post}), "
                              f"rel {cfg.mg.tol:g}, {mode}, exact coarsest solve, surface-row prolongation",
                        "parallelism": f"replicas x{world}", "l2": "flushed before every timed step"},

@@ -243,6 +243,40 @@ int qd_rk43_set_state(qd_solver *s, const double *Slip, const double *psi,
                       const double *V, const double *dpsi, double t, double dt,
                       double errA0, double errA1, int it);
 
+/* ---------------------------------------------------------------------
+ * Files.
+ * ------------------------------------------------------------------- */
+/* The initial displacement file RK43 reads (odeSolver.cpp:96-128): ni * nk
+ * doubles, column index fastest, the interior nodes of the ghosted
+ * (ni+2) x (nk+2) array U.  load fills U's interior (ghosts untouched) and
+ * fails with QD_ERR_ARG on a short file, where the reference prints
+ * "Read error!" and continues; save writes that layout from U's interior. */
+int qd_load_initial_u(const char *path, int ni, int nk, double *U);
+int qd_save_initial_u(const char *path, int ni, int nk, const double *U);
+
+/* Snapshot record of the current state in the reference's format:
+ * full = 1 is the first record (odeSolver.cpp:1442-1456: t, V, Slip, Ts, psi,
+ * U with ghosts, Tn, a, b, dt), full = 0 the periodic one (:1638-1652: t, V,
+ * Slip, Ts, psi, dt).  With async = 1 the device-to-host copies are queued on
+ * the solver's stream and a host thread writes the file once they land, so
+ * the solver keeps stepping; one snapshot is in flight per solver (a new one
+ * first waits for the last).  qd_snapshot_wait joins it and returns its
+ * status.  No counterpart in the reference beyond the record layout. */
+int qd_snapshot(qd_solver *s, const char *path, int full, int async);
+int qd_snapshot_wait(qd_solver *s);
+
+/* Checkpoint / restart: every piece of state the next accepted step reads
+ * (Slip, psi, V, Ts, dpsi, t, dt, the error history, the step count, the
+ * time-stepping parameters and u), so that a run loaded from a checkpoint
+ * continues bit for bit as the saved run would have; loading replaces
+ * qd_rk43_start.  The solver loading it must have the same grid, medium,
+ * fault set-up and multigrid options.  File: "QDEQCKP1", int32 ni, nk, it,
+ * maxNumSteps, doubles t, dt, errA0, errA1, tmax, ini_dt, mindt, maxdt,
+ * totTol, then Slip, psi, V, Ts, dpsi (nz each) and u (nk rows of ni).  No
+ * counterpart in the reference. */
+int qd_checkpoint_save(qd_solver *s, const char *path);
+int qd_checkpoint_load(qd_solver *s, const char *path);
+
 #ifdef __cplusplus
 }
 #endif

@@ -54,6 +54,12 @@ EXPORTS = [
     ("qd_rk43_get_scalars", C.c_int, [C.c_void_p, _dp, _ip]),
     ("qd_rk43_set_state", C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp, C.c_double, C.c_double,
                                     C.c_double, C.c_double, C.c_int]),
+    ("qd_load_initial_u", C.c_int, [C.c_char_p, C.c_int, C.c_int, _dp]),
+    ("qd_save_initial_u", C.c_int, [C.c_char_p, C.c_int, C.c_int, _dp]),
+    ("qd_snapshot", C.c_int, [C.c_void_p, C.c_char_p, C.c_int, C.c_int]),
+    ("qd_snapshot_wait", C.c_int, [C.c_void_p]),
+    ("qd_checkpoint_save", C.c_int, [C.c_void_p, C.c_char_p]),
+    ("qd_checkpoint_load", C.c_int, [C.c_void_p, C.c_char_p]),
     # include/qdeq_unet.h
     ("qd_unet_create", C.c_int, [C.c_int, C.c_int, C.c_ulonglong, C.POINTER(C.c_void_p)]),
     ("qd_unet_destroy", None, [C.c_void_p]),

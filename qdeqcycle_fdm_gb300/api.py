@@ -37,6 +37,21 @@ def mg_options(mg: MGConfig) -> MgOptions:
                      mg.max_cycles, mg.precision, mg.surface_prolong, mg.coarse_solve)
 
 
+def load_initial_u(path, ni: int, nk: int) -> np.ndarray:
+    """The reference's initial-displacement file (odeSolver.cpp:96-128) as
+    the ghosted (nk+2, ni+2) array U (ghosts zero)."""
+    U = np.zeros((nk + 2, ni + 2))
+    check(_lib.load().qd_load_initial_u(str(path).encode(), ni, nk, _p(U)))
+    return U
+
+
+def save_initial_u(path, U: np.ndarray) -> None:
+    """Write U's interior in the layout load_initial_u reads."""
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    nk, ni = U.shape[0] - 2, U.shape[1] - 2
+    check(_lib.load().qd_save_initial_u(str(path).encode(), ni, nk, _p(U)))
+
+
 def set_medium(ni: int, nk: int, mu_node: np.ndarray) -> np.ndarray:
     """SetMedium's homogenisation on the GPU (odeSolver.cpp:337-589)."""
     L = _lib.load()
@@ -176,6 +191,20 @@ class Solver:
     def rk43_set_state(self, Slip, psi, V, dpsi, t, dt, errA0, errA1, it):
         check(self.L.qd_rk43_set_state(self.h, _p(Slip), _p(psi), _p(V), _p(dpsi), t, dt, errA0,
                                        errA1, it))
+
+    # -- files -------------------------------------------------------------
+    def snapshot(self, path, full=True, asynchronous=False):
+        """The reference's snapshot record of the current state (qd_snapshot)."""
+        check(self.L.qd_snapshot(self.h, str(path).encode(), int(full), int(asynchronous)))
+
+    def snapshot_wait(self):
+        check(self.L.qd_snapshot_wait(self.h))
+
+    def checkpoint_save(self, path):
+        check(self.L.qd_checkpoint_save(self.h, str(path).encode()))
+
+    def checkpoint_load(self, path):
+        check(self.L.qd_checkpoint_load(self.h, str(path).encode()))
 
 
 class Simulation:

@@ -228,6 +228,7 @@ int qd_solver_destroy(qd_solver *s) {
     if (!s) return QD_OK;
     if (s->stream) cudaStreamSynchronize(s->stream);
     warm_start_detach(s);            // the network outlives the solver
+    snapshot_free(s);                // waits for a snapshot still being written
     mg_free(s);
     fault_free(s);
     solve_graph_free(s);

@@ -151,6 +151,7 @@ struct qd_solver {
     void *tma_cache;       // tensor maps of the tile kernels (mg_fused.cu)
     void *d_tail_img[2];   // coarse-tail coefficient images, FP32 [0] and FP64 [1]
     void *unet;            // attached warm-start network (unet.cu), or null
+    void *snapshot;        // the snapshot writer in flight (io.cu), or null
     int tail_l0;           // first level of the coarse tail
     void *solve_graph;     // the instantiated multigrid graph (mg_graph.cu)
     qd::SolveState *d_solve, *h_solve;
@@ -214,4 +215,6 @@ int warm_start_before_boundary(qd_solver *s);
 int warm_start_after_boundary(qd_solver *s);
 int warm_start_after_solve(qd_solver *s);
 void warm_start_detach(qd_solver *s);
+// io.cu
+void snapshot_free(qd_solver *s);
 }  // namespace qd

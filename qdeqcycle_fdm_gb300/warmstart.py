@@ -91,3 +91,27 @@ class UNet:
         loss = C.c_float(0)
         check(self.L.qd_unet_stats(self.h, C.byref(n), C.byref(loss)))
         return int(n.value), float(loss.value)
+
+
+def _main():
+    """python -m qdeqcycle_fdm_gb300.warmstart [n] [reps]: time one inference
+    and one training step of a freshly initialised network on an n x n grid
+    (random input and target)."""
+    import sys
+    n = int(sys.argv[1]) if len(sys.argv) > 1 else 1025
+    reps = int(sys.argv[2]) if len(sys.argv) > 2 else 10
+    rng = np.random.default_rng(0)
+    net = UNet(n, n, seed=1)
+    theta = net.get_params()
+    net.set_params(theta + 0.01 * rng.standard_normal(theta.size).astype(np.float32))
+    x = rng.standard_normal((4, n, n)).astype(np.float32)
+    t = rng.standard_normal((n, n)).astype(np.float32)
+    net.loss_grad(x, t)                       # uploads input and target
+    for what in ("forward", "train"):
+        us, fl = net.time(what, reps)
+        print(f"{what}: {us:.1f} us, {fl / 1e9:.1f} GFLOP, {fl / (us * 1e-6) / 1e12:.1f} TFLOP/s")
+    net.close()
+
+
+if __name__ == "__main__":
+    _main()
