@@ -11,10 +11,15 @@
  *
  * Parameters are flat FP32 arrays: for each of the 15 convolutions in order
  * (encoder 8, decoder 6, head 1), weights [9 taps][cout][cin] (tap = 3*(dy+1)
- * + (dx+1)) followed by the bias [cout].  The first layer has cin = 16 (four
+ * + (dx+1)) followed by the bias [cout].  The first layer has cin = 16 (five
  * input channels used), the head cout = 16 (channel 0 used).
  * Host inputs are planar float arrays over the nk x ni level-0 grid:
- * x = [4][nk][ni] input channels, target / y = [nk][ni].
+ * x = [5][nk][ni] input channels, target / y = [nk][ni].  Attached to a
+ * solver the inputs are u / (largest boundary value), the change of the
+ * fault and far Dirichlet data (each over s, the largest such change)
+ * broadcast along the rows, the column position, and the change the
+ * previous solve made to u over that solve's s; the target is the change
+ * this solve makes to u, over s.
  */
 #ifndef QDEQ_UNET_H
 #define QDEQ_UNET_H

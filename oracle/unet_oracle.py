@@ -142,7 +142,7 @@ def up_bwd(g):
 
 
 class UNet:
-    """Forward, loss and parameter gradient of the network for x (H, W, 4)."""
+    """Forward, loss and parameter gradient of the network for x (H, W, 5)."""
 
     def __init__(self, theta, bf16_mode=True):
         self.q = bf16 if bf16_mode else (lambda a: np.asarray(a, dtype=np.float64))
@@ -153,7 +153,7 @@ class UNet:
         q = self.q
         H, W = x.shape[:2]
         x0 = np.zeros((H, W, 16))
-        x0[..., :4] = x
+        x0[..., :x.shape[2]] = x
         x0 = q(x0)
         L = self.layers
         cache = {"x0": x0}

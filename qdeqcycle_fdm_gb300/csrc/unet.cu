@@ -17,10 +17,11 @@
 // up: bilinear, the multigrid prolongation's weights.
 //
 // Input channels (x0, padded to 16): u/s_u, d_fault/s_bc broadcast along
-// each row, d_far/s_bc, and the column position k/(K-1); d_fault and d_far
-// are the stage's change of the Dirichlet data on the fault and far columns,
-// s_bc the largest of their magnitudes and s_u the largest boundary value.
-// The prediction of the change of u is s_bc * out.
+// each row, d_far/s_bc, the column position k/(K-1), and the change the
+// previous solve made to u divided by its own s_bc; d_fault and d_far are the
+// stage's change of the Dirichlet data on the fault and far columns, s_bc
+// the largest of their magnitudes and s_u the largest boundary value.  The
+// prediction of the change of u is s_bc * out.
 #include <cuda_bf16.h>
 #include <math.h>
 #include <string.h>
@@ -32,6 +33,8 @@
 #include "../../include/qdeq_unet.h"
 
 namespace qd {
+
+static constexpr int UNET_NIN = 5;   // input channels in use (of the 16 staged)
 
 __host__ __device__ static inline int cdv(long a, long b) { return (int)((a + b - 1) / b); }
 
@@ -71,10 +74,11 @@ struct qd_unet {
     std::vector<qd::UTensor *> acts, grads;
     qd::UTensor *x0, *head_gout;
     float *out32, *target32;       // P0 floats
+    float *d_prev;                 // the last solve's change of u / s_bc (P0 floats): input channel 4
     float *d_loss;                 // [0] loss sum
     float *d_scale;                // [0] s_bc, [1] s_u
     double *d_bc_old;              // saved boundary columns: fault (N), far (N)
-    double *d_u_start;             // u at the start of a training solve (level-0 layout)
+    double *d_u_start;             // u a solve would start from without the network (level-0 layout)
     __nv_bfloat16 *planar;         // dY planar + 3 shifted X planar copies
     size_t planar_elems;
     unsigned *d_status;
@@ -95,67 +99,110 @@ __device__ __forceinline__ bool uin(int r, int c, const UGrid &g) {
     return r >= 1 && r <= g.H && c >= 1 && c <= g.W;
 }
 
+// Eight channels per thread (C is a multiple of 8): 16-byte loads and
+// stores, the pixel index from one 32-bit division per thread.
+struct F8 {
+    float v[8];
+};
+
+__device__ __forceinline__ F8 ld8(const __nv_bfloat16 *p) {
+    const uint4 u = *reinterpret_cast<const uint4 *>(p);
+    const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&u);
+    F8 f;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const float2 t = __bfloat1622float2(h[i]);
+        f.v[2 * i] = t.x;
+        f.v[2 * i + 1] = t.y;
+    }
+    return f;
+}
+
+__device__ __forceinline__ void st8(__nv_bfloat16 *p, const F8 &f) {
+    uint4 u;
+    __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(&u);
+#pragma unroll
+    for (int i = 0; i < 4; i++) h[i] = __floats2bfloat162_rn(f.v[2 * i], f.v[2 * i + 1]);
+    *reinterpret_cast<uint4 *>(p) = u;
+}
+
+__device__ __forceinline__ void axpy8(F8 &y, float a, const F8 &x) {
+#pragma unroll
+    for (int i = 0; i < 8; i++) y.v[i] += a * x.v[i];
+}
+
 // 2x2 mean pool, fine level f -> coarse level c
 __global__ void k_pool(const __nv_bfloat16 *in, __nv_bfloat16 *out, UGrid f, UGrid c, int C) {
-    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (long)c.P * C) return;
-    const int ch = (int)(idx % C), p = (int)(idx / C);
+    const int C8 = C >> 3, idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= c.P * C8) return;
+    const int p = idx / C8, ch = (idx - p * C8) * 8;
     const int r = p / c.Wp, q = p - r * c.Wp;
-    float v = 0.f;
+    F8 v = {};
     if (uin(r, q, c)) {
         const int y0 = 2 * (r - 1), x0 = 2 * (q - 1);
         int n = 0;
         for (int a = 0; a < 2; a++)
             for (int b = 0; b < 2; b++)
                 if (y0 + a < f.H && x0 + b < f.W) {
-                    v += __bfloat162float(in[((long)(y0 + a + 1) * f.Wp + (x0 + b + 1)) * C + ch]);
+                    axpy8(v, 1.f, ld8(in + ((long)(y0 + a + 1) * f.Wp + (x0 + b + 1)) * C + ch));
                     n++;
                 }
-        v /= (float)n;
+#pragma unroll
+        for (int i = 0; i < 8; i++) v.v[i] /= (float)n;
     }
-    out[idx] = __float2bfloat16_rn(v);
+    st8(out + (long)p * C + ch, v);
 }
 
 // gradient of k_pool, added into gin (fine)
 __global__ void k_pool_bwd(const __nv_bfloat16 *gout, __nv_bfloat16 *gin, UGrid f, UGrid c, int C) {
-    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (long)f.P * C) return;
-    const int ch = (int)(idx % C), p = (int)(idx / C);
+    const int C8 = C >> 3, idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= f.P * C8) return;
+    const int p = idx / C8, ch = (idx - p * C8) * 8;
     const int r = p / f.Wp, q = p - r * f.Wp;
     if (!uin(r, q, f)) return;
     const int y = r - 1, x = q - 1, yc = y >> 1, xc = x >> 1;
     const int ny = (2 * yc + 1 < f.H) ? 2 : 1, nx = (2 * xc + 1 < f.W) ? 2 : 1;
-    const float gv = __bfloat162float(gout[((long)(yc + 1) * c.Wp + (xc + 1)) * C + ch]) / (float)(ny * nx);
-    gin[idx] = __float2bfloat16_rn(__bfloat162float(gin[idx]) + gv);
+    F8 g = ld8(gin + (long)p * C + ch);
+    axpy8(g, 1.f / (float)(ny * nx), ld8(gout + ((long)(yc + 1) * c.Wp + (xc + 1)) * C + ch));
+    st8(gin + (long)p * C + ch, g);
 }
 
 // bilinear up-sampling, coarse c -> fine f
 __global__ void k_up(const __nv_bfloat16 *in, __nv_bfloat16 *out, UGrid c, UGrid f, int C) {
-    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (long)f.P * C) return;
-    const int ch = (int)(idx % C), p = (int)(idx / C);
+    const int C8 = C >> 3, idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= f.P * C8) return;
+    const int p = idx / C8, ch = (idx - p * C8) * 8;
     const int r = p / f.Wp, q = p - r * f.Wp;
-    float v = 0.f;
+    F8 v = {};
     if (uin(r, q, f)) {
         const int y = r - 1, x = q - 1, yc = y >> 1, xc = x >> 1, fy = y & 1, fx = x & 1;
-        auto at = [&](int a, int b) {
-            return __bfloat162float(in[((long)(yc + a + 1) * c.Wp + (xc + b + 1)) * C + ch]);
-        };
-        if (!fy && !fx) v = at(0, 0);
-        else if (fy && !fx) v = 0.5f * (at(0, 0) + at(1, 0));
-        else if (!fy && fx) v = 0.5f * (at(0, 0) + at(0, 1));
-        else v = 0.25f * (at(0, 0) + at(1, 0) + at(0, 1) + at(1, 1));
+        const __nv_bfloat16 *b = in + ((long)(yc + 1) * c.Wp + (xc + 1)) * C + ch;
+        const long dn = (long)c.Wp * C;
+        if (!fy && !fx) {
+            v = ld8(b);
+        } else if (fy && !fx) {
+            axpy8(v, 0.5f, ld8(b));
+            axpy8(v, 0.5f, ld8(b + dn));
+        } else if (!fy && fx) {
+            axpy8(v, 0.5f, ld8(b));
+            axpy8(v, 0.5f, ld8(b + C));
+        } else {
+            axpy8(v, 0.25f, ld8(b));
+            axpy8(v, 0.25f, ld8(b + dn));
+            axpy8(v, 0.25f, ld8(b + C));
+            axpy8(v, 0.25f, ld8(b + dn + C));
+        }
     }
-    out[idx] = __float2bfloat16_rn(v);
+    st8(out + (long)p * C + ch, v);
 }
 
 // gradient of k_up (its transpose), written into gin (coarse)
 __global__ void k_up_bwd(const __nv_bfloat16 *gout, __nv_bfloat16 *gin, UGrid c, UGrid f, int C) {
-    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (long)c.P * C) return;
-    const int ch = (int)(idx % C), p = (int)(idx / C);
+    const int C8 = C >> 3, idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= c.P * C8) return;
+    const int p = idx / C8, ch = (idx - p * C8) * 8;
     const int r = p / c.Wp, q = p - r * c.Wp;
-    float v = 0.f;
+    F8 v = {};
     if (uin(r, q, c)) {
         const int y = 2 * (r - 1), x = 2 * (q - 1);
         for (int dy = -1; dy <= 1; dy++) {
@@ -165,31 +212,40 @@ __global__ void k_up_bwd(const __nv_bfloat16 *gout, __nv_bfloat16 *gin, UGrid c,
             for (int dx = -1; dx <= 1; dx++) {
                 const int xx = x + dx;
                 if (xx < 0 || xx >= f.W) continue;
-                const float wx = dx ? 0.5f : 1.f;
-                v += wy * wx * __bfloat162float(gout[((long)(yy + 1) * f.Wp + (xx + 1)) * C + ch]);
+                axpy8(v, wy * (dx ? 0.5f : 1.f), ld8(gout + ((long)(yy + 1) * f.Wp + (xx + 1)) * C + ch));
             }
         }
     }
-    gin[idx] = __float2bfloat16_rn(v);
+    st8(gin + (long)p * C + ch, v);
 }
 
+// the element kernels below take n = pixels * channels (a multiple of 8)
 __global__ void k_add(const __nv_bfloat16 *a, const __nv_bfloat16 *b, __nv_bfloat16 *out, long n) {
-    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = __float2bfloat16_rn(__bfloat162float(a[i]) + __bfloat162float(b[i]));
+    const long i = 8L * (blockIdx.x * (long)blockDim.x + threadIdx.x);
+    if (i >= n) return;
+    F8 x = ld8(a + i);
+    axpy8(x, 1.f, ld8(b + i));
+    st8(out + i, x);
 }
 
 __global__ void k_copy2(const __nv_bfloat16 *g, __nv_bfloat16 *a, __nv_bfloat16 *b, long n) {
-    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) {
-        a[i] = g[i];
-        b[i] = g[i];
-    }
+    const long i = 8L * (blockIdx.x * (long)blockDim.x + threadIdx.x);
+    if (i >= n) return;
+    const uint4 u = *reinterpret_cast<const uint4 *>(g + i);
+    *reinterpret_cast<uint4 *>(a + i) = u;
+    *reinterpret_cast<uint4 *>(b + i) = u;
 }
 
 // g *= (y > 0), in place
 __global__ void k_relu_bwd(__nv_bfloat16 *g, const __nv_bfloat16 *y, long n) {
-    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n && !(__bfloat162float(y[i]) > 0.f)) g[i] = __float2bfloat16_rn(0.f);
+    const long i = 8L * (blockIdx.x * (long)blockDim.x + threadIdx.x);
+    if (i >= n) return;
+    F8 gv = ld8(g + i);
+    const F8 yv = ld8(y + i);
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+        if (!(yv.v[k] > 0.f)) gv.v[k] = 0.f;
+    st8(g + i, gv);
 }
 
 // NHWC [P][C] -> planar [C][P], shifted by dx pixels (zero outside)
@@ -308,11 +364,11 @@ __global__ void k_scales(const double *u, int N, int K, int P, const double *bc,
 }
 
 __global__ void k_features(const double *u, int N, int K, int P, const double *bc, const float *scale,
-                           __nv_bfloat16 *x0, UGrid g) {
+                           const float *prev, __nv_bfloat16 *x0, UGrid g) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= g.P) return;
     const int r = p / g.Wp, q = p - r * g.Wp;
-    float f[4] = {0.f, 0.f, 0.f, 0.f};
+    float f[UNET_NIN] = {0.f, 0.f, 0.f, 0.f, 0.f};
     if (uin(r, q, g)) {
         const int j = r - 1, k = q - 1;
         const float sb = scale[0], su = scale[1];
@@ -320,12 +376,13 @@ __global__ void k_features(const double *u, int N, int K, int P, const double *b
         f[1] = (float)((u[(long)j * P] - bc[j]) / sb);
         f[2] = (float)((u[(long)j * P + K - 1] - bc[N + j]) / sb);
         f[3] = (float)k / (float)(K - 1);
+        f[4] = prev[p];
     }
     uint4 lo, hi = make_uint4(0, 0, 0, 0);
     __nv_bfloat162 *lv = reinterpret_cast<__nv_bfloat162 *>(&lo);
     lv[0] = __floats2bfloat162_rn(f[0], f[1]);
     lv[1] = __floats2bfloat162_rn(f[2], f[3]);
-    lv[2] = __floats2bfloat162_rn(0.f, 0.f);
+    lv[2] = __floats2bfloat162_rn(f[4], 0.f);
     lv[3] = __floats2bfloat162_rn(0.f, 0.f);
     uint4 *dst = reinterpret_cast<uint4 *>(x0 + (long)p * 16);
     dst[0] = lo;
@@ -377,7 +434,8 @@ static int map_w(CUtensorMap *m, const __nv_bfloat16 *w, int rows, int K) {
 
 template <int KB, int COUT>
 static int conv_launch(qd_unet *u, const CUtensorMap &ta, const CUtensorMap &tb, const ConvArgs &a) {
-    constexpr int STAGE = ((128 * KB * 2 + COUT * KB * 2) + 1023) / 1024 * 1024;
+    constexpr int MT = conv_mt<KB, COUT>();
+    constexpr int STAGE = ((MT * 128 * KB * 2 + COUT * KB * 2) + 1023) / 1024 * 1024;
     const size_t smem = (size_t)CONV_STAGES * STAGE + 1024;
     static bool raised = false;
     if (!raised) {
@@ -385,7 +443,7 @@ static int conv_launch(qd_unet *u, const CUtensorMap &ta, const CUtensorMap &tb,
                                      (int)smem));
         raised = true;
     }
-    k_conv_fwd<KB, COUT><<<cdv(a.P, 128), CONV_THREADS, smem, u->stream>>>(ta, tb, a);
+    k_conv_fwd<KB, COUT><<<cdv(a.P, 128 * MT), CONV_THREADS, smem, u->stream>>>(ta, tb, a);
     QD_CUDA(cudaPeekAtLastError());
     return QD_OK;
 }
@@ -427,6 +485,7 @@ static ConvArgs conv_args(const qd_unet *u, const UGrid &g, int cin, int cout) {
 }
 
 #define EW_GRID(n) cdv((long)(n), 256), 256, 0, u->stream
+#define EW8_GRID(n) cdv((long)(n) / 8, 256), 256, 0, u->stream   // eight channels per thread
 
 // forward through every layer; the head writes out32
 static int forward(qd_unet *u) {
@@ -441,13 +500,13 @@ static int forward(qd_unet *u) {
             QD_TRY(conv_dispatch(u, Ly.m_in, Ly.m_w, a));
         } else if (op.k == OP_POOL) {
             const long n = (long)u->g[op.out->lvl].P * op.out->C;
-            k_pool<<<EW_GRID(n)>>>(op.a->p, op.out->p, u->g[op.a->lvl], u->g[op.out->lvl], op.a->C);
+            k_pool<<<EW8_GRID(n)>>>(op.a->p, op.out->p, u->g[op.a->lvl], u->g[op.out->lvl], op.a->C);
         } else if (op.k == OP_UP) {
             const long n = (long)u->g[op.out->lvl].P * op.out->C;
-            k_up<<<EW_GRID(n)>>>(op.a->p, op.out->p, u->g[op.a->lvl], u->g[op.out->lvl], op.a->C);
+            k_up<<<EW8_GRID(n)>>>(op.a->p, op.out->p, u->g[op.a->lvl], u->g[op.out->lvl], op.a->C);
         } else {
             const long n = (long)u->g[op.out->lvl].P * op.out->C;
-            k_add<<<EW_GRID(n)>>>(op.a->p, op.b->p, op.out->p, n);
+            k_add<<<EW8_GRID(n)>>>(op.a->p, op.b->p, op.out->p, n);
         }
         QD_CUDA(cudaPeekAtLastError());
     }
@@ -492,7 +551,7 @@ static int backward(qd_unet *u) {
             ULayer &Ly = u->L[op.layer];
             const UGrid &g = u->g[Ly.lvl];
             const long n = (long)g.P * Ly.cout;
-            if (Ly.relu) k_relu_bwd<<<EW_GRID(n)>>>(Ly.gout->p, Ly.out->p, n);
+            if (Ly.relu) k_relu_bwd<<<EW8_GRID(n)>>>(Ly.gout->p, Ly.out->p, n);
             k_bias_grad<<<std::min(cdv(g.P, 256), 1024), 256, 0, u->stream>>>(Ly.gout->p, Ly.gb, g.P, Ly.cout);
             QD_CUDA(cudaPeekAtLastError());
             switch (Ly.cin) {
@@ -510,13 +569,13 @@ static int backward(qd_unet *u) {
             }
         } else if (op.k == OP_POOL) {
             const long n = (long)u->g[op.a->lvl].P * op.a->C;
-            k_pool_bwd<<<EW_GRID(n)>>>(op.gout->p, op.ga->p, u->g[op.a->lvl], u->g[op.out->lvl], op.a->C);
+            k_pool_bwd<<<EW8_GRID(n)>>>(op.gout->p, op.ga->p, u->g[op.a->lvl], u->g[op.out->lvl], op.a->C);
         } else if (op.k == OP_UP) {
             const long n = (long)u->g[op.a->lvl].P * op.a->C;
-            k_up_bwd<<<EW_GRID(n)>>>(op.gout->p, op.ga->p, u->g[op.a->lvl], u->g[op.out->lvl], op.a->C);
+            k_up_bwd<<<EW8_GRID(n)>>>(op.gout->p, op.ga->p, u->g[op.a->lvl], u->g[op.out->lvl], op.a->C);
         } else {
             const long n = (long)u->g[op.out->lvl].P * op.out->C;
-            k_copy2<<<EW_GRID(n)>>>(op.gout->p, op.ga->p, op.gb->p, n);
+            k_copy2<<<EW8_GRID(n)>>>(op.gout->p, op.ga->p, op.gb->p, n);
         }
         QD_CUDA(cudaPeekAtLastError());
     }
@@ -588,7 +647,7 @@ static void unet_free(qd_unet *u) {
         cudaFree(Ly.w32); cudaFree(Ly.b32); cudaFree(Ly.mw); cudaFree(Ly.vw); cudaFree(Ly.mb);
         cudaFree(Ly.vb); cudaFree(Ly.gw); cudaFree(Ly.gb); cudaFree(Ly.w); cudaFree(Ly.wt);
     }
-    cudaFree(u->out32); cudaFree(u->target32); cudaFree(u->d_loss); cudaFree(u->d_scale);
+    cudaFree(u->out32); cudaFree(u->target32); cudaFree(u->d_prev); cudaFree(u->d_loss); cudaFree(u->d_scale);
     cudaFree(u->d_bc_old); cudaFree(u->d_u_start); cudaFree(u->planar); cudaFree(u->d_status);
     if (u->own_stream) cudaStreamDestroy(u->own_stream);
     delete u;
@@ -705,7 +764,7 @@ static int unet_build(qd_unet *u, unsigned long long seed) {
     for (size_t li = 0; li < u->L.size(); li++) {
         ULayer &Ly = u->L[li];
         const bool head = li + 1 == u->L.size();
-        const int cin_real = li == 0 ? 4 : Ly.cin;
+        const int cin_real = li == 0 ? UNET_NIN : Ly.cin;
         const double sd = sqrt(2.0 / (9.0 * cin_real));
         std::vector<float> w((size_t)9 * Ly.cout * Ly.cin, 0.f);
         for (int t = 0; t < 9; t++)
@@ -730,6 +789,7 @@ static int unet_build(qd_unet *u, unsigned long long seed) {
     u->planar_elems = need;
     u->out32 = dalloc_z<float>(u->g[0].P, &rc);
     u->target32 = dalloc_z<float>(u->g[0].P, &rc);
+    u->d_prev = dalloc_z<float>(u->g[0].P, &rc);
     u->d_loss = dalloc_z<float>(1, &rc);
     u->d_scale = dalloc_z<float>(2, &rc);
     u->d_status = dalloc_z<unsigned>(1, &rc);
@@ -769,15 +829,15 @@ static int upload_input(qd_unet *u, const float *x_host, const float *target_hos
     const UGrid &g = u->g[0];
     const size_t n = (size_t)g.H * g.W;
     float *tmp = nullptr;
-    QD_CUDA(cudaMalloc(&tmp, sizeof(float) * n * 5));
+    QD_CUDA(cudaMalloc(&tmp, sizeof(float) * n * (UNET_NIN + 1)));
     int rc = QD_OK;
-    if (cudaMemcpy(tmp, x_host, sizeof(float) * n * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+    if (cudaMemcpy(tmp, x_host, sizeof(float) * n * UNET_NIN, cudaMemcpyHostToDevice) != cudaSuccess ||
         (target_host &&
-         cudaMemcpy(tmp + 4 * n, target_host, sizeof(float) * n, cudaMemcpyHostToDevice) != cudaSuccess))
+         cudaMemcpy(tmp + UNET_NIN * n, target_host, sizeof(float) * n, cudaMemcpyHostToDevice) != cudaSuccess))
         rc = QD_ERR_CUDA;
     if (rc == QD_OK) {
-        k_x0_from_host<<<cdv(g.P, 256), 256, 0, u->stream>>>(tmp, 4, u->x0->p, g);
-        if (target_host) k_pad_f32<<<cdv(g.P, 256), 256, 0, u->stream>>>(tmp + 4 * n, u->target32, g);
+        k_x0_from_host<<<cdv(g.P, 256), 256, 0, u->stream>>>(tmp, UNET_NIN, u->x0->p, g);
+        if (target_host) k_pad_f32<<<cdv(g.P, 256), 256, 0, u->stream>>>(tmp + UNET_NIN * n, u->target32, g);
         if (cudaStreamSynchronize(u->stream) != cudaSuccess) rc = QD_ERR_CUDA;
     }
     cudaFree(tmp);
@@ -812,29 +872,34 @@ int warm_start_after_boundary(qd_solver *s) {
     const UGrid &g = u->g[0];
     k_scales<<<1, 1024, 0, s->stream>>>(s->L64[0].u, d.N, d.K, d.P, u->d_bc_old, u->d_scale);
     k_features<<<cdv(g.P, 256), 256, 0, s->stream>>>(s->L64[0].u, d.N, d.K, d.P, u->d_bc_old, u->d_scale,
-                                                     u->x0->p, g);
+                                                     u->d_prev, u->x0->p, g);
     QD_LAUNCH_CHECK(s);
+    // the field the solve would start from without the network: the change
+    // the solve then makes is the training target and the next input
+    QD_CUDA(cudaMemcpyAsync(u->d_u_start, s->L64[0].u, sizeof(double) * (size_t)d.N * d.P,
+                            cudaMemcpyDeviceToDevice, s->stream));
     if (u->mode == 2) {
         QD_TRY(forward(u));
         k_apply<<<dim3(cdv(d.K, 256), d.N), 256, 0, s->stream>>>(s->L64[0].u, d.N, d.K, d.P, u->out32,
                                                                  u->d_scale, g);
         QD_LAUNCH_CHECK(s);
-    } else {
-        QD_CUDA(cudaMemcpyAsync(u->d_u_start, s->L64[0].u, sizeof(double) * (size_t)d.N * d.P,
-                                cudaMemcpyDeviceToDevice, s->stream));
     }
     return QD_OK;
 }
 
-// mode 1: one Adam step on (features, solved change)
+// the solved change (the next solve's input channel 4); in mode 1 also one
+// Adam step on (features, solved change)
 int warm_start_after_solve(qd_solver *s) {
     qd_unet *u = static_cast<qd_unet *>(s->unet);
-    if (!u || u->mode != 1) return QD_OK;
+    if (!u || !u->mode) return QD_OK;
     const LevelDims &d = s->dims[0];
     const UGrid &g = u->g[0];
     k_target<<<cdv(g.P, 256), 256, 0, s->stream>>>(s->L64[0].u, u->d_u_start, d.N, d.K, d.P, u->d_scale,
                                                    u->target32, g);
     QD_LAUNCH_CHECK(s);
+    QD_CUDA(cudaMemcpyAsync(u->d_prev, u->target32, sizeof(float) * (size_t)g.P, cudaMemcpyDeviceToDevice,
+                            s->stream));
+    if (u->mode != 1) return QD_OK;
     QD_TRY(loss_and_grad(u));
     return adam(u);
 }
@@ -975,6 +1040,7 @@ int qd_solver_warm_start(qd_solver *s, qd_unet *u, int mode, float lr) {
     }
     QD_CUDA(cudaStreamSynchronize(u->stream));
     if (!u->d_u_start) QD_CUDA(cudaMalloc(&u->d_u_start, sizeof(double) * (size_t)s->dims[0].N * s->dims[0].P));
+    if (s->unet != u) QD_CUDA(cudaMemset(u->d_prev, 0, sizeof(float) * (size_t)u->g[0].P));   // a new run
     u->stream = s->stream;   // the net runs on the solver's stream while attached
     u->mode = mode;
     u->lr = mode == 1 ? lr : u->lr;

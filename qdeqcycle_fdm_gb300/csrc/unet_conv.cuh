@@ -12,8 +12,9 @@
 // coordinate, which needs no alignment, and out-of-range rows arrive as
 // zeros.  No im2col buffer exists.
 //
-// k_conv_fwd: one CTA per 128 output pixels, N = Cout accumulator columns
-//   in tensor memory.  K steps = 9 taps x (Cin / KB) channel blocks of
+// k_conv_fwd: one CTA per MT x 128 output pixels (MT sub-tiles sharing each
+//   staged weight tile), N = Cout accumulator columns per sub-tile in tensor
+//   memory.  K steps = 9 taps x (Cin / KB) channel blocks of
 //   KB = min(Cin, 64) channels (rows of 32, 64 or 128 bytes, matching
 //   swizzle).  Warp 0 lane 0 streams A/B tiles with TMA through a STAGES-deep
 //   ring of mbarriers, warp 1 lane 0 issues the MMAs, warp 2 owns the tensor
@@ -38,7 +39,7 @@
 namespace qd {
 
 static constexpr unsigned ST_UNET_TIMEOUT = 16u;
-static constexpr int CONV_STAGES = 4;
+static constexpr int CONV_STAGES = 3;
 static constexpr int CONV_THREADS = 128;
 
 struct ConvArgs {
@@ -60,20 +61,30 @@ __device__ __forceinline__ bool interior_pixel(int p, const ConvArgs &a) {
     return r >= 1 && r <= a.H && c >= 1 && c <= a.W;
 }
 
+// 128-row sub-tiles per CTA: the weights of a K step are staged once for MT
+// pixel tiles, and the per-CTA set-up (barriers, tensor memory) is paid once
+// per MT tiles; MT * COUT accumulator columns stay within 256
+template <int KB, int COUT>
+__host__ __device__ constexpr int conv_mt() {
+    return (128 / KB) < (256 / COUT) ? (128 / KB) : (256 / COUT);
+}
+
 template <int KB, int COUT>
 __global__ void __launch_bounds__(CONV_THREADS) k_conv_fwd(const __grid_constant__ CUtensorMap ta,
                                                            const __grid_constant__ CUtensorMap tb,
                                                            ConvArgs a) {
+    constexpr int MT = conv_mt<KB, COUT>();
     constexpr int ROWB = KB * 2;                        // bytes per operand row
-    constexpr int ABYTES = 128 * ROWB, BBYTES = COUT * ROWB;
+    constexpr int ATILE = 128 * ROWB, ABYTES = MT * ATILE, BBYTES = COUT * ROWB;
     constexpr int STAGE = ((ABYTES + BBYTES) + 1023) / 1024 * 1024;
-    constexpr uint32_t TCOLS = COUT <= 32 ? 32 : (COUT <= 64 ? 64 : (COUT <= 128 ? 128 : 256));
+    constexpr int NC = MT * COUT;
+    constexpr uint32_t TCOLS = NC <= 32 ? 32 : (NC <= 64 ? 64 : (NC <= 128 ? 128 : 256));
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t full[CONV_STAGES], empty[CONV_STAGES], done;
     __shared__ uint32_t tmem_base;
     unsigned char *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m0 = blockIdx.x * 128;
+    const int m0 = blockIdx.x * 128 * MT;
     const int nkb = a.Cin / KB, nsteps = 9 * nkb;
 
     if (threadIdx.x == 0) {
@@ -90,7 +101,7 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv_fwd(const __grid_constant
     const uint32_t tmem = tmem_base;
 
     if (warp == 0 && lane == 0) {
-        // producer
+        // producer: MT activation tiles and one weight tile per K step
         for (int s = 0; s < nsteps; s++) {
             const int st = s % CONV_STAGES;
             if (s >= CONV_STAGES && !mbar_wait(&empty[st], ((s / CONV_STAGES) - 1) & 1)) {
@@ -98,70 +109,75 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv_fwd(const __grid_constant
                 break;
             }
             const int t = s / nkb, kb = s - t * nkb;
-            const int ts = a.tap_reverse ? 8 - t : t;
+            const int sh = tap_shift(a.tap_reverse ? 8 - t : t, a.Wp);
             unsigned char *sa = smem + st * STAGE, *sb = sa + ABYTES;
             mbar_expect_tx(&full[st], ABYTES + BBYTES);
-            tma_load_2d(sa, &ta, kb * KB, m0 + tap_shift(ts, a.Wp), &full[st]);
+#pragma unroll
+            for (int mt = 0; mt < MT; mt++)
+                tma_load_2d(sa + mt * ATILE, &ta, kb * KB, m0 + mt * 128 + sh, &full[st]);
             tma_load_2d(sb, &tb, kb * KB, t * COUT, &full[st]);
         }
     } else if (warp == 1 && lane == 0) {
-        // MMA issuer
+        // MMA issuer: sub-tile mt accumulates into columns mt*COUT ..
         constexpr uint32_t idesc = idesc_bf16_f32(COUT);
-        bool ok = true;
-        for (int s = 0; s < nsteps && ok; s++) {
+        for (int s = 0; s < nsteps; s++) {
             const int st = s % CONV_STAGES;
             if (!mbar_wait(&full[st], (s / CONV_STAGES) & 1)) {
                 atomicOr(a.status, ST_UNET_TIMEOUT);
-                ok = false;
                 break;
             }
             tc_fence_after();
             const uint32_t sa = smem_u32(smem + st * STAGE), sb = sa + ABYTES;
 #pragma unroll
-            for (int k = 0; k < KB / 16; k++)
-                mma_bf16(tmem, smem_desc(sa + 32 * k, ROWB), smem_desc(sb + 32 * k, ROWB), idesc,
-                         (s > 0 || k > 0) ? 1u : 0u);
+            for (int mt = 0; mt < MT; mt++)
+#pragma unroll
+                for (int k = 0; k < KB / 16; k++)
+                    mma_bf16(tmem + (uint32_t)(mt * COUT), smem_desc(sa + mt * ATILE + 32 * k, ROWB),
+                             smem_desc(sb + 32 * k, ROWB), idesc, (s > 0 || k > 0) ? 1u : 0u);
             mma_commit(&empty[st]);
         }
         mma_commit(&done);
     }
     __syncwarp();
-    // epilogue: thread (warp, lane) owns pixel m0 + 32*warp + lane
+    // epilogue: thread (warp, lane) owns pixel m0 + 128*mt + 32*warp + lane
     const bool ok = mbar_wait(&done, 0);
     if (!ok && threadIdx.x == 0) atomicOr(a.status, ST_UNET_TIMEOUT);
     tc_fence_after();
-    const int p = m0 + 32 * warp + lane;
-    const bool in = p < a.P && interior_pixel(p, a);
+#pragma unroll 1
+    for (int mt = 0; mt < MT; mt++) {
+        const int p = m0 + mt * 128 + 32 * warp + lane;
+        const bool in = p < a.P && interior_pixel(p, a);
 #pragma unroll
-    for (int n0 = 0; n0 < COUT; n0 += 8) {
-        float v[8];
-        tmem_ld8(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)n0, v);
-        if (p >= a.P || !ok) continue;
+        for (int n0 = 0; n0 < COUT; n0 += 8) {
+            float v[8];
+            tmem_ld8(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(mt * COUT + n0), v);
+            if (p >= a.P || !ok) continue;
 #pragma unroll
-        for (int i = 0; i < 8; i++) {
-            float x = v[i] + (a.bias ? a.bias[n0 + i] : 0.f);
-            if (a.relu) x = fmaxf(x, 0.f);
-            v[i] = x;
-        }
-        if (a.mask && in) {
-            const uint4 mk = *reinterpret_cast<const uint4 *>(a.mask + (size_t)p * COUT + n0);
-            const __nv_bfloat16 *mv = reinterpret_cast<const __nv_bfloat16 *>(&mk);
+            for (int i = 0; i < 8; i++) {
+                float x = v[i] + (a.bias ? a.bias[n0 + i] : 0.f);
+                if (a.relu) x = fmaxf(x, 0.f);
+                v[i] = x;
+            }
+            if (a.mask && in) {
+                const uint4 mk = *reinterpret_cast<const uint4 *>(a.mask + (size_t)p * COUT + n0);
+                const __nv_bfloat16 *mv = reinterpret_cast<const __nv_bfloat16 *>(&mk);
 #pragma unroll
-            for (int i = 0; i < 8; i++)
-                if (!(__bfloat162float(mv[i]) > 0.f)) v[i] = 0.f;
-        }
-        if (!in) {
+                for (int i = 0; i < 8; i++)
+                    if (!(__bfloat162float(mv[i]) > 0.f)) v[i] = 0.f;
+            }
+            if (!in) {
 #pragma unroll
-            for (int i = 0; i < 8; i++) v[i] = 0.f;
-        }
-        if (a.out_f32) {
-            if (n0 == 0) a.out_f32[p] = v[0];
-        } else {
-            uint4 o;
-            __nv_bfloat162 *ov = reinterpret_cast<__nv_bfloat162 *>(&o);
+                for (int i = 0; i < 8; i++) v[i] = 0.f;
+            }
+            if (a.out_f32) {
+                if (n0 == 0) a.out_f32[p] = v[0];
+            } else {
+                uint4 o;
+                __nv_bfloat162 *ov = reinterpret_cast<__nv_bfloat162 *>(&o);
 #pragma unroll
-            for (int i = 0; i < 4; i++) ov[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
-            *reinterpret_cast<uint4 *>(a.out + (size_t)p * COUT + n0) = o;
+                for (int i = 0; i < 4; i++) ov[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+                *reinterpret_cast<uint4 *>(a.out + (size_t)p * COUT + n0) = o;
+            }
         }
     }
     tc_fence_before();

@@ -2,7 +2,7 @@
 predicts the change a stage solve makes to u, trained online on the
 multigrid's own solutions with the library's tensor-core kernels.
 
-Host arrays follow the header: inputs ``x`` are float32 [4, nk, ni],
+Host arrays follow the header: inputs ``x`` are float32 [5, nk, ni],
 targets and outputs float32 [nk, ni], parameters a flat float32 vector.
 """
 from __future__ import annotations
@@ -104,7 +104,7 @@ def _main():
     net = UNet(n, n, seed=1)
     theta = net.get_params()
     net.set_params(theta + 0.01 * rng.standard_normal(theta.size).astype(np.float32))
-    x = rng.standard_normal((4, n, n)).astype(np.float32)
+    x = rng.standard_normal((5, n, n)).astype(np.float32)
     t = rng.standard_normal((n, n)).astype(np.float32)
     net.loss_grad(x, t)                       # uploads input and target
     for what in ("forward", "train"):

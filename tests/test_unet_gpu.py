@@ -41,7 +41,7 @@ def net():
 
 
 def test_fresh_network_predicts_zero(net):
-    x = np.random.default_rng(0).normal(size=(4, N, N)).astype(np.float32)
+    x = np.random.default_rng(0).normal(size=(5, N, N)).astype(np.float32)
     assert np.all(net.forward(x) == 0.0)
     assert net.num_params == uo.num_params()
 
@@ -50,7 +50,7 @@ def test_forward_matches_oracle(net):
     theta = random_theta(1)
     net.set_params(theta)
     assert np.array_equal(net.get_params(), theta)
-    x = np.random.default_rng(2).normal(size=(4, N, N)).astype(np.float32)
+    x = np.random.default_rng(2).normal(size=(5, N, N)).astype(np.float32)
     y = net.forward(x)
     yo = uo.UNet(theta, bf16_mode=True).forward(np.moveaxis(x, 0, -1))
     assert np.all(np.isfinite(y))
@@ -61,7 +61,7 @@ def test_loss_and_gradients_match_oracle(net):
     theta = random_theta(4)
     net.set_params(theta)
     rng = np.random.default_rng(5)
-    x = rng.normal(size=(4, N, N)).astype(np.float32)
+    x = rng.normal(size=(5, N, N)).astype(np.float32)
     target = rng.normal(size=(N, N)).astype(np.float32)
     loss, g = net.loss_grad(x, target)
     lo, _, go = uo.UNet(theta, bf16_mode=True).loss_grad(np.moveaxis(x, 0, -1), target)
@@ -84,7 +84,7 @@ def test_adam_training_reduces_the_loss(net):
     theta = random_theta(6) * 0.5
     net.set_params(theta)
     rng = np.random.default_rng(7)
-    x = rng.normal(size=(4, N, N)).astype(np.float32)
+    x = rng.normal(size=(5, N, N)).astype(np.float32)
     yy, xx = np.mgrid[0:N, 0:N] / (N - 1)
     target = (np.sin(3 * yy) * np.exp(-2 * xx)).astype(np.float32)
     losses = [net.train_step(x, target, 3e-3) for _ in range(80)]
