@@ -231,6 +231,16 @@ int qd_cal_dpsi(qd_solver *s, const double *psi, const double *V, double *dpsi);
 int qd_rk43_start(qd_solver *s, const qd_rk43_params *p, const double *Slip,
                   const double *psi);
 int qd_rk43_step(qd_solver *s, int nsteps, int *steps_done);
+/* Batched ensemble: advance n independent, started solvers (any grids and
+ * parameters, each with its own adaptive dt) by nsteps accepted steps each,
+ * interleaving their GPU work: every instance's attempt (stages 2-6 and the
+ * error estimate) is queued on its own stream before the host waits on any,
+ * so the kernels of small instances fill the GPU together.  Each instance
+ * follows exactly the operations qd_rk43_step would run on it.  An instance
+ * at tmax or maxNumSteps stops; steps_done (n entries, may be NULL) gets the
+ * steps each took.  No counterpart in the reference, which runs one
+ * simulation per process. */
+int qd_ensemble_step(qd_solver **s, int n, int nsteps, int *steps_done);
 /* State read-back (any pointer may be NULL): Slip, psi, V (= f1.V_f),
  * Ts, dpsi (= f1.dpsi). */
 int qd_rk43_get_state(qd_solver *s, double *Slip, double *psi, double *V,

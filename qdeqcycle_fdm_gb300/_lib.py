@@ -50,6 +50,7 @@ EXPORTS = [
     ("qd_cal_dpsi", C.c_int, [C.c_void_p, _dp, _dp, _dp]),
     ("qd_rk43_start", C.c_int, [C.c_void_p, C.c_void_p, _dp, _dp]),
     ("qd_rk43_step", C.c_int, [C.c_void_p, C.c_int, _ip]),
+    ("qd_ensemble_step", C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_int, _ip]),
     ("qd_rk43_get_state", C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp, _dp]),
     ("qd_rk43_get_scalars", C.c_int, [C.c_void_p, _dp, _ip]),
     ("qd_rk43_set_state", C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp, C.c_double, C.c_double,

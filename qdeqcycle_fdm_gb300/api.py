@@ -37,6 +37,16 @@ def mg_options(mg: MGConfig) -> MgOptions:
                      mg.max_cycles, mg.precision, mg.surface_prolong, mg.coarse_solve)
 
 
+def ensemble_step(sims, nsteps: int = 1):
+    """qd_ensemble_step over started Simulations (or Solvers): their GPU work
+    interleaved; returns the steps each took."""
+    solvers = [getattr(x, "solver", x) for x in sims]
+    hs = (C.c_void_p * len(solvers))(*[s.h.value for s in solvers])
+    done = (C.c_int * len(solvers))()
+    check(_lib.load().qd_ensemble_step(hs, len(solvers), nsteps, done))
+    return list(done)
+
+
 def load_initial_u(path, ni: int, nk: int) -> np.ndarray:
     """The reference's initial-displacement file (odeSolver.cpp:96-128) as
     the ghosted (nk+2, ni+2) array U (ghosts zero)."""

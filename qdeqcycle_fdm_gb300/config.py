@@ -115,4 +115,28 @@ def small(n: int = 33, **kw) -> ProblemConfig:
     return c.replace(**kw) if kw else c
 
 
+
+def ensemble_instance(n: int, index: int, base_seed: int = 777) -> ProblemConfig:
+    """Member `index` of the batched ensemble (config 4) on an n x n grid, with
+    its parameters drawn from the seed base_seed + index: b - a in the
+    seismogenic zone uniform in [0.002, 0.006] with a = 0.008, Dc log-uniform
+    in [2, 20] mm, sigma_n uniform in [20, 80] MPa, seismogenic depth uniform
+    in [10, 16] km, homogeneous mu uniform in [25, 35] GPa.  Mixed-precision
+    multigrid with log2(n-1) - 1 levels (coarsest 5 x 5, solved exactly)."""
+    import math
+    import random
+    rng = random.Random(base_seed + index)
+    bma = rng.uniform(0.002, 0.006)
+    dc = math.exp(rng.uniform(math.log(2e-3), math.log(20e-3)))
+    sn = rng.uniform(20.0, 80.0)
+    sd = rng.uniform(10.0, 16.0)
+    mu = rng.uniform(25.0, 35.0)
+    levels = int(round(math.log2(n - 1))) - 1
+    return ProblemConfig(name=f"ensemble_{n}_{index}", ni=n, nk=n, mu_profile="uniform", mu_gpa=mu,
+                         a_shallow=0.008, b=0.008 + bma, seis_depth_km=sd, taper_depth_km=sd + 4.0,
+                         Dc_m=dc, sigma_n_mpa=sn, years=200.0, seed=base_seed + index,
+                         mg=MGConfig(n_levels=levels, nu_pre=2, nu_post=2, nu_coarse=32, tol_mode=1,
+                                     tol=1e-9, max_cycles=200, precision=1, surface_prolong=1,
+                                     coarse_solve=1))
+
 CONFIGS = {"config0": config0, "config1": config1, "config1_mixed": config1_mixed}

@@ -121,34 +121,56 @@ static int rk_start(qd_solver *s) {
     return QD_OK;
 }
 
-// the outer while-loop body, odeSolver.cpp:1464-1636
-static int rk_step(qd_solver *s) {
+// The outer while-loop body, odeSolver.cpp:1464-1636, in phases that only
+// enqueue work (step_begin, attempt_enqueue, commit_enqueue) and phases that
+// wait for it (attempt_finish, commit_finish), so that several solvers can
+// interleave their GPU work (qd_ensemble_step).
+static const double *rk_c() {
     static double c[7], b[7], hb[7], a[7][7];
     static bool init = false;
     if (!init) { rk_tableau(c, b, hb, a); init = true; }
-    double totErr = 0.0;
+    return c;
+}
+
+static int step_begin(qd_solver *s) {
     s->it = s->it + 1;
-    QD_TRY(solve_state_clear_flag(s));
-    int attemptCount = 0;
-    while (attemptCount < 100) {
-        attemptCount++;
-        s->attempts++;
-        if (s->t + s->dt > s->P.tmax) s->dt = s->P.tmax - s->t;
-        for (int st = 2; st <= 6; st++) QD_TRY(stage(s, st, c[st]));
-        QD_TRY(launch_error(s));
-        QD_CUDA(cudaMemcpyAsync(s->h_scal + 2, s->d_scal + 2, sizeof(double), cudaMemcpyDeviceToHost,
-                                s->stream));
-        SolveState sst;
-        QD_TRY(solve_state_read(s, &sst));                        // the attempt's one sync
-        QD_TRY(solve_flag_error(sst));
-        totErr = s->h_scal[2];
-        if (totErr < s->P.totTol) break;
-        s->dt = step_size(s->it, s->dt, s->P, totErr, s->errA);
-        if (s->P.mindt == s->dt) break;
-    }
+    return solve_state_clear_flag(s);
+}
+
+// stages 2..6 and the error estimate of one attempt, and the copies of the
+// error and of the solve state the host will read
+static int attempt_enqueue(qd_solver *s) {
+    const double *c = rk_c();
+    s->attempts++;
+    if (s->t + s->dt > s->P.tmax) s->dt = s->P.tmax - s->t;
+    for (int st = 2; st <= 6; st++) QD_TRY(stage(s, st, c[st]));
+    QD_TRY(launch_error(s));
+    QD_CUDA(cudaMemcpyAsync(s->h_scal + 2, s->d_scal + 2, sizeof(double), cudaMemcpyDeviceToHost,
+                            s->stream));
+    QD_CUDA(cudaMemcpyAsync(s->h_solve, s->d_solve, sizeof(SolveState), cudaMemcpyDeviceToHost, s->stream));
+    return QD_OK;
+}
+
+// the attempt's one synchronisation; *retry: reduce dt and attempt again
+static int attempt_finish(qd_solver *s, int attemptCount, double *totErr, int *retry) {
+    QD_CUDA(cudaStreamSynchronize(s->stream));
+    QD_TRY(solve_flag_error(*s->h_solve));
+    *totErr = s->h_scal[2];
+    *retry = 0;
+    if (*totErr < s->P.totTol) return QD_OK;
+    s->dt = step_size(s->it, s->dt, s->P, *totErr, s->errA);
+    if (s->P.mindt == s->dt) return QD_OK;
+    *retry = attemptCount < 100;
+    return QD_OK;
+}
+
+static int commit_enqueue(qd_solver *s) {
     s->t = s->t + s->dt;
     QD_TRY(launch_commit(s));
-    QD_TRY(stage(s, 1, 0.0));                                     // :1615-1619
+    return stage(s, 1, 0.0);                                      // :1615-1619
+}
+
+static int commit_finish(qd_solver *s, double totErr) {
     const double newDeltaT = (totErr != 0.0) ? step_size(s->it, s->dt, s->P, totErr, s->errA) : s->dt;
     s->errA[1] = s->errA[0];
     s->errA[0] = totErr;
@@ -156,6 +178,20 @@ static int rk_step(qd_solver *s) {
     s->steps++;
     return check_status(s);
 }
+
+static int rk_step(qd_solver *s) {
+    QD_TRY(step_begin(s));
+    double totErr = 0.0;
+    int retry = 1;
+    for (int attemptCount = 1; retry; attemptCount++) {
+        QD_TRY(attempt_enqueue(s));
+        QD_TRY(attempt_finish(s, attemptCount, &totErr, &retry));
+    }
+    QD_TRY(commit_enqueue(s));
+    return commit_finish(s, totErr);
+}
+
+static bool can_step(const qd_solver *s) { return s->it < s->P.maxNumSteps && s->t < s->P.tmax; }
 
 }  // namespace qd
 
@@ -456,6 +492,60 @@ int qd_rk43_start(qd_solver *s, const qd_rk43_params *p, const double *Slip, con
     s->it = 0;
     s->errA[0] = s->errA[1] = 0.0;
     return rk_start(s);
+}
+
+int qd_ensemble_step(qd_solver **ss, int n, int nsteps, int *steps_done) {
+    if (!ss || n < 1 || nsteps < 0) {
+        set_error("qd_ensemble_step: bad arguments");
+        return QD_ERR_ARG;
+    }
+    for (int i = 0; i < n; i++) {
+        if (!ss[i]) { set_error("qd_ensemble_step: solver %d is NULL", i); return QD_ERR_ARG; }
+        if (!ss[i]->started) { set_error("qd_ensemble_step: solver %d not started", i); return QD_ERR_STATE; }
+        for (int j = 0; j < i; j++)
+            if (ss[j] == ss[i]) { set_error("qd_ensemble_step: solver %d listed twice", i); return QD_ERR_ARG; }
+        if (steps_done) steps_done[i] = 0;
+    }
+    std::vector<char> act(n), trying(n);
+    std::vector<int> att(n);
+    std::vector<double> err(n);
+    for (int k = 0; k < nsteps; k++) {
+        int nact = 0;
+        for (int i = 0; i < n; i++) {
+            act[i] = can_step(ss[i]);
+            if (!act[i]) continue;
+            nact++;
+            QD_TRY(step_begin(ss[i]));
+            trying[i] = 1;
+            att[i] = 0;
+        }
+        if (!nact) break;
+        for (int left = nact; left > 0;) {
+            // every instance still trying enqueues its attempt before any waits
+            for (int i = 0; i < n; i++)
+                if (act[i] && trying[i]) {
+                    att[i]++;
+                    QD_TRY(attempt_enqueue(ss[i]));
+                }
+            for (int i = 0; i < n; i++)
+                if (act[i] && trying[i]) {
+                    int retry = 0;
+                    QD_TRY(attempt_finish(ss[i], att[i], &err[i], &retry));
+                    if (!retry) {
+                        trying[i] = 0;
+                        left--;
+                    }
+                }
+        }
+        for (int i = 0; i < n; i++)
+            if (act[i]) QD_TRY(commit_enqueue(ss[i]));
+        for (int i = 0; i < n; i++)
+            if (act[i]) {
+                QD_TRY(commit_finish(ss[i], err[i]));
+                if (steps_done) steps_done[i]++;
+            }
+    }
+    return QD_OK;
 }
 
 int qd_rk43_step(qd_solver *s, int nsteps, int *steps_done) {

@@ -120,12 +120,27 @@ struct TV {                       // one tail level as the kernel sees it
     const T *cx, *cz, *dinv;      // shared or global (the image), row pitch K
     int N, K;
     T h2, inv_h2;
+    int ou, of, orr, ocx, ocz, odv;   // the same arrays as element offsets in shared memory
 };
+
+// When every array of the tail is in shared memory the views are rebuilt
+// from offsets against the kernel's own shared-memory base, so that the
+// compiler sees shared-space pointers and issues shared-memory loads (a
+// pointer read back from a struct is generic, and generic loads wait on the
+// long scoreboard even when they hit shared memory).
+template <typename T, bool ALLS>
+__device__ __forceinline__ TV<T> tv_local(TV<T> v, T *sb) {
+    if (ALLS) {
+        v.u = sb + v.ou; v.f = sb + v.of; v.r = sb + v.orr;
+        v.cx = sb + v.ocx; v.cz = sb + v.ocz; v.dinv = sb + v.odv;
+    }
+    return v;
+}
 
 // one colour, warp per row and lane per node of that colour (a tail level
 // has at most 65 columns, so one pass of a warp covers a row)
 template <typename T>
-__device__ void tv_halfsweep(const TV<T> &g, int color) {
+__device__ __forceinline__ void tv_halfsweep(const TV<T> &g, int color) {
     for (int j = TWARP; j < g.N; j += TNWARP) {
         const int up = (j == 0) ? g.K : -g.K;
         const int dn = (j == g.N - 1) ? -g.K : g.K;
@@ -141,7 +156,7 @@ __device__ void tv_halfsweep(const TV<T> &g, int color) {
 }
 
 template <typename T>
-__device__ void tv_smooth(const TV<T> &g, int nsweeps) {
+__device__ __forceinline__ void tv_smooth(const TV<T> &g, int nsweeps) {
     for (int s = 0; s < nsweeps; s++) {
         tv_halfsweep(g, 0);
         __syncthreads();
@@ -165,13 +180,14 @@ __device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned b
         : "memory");
 }
 
-template <typename T>
+template <typename T, bool ALLS>
 __global__ void __launch_bounds__(NT_TAIL) k_tail(TailArgs<T> a) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bar;
     __shared__ TV<T> V[QD_MAXLEV];   // per-level views, read by every thread
     __shared__ const T *ainv;
     unsigned char *smem = align_smem128(smem_raw);
+    T *sb = reinterpret_cast<T *>(smem);
     const TailLevels &p = a.p;
     if (threadIdx.x == 0) {
         mbar_init(&bar, 1);
@@ -199,6 +215,8 @@ __global__ void __launch_bounds__(NT_TAIL) k_tail(TailArgs<T> a) {
             v.cx = pick(ox, n);
             v.cz = pick(oz, n + K);
             v.dinv = pick(od, n);
+            v.ou = (int)(v.u - sb); v.of = (int)(v.f - sb); v.orr = (int)(v.r - sb);
+            v.ocx = (int)ox; v.ocz = (int)oz; v.odv = (int)od;
             V[l] = v;
         }
         ainv = p.ainv_off >= 0 ? pick(p.ainv_off, (long)p.nint * p.nint) : nullptr;
@@ -207,11 +225,11 @@ __global__ void __launch_bounds__(NT_TAIL) k_tail(TailArgs<T> a) {
     {   // right-hand side of the first tail level; every correction starts at zero
         const LvArgs<T> &g = a.L[p.l0];
         const T *__restrict__ gf = g.f;
-        T *sf = V[p.l0].f;
+        T *sf = tv_local<T, ALLS>(V[p.l0], sb).f;
         for (int j = TWARP; j < g.N; j += TNWARP)
             for (int k = TLANE; k < g.K; k += 32) sf[j * g.K + k] = __ldg(gf + (long)j * g.P + k);
         for (int l = p.l0; l < p.nlev; l++) {
-            const TV<T> v = V[l];
+            const TV<T> v = tv_local<T, ALLS>(V[l], sb);
             for (int i = threadIdx.x; i < v.N * v.K; i += blockDim.x) v.u[i] = (T)0;
         }
     }
@@ -222,13 +240,13 @@ __global__ void __launch_bounds__(NT_TAIL) k_tail(TailArgs<T> a) {
         return;
     }
     for (int l = p.l0; l < p.nlev; l++) {
-        const TV<T> g = V[l];   // by value: stores through g.u cannot clobber it
+        const TV<T> g = tv_local<T, ALLS>(V[l], sb);   // by value: stores through g.u cannot clobber it
         if (l == p.nlev - 1) {
             if (p.coarse_solve) {
                 // e = A^-1 f over the interior nodes: a warp per row of the
                 // inverse, lanes along the row, then a butterfly sum
                 const int KI = g.K - 2;
-                const T *ai = ainv;
+                const T *ai = ALLS ? sb + p.ainv_off : ainv;
                 for (int i = TWARP; i < p.nint; i += TNWARP) {
                     const T *row = ai + (long)i * p.nint;
                     T acc = (T)0;
@@ -262,7 +280,7 @@ __global__ void __launch_bounds__(NT_TAIL) k_tail(TailArgs<T> a) {
             }
         }
         __syncthreads();
-        const TV<T> cl = V[l + 1];
+        const TV<T> cl = tv_local<T, ALLS>(V[l + 1], sb);
         for (int j = TWARP; j < cl.N; j += TNWARP) {
             const int rn = (j == 0) ? 2 * j + 1 : 2 * j - 1;
             const int rs = (j == cl.N - 1) ? 2 * j - 1 : 2 * j + 1;
@@ -278,8 +296,8 @@ __global__ void __launch_bounds__(NT_TAIL) k_tail(TailArgs<T> a) {
         __syncthreads();
     }
     for (int l = p.nlev - 2; l >= p.l0; l--) {
-        const TV<T> g = V[l];
-        const TV<T> cl = V[l + 1];
+        const TV<T> g = tv_local<T, ALLS>(V[l], sb);
+        const TV<T> cl = tv_local<T, ALLS>(V[l + 1], sb);
         const int jmax = g.N - 1 + p.surface;
         for (int jf = TWARP; jf < jmax; jf += TNWARP) {
             const T *er = cl.u + (jf >> 1) * cl.K;
@@ -299,7 +317,7 @@ __global__ void __launch_bounds__(NT_TAIL) k_tail(TailArgs<T> a) {
     }
     {   // the first tail level's correction, for k_up of the level above
         const LvArgs<T> &g = a.L[p.l0];
-        const T *su = V[p.l0].u;
+        const T *su = tv_local<T, ALLS>(V[p.l0], sb).u;
         for (int j = TWARP; j < g.N; j += TNWARP)
             for (int k = TLANE; k < g.K; k += 32) g.u[(long)j * g.P + k] = su[j * g.K + k];
     }
@@ -648,8 +666,13 @@ static int launch_tail(qd_solver *s, Level<T> *Ls, int lt) {
     ta.p.img_smem = (int)prefix;
     ta.p.work_off = (int)prefix;
     const size_t smem = prefix + work + kSmemSlack;
-    QD_TRY(set_smem(k_tail<T>, smem));
-    k_tail<T><<<1, NT_TAIL, smem, s->stream>>>(ta);
+    if (prefix == img) {   // every array in shared memory
+        QD_TRY(set_smem(k_tail<T, true>, smem));
+        k_tail<T, true><<<1, NT_TAIL, smem, s->stream>>>(ta);
+    } else {
+        QD_TRY(set_smem(k_tail<T, false>, smem));
+        k_tail<T, false><<<1, NT_TAIL, smem, s->stream>>>(ta);
+    }
     QD_LAUNCH_CHECK(s);
     return QD_OK;
 }
