@@ -345,6 +345,47 @@ def run_ours(args):
         sim64s.close()
         plain_value = plain["yrs"] / (reduce_max(plain["ms"]) / 3.6e6)
 
+    def ensemble_run(ksteps=8):
+        """Config 4 in miniature: 12 x 257^2 + 6 x 513^2 + 2 x 1025^2 seeded
+        instances (each its own parameters and adaptive dt), advanced by
+        qd_ensemble_step (GPU work of all instances interleaved) and, for
+        comparison, one instance after the other.  Host wall clock with the
+        device synchronised on both sides (the instances use 20 streams)."""
+        sizes = [257] * 12 + [513] * 6 + [1025] * 2
+        cfgs = [config.ensemble_instance(n, i) for i, n in enumerate(sizes)]
+        probs = [problem.build_problem(c) for c in cfgs]
+        out = {"instances": "12 x 257^2 + 6 x 513^2 + 2 x 1025^2 (config-4 parameter draws)",
+               "steps_timed": ksteps, "warmup": 3}
+        for mode in ("batched", "sequential"):
+            sims = [api.Simulation(p, c.mg) for p, c in zip(probs, cfgs)]
+            for x in sims:
+                x.start()
+            if mode == "batched":
+                api.ensemble_step(sims, 3)
+            else:
+                for x in sims:
+                    x.step(3)
+            t0 = [x.solver.rk43_state()["t"] for x in sims]
+            torch.cuda.synchronize()
+            w0 = time.perf_counter()
+            if mode == "batched":
+                api.ensemble_step(sims, ksteps)
+            else:
+                for x in sims:
+                    x.step(ksteps)
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - w0
+            yrs = sum(x.solver.rk43_state()["t"] - a for x, a in zip(sims, t0)) / YEAR_S
+            out[mode] = {"wall_s": wall, "ms_per_ensemble_step": 1e3 * wall / ksteps,
+                         "instance_years_per_hr": yrs / (wall / 3600.0)}
+            for x in sims:
+                x.close()
+        out["batched_speedup"] = out["sequential"]["wall_s"] / out["batched"]["wall_s"]
+        return out
+
+    if not args.headline_only:
+        extra["ensemble"] = ensemble_run()
+
     # Roofline of the V-cycle's kernels (the headline solver's hierarchy).
     # Inside a solve they run in a CUDA graph, so each is timed by
     # qd_mg_time_kernel: REPS back-to-back launches on the solver's stream
