@@ -43,7 +43,7 @@ sys.path.insert(0, ROOT)
 YEAR_S = 365.25 * 86400.0
 # DRAM bytes (read + write) per launch of the V-cycle kernels at 1025^2,
 # from one ncu capture of the headline solver (profiles/vcycle_kernels_1025.md)
-TRAFFIC = {"up0": 26.86e6, "down0": 13.02e6, "residual": 33.74e6}
+TRAFFIC = {"up0": 31.19e6, "down0": 17.35e6, "residual": 33.74e6}
 METRIC = "simulated yr/hr at 1025² (learned+mixed vs plain FP64 MG, 1e-9 rel residual)"
 
 
