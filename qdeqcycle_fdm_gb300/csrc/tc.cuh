@@ -64,6 +64,19 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, int row_bytes) {
     return d;
 }
 
+// Unswizzled K-major operand: core matrices of 8 rows x 16 bytes (rows 16
+// bytes apart), sbo bytes between 8-row groups along M/N and lbo bytes
+// between the 16-byte column chunks along K.  Any 16-byte-aligned start
+// address is valid, so a tile may start one row further down.
+__device__ __forceinline__ uint64_t smem_desc_noswz(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
 // Instruction descriptor of kind::f16 with BF16 A and B, FP32 D, both
 // operands K-major, M = 128, N = n (a multiple of 16, 16..256).
 __host__ __device__ constexpr uint32_t idesc_bf16_f32(int n) {

@@ -54,6 +54,7 @@ struct ULayer {
     float *w32, *b32, *mw, *vw, *mb, *vb, *gw, *gb;
     __nv_bfloat16 *w, *wt;             // [9][cout][cin], [9][cin][cout]
     CUtensorMap m_in, m_w, m_gout, m_wt;   // A/B operands of forward and data gradient
+    CUtensorMap m_in_rows, m_gout_rows;    // A operands as 8-channel row boxes (16/32 channels)
 };
 
 enum UOpKind { OP_CONV, OP_POOL, OP_UP, OP_ADD };
@@ -425,6 +426,12 @@ static int map_act(CUtensorMap *m, const UTensor &t, const UGrid &g) {
                            swz(KB * 2));
 }
 
+// A operand of k_conv_rows: 8-channel x 130-row unswizzled boxes
+static int map_act_rows(CUtensorMap *m, const UTensor &t, const UGrid &g) {
+    return encode_tiled_2d(m, t.p, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, t.C, g.P, (long)t.C * 2, 8, ROWS_BOX,
+                           CU_TENSOR_MAP_SWIZZLE_NONE);
+}
+
 // B operand: weights [9*rows][K], box KB x rows
 static int map_w(CUtensorMap *m, const __nv_bfloat16 *w, int rows, int K) {
     const int KB = K < 64 ? K : 64;
@@ -448,7 +455,31 @@ static int conv_launch(qd_unet *u, const CUtensorMap &ta, const CUtensorMap &tb,
     return QD_OK;
 }
 
-static int conv_dispatch(qd_unet *u, const CUtensorMap &ta, const CUtensorMap &tb, const ConvArgs &a) {
+template <int CIN, int COUT>
+static int conv_rows_launch(qd_unet *u, const CUtensorMap &ta, const CUtensorMap &tb, const ConvArgs &a) {
+    constexpr int MT = conv_rows_mt<CIN, COUT>();
+    const size_t smem = 3 * (size_t)conv_rows_stage<CIN, COUT>() + 1024;
+    static bool raised = false;
+    if (!raised) {
+        QD_CUDA(cudaFuncSetAttribute(k_conv_rows<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+        raised = true;
+    }
+    k_conv_rows<CIN, COUT><<<cdv(a.P, 128 * MT), CONV_THREADS, smem, u->stream>>>(ta, tb, a);
+    QD_CUDA(cudaPeekAtLastError());
+    return QD_OK;
+}
+
+// ta_rows: the row-box map of the A operand (16 or 32 channels), or null
+static int conv_dispatch(qd_unet *u, const CUtensorMap &ta, const CUtensorMap *ta_rows, const CUtensorMap &tb,
+                         const ConvArgs &a) {
+    if (ta_rows) {
+#define QD_ROWS_CASE(ci, co) \
+    if (a.Cin == ci && a.Cout == co) return conv_rows_launch<ci, co>(u, *ta_rows, tb, a);
+        QD_ROWS_CASE(16, 16) QD_ROWS_CASE(16, 32) QD_ROWS_CASE(16, 64)
+        QD_ROWS_CASE(32, 16) QD_ROWS_CASE(32, 32) QD_ROWS_CASE(32, 64)
+#undef QD_ROWS_CASE
+    }
     const int KB = a.Cin < 64 ? a.Cin : 64;
 #define QD_CONV_CASE(kb, co) \
     if (KB == kb && a.Cout == co) return conv_launch<kb, co>(u, ta, tb, a);
@@ -497,7 +528,7 @@ static int forward(qd_unet *u) {
             a.relu = Ly.relu;
             a.bias = Ly.b32;
             if (Ly.out) a.out = Ly.out->p; else a.out_f32 = u->out32;
-            QD_TRY(conv_dispatch(u, Ly.m_in, Ly.m_w, a));
+            QD_TRY(conv_dispatch(u, Ly.m_in, Ly.in->C <= 32 ? &Ly.m_in_rows : nullptr, Ly.m_w, a));
         } else if (op.k == OP_POOL) {
             const long n = (long)u->g[op.out->lvl].P * op.out->C;
             k_pool<<<EW8_GRID(n)>>>(op.a->p, op.out->p, u->g[op.a->lvl], u->g[op.out->lvl], op.a->C);
@@ -565,7 +596,7 @@ static int backward(qd_unet *u) {
                 ConvArgs a = conv_args(u, g, Ly.cout, Ly.cin);
                 a.out = Ly.gin->p;
                 a.tap_reverse = 1;
-                QD_TRY(conv_dispatch(u, Ly.m_gout, Ly.m_wt, a));
+                QD_TRY(conv_dispatch(u, Ly.m_gout, Ly.gout->C <= 32 ? &Ly.m_gout_rows : nullptr, Ly.m_wt, a));
             }
         } else if (op.k == OP_POOL) {
             const long n = (long)u->g[op.a->lvl].P * op.a->C;
@@ -780,6 +811,8 @@ static int unet_build(qd_unet *u, unsigned long long seed) {
         QD_TRY(map_act(&Ly.m_in, *Ly.in, u->g[Ly.lvl]));
         QD_TRY(map_w(&Ly.m_w, Ly.w, Ly.cout, Ly.cin));
         QD_TRY(map_act(&Ly.m_gout, *Ly.gout, u->g[Ly.lvl]));
+        if (Ly.in->C <= 32) QD_TRY(map_act_rows(&Ly.m_in_rows, *Ly.in, u->g[Ly.lvl]));
+        if (Ly.gout->C <= 32) QD_TRY(map_act_rows(&Ly.m_gout_rows, *Ly.gout, u->g[Ly.lvl]));
         QD_TRY(map_w(&Ly.m_wt, Ly.wt, Ly.cin, Ly.cout));
     }
     // planar scratch: dY (<= 128 rows at the layer's level) + 3 shifted X copies

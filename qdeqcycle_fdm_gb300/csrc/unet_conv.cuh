@@ -185,6 +185,143 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv_fwd(const __grid_constant
     if (warp == 2) tmem_free(tmem, TCOLS);
 }
 
+// k_conv_rows: the 3x3 convolution for 16 or 32 input channels, one TMA load
+// per (sub-tile, tap row) instead of per tap.  A pixel row of the operand is
+// 32 or 64 bytes, too narrow for efficient swizzled boxes and read nine times
+// by k_conv_fwd; here the activation is staged unswizzled in 16-byte column
+// chunks (boxes of 8 channels x 130 pixel rows: the 128 rows of a sub-tile
+// and one more on each side) for each of the three tap rows dy, and the
+// three taps dx = -1, 0, 1 of that row are the same tiles started 0, 1 and 2
+// rows down -- a 16-byte shift of the descriptor's start address.  The three
+// tap rows are the three pipeline stages, all in flight at once; the weights
+// of the three taps of a row ride in the same stage.
+template <int CIN, int COUT>
+__host__ __device__ constexpr int conv_rows_mt() {
+    return CIN == 16 ? (4 * COUT <= 256 ? 4 : 256 / COUT) : (2 * COUT <= 256 ? 2 : 256 / COUT);
+}
+static constexpr int ROWS_BOX = 130;       // pixel rows per staged box
+static constexpr int ROWS_ABOX = 2176;     // bytes per box slot (130 x 16 rounded up to 128)
+
+template <int CIN, int COUT>
+__host__ __device__ constexpr int conv_rows_stage() {
+    return (conv_rows_mt<CIN, COUT>() * (CIN / 8) * ROWS_ABOX + 3 * ((COUT * CIN * 2 + 1023) / 1024 * 1024) +
+            1023) / 1024 * 1024;
+}
+
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(CONV_THREADS) k_conv_rows(const __grid_constant__ CUtensorMap ta,
+                                                            const __grid_constant__ CUtensorMap tb,
+                                                            ConvArgs a) {
+    constexpr int MT = conv_rows_mt<CIN, COUT>();
+    constexpr int NCH = CIN / 8;                                    // 16-byte chunks per pixel
+    constexpr int ABYTES = MT * NCH * ROWS_ABOX;
+    constexpr int BT = (COUT * CIN * 2 + 1023) / 1024 * 1024;       // one tap's weights, 1 KB aligned
+    constexpr int STAGE = conv_rows_stage<CIN, COUT>();
+    constexpr int NC = MT * COUT;
+    constexpr uint32_t TCOLS = NC <= 32 ? 32 : (NC <= 64 ? 64 : (NC <= 128 ? 128 : 256));
+    constexpr unsigned TX = MT * NCH * ROWS_BOX * 16 + 3 * COUT * CIN * 2;
+    static_assert(CIN == 16 || CIN == 32, "row boxes serve 16 or 32 input channels");
+    static_assert(ABYTES % 1024 == 0, "weight tiles must start 1024-byte aligned");
+    static_assert(NC <= 256 && ROWS_ABOX % 128 == 0 && ROWS_ABOX >= ROWS_BOX * 16, "layout");
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t full[3], done;
+    __shared__ uint32_t tmem_base;
+    unsigned char *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = blockIdx.x * 128 * MT;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < 3; s++) mbar_init(&full[s], 1);
+        mbar_init(&done, 1);
+    }
+    if (warp == 2) tmem_alloc(&tmem_base, TCOLS);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base;
+
+    if (warp == 0 && lane == 0) {
+        // stage di: the operand rows shifted by dy = di - 1 (and dx = -1),
+        // and the weights of the taps (di, dx = -1, 0, 1)
+        for (int di = 0; di < 3; di++) {
+            unsigned char *sa = smem + di * STAGE, *sb = sa + ABYTES;
+            mbar_expect_tx(&full[di], TX);
+            const int row0 = m0 + (di - 1) * a.Wp - 1;
+#pragma unroll
+            for (int mt = 0; mt < MT; mt++)
+#pragma unroll
+                for (int c = 0; c < NCH; c++)
+                    tma_load_2d(sa + (mt * NCH + c) * ROWS_ABOX, &ta, 8 * c, row0 + mt * 128, &full[di]);
+#pragma unroll
+            for (int dx = 0; dx < 3; dx++) {
+                const int t = 3 * di + dx;
+                tma_load_2d(sb + dx * BT, &tb, 0, (a.tap_reverse ? 8 - t : t) * COUT, &full[di]);
+            }
+        }
+    } else if (warp == 1 && lane == 0) {
+        constexpr uint32_t idesc = idesc_bf16_f32(COUT);
+        for (int di = 0; di < 3; di++) {
+            if (!mbar_wait(&full[di], 0)) {
+                atomicOr(a.status, ST_UNET_TIMEOUT);
+                break;
+            }
+            tc_fence_after();
+            const uint32_t sa = smem_u32(smem + di * STAGE), sb = sa + ABYTES;
+#pragma unroll
+            for (int dx = 0; dx < 3; dx++)
+#pragma unroll
+                for (int mt = 0; mt < MT; mt++)
+#pragma unroll
+                    for (int ks = 0; ks < CIN / 16; ks++)
+                        mma_bf16(tmem + (uint32_t)(mt * COUT),
+                                 smem_desc_noswz(sa + (mt * NCH + 2 * ks) * ROWS_ABOX + 16 * dx, ROWS_ABOX, 128),
+                                 smem_desc(sb + dx * BT + 32 * ks, CIN * 2), idesc,
+                                 (di > 0 || dx > 0 || ks > 0) ? 1u : 0u);
+        }
+        mma_commit(&done);
+    }
+    __syncwarp();
+    const bool ok = mbar_wait(&done, 0);
+    if (!ok && threadIdx.x == 0) atomicOr(a.status, ST_UNET_TIMEOUT);
+    tc_fence_after();
+#pragma unroll 1
+    for (int mt = 0; mt < MT; mt++) {
+        const int p = m0 + mt * 128 + 32 * warp + lane;
+        const bool in = p < a.P && interior_pixel(p, a);
+#pragma unroll
+        for (int n0 = 0; n0 < COUT; n0 += 8) {
+            float v[8];
+            tmem_ld8(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(mt * COUT + n0), v);
+            if (p >= a.P || !ok) continue;
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                float x = v[i] + (a.bias ? a.bias[n0 + i] : 0.f);
+                if (a.relu) x = fmaxf(x, 0.f);
+                v[i] = (in ? x : 0.f);
+            }
+            if (a.mask && in) {
+                const uint4 mk = *reinterpret_cast<const uint4 *>(a.mask + (size_t)p * COUT + n0);
+                const __nv_bfloat16 *mv = reinterpret_cast<const __nv_bfloat16 *>(&mk);
+#pragma unroll
+                for (int i = 0; i < 8; i++)
+                    if (!(__bfloat162float(mv[i]) > 0.f)) v[i] = 0.f;
+            }
+            if (a.out_f32) {
+                if (n0 == 0) a.out_f32[p] = v[0];
+            } else {
+                uint4 o;
+                __nv_bfloat162 *ov = reinterpret_cast<__nv_bfloat162 *>(&o);
+#pragma unroll
+                for (int i = 0; i < 4; i++) ov[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+                *reinterpret_cast<uint4 *>(a.out + (size_t)p * COUT + n0) = o;
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 2) tmem_free(tmem, TCOLS);
+}
+
 struct WgradArgs {
     int Cin, Cout, Wp, P;
     int chunk;                // pixels per CTA (a multiple of 64)
