@@ -64,6 +64,9 @@ def parse():
     p.add_argument("--no-learned", action="store_true", help="headline without the learned warm start")
     p.add_argument("--lr", type=float, default=1e-3)
     p.add_argument("--seed", type=int, default=1)
+    p.add_argument("--history", type=int, default=4,
+                   help="stored solutions of the solution-history guess (0: start every solve "
+                        "from the previous solution, as the reference)")
     return p.parse_args()
 
 
@@ -210,6 +213,7 @@ def run_ours(args):
     prob = problem.build_problem(cfg)            # face moduli homogenised on the GPU
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     T = args.train_steps
+    H = args.history
 
     def barrier():
         if world > 1:
@@ -225,6 +229,7 @@ def run_ours(args):
         tcfg = cfg.replace(seed=cfg.seed + 1)
         tprob = problem.build_problem(tcfg)
         tsim = api.Simulation(tprob, mg)
+        tsim.solver.set_solution_history(H)
         net = warmstart.UNet(tprob.nk, tprob.ni, seed=args.seed)
         net.attach(tsim.solver, warmstart.MODE_TRAIN, args.lr)
         tsim.start()
@@ -234,14 +239,16 @@ def run_ours(args):
         tsim.close()
         return net, {"train_samples": n, "last_loss": loss, "train_instance_seed": tcfg.seed}
 
-    def timed_run(mg, host_io=False, net=None):
+    def timed_run(mg, host_io=False, net=None, history=0):
         """W untimed warm-up steps from steady sliding, then K steps each
         bracketed by CUDA events on the solver's stream (L2 flushed before
-        each); with `net` the solve of every stage starts from the network's
-        prediction.  host_io: every step goes through the C ABI with host
+        each); with `history` >= 2 every stage solve starts from the
+        solution-history guess, and with `net` from the network's correction
+        of that guess.  host_io: every step goes through the C ABI with host
         buffers -- state and u uploaded from pinned memory before, read back
         after (the e2e measurement)."""
         sim = api.Simulation(prob, mg)
+        sim.solver.set_solution_history(history)
         if net is not None:
             net.attach(sim.solver, warmstart.MODE_PREDICT)
         sim.start()
@@ -316,13 +323,13 @@ def run_ours(args):
     net, tinfo = train_network(mixed_cfg) if learned else (None, {})
     clocks = Clocks(local)
     clocks.start()
-    sim, head = timed_run(mixed_cfg, net=net)
+    sim, head = timed_run(mixed_cfg, net=net, history=H)
     clk = clocks.stop()
     ms_max = reduce_max(head["ms"])
     value = job_value(head)
     extra = {}
     if learned:
-        simm, mixed = timed_run(mixed_cfg)
+        simm, mixed = timed_run(mixed_cfg, history=H)
         simm.close()
         extra["mixed_no_learned"] = summary(mixed)
         us_f, fl_f = net.time("forward", 10)
@@ -334,6 +341,10 @@ def run_ours(args):
             "inference_us": us_f, "inference_tflops": fl_f / (us_f * 1e-6) / 1e12,
             "train_step_us": us_t, "train_tflops": fl_t / (us_t * 1e-6) / 1e12,
             "tensor_peak_tflops": bf, "inference_frac_of_peak": fl_f / (us_f * 1e-6) / 1e12 / bf}
+    if H >= 2:
+        simp, prev = timed_run(mixed_cfg)
+        simp.close()
+        extra["mixed_previous_solution_start"] = summary(prev)
     if args.headline_only:
         args.no_e2e = args.no_cpu_baseline = True
         plain = plain_s = None
@@ -355,10 +366,11 @@ def run_ours(args):
         cfgs = [config.ensemble_instance(n, i) for i, n in enumerate(sizes)]
         probs = [problem.build_problem(c) for c in cfgs]
         out = {"instances": "12 x 257^2 + 6 x 513^2 + 2 x 1025^2 (config-4 parameter draws)",
-               "steps_timed": ksteps, "warmup": 3}
+               "steps_timed": ksteps, "warmup": 3, "history": H}
         for mode in ("batched", "sequential"):
             sims = [api.Simulation(p, c.mg) for p, c in zip(probs, cfgs)]
             for x in sims:
+                x.solver.set_solution_history(H)
                 x.start()
             if mode == "batched":
                 api.ensemble_step(sims, 3)
@@ -425,7 +437,7 @@ def run_ours(args):
     # end to end through the C ABI with host buffers (pinned), the same steps
     e2e = None
     if not args.no_e2e:
-        sim_e, io = timed_run(mixed_cfg, host_io=True, net=net)
+        sim_e, io = timed_run(mixed_cfg, host_io=True, net=net, history=H)
         sim_e.close()
         e2e = {"value": job_value(io), "unit": "sim_yr/hr",
                "h2d_bytes_per_step": 8 * (4 * prob.nz + prob.ni * prob.nk),
@@ -441,8 +453,9 @@ def run_ours(args):
                          f"{r['wall_s']:.1f}s"}
 
     if rank == 0:
-        mode = ("learned warm start + FP32 cycles in FP64 refinement" if learned
-                else "FP32 cycles in FP64 refinement")
+        guess = f"solution-history guess (last {H} solutions)" if H >= 2 else "previous-solution start"
+        mode = (f"learned warm start on the {guess} + FP32 cycles in FP64 refinement" if learned
+                else f"{guess} + FP32 cycles in FP64 refinement")
         line = {
             "metric": METRIC, "value": value, "unit": "sim_yr/hr", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,

@@ -253,6 +253,25 @@ int qd_rk43_set_state(qd_solver *s, const double *Slip, const double *psi,
                       const double *V, const double *dpsi, double t, double dt,
                       double errA0, double errA1, int it);
 
+/* Initial guess of the RK43 driver's stage solves from the solution history
+ * (no counterpart in the reference, which starts every solve from the last
+ * solution, odeSolver.cpp:669-677).  With m >= 2 the solver keeps its last m
+ * level-0 solutions (m x 8*nk*pitch bytes of device memory) and starts each
+ * stage solve from A + sum_k c_k (S_k - A): A the latest solution, S_k the
+ * earlier ones, c the least-squares fit of the stage's new fault and far
+ * boundary columns by theirs.  The multigrid still iterates to the same
+ * residual tolerance; only the V-cycle count changes.  m = 0 or 1: off (the
+ * default).  m at most 8.  The stored solutions are solutions of the
+ * solver's fixed operator, so they stay valid when u or the RK state is
+ * replaced (qd_upload_u, qd_rk43_set_state); a new run (qd_rk43_start) and
+ * qd_checkpoint_load clear them, and a checkpoint file does not hold them. */
+int qd_set_solution_history(qd_solver *s, int m);
+/* The last fit: coef[0..6] the coefficients of the earlier solutions
+ * (newest first), coef[7] the fit's boundary misfit over the change from
+ * the latest solution's boundary data (1: no gain); *nd coefficients are
+ * in use.  Synchronises the solver's stream. */
+int qd_solution_history_fit(qd_solver *s, double *coef, int *nd);
+
 /* ---------------------------------------------------------------------
  * Files.
  * ------------------------------------------------------------------- */

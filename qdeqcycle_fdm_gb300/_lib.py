@@ -55,6 +55,8 @@ EXPORTS = [
     ("qd_rk43_get_scalars", C.c_int, [C.c_void_p, _dp, _ip]),
     ("qd_rk43_set_state", C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp, C.c_double, C.c_double,
                                     C.c_double, C.c_double, C.c_int]),
+    ("qd_set_solution_history", C.c_int, [C.c_void_p, C.c_int]),
+    ("qd_solution_history_fit", C.c_int, [C.c_void_p, _dp, _ip]),
     ("qd_load_initial_u", C.c_int, [C.c_char_p, C.c_int, C.c_int, _dp]),
     ("qd_save_initial_u", C.c_int, [C.c_char_p, C.c_int, C.c_int, _dp]),
     ("qd_snapshot", C.c_int, [C.c_void_p, C.c_char_p, C.c_int, C.c_int]),

@@ -202,6 +202,19 @@ class Solver:
         check(self.L.qd_rk43_set_state(self.h, _p(Slip), _p(psi), _p(V), _p(dpsi), t, dt, errA0,
                                        errA1, it))
 
+    def set_solution_history(self, m):
+        """Start each stage solve from the least-squares combination of the
+        last m solutions that best matches the new boundary data (m < 2: off,
+        the previous solution as the reference)."""
+        check(self.L.qd_set_solution_history(self.h, int(m)))
+
+    def solution_history_fit(self):
+        """(coefficients in use, boundary misfit / change) of the last fit."""
+        c = np.zeros(8)
+        nd = C.c_int(0)
+        check(self.L.qd_solution_history_fit(self.h, _p(c), C.byref(nd)))
+        return c[:nd.value].copy(), float(c[7])
+
     # -- files -------------------------------------------------------------
     def snapshot(self, path, full=True, asynchronous=False):
         """The reference's snapshot record of the current state (qd_snapshot)."""

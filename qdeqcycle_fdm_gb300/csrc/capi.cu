@@ -105,8 +105,10 @@ static int reset_status(qd_solver *s) {
 static int stage(qd_solver *s, int st, double ratio) {
     QD_TRY(warm_start_before_boundary(s));     // no-ops without an attached network
     QD_TRY(launch_stage_boundary(s, st, ratio, nullptr, nullptr));
+    QD_TRY(history_guess(s, warm_start_bc_buffer(s)));   // no-op unless enabled
     QD_TRY(warm_start_after_boundary(s));
     QD_TRY(mg_solve_async(s));
+    QD_TRY(history_push(s));
     QD_TRY(warm_start_after_solve(s));
     return launch_fault(s, st, 0);
 }
@@ -264,6 +266,7 @@ int qd_solver_destroy(qd_solver *s) {
     if (!s) return QD_OK;
     if (s->stream) cudaStreamSynchronize(s->stream);
     warm_start_detach(s);            // the network outlives the solver
+    history_free(s);
     snapshot_free(s);                // waits for a snapshot still being written
     mg_free(s);
     fault_free(s);
@@ -491,6 +494,7 @@ int qd_rk43_start(qd_solver *s, const qd_rk43_params *p, const double *Slip, con
     s->t = 0.0;
     s->it = 0;
     s->errA[0] = s->errA[1] = 0.0;
+    history_reset(s);
     return rk_start(s);
 }
 
@@ -592,6 +596,16 @@ int qd_rk43_set_state(qd_solver *s, const double *Slip, const double *psi, const
     s->t = t; s->dt = dt; s->errA[0] = errA0; s->errA[1] = errA1; s->it = it;
     s->started = 1;
     return QD_OK;
+}
+
+int qd_set_solution_history(qd_solver *s, int m) {
+    if (!s) return QD_ERR_ARG;
+    return history_set(s, m);
+}
+
+int qd_solution_history_fit(qd_solver *s, double *coef, int *nd) {
+    if (!s || !coef || !nd) return QD_ERR_ARG;
+    return history_last_fit(s, coef, nd);
 }
 
 }  // extern "C"

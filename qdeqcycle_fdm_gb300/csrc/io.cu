@@ -208,6 +208,7 @@ int qd_checkpoint_load(qd_solver *s, const char *path) {
     s->t = sc[0]; s->dt = sc[1]; s->errA[0] = sc[2]; s->errA[1] = sc[3];
     s->P.tmax = sc[4]; s->P.ini_dt = sc[5]; s->P.mindt = sc[6]; s->P.maxdt = sc[7]; s->P.totTol = sc[8];
     s->started = 1;
+    history_reset(s);     // the file holds no solution history: it restarts here
     return QD_OK;
 }
 

@@ -151,6 +151,7 @@ struct qd_solver {
     void *tma_cache;       // tensor maps of the tile kernels (mg_fused.cu)
     void *d_tail_img[2];   // coarse-tail coefficient images, FP32 [0] and FP64 [1]
     void *unet;            // attached warm-start network (unet.cu), or null
+    void *history;         // ring of earlier solutions for the initial guess (history.cu), or null
     void *snapshot;        // the snapshot writer in flight (io.cu), or null
     int tail_l0;           // first level of the coarse tail
     void *solve_graph;     // the instantiated multigrid graph (mg_graph.cu)
@@ -215,6 +216,14 @@ int warm_start_before_boundary(qd_solver *s);
 int warm_start_after_boundary(qd_solver *s);
 int warm_start_after_solve(qd_solver *s);
 void warm_start_detach(qd_solver *s);
+double *warm_start_bc_buffer(qd_solver *s);
+// history.cu: initial guess from the solution history
+int history_set(qd_solver *s, int m);
+int history_guess(qd_solver *s, double *implied_bc);
+int history_push(qd_solver *s);
+void history_reset(qd_solver *s);
+void history_free(qd_solver *s);
+int history_last_fit(qd_solver *s, double *out, int *nd);
 // io.cu
 void snapshot_free(qd_solver *s);
 }  // namespace qd

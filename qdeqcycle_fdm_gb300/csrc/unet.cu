@@ -937,6 +937,14 @@ int warm_start_after_solve(qd_solver *s) {
     return adam(u);
 }
 
+// where the solution-history guess leaves the boundary data its combination
+// implies, so that the network's boundary-change inputs describe what the
+// guess still misses (null when no network is in use)
+double *warm_start_bc_buffer(qd_solver *s) {
+    qd_unet *u = static_cast<qd_unet *>(s->unet);
+    return (u && u->mode) ? u->d_bc_old : nullptr;
+}
+
 void warm_start_detach(qd_solver *s) {
     qd_unet *u = static_cast<qd_unet *>(s->unet);
     if (!u) return;
