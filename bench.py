@@ -341,7 +341,7 @@ def run_ours(args):
             "inference_us": us_f, "inference_tflops": fl_f / (us_f * 1e-6) / 1e12,
             "train_step_us": us_t, "train_tflops": fl_t / (us_t * 1e-6) / 1e12,
             "tensor_peak_tflops": bf, "inference_frac_of_peak": fl_f / (us_f * 1e-6) / 1e12 / bf}
-    if H >= 2:
+    if H >= 2 and not args.headline_only:
         simp, prev = timed_run(mixed_cfg)
         simp.close()
         extra["mixed_previous_solution_start"] = summary(prev)

@@ -337,8 +337,13 @@ int launch_stage_boundary(qd_solver *s, int stage, double ratio, const double *,
     return QD_OK;
 }
 
+// The stress/Newton/aging kernels are FP64-pipe bound with one thread per
+// fault node: 32-thread blocks spread the nk nodes over nk/32 SMs instead of
+// packing four warps onto each of nk/128 SMs' FP64 pipes.
+static constexpr int kNewtonBlock = 32;
+
 int launch_fault(qd_solver *s, int stage, int) {
-    k_fault_stage<<<nblk(s->nk, 128), 128, 0, s->stream>>>(fargs(s), stage);
+    k_fault_stage<<<nblk(s->nk, kNewtonBlock), kNewtonBlock, 0, s->stream>>>(fargs(s), stage);
     QD_LAUNCH_CHECK(s);
     return QD_OK;
 }
@@ -362,7 +367,7 @@ int launch_stress(qd_solver *s) {
 }
 
 int launch_newton(qd_solver *s, const double *Ts, const double *psi, double *V, int *iters) {
-    k_newton<<<nblk(s->nk, 128), 128, 0, s->stream>>>(fargs(s), Ts, psi, V, iters);
+    k_newton<<<nblk(s->nk, kNewtonBlock), kNewtonBlock, 0, s->stream>>>(fargs(s), Ts, psi, V, iters);
     QD_LAUNCH_CHECK(s);
     return QD_OK;
 }

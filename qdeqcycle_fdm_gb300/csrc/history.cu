@@ -21,30 +21,35 @@
 //
 // Device data: a ring of m level-0 FP64 fields (the last m solutions, N x P
 // each) and their boundary columns packed as [fault rows 0..N-1, far rows
-// 0..N-1].  One CTA forms the normal equations of the fit (at most 7
-// unknowns), scales them to a unit diagonal, adds a 1e-12 ridge, solves by
-// Cholesky and keeps the fit only if its misfit is below the unfitted
-// change; a grid then writes the guess into the interior columns.
+// 0..N-1].  Sixteen CTAs form the normal equations of the fit (at most 7
+// unknowns); the last one scales them to a unit diagonal, adds a 1e-12
+// ridge, solves by Cholesky and keeps the fit only if its misfit is below
+// the unfitted change; a grid then writes the guess into the interior
+// columns as a weighted sum of the stored fields.
 #include <math.h>
+
+#include <algorithm>
 
 #include "qdeq_internal.cuh"
 
 namespace qd {
 
 static constexpr int HIST_MAX = 8;              // stored solutions
-static constexpr int HIST_ND = HIST_MAX - 1;     // fit unknowns
-static constexpr int HIST_NTRI = HIST_ND * (HIST_ND + 1) / 2;
-static constexpr int HIST_NACC = HIST_NTRI + HIST_ND + 1;
-static constexpr int HIST_THREADS = 512;
+static constexpr int HIST_ND = HIST_MAX - 1;     // fit unknowns at most
+static constexpr int FIT_THREADS = 128;
+static constexpr int FIT_CTAS = 16;
+static constexpr int FIT_NA_MAX = HIST_ND * (HIST_ND + 1) / 2 + HIST_ND + 1;
 
 struct History {
     int m = 0;          // capacity (0: off)
     int n = 0;          // stored solutions
     int head = 0;       // next slot to write
     size_t field = 0;   // doubles per stored field (N * P)
-    double *u = nullptr;     // m fields
-    double *bc = nullptr;    // m x 2N boundary values
-    double *coef = nullptr;  // [HIST_ND] fit coefficients, [HIST_ND] misfit / change
+    double *u = nullptr;       // m fields
+    double *bc = nullptr;      // m x 2N boundary values
+    double *coef = nullptr;    // [HIST_ND] fit coefficients, [HIST_ND] misfit / change
+    double *partial = nullptr; // FIT_CTAS x FIT_NA_MAX block sums of the fit
+    unsigned *count = nullptr; // CTAs of the fit done
     long long guesses = 0;
 };
 
@@ -54,191 +59,181 @@ __device__ __forceinline__ double bc_of(const double *u, int i, int N, int K, in
     return i < N ? u[(long)i * P] : u[(long)(i - N) * P + K - 1];
 }
 
-// packed index of G[k][l], k <= l
-__host__ __device__ constexpr int tri(int k, int l) { return k * HIST_ND - k * (k - 1) / 2 + (l - k); }
-
-// block-wide sum of v[0..n) into out[0..n) (every thread gets the sums)
-template <int NV>
-__device__ void block_sum(double (&v)[NV], int n, double (*red)[NV + 1], double *out) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll
-    for (int i = 0; i < NV; i++) {
-        if (i >= n) break;
-        double x = v[i];
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-        if (lane == 0) red[warp][i] = x;
-    }
-    __syncthreads();
-    if (threadIdx.x < n) {
-        double x = 0.0;
-        for (int w = 0; w < nw; w++) x += red[w][threadIdx.x];   // fixed order: deterministic
-        out[threadIdx.x] = x;
-    }
-    __syncthreads();
-}
-
 // anchor = slot a, the other stored solutions = slots oth[0..nd)
 struct FitArgs {
     const double *u;      // the solver's u with the new boundary data in columns 0, K-1
     const double *bc;     // ring of boundary values
-    int N, K, P, nd, a;
+    int N, K, P, a;
     int oth[HIST_ND];
-    double *coef;
-    double *implied;      // nullable: receives g_A + sum c_k (g_k - g_A) (2N values)
+    double *coef, *partial;
+    unsigned *count;
 };
 
-__global__ void __launch_bounds__(HIST_THREADS) k_hist_fit(FitArgs F) {
-    __shared__ double red[HIST_THREADS / 32][HIST_NACC + 1];
-    __shared__ double sums[HIST_NACC];
-    __shared__ double c[HIST_ND];
-    const int n2 = 2 * F.N, nd = F.nd;
+// Normal equations of the fit over the 2N boundary values, split over
+// FIT_CTAS blocks; the last block to finish sums the block partials in a
+// fixed order (deterministic) and solves.  Accumulators per boundary value:
+// G = D^T D (upper triangle), b = D^T t, |t|^2.
+template <int ND>
+__global__ void __launch_bounds__(FIT_THREADS) k_hist_fit(FitArgs F) {
+    constexpr int NT = ND * (ND + 1) / 2, NA = NT + ND + 1;
+    __shared__ double red[FIT_THREADS / 32][NA];
+    __shared__ double sums[NA];
+    __shared__ int is_last;
+    const int n2 = 2 * F.N, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const double *gA = F.bc + (size_t)F.a * n2;
 
-    // pass 1: G = D^T D (upper triangle), b = D^T t, |t|^2, packed at fixed
-    // places for all HIST_ND unknowns (differences past nd are zero)
-    double acc[HIST_NACC];
+    double acc[NA];
 #pragma unroll
-    for (int i = 0; i < HIST_NACC; i++) acc[i] = 0.0;
-    for (int i = threadIdx.x; i < n2; i += blockDim.x) {
+    for (int i = 0; i < NA; i++) acc[i] = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x) {
         const double ga = gA[i], t = bc_of(F.u, i, F.N, F.K, F.P) - ga;
-        double d[HIST_ND];
+        double d[ND];
 #pragma unroll
-        for (int k = 0; k < HIST_ND; k++) d[k] = k < nd ? F.bc[(size_t)F.oth[k] * n2 + i] - ga : 0.0;
+        for (int k = 0; k < ND; k++) d[k] = F.bc[(size_t)F.oth[k] * n2 + i] - ga;
+        int q = 0;
 #pragma unroll
-        for (int k = 0; k < HIST_ND; k++)
+        for (int k = 0; k < ND; k++)
 #pragma unroll
-            for (int l = k; l < HIST_ND; l++) acc[tri(k, l)] += d[k] * d[l];
+            for (int l = k; l < ND; l++) acc[q++] += d[k] * d[l];
 #pragma unroll
-        for (int k = 0; k < HIST_ND; k++) acc[HIST_NTRI + k] += d[k] * t;
-        acc[HIST_NACC - 1] += t * t;
+        for (int k = 0; k < ND; k++) acc[NT + k] += d[k] * t;
+        acc[NA - 1] += t * t;
     }
-    block_sum<HIST_NACC>(acc, HIST_NACC, red, sums);
-
-    if (threadIdx.x == 0) {
-        double G[HIST_ND][HIST_ND], b[HIST_ND], sc[HIST_ND], L[HIST_ND][HIST_ND], y[HIST_ND];
-        for (int k = 0; k < nd; k++)
-            for (int l = k; l < nd; l++) G[k][l] = G[l][k] = sums[tri(k, l)];
-        for (int k = 0; k < nd; k++) b[k] = sums[HIST_NTRI + k];
-        bool ok = true;
-        for (int k = 0; k < nd; k++) sc[k] = G[k][k] > 0.0 ? 1.0 / sqrt(G[k][k]) : 0.0;
-        for (int j = 0; j < nd && ok; j++) {
-            double sjj = (sc[j] > 0.0 ? G[j][j] * sc[j] * sc[j] : 1.0) + 1e-12;
-            for (int k = 0; k < j; k++) sjj -= L[j][k] * L[j][k];
-            if (!(sjj > 0.0)) { ok = false; break; }
-            L[j][j] = sqrt(sjj);
-            for (int i = j + 1; i < nd; i++) {
-                double sij = G[i][j] * sc[i] * sc[j];
-                for (int k = 0; k < j; k++) sij -= L[i][k] * L[j][k];
-                L[i][j] = sij / L[j][j];
-            }
-        }
-        if (ok) {
-            for (int i = 0; i < nd; i++) {
-                double r = b[i] * sc[i];
-                for (int k = 0; k < i; k++) r -= L[i][k] * y[k];
-                y[i] = r / L[i][i];
-            }
-            for (int i = nd - 1; i >= 0; i--) {
-                double r = y[i];
-                for (int k = i + 1; k < nd; k++) r -= L[k][i] * c[k];
-                c[i] = r / L[i][i];
-            }
-            for (int i = 0; i < nd; i++) {
-                c[i] *= sc[i];
-                if (!isfinite(c[i])) ok = false;
-            }
-        }
-        if (!ok)
-            for (int i = 0; i < nd; i++) c[i] = 0.0;
+#pragma unroll
+    for (int i = 0; i < NA; i++) {
+        double x = acc[i];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if (lane == 0) red[warp][i] = x;
     }
     __syncthreads();
-
-    // pass 2: misfit of the fit; keep it only below the unfitted change
-    double mis[1] = {0.0};
-    for (int i = threadIdx.x; i < n2; i += blockDim.x) {
-        const double ga = gA[i];
-        double r = bc_of(F.u, i, F.N, F.K, F.P) - ga;
-        for (int k = 0; k < nd; k++) r -= c[k] * (F.bc[(size_t)F.oth[k] * n2 + i] - ga);
-        mis[0] += r * r;
+    if (threadIdx.x < NA) {
+        double x = 0.0;
+        for (int w = 0; w < FIT_THREADS / 32; w++) x += red[w][threadIdx.x];
+        F.partial[blockIdx.x * NA + threadIdx.x] = x;
     }
-    __shared__ double red1[HIST_THREADS / 32][2];
-    __shared__ double msum[1];
-    block_sum<1>(mis, 1, red1, msum);
-    const double tt = sums[HIST_NACC - 1];
-    const bool keep = msum[0] <= tt;
-    if (threadIdx.x == 0) {
-        for (int k = 0; k < HIST_ND; k++) F.coef[k] = (keep && k < nd) ? c[k] : 0.0;
-        F.coef[HIST_ND] = tt > 0.0 ? sqrt((keep ? msum[0] : tt) / tt) : 0.0;
-    }
-    if (!keep) {
-        __syncthreads();
-        if (threadIdx.x < nd) c[threadIdx.x] = 0.0;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) is_last = atomicAdd(F.count, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    if (threadIdx.x < NA) {
+        double x = 0.0;
+        for (int b = 0; b < (int)gridDim.x; b++) x += __ldcg(F.partial + b * NA + threadIdx.x);
+        sums[threadIdx.x] = x;
     }
     __syncthreads();
-    if (F.implied)
-        for (int i = threadIdx.x; i < n2; i += blockDim.x) {
-            const double ga = gA[i];
-            double v = ga;
-            for (int k = 0; k < nd; k++) v += c[k] * (F.bc[(size_t)F.oth[k] * n2 + i] - ga);
-            F.implied[i] = v;
+    if (threadIdx.x != 0) return;
+    *F.count = 0;                                   // ready for the next fit
+
+    // unit-diagonal scaling, 1e-12 ridge, Cholesky
+    double G[ND][ND], b[ND], sc[ND], L[ND][ND], y[ND], c[ND];
+    int q = 0;
+    for (int k = 0; k < ND; k++)
+        for (int l = k; l < ND; l++) {
+            G[k][l] = G[l][k] = sums[q];
+            q++;
         }
+    for (int k = 0; k < ND; k++) b[k] = sums[NT + k];
+    const double tt = sums[NA - 1];
+    bool ok = true;
+    for (int k = 0; k < ND; k++) sc[k] = G[k][k] > 0.0 ? 1.0 / sqrt(G[k][k]) : 0.0;
+    for (int j = 0; j < ND && ok; j++) {
+        double sjj = (sc[j] > 0.0 ? G[j][j] * sc[j] * sc[j] : 1.0) + 1e-12;
+        for (int k = 0; k < j; k++) sjj -= L[j][k] * L[j][k];
+        if (!(sjj > 0.0)) { ok = false; break; }
+        L[j][j] = sqrt(sjj);
+        for (int i = j + 1; i < ND; i++) {
+            double sij = G[i][j] * sc[i] * sc[j];
+            for (int k = 0; k < j; k++) sij -= L[i][k] * L[j][k];
+            L[i][j] = sij / L[j][j];
+        }
+    }
+    if (ok) {
+        for (int i = 0; i < ND; i++) {
+            double r = b[i] * sc[i];
+            for (int k = 0; k < i; k++) r -= L[i][k] * y[k];
+            y[i] = r / L[i][i];
+        }
+        for (int i = ND - 1; i >= 0; i--) {
+            double r = y[i];
+            for (int k = i + 1; k < ND; k++) r -= L[k][i] * c[k];
+            c[i] = r / L[i][i];
+        }
+        for (int i = 0; i < ND; i++) {
+            c[i] *= sc[i];
+            if (!isfinite(c[i])) ok = false;
+        }
+    }
+    // misfit |t - D c|^2 = |t|^2 - 2 c.b + c^T G c; keep the fit only below
+    // the unfitted change
+    double mis = tt;
+    if (ok) {
+        for (int k = 0; k < ND; k++) {
+            double gc = 0.0;
+            for (int l = 0; l < ND; l++) gc += G[k][l] * c[l];
+            mis += c[k] * (gc - 2.0 * b[k]);
+        }
+        if (!(mis <= tt)) ok = false;
+    }
+    for (int k = 0; k < HIST_ND; k++) F.coef[k] = (ok && k < ND) ? c[k] : 0.0;
+    F.coef[HIST_ND] = tt > 0.0 ? sqrt(fmax(ok ? mis : tt, 0.0) / tt) : 0.0;
 }
 
 struct ApplyArgs {
     double *u;
     const double *ring;
     size_t field;
-    int N, K, P, nd, a;
+    int N, K, P, a;
     int oth[HIST_ND];
     const double *coef;
+    double *implied;      // nullable: the combination's boundary values (2N)
 };
 
-// interior columns 1..K-2: u = A + sum_k c_k (S_k - A); two nodes per thread
+// u = (1 - sum c_k) A + sum_k c_k S_k on the interior columns 1..K-2; the
+// boundary columns keep the new data (their combination goes to `implied`).
+// One row per blockIdx.y, two nodes per thread.
+template <int ND>
 __global__ void k_hist_apply(ApplyArgs A) {
-    const long pairs = (long)A.N * A.P / 2;
-    double c[HIST_ND];
+    const int row = blockIdx.y, col = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    if (col >= A.K) return;
+    double c[ND], wa = 1.0;
 #pragma unroll
-    for (int k = 0; k < HIST_ND; k++) c[k] = k < A.nd ? A.coef[k] : 0.0;
-    const double *Ua = A.ring + (size_t)A.a * A.field;
-    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < pairs; q += (long)gridDim.x * blockDim.x) {
-        const long e = 2 * q;
-        const int col = (int)(e % A.P);
-        if (col >= A.K) continue;
-        const double2 av = __ldcs(reinterpret_cast<const double2 *>(Ua + e));
-        double2 v = av;
+    for (int k = 0; k < ND; k++) {
+        c[k] = A.coef[k];
+        wa -= c[k];
+    }
+    const size_t e = (size_t)row * A.P + col;
+    const double2 av = __ldcs(reinterpret_cast<const double2 *>(A.ring + (size_t)A.a * A.field + e));
+    double2 v = make_double2(wa * av.x, wa * av.y);
 #pragma unroll
-        for (int k = 0; k < HIST_ND; k++) {
-            if (k >= A.nd) break;
-            const double2 sk = __ldcs(reinterpret_cast<const double2 *>(A.ring + (size_t)A.oth[k] * A.field + e));
-            v.x += c[k] * (sk.x - av.x);
-            v.y += c[k] * (sk.y - av.y);
-        }
-        double2 *dst = reinterpret_cast<double2 *>(A.u + e);
-        double2 o = *dst;                       // columns 0 and K-1 keep the new boundary data
-        if (col >= 1 && col <= A.K - 2) o.x = v.x;
-        if (col + 1 >= 1 && col + 1 <= A.K - 2) o.y = v.y;
-        *dst = o;
+    for (int k = 0; k < ND; k++) {
+        const double2 sk = __ldcs(reinterpret_cast<const double2 *>(A.ring + (size_t)A.oth[k] * A.field + e));
+        v.x = fma(c[k], sk.x, v.x);
+        v.y = fma(c[k], sk.y, v.y);
+    }
+    double2 *dst = reinterpret_cast<double2 *>(A.u + e);
+    double2 o = *dst;
+    if (col >= 1 && col <= A.K - 2) o.x = v.x;
+    if (col + 1 <= A.K - 2) o.y = v.y;
+    *dst = o;
+    if (A.implied) {
+        if (col == 0) A.implied[row] = v.x;
+        if (col == A.K - 1) A.implied[A.N + row] = v.x;
+        if (col + 1 == A.K - 1) A.implied[A.N + row] = v.y;
     }
 }
 
-// copy the solved u into ring slot `slot` and pack its boundary columns
-__global__ void k_hist_push(const double *u, double *dst, double *bc, size_t field, int N, int K, int P) {
-    const long pairs = (long)field / 2;
-    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < pairs; q += (long)gridDim.x * blockDim.x) {
-        const double2 v = reinterpret_cast<const double2 *>(u)[q];
-        reinterpret_cast<double2 *>(dst)[q] = v;
-        const long e = 2 * q;
-        const int row = (int)(e / P), col = (int)(e - (long)row * P);
-        if (col == 0) bc[row] = v.x;
-        if (col == K - 2) bc[N + row] = v.y;
-        if (col == K - 1) bc[N + row] = v.x;
-    }
-}
-
-static int stream_grid(long items) {
-    long g = (items + 255) / 256;
-    const long cap = 152L * 8;
-    return (int)(g < 1 ? 1 : (g > cap ? cap : g));
+// copy the solved u into a ring slot and pack its boundary columns
+__global__ void k_hist_push(const double *u, double *dst, double *bc, int N, int K, int P) {
+    const int row = blockIdx.y, col = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    if (col >= P) return;
+    const size_t e = (size_t)row * P + col;
+    const double2 v = *reinterpret_cast<const double2 *>(u + e);
+    *reinterpret_cast<double2 *>(dst + e) = v;
+    if (col == 0) bc[row] = v.x;
+    if (col == K - 1) bc[N + row] = v.x;
+    if (col + 1 == K - 1) bc[N + row] = v.y;
 }
 
 void history_free(qd_solver *s) {
@@ -247,6 +242,8 @@ void history_free(qd_solver *s) {
     cudaFree(H->u);
     cudaFree(H->bc);
     cudaFree(H->coef);
+    cudaFree(H->partial);
+    cudaFree(H->count);
     delete H;
     s->history = nullptr;
 }
@@ -273,13 +270,16 @@ int history_set(qd_solver *s, int m) {
     s->history = H;
     if (cudaMalloc(&H->u, sizeof(double) * H->field * m) != cudaSuccess ||
         cudaMalloc(&H->bc, sizeof(double) * 2 * (size_t)d.N * m) != cudaSuccess ||
-        cudaMalloc(&H->coef, sizeof(double) * (HIST_ND + 1)) != cudaSuccess) {
+        cudaMalloc(&H->coef, sizeof(double) * (HIST_ND + 1)) != cudaSuccess ||
+        cudaMalloc(&H->partial, sizeof(double) * FIT_CTAS * FIT_NA_MAX) != cudaSuccess ||
+        cudaMalloc(&H->count, sizeof(unsigned)) != cudaSuccess) {
         (void)cudaGetLastError();
         history_free(s);
         set_error("solution history: out of device memory (%d fields of %zu doubles)", m, (size_t)d.N * d.P);
         return QD_ERR_CUDA;
     }
     QD_CUDA(cudaMemset(H->coef, 0, sizeof(double) * (HIST_ND + 1)));
+    QD_CUDA(cudaMemset(H->count, 0, sizeof(unsigned)));
     return QD_OK;
 }
 
@@ -301,21 +301,36 @@ int history_guess(qd_solver *s, double *implied_bc) {
     F.u = s->L64[0].u;
     F.bc = H->bc;
     F.N = d.N; F.K = d.K; F.P = d.P;
-    F.nd = history_slots(H, &F.a, F.oth);
+    const int nd = history_slots(H, &F.a, F.oth);
     F.coef = H->coef;
-    F.implied = implied_bc;
-    k_hist_fit<<<1, HIST_THREADS, 0, s->stream>>>(F);
-    QD_LAUNCH_CHECK(s);
+    F.partial = H->partial;
+    F.count = H->count;
     ApplyArgs A{};
     A.u = s->L64[0].u;
     A.ring = H->u;
     A.field = H->field;
     A.N = d.N; A.K = d.K; A.P = d.P;
-    A.nd = F.nd; A.a = F.a;
+    A.a = F.a;
     for (int k = 0; k < HIST_ND; k++) A.oth[k] = F.oth[k];
     A.coef = H->coef;
-    k_hist_apply<<<stream_grid((long)H->field / 2), 256, 0, s->stream>>>(A);
-    QD_LAUNCH_CHECK(s);
+    A.implied = implied_bc;
+    const int fit_ctas = std::min(FIT_CTAS, (2 * d.N + FIT_THREADS - 1) / FIT_THREADS);
+    const dim3 agrid((d.K + 255) / 256, d.N);
+    switch (nd) {
+#define QD_HIST_CASE(n)                                                       \
+    case n:                                                                   \
+        k_hist_fit<n><<<fit_ctas, FIT_THREADS, 0, s->stream>>>(F);            \
+        QD_LAUNCH_CHECK(s);                                                   \
+        k_hist_apply<n><<<agrid, 128, 0, s->stream>>>(A);                     \
+        QD_LAUNCH_CHECK(s);                                                   \
+        break;
+        QD_HIST_CASE(1) QD_HIST_CASE(2) QD_HIST_CASE(3) QD_HIST_CASE(4)
+        QD_HIST_CASE(5) QD_HIST_CASE(6) QD_HIST_CASE(7)
+#undef QD_HIST_CASE
+        default:
+            set_error("solution history: %d stored solutions", H->n);
+            return QD_ERR_STATE;
+    }
     H->guesses++;
     return QD_OK;
 }
@@ -326,8 +341,8 @@ int history_push(qd_solver *s) {
     if (!H) return QD_OK;
     const LevelDims &d = s->dims[0];
     const int slot = H->head;
-    k_hist_push<<<stream_grid((long)H->field / 2), 256, 0, s->stream>>>(
-        s->L64[0].u, H->u + (size_t)slot * H->field, H->bc + (size_t)slot * 2 * d.N, H->field, d.N, d.K, d.P);
+    k_hist_push<<<dim3((d.P / 2 + 127) / 128, d.N), 128, 0, s->stream>>>(
+        s->L64[0].u, H->u + (size_t)slot * H->field, H->bc + (size_t)slot * 2 * d.N, d.N, d.K, d.P);
     QD_LAUNCH_CHECK(s);
     H->head = (H->head + 1) % H->m;
     if (H->n < H->m) H->n++;
