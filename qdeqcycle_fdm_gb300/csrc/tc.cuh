@@ -108,6 +108,25 @@ __device__ __forceinline__ void mma_commit(uint64_t *bar) {
 }
 
 // ---- epilogue --------------------------------------------------------------
+// the load without the wait: issue several, then tmem_ld_wait() on each
+// group of destination registers
+__device__ __forceinline__ void tmem_ld8_issue(uint32_t taddr, uint32_t r[8]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+        : "r"(taddr)
+        : "memory");
+}
+// Wait for this thread's outstanding tensor-memory loads.  The destination
+// registers pass through the instruction as operands, so no use of them can
+// be scheduled before it (the first call waits, repeated ones are free).
+__device__ __forceinline__ void tmem_ld_wait(uint32_t r[8]) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7])
+                 :
+                 : "memory");
+}
+
 // 8 consecutive FP32 columns of this thread's lane
 __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float v[8]) {
     uint32_t r[8];
@@ -116,7 +135,7 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float v[8]) {
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
         : "r"(taddr)
         : "memory");
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    tmem_ld_wait(r);
 #pragma unroll
     for (int i = 0; i < 8; i++) v[i] = __uint_as_float(r[i]);
 }

@@ -26,6 +26,7 @@
 #include <math.h>
 #include <string.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "qdeq_internal.cuh"
@@ -455,17 +456,36 @@ static int conv_launch(qd_unet *u, const CUtensorMap &ta, const CUtensorMap &tb,
     return QD_OK;
 }
 
+static int sm_count() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1)
+            n = 1;
+    }
+    return n;
+}
+
+// persistent: as many CTAs as fit on the GPU at once, at most one per tile
 template <int CIN, int COUT>
 static int conv_rows_launch(qd_unet *u, const CUtensorMap &ta, const CUtensorMap &tb, const ConvArgs &a) {
-    constexpr int MT = conv_rows_mt<CIN, COUT>();
-    const size_t smem = 3 * (size_t)conv_rows_stage<CIN, COUT>() + 1024;
-    static bool raised = false;
-    if (!raised) {
+    using R = RowsCfg<CIN, COUT>;
+    static int per_sm = 0;
+    if (!per_sm) {
         QD_CUDA(cudaFuncSetAttribute(k_conv_rows<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem));
-        raised = true;
+                                     (int)R::SMEM));
+        QD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv_rows<CIN, COUT>, ROWS_THREADS,
+                                                              R::SMEM));
+        if (per_sm < 1) {
+            set_error("k_conv_rows<%d,%d>: no CTA fits on an SM", CIN, COUT);
+            return QD_ERR_CUDA;
+        }
+        if (per_sm * 2 * R::NC > 512) per_sm = 512 / (2 * R::NC);    // tensor-memory columns per SM
     }
-    k_conv_rows<CIN, COUT><<<cdv(a.P, 128 * MT), CONV_THREADS, smem, u->stream>>>(ta, tb, a);
+    const int tiles = cdv(a.P, 128 * R::MT);
+    const int grid = std::min(tiles, per_sm * sm_count());
+    k_conv_rows<CIN, COUT><<<grid, ROWS_THREADS, R::SMEM, u->stream>>>(ta, tb, a);
     QD_CUDA(cudaPeekAtLastError());
     return QD_OK;
 }

@@ -54,6 +54,8 @@ struct ConvArgs {
     unsigned *status;
 };
 
+__device__ __forceinline__ int cdiv_dev(int a, int b) { return (a + b - 1) / b; }
+
 __device__ __forceinline__ int tap_shift(int t, int Wp) { return (t / 3 - 1) * Wp + (t % 3 - 1); }
 
 __device__ __forceinline__ bool interior_pixel(int p, const ConvArgs &a) {
@@ -185,141 +187,215 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv_fwd(const __grid_constant
     if (warp == 2) tmem_free(tmem, TCOLS);
 }
 
-// k_conv_rows: the 3x3 convolution for 16 or 32 input channels, one TMA load
-// per (sub-tile, tap row) instead of per tap.  A pixel row of the operand is
-// 32 or 64 bytes, too narrow for efficient swizzled boxes and read nine times
-// by k_conv_fwd; here the activation is staged unswizzled in 16-byte column
+// k_conv_rows: the 3x3 convolution for 16 or 32 input channels, persistent.
+// A pixel row of the operand is 32 or 64 bytes, too narrow for efficient
+// swizzled boxes; here the activation is staged unswizzled in 16-byte column
 // chunks (boxes of 8 channels x 130 pixel rows: the 128 rows of a sub-tile
-// and one more on each side) for each of the three tap rows dy, and the
-// three taps dx = -1, 0, 1 of that row are the same tiles started 0, 1 and 2
-// rows down -- a 16-byte shift of the descriptor's start address.  The three
-// tap rows are the three pipeline stages, all in flight at once; the weights
-// of the three taps of a row ride in the same stage.
+// and one more on each side) once per tap row dy, and the three taps
+// dx = -1, 0, 1 of that row are the same boxes started 0, 1 and 2 rows
+// down -- a 16-byte shift of the descriptor's start address.  A tile is MT
+// sub-tiles of 128 output pixels; each CTA walks the tiles with stride
+// gridDim.x:
+//   warp 0 lane 0  TMA producer: three tap-row stages per tile through a
+//                  ring of CONV_RING slots (two tiles in flight);
+//   warp 1 lane 0  MMA issuer into one of two tensor-memory accumulators
+//                  (tile parity), so a tile's epilogue overlaps the next
+//                  tile's loads and MMAs;
+//   warps 2..9     epilogue: warp w reads tensor-memory lanes 32*(w%4)..
+//                  of every other sub-tile (two warps per lane quarter).
+// The nine taps' weights are staged once per CTA.  Every wait is bounded;
+// a wait that gives up sets ST_UNET_TIMEOUT and a shared abort flag that
+// ends every role's loop, after which the producer waits (bounded) for its
+// copies still in flight and the MMA issuer for its MMAs before the tensor
+// memory is freed.
 template <int CIN, int COUT>
 __host__ __device__ constexpr int conv_rows_mt() {
     return CIN == 16 ? (4 * COUT <= 256 ? 4 : 256 / COUT) : (2 * COUT <= 256 ? 2 : 256 / COUT);
 }
 static constexpr int ROWS_BOX = 130;       // pixel rows per staged box
 static constexpr int ROWS_ABOX = 2176;     // bytes per box slot (130 x 16 rounded up to 128)
+static constexpr int CONV_RING = 5;        // A-operand stages in flight (a tile and two thirds)
+static constexpr int ROWS_THREADS = 320;   // producer, MMA, eight epilogue warps
+static constexpr int ROWS_EPI_WARPS = 8;
 
 template <int CIN, int COUT>
-__host__ __device__ constexpr int conv_rows_stage() {
-    return (conv_rows_mt<CIN, COUT>() * (CIN / 8) * ROWS_ABOX + 3 * ((COUT * CIN * 2 + 1023) / 1024 * 1024) +
-            1023) / 1024 * 1024;
-}
+struct RowsCfg {
+    static constexpr int MT = conv_rows_mt<CIN, COUT>();
+    static constexpr int NCH = CIN / 8;                                 // 16-byte chunks per pixel
+    static constexpr int ASLOT = MT * NCH * ROWS_ABOX;                  // one tap row of a tile
+    static constexpr int BT = (COUT * CIN * 2 + 1023) / 1024 * 1024;    // one tap's weights
+    static constexpr int NC = MT * COUT;                                // columns per accumulator
+    static constexpr uint32_t TCOLS = 2 * NC <= 32 ? 32 : (2 * NC <= 64 ? 64 : (2 * NC <= 128 ? 128 : (2 * NC <= 256 ? 256 : 512)));
+    static constexpr unsigned ATX = MT * NCH * ROWS_BOX * 16;
+    static constexpr unsigned BTX = 9 * COUT * CIN * 2;
+    static constexpr size_t SMEM = 9 * (size_t)BT + CONV_RING * (size_t)ASLOT + 1024;
+    static_assert(CIN == 16 || CIN == 32, "row boxes serve 16 or 32 input channels");
+    static_assert(ASLOT % 1024 == 0 && BT % 1024 == 0, "operand tiles start 1024-byte aligned");
+    static_assert(2 * NC <= 512 && ROWS_ABOX % 128 == 0 && ROWS_ABOX >= ROWS_BOX * 16, "layout");
+};
 
 template <int CIN, int COUT>
-__global__ void __launch_bounds__(CONV_THREADS) k_conv_rows(const __grid_constant__ CUtensorMap ta,
+__global__ void __launch_bounds__(ROWS_THREADS) k_conv_rows(const __grid_constant__ CUtensorMap ta,
                                                             const __grid_constant__ CUtensorMap tb,
                                                             ConvArgs a) {
-    constexpr int MT = conv_rows_mt<CIN, COUT>();
-    constexpr int NCH = CIN / 8;                                    // 16-byte chunks per pixel
-    constexpr int ABYTES = MT * NCH * ROWS_ABOX;
-    constexpr int BT = (COUT * CIN * 2 + 1023) / 1024 * 1024;       // one tap's weights, 1 KB aligned
-    constexpr int STAGE = conv_rows_stage<CIN, COUT>();
-    constexpr int NC = MT * COUT;
-    constexpr uint32_t TCOLS = NC <= 32 ? 32 : (NC <= 64 ? 64 : (NC <= 128 ? 128 : 256));
-    constexpr unsigned TX = MT * NCH * ROWS_BOX * 16 + 3 * COUT * CIN * 2;
-    static_assert(CIN == 16 || CIN == 32, "row boxes serve 16 or 32 input channels");
-    static_assert(ABYTES % 1024 == 0, "weight tiles must start 1024-byte aligned");
-    static_assert(NC <= 256 && ROWS_ABOX % 128 == 0 && ROWS_ABOX >= ROWS_BOX * 16, "layout");
+    using R = RowsCfg<CIN, COUT>;
+    constexpr int MT = R::MT, NCH = R::NCH;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    __shared__ __align__(8) uint64_t full[3], done;
+    __shared__ __align__(8) uint64_t full[CONV_RING], empty[CONV_RING], tfull[2], tempty[2], wfull, done;
     __shared__ uint32_t tmem_base;
+    __shared__ volatile int abort_;
     unsigned char *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+    unsigned char *sw = smem, *ring = smem + 9 * R::BT;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m0 = blockIdx.x * 128 * MT;
+    const int ntiles = cdiv_dev(a.P, 128 * MT);
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < 3; s++) mbar_init(&full[s], 1);
+        for (int s = 0; s < CONV_RING; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; b++) {
+            mbar_init(&tfull[b], 1);
+            mbar_init(&tempty[b], ROWS_EPI_WARPS);
+        }
+        mbar_init(&wfull, 1);
         mbar_init(&done, 1);
+        abort_ = 0;
     }
-    if (warp == 2) tmem_alloc(&tmem_base, TCOLS);
+    if (warp == 1) tmem_alloc(&tmem_base, R::TCOLS);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = tmem_base;
 
     if (warp == 0 && lane == 0) {
-        // stage di: the operand rows shifted by dy = di - 1 (and dx = -1),
-        // and the weights of the taps (di, dx = -1, 0, 1)
-        for (int di = 0; di < 3; di++) {
-            unsigned char *sa = smem + di * STAGE, *sb = sa + ABYTES;
-            mbar_expect_tx(&full[di], TX);
-            const int row0 = m0 + (di - 1) * a.Wp - 1;
-#pragma unroll
-            for (int mt = 0; mt < MT; mt++)
-#pragma unroll
-                for (int c = 0; c < NCH; c++)
-                    tma_load_2d(sa + (mt * NCH + c) * ROWS_ABOX, &ta, 8 * c, row0 + mt * 128, &full[di]);
-#pragma unroll
-            for (int dx = 0; dx < 3; dx++) {
-                const int t = 3 * di + dx;
-                tma_load_2d(sb + dx * BT, &tb, 0, (a.tap_reverse ? 8 - t : t) * COUT, &full[di]);
-            }
-        }
-    } else if (warp == 1 && lane == 0) {
-        constexpr uint32_t idesc = idesc_bf16_f32(COUT);
-        for (int di = 0; di < 3; di++) {
-            if (!mbar_wait(&full[di], 0)) {
-                atomicOr(a.status, ST_UNET_TIMEOUT);
-                break;
-            }
-            tc_fence_after();
-            const uint32_t sa = smem_u32(smem + di * STAGE), sb = sa + ABYTES;
-#pragma unroll
-            for (int dx = 0; dx < 3; dx++)
+        mbar_expect_tx(&wfull, R::BTX);
+        for (int t = 0; t < 9; t++) tma_load_2d(sw + t * R::BT, &tb, 0, (a.tap_reverse ? 8 - t : t) * COUT, &wfull);
+        int s = 0;
+        for (int tile = blockIdx.x; tile < ntiles && !abort_; tile += gridDim.x) {
+            const int m0 = tile * 128 * MT;
+            for (int di = 0; di < 3; di++, s++) {
+                const int slot = s % CONV_RING;
+                if (s >= CONV_RING && !mbar_wait(&empty[slot], ((s / CONV_RING) - 1) & 1)) {
+                    atomicOr(a.status, ST_UNET_TIMEOUT);
+                    abort_ = 1;
+                    break;
+                }
+                unsigned char *sa = ring + slot * R::ASLOT;
+                mbar_expect_tx(&full[slot], R::ATX);
+                const int row0 = m0 + (di - 1) * a.Wp - 1;
 #pragma unroll
                 for (int mt = 0; mt < MT; mt++)
 #pragma unroll
-                    for (int ks = 0; ks < CIN / 16; ks++)
-                        mma_bf16(tmem + (uint32_t)(mt * COUT),
-                                 smem_desc_noswz(sa + (mt * NCH + 2 * ks) * ROWS_ABOX + 16 * dx, ROWS_ABOX, 128),
-                                 smem_desc(sb + dx * BT + 32 * ks, CIN * 2), idesc,
-                                 (di > 0 || dx > 0 || ks > 0) ? 1u : 0u);
+                    for (int c = 0; c < NCH; c++)
+                        tma_load_2d(sa + (mt * NCH + c) * ROWS_ABOX, &ta, 8 * c, row0 + mt * 128, &full[slot]);
+            }
         }
+        // the copies of the last ring round have landed before the CTA exits
+        for (int q = s - CONV_RING < 0 ? 0 : s - CONV_RING; q < s; q++)
+            if (!mbar_wait(&full[q % CONV_RING], (q / CONV_RING) & 1)) atomicOr(a.status, ST_UNET_TIMEOUT);
+        if (!mbar_wait(&wfull, 0)) atomicOr(a.status, ST_UNET_TIMEOUT);
+    } else if (warp == 1 && lane == 0) {
+        constexpr uint32_t idesc = idesc_bf16_f32(COUT);
+        const uint32_t sb = smem_u32(sw), sring = smem_u32(ring);
+        bool ok = mbar_wait(&wfull, 0);
+        int s = 0, li = 0;
+        for (int tile = blockIdx.x; ok && tile < ntiles && !abort_; tile += gridDim.x, li++) {
+            const int buf = li & 1;
+            if (li >= 2 && !mbar_wait(&tempty[buf], ((li >> 1) - 1) & 1)) { ok = false; break; }
+            tc_fence_after();
+            const uint32_t acc = tmem + (uint32_t)(buf * R::NC);
+            for (int di = 0; di < 3; di++, s++) {
+                const int slot = s % CONV_RING;
+                if (!mbar_wait(&full[slot], (s / CONV_RING) & 1)) { ok = false; break; }
+                tc_fence_after();
+                const uint32_t sa = sring + slot * R::ASLOT;
+#pragma unroll
+                for (int dx = 0; dx < 3; dx++)
+#pragma unroll
+                    for (int mt = 0; mt < MT; mt++)
+#pragma unroll
+                        for (int ks = 0; ks < CIN / 16; ks++)
+                            mma_bf16(acc + (uint32_t)(mt * COUT),
+                                     smem_desc_noswz(sa + (mt * NCH + 2 * ks) * ROWS_ABOX + 16 * dx, ROWS_ABOX, 128),
+                                     smem_desc(sb + (3 * di + dx) * R::BT + 32 * ks, CIN * 2), idesc,
+                                     (di > 0 || dx > 0 || ks > 0) ? 1u : 0u);
+                mma_commit(&empty[slot]);
+            }
+            if (!ok) break;
+            mma_commit(&tfull[buf]);
+        }
+        if (!ok) {
+            atomicOr(a.status, ST_UNET_TIMEOUT);
+            abort_ = 1;
+        }
+        // every MMA this thread issued has completed before the memory is freed
         mma_commit(&done);
+        if (!mbar_wait(&done, 0)) atomicOr(a.status, ST_UNET_TIMEOUT);
+    } else if (warp >= 2) {
+        const int q = warp & 3;                     // tensor-memory lane quarter of this warp
+        const int half = (warp - 2) >> 2;           // sub-tiles half, half + 2, ...
+        int li = 0;
+        for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, li++) {
+            const int buf = li & 1;
+            const bool ok = !abort_ && mbar_wait(&tfull[buf], (li >> 1) & 1);
+            if (!ok) {
+                if (lane == 0 && !abort_) {
+                    atomicOr(a.status, ST_UNET_TIMEOUT);
+                    abort_ = 1;
+                }
+                break;
+            }
+            tc_fence_after();
+            const int m0 = tile * 128 * MT;
+#pragma unroll 1
+            for (int mt = half; mt < MT; mt += 2) {
+                const int p = m0 + mt * 128 + 32 * q + lane;
+                const bool in = p < a.P && interior_pixel(p, a);
+                uint32_t r[COUT];
+#pragma unroll
+                for (int n0 = 0; n0 < COUT; n0 += 8)
+                    tmem_ld8_issue(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(buf * R::NC + mt * COUT + n0),
+                                   r + n0);
+#pragma unroll
+                for (int n0 = 0; n0 < COUT; n0 += 8) tmem_ld_wait(r + n0);
+                if (p >= a.P) continue;
+#pragma unroll
+                for (int n0 = 0; n0 < COUT; n0 += 8) {
+                    float v[8];
+#pragma unroll
+                    for (int i = 0; i < 8; i++) {
+                        float x = __uint_as_float(r[n0 + i]) + (a.bias ? a.bias[n0 + i] : 0.f);
+                        if (a.relu) x = fmaxf(x, 0.f);
+                        v[i] = (in ? x : 0.f);
+                    }
+                    if (a.mask && in) {
+                        const uint4 mk = *reinterpret_cast<const uint4 *>(a.mask + (size_t)p * COUT + n0);
+                        const __nv_bfloat16 *mv = reinterpret_cast<const __nv_bfloat16 *>(&mk);
+#pragma unroll
+                        for (int i = 0; i < 8; i++)
+                            if (!(__bfloat162float(mv[i]) > 0.f)) v[i] = 0.f;
+                    }
+                    if (a.out_f32) {
+                        if (n0 == 0) a.out_f32[p] = v[0];
+                    } else {
+                        uint4 o;
+                        __nv_bfloat162 *ov = reinterpret_cast<__nv_bfloat162 *>(&o);
+#pragma unroll
+                        for (int i = 0; i < 4; i++) ov[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+                        *reinterpret_cast<uint4 *>(a.out + (size_t)p * COUT + n0) = o;
+                    }
+                }
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&tempty[buf]);
+        }
     }
     __syncwarp();
-    const bool ok = mbar_wait(&done, 0);
-    if (!ok && threadIdx.x == 0) atomicOr(a.status, ST_UNET_TIMEOUT);
-    tc_fence_after();
-#pragma unroll 1
-    for (int mt = 0; mt < MT; mt++) {
-        const int p = m0 + mt * 128 + 32 * warp + lane;
-        const bool in = p < a.P && interior_pixel(p, a);
-#pragma unroll
-        for (int n0 = 0; n0 < COUT; n0 += 8) {
-            float v[8];
-            tmem_ld8(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(mt * COUT + n0), v);
-            if (p >= a.P || !ok) continue;
-#pragma unroll
-            for (int i = 0; i < 8; i++) {
-                float x = v[i] + (a.bias ? a.bias[n0 + i] : 0.f);
-                if (a.relu) x = fmaxf(x, 0.f);
-                v[i] = (in ? x : 0.f);
-            }
-            if (a.mask && in) {
-                const uint4 mk = *reinterpret_cast<const uint4 *>(a.mask + (size_t)p * COUT + n0);
-                const __nv_bfloat16 *mv = reinterpret_cast<const __nv_bfloat16 *>(&mk);
-#pragma unroll
-                for (int i = 0; i < 8; i++)
-                    if (!(__bfloat162float(mv[i]) > 0.f)) v[i] = 0.f;
-            }
-            if (a.out_f32) {
-                if (n0 == 0) a.out_f32[p] = v[0];
-            } else {
-                uint4 o;
-                __nv_bfloat162 *ov = reinterpret_cast<__nv_bfloat162 *>(&o);
-#pragma unroll
-                for (int i = 0; i < 4; i++) ov[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
-                *reinterpret_cast<uint4 *>(a.out + (size_t)p * COUT + n0) = o;
-            }
-        }
-    }
     tc_fence_before();
     __syncthreads();
-    if (warp == 2) tmem_free(tmem, TCOLS);
+    if (warp == 1) tmem_free(tmem, R::TCOLS);
 }
 
 struct WgradArgs {
