@@ -467,6 +467,28 @@ static int sm_count() {
     return n;
 }
 
+// CTAs of a kernel that fit on one SM at once, from its attributes: shared
+// memory (static + dynamic + the 1 KB the driver reserves per CTA),
+// registers (allocated per warp in units of 256), threads, and tensor-memory
+// columns (512 per SM)
+static int ctas_per_sm(const void *fn, int threads, size_t dyn_smem, int tmem_cols) {
+    cudaFuncAttributes fa{};
+    int dev = 0, smem_sm = 0, regs_sm = 0, thr_sm = 0;
+    if (cudaFuncGetAttributes(&fa, fn) != cudaSuccess || cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev) != cudaSuccess)
+        return 1;
+    const long smem_cta = (long)fa.sharedSizeBytes + (long)dyn_smem + 1024;
+    const int warps = (threads + 31) / 32;
+    const long regs_cta = (long)warps * (((long)fa.numRegs * 32 + 255) / 256 * 256);
+    long n = smem_sm / smem_cta;
+    n = std::min(n, regs_sm / std::max(1L, regs_cta));
+    n = std::min(n, (long)(thr_sm / threads));
+    n = std::min(n, (long)(512 / tmem_cols));
+    return (int)std::max(1L, n);
+}
+
 // persistent: as many CTAs as fit on the GPU at once, at most one per tile
 template <int CIN, int COUT>
 static int conv_rows_launch(qd_unet *u, const CUtensorMap &ta, const CUtensorMap &tb, const ConvArgs &a) {
@@ -475,13 +497,9 @@ static int conv_rows_launch(qd_unet *u, const CUtensorMap &ta, const CUtensorMap
     if (!per_sm) {
         QD_CUDA(cudaFuncSetAttribute(k_conv_rows<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)R::SMEM));
-        QD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv_rows<CIN, COUT>, ROWS_THREADS,
-                                                              R::SMEM));
-        if (per_sm < 1) {
-            set_error("k_conv_rows<%d,%d>: no CTA fits on an SM", CIN, COUT);
-            return QD_ERR_CUDA;
-        }
-        if (per_sm * 2 * R::NC > 512) per_sm = 512 / (2 * R::NC);    // tensor-memory columns per SM
+        QD_CUDA(cudaFuncSetAttribute(k_conv_rows<CIN, COUT>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     (int)cudaSharedmemCarveoutMaxShared));
+        per_sm = ctas_per_sm((const void *)k_conv_rows<CIN, COUT>, ROWS_THREADS, R::SMEM, (int)R::TCOLS);
     }
     const int tiles = cdv(a.P, 128 * R::MT);
     const int grid = std::min(tiles, per_sm * sm_count());
