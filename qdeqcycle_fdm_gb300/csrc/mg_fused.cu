@@ -598,6 +598,40 @@ int encode_tiled_2d(CUtensorMap *map, const void *base, int dtype, int esz, long
     return QD_OK;
 }
 
+int encode_tiled_3d(CUtensorMap *map, const void *base, int dtype, int esz, long d0, long d1, long d2,
+                    long stride1_bytes, long stride2_bytes, int box0, int box1, int box2) {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        QD_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                                 &q));
+        if (!p || q != cudaDriverEntryPointSuccess) {
+            set_error("cuTensorMapEncodeTiled is not available from the driver");
+            return QD_ERR_CUDA;
+        }
+        fn = (EncodeTiledFn)p;
+    }
+    if (!base || ((uintptr_t)base & 15) || stride1_bytes % 16 || stride2_bytes % 16 || ((long)box0 * esz) % 16 ||
+        box0 < 1 || box0 > 256 || box1 < 1 || box1 > 256 || box2 < 1 || box2 > 256 || d0 < 1 || d1 < 1 ||
+        d2 < 1) {
+        set_error("tensor map %ldx%ldx%ld box %dx%dx%d violates the TMA rules", d0, d1, d2, box0, box1, box2);
+        return QD_ERR_ARG;
+    }
+    const cuuint64_t dims[3] = {(cuuint64_t)d0, (cuuint64_t)d1, (cuuint64_t)d2};
+    const cuuint64_t strides[2] = {(cuuint64_t)stride1_bytes, (cuuint64_t)stride2_bytes};
+    const cuuint32_t box[3] = {(cuuint32_t)box0, (cuuint32_t)box1, (cuuint32_t)box2};
+    const cuuint32_t es[3] = {1, 1, 1};
+    const CUresult r = fn(map, (CUtensorMapDataType)dtype, 3, const_cast<void *>(base), dims, strides, box, es,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("cuTensorMapEncodeTiled (3-D) failed (%d)", (int)r);
+        return QD_ERR_CUDA;
+    }
+    return QD_OK;
+}
+
 int make_tensor_map_2d(CUtensorMap *map, const void *base, bool fp64, int width, int height,
                        int pitch, int box_w, int box_h) {
     const int esz = fp64 ? 8 : 4;

@@ -67,6 +67,16 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, i
         : "memory");
 }
 
+// 3-D tile load: box at (x, y, z)
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z,
+                                            uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+        "l"((uint64_t)map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+
 // host: build a 2-D tiled tensor map (rows of `width` elements, `pitch`
 // elements apart, `height` rows) with a box of box_w x box_h elements
 int make_tensor_map_2d(CUtensorMap *map, const void *base, bool fp64, int width, int height,
@@ -75,5 +85,8 @@ int make_tensor_map_2d(CUtensorMap *map, const void *base, bool fp64, int width,
 // CUtensorMapSwizzle (the box row must fit the swizzle span)
 int encode_tiled_2d(CUtensorMap *map, const void *base, int dtype, int esz, long width, long height,
                     long pitch_bytes, int box_w, int box_h, int swizzle);
+// unswizzled 3-D map: d0 innermost; strides of dimensions 1 and 2 in bytes
+int encode_tiled_3d(CUtensorMap *map, const void *base, int dtype, int esz, long d0, long d1, long d2,
+                    long stride1_bytes, long stride2_bytes, int box0, int box1, int box2);
 
 }  // namespace qd

@@ -56,6 +56,7 @@ struct ULayer {
     __nv_bfloat16 *w, *wt;             // [9][cout][cin], [9][cin][cout]
     CUtensorMap m_in, m_w, m_gout, m_wt;   // A/B operands of forward and data gradient
     CUtensorMap m_in_rows, m_gout_rows;    // A operands as 8-channel row boxes (16/32 channels)
+    bool rows_fwd, rows_dgrad;             // which of the two have them
 };
 
 enum UOpKind { OP_CONV, OP_POOL, OP_UP, OP_ADD };
@@ -427,10 +428,22 @@ static int map_act(CUtensorMap *m, const UTensor &t, const UGrid &g) {
                            swz(KB * 2));
 }
 
-// A operand of k_conv_rows: 8-channel x 130-row unswizzled boxes
-static int map_act_rows(CUtensorMap *m, const UTensor &t, const UGrid &g) {
-    return encode_tiled_2d(m, t.p, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, t.C, g.P, (long)t.C * 2, 8, ROWS_BOX,
-                           CU_TENSOR_MAP_SWIZZLE_NONE);
+// A operand of k_conv_rows: the tensor as (channel, column, row) with
+// unswizzled boxes of 8 channels x 130 columns x (mt + 2) rows, mt the
+// convolution's tile height
+static int map_act_rows(CUtensorMap *m, const UTensor &t, const UGrid &g, int mt) {
+    return encode_tiled_3d(m, t.p, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, t.C, g.Wp, g.H + 2, (long)t.C * 2,
+                           (long)g.Wp * t.C * 2, 8, ROWS_BOXW, mt + 2);
+}
+
+// tile height of k_conv_rows for cin -> cout channels (0: not a row-box case)
+static int rows_mt(int cin, int cout) {
+#define QD_MT_CASE(ci, co) \
+    if (cin == ci && cout == co) return conv_rows_mt<ci, co>();
+    QD_MT_CASE(16, 16) QD_MT_CASE(16, 32) QD_MT_CASE(16, 64)
+    QD_MT_CASE(32, 16) QD_MT_CASE(32, 32) QD_MT_CASE(32, 64)
+#undef QD_MT_CASE
+    return 0;
 }
 
 // B operand: weights [9*rows][K], box KB x rows
@@ -501,7 +514,7 @@ static int conv_rows_launch(qd_unet *u, const CUtensorMap &ta, const CUtensorMap
                                      (int)cudaSharedmemCarveoutMaxShared));
         per_sm = ctas_per_sm((const void *)k_conv_rows<CIN, COUT>, ROWS_THREADS, R::SMEM, (int)R::TCOLS);
     }
-    const int tiles = cdv(a.P, 128 * R::MT);
+    const int tiles = cdv(a.H + 2, R::MT) * cdv(a.Wp, 128);
     const int grid = std::min(tiles, per_sm * sm_count());
     k_conv_rows<CIN, COUT><<<grid, ROWS_THREADS, R::SMEM, u->stream>>>(ta, tb, a);
     QD_CUDA(cudaPeekAtLastError());
@@ -566,7 +579,7 @@ static int forward(qd_unet *u) {
             a.relu = Ly.relu;
             a.bias = Ly.b32;
             if (Ly.out) a.out = Ly.out->p; else a.out_f32 = u->out32;
-            QD_TRY(conv_dispatch(u, Ly.m_in, Ly.in->C <= 32 ? &Ly.m_in_rows : nullptr, Ly.m_w, a));
+            QD_TRY(conv_dispatch(u, Ly.m_in, Ly.rows_fwd ? &Ly.m_in_rows : nullptr, Ly.m_w, a));
         } else if (op.k == OP_POOL) {
             const long n = (long)u->g[op.out->lvl].P * op.out->C;
             k_pool<<<EW8_GRID(n)>>>(op.a->p, op.out->p, u->g[op.a->lvl], u->g[op.out->lvl], op.a->C);
@@ -634,7 +647,7 @@ static int backward(qd_unet *u) {
                 ConvArgs a = conv_args(u, g, Ly.cout, Ly.cin);
                 a.out = Ly.gin->p;
                 a.tap_reverse = 1;
-                QD_TRY(conv_dispatch(u, Ly.m_gout, Ly.gout->C <= 32 ? &Ly.m_gout_rows : nullptr, Ly.m_wt, a));
+                QD_TRY(conv_dispatch(u, Ly.m_gout, Ly.rows_dgrad ? &Ly.m_gout_rows : nullptr, Ly.m_wt, a));
             }
         } else if (op.k == OP_POOL) {
             const long n = (long)u->g[op.a->lvl].P * op.a->C;
@@ -849,8 +862,11 @@ static int unet_build(qd_unet *u, unsigned long long seed) {
         QD_TRY(map_act(&Ly.m_in, *Ly.in, u->g[Ly.lvl]));
         QD_TRY(map_w(&Ly.m_w, Ly.w, Ly.cout, Ly.cin));
         QD_TRY(map_act(&Ly.m_gout, *Ly.gout, u->g[Ly.lvl]));
-        if (Ly.in->C <= 32) QD_TRY(map_act_rows(&Ly.m_in_rows, *Ly.in, u->g[Ly.lvl]));
-        if (Ly.gout->C <= 32) QD_TRY(map_act_rows(&Ly.m_gout_rows, *Ly.gout, u->g[Ly.lvl]));
+        Ly.rows_fwd = rows_mt(Ly.cin, Ly.cout) > 0;
+        Ly.rows_dgrad = rows_mt(Ly.cout, Ly.cin) > 0;
+        if (Ly.rows_fwd) QD_TRY(map_act_rows(&Ly.m_in_rows, *Ly.in, u->g[Ly.lvl], rows_mt(Ly.cin, Ly.cout)));
+        if (Ly.rows_dgrad)
+            QD_TRY(map_act_rows(&Ly.m_gout_rows, *Ly.gout, u->g[Ly.lvl], rows_mt(Ly.cout, Ly.cin)));
         QD_TRY(map_w(&Ly.m_wt, Ly.wt, Ly.cin, Ly.cout));
     }
     // planar scratch: dY (<= 128 rows at the layer's level) + 3 shifted X copies

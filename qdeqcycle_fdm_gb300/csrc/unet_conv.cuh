@@ -187,22 +187,26 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv_fwd(const __grid_constant
     if (warp == 2) tmem_free(tmem, TCOLS);
 }
 
-// k_conv_rows: the 3x3 convolution for 16 or 32 input channels, persistent.
-// A pixel row of the operand is 32 or 64 bytes, too narrow for efficient
-// swizzled boxes; here the activation is staged unswizzled in 16-byte column
-// chunks (boxes of 8 channels x 130 pixel rows: the 128 rows of a sub-tile
-// and one more on each side) once per tap row dy, and the three taps
-// dx = -1, 0, 1 of that row are the same boxes started 0, 1 and 2 rows
-// down -- a 16-byte shift of the descriptor's start address.  A tile is MT
-// sub-tiles of 128 output pixels; each CTA walks the tiles with stride
-// gridDim.x:
-//   warp 0 lane 0  TMA producer: three tap-row stages per tile through a
-//                  ring of CONV_RING slots (two tiles in flight);
+// k_conv_rows: the 3x3 convolution for 16 or 32 input channels, persistent,
+// on 2-D tiles of MT image rows x 128 columns of the padded grid.  A pixel
+// row of the operand is 32 or 64 bytes, too narrow for efficient swizzled
+// boxes; here the activation is staged unswizzled in 16-byte channel chunks:
+// per chunk one 3-D box of 8 channels x 130 columns x (MT + 2) rows (the
+// tile with a one-pixel halo), so that
+//   * the operand of output row mt at tap (dy, dx) is the box's row mt + dy
+//     started dx columns in -- a 16-byte multiple added to the descriptor's
+//     start address (core matrices are 8 columns x 16 bytes, rows 16 bytes
+//     apart; the K-adjacent chunk is the next chunk plane);
+//   * the three tap rows of neighbouring output rows share staged rows, so a
+//     tile stages (MT + 2) / (3 MT) of what one box per tap row would.
+// Each CTA walks the tiles with stride gridDim.x:
+//   warp 0 lane 0  TMA producer: one stage per tile through a ring of
+//                  ROWS_RING slots;
 //   warp 1 lane 0  MMA issuer into one of two tensor-memory accumulators
 //                  (tile parity), so a tile's epilogue overlaps the next
 //                  tile's loads and MMAs;
 //   warps 2..9     epilogue: warp w reads tensor-memory lanes 32*(w%4)..
-//                  of every other sub-tile (two warps per lane quarter).
+//                  of every other output row (two warps per lane quarter).
 // The nine taps' weights are staged once per CTA.  Every wait is bounded;
 // a wait that gives up sets ST_UNET_TIMEOUT and a shared abort flag that
 // ends every role's loop, after which the producer waits (bounded) for its
@@ -210,11 +214,10 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv_fwd(const __grid_constant
 // memory is freed.
 template <int CIN, int COUT>
 __host__ __device__ constexpr int conv_rows_mt() {
-    return CIN == 16 ? (4 * COUT <= 256 ? 4 : 256 / COUT) : (2 * COUT <= 256 ? 2 : 256 / COUT);
+    return CIN == 16 ? (COUT <= 32 ? 8 : 4) : (COUT <= 32 ? 4 : 4);
 }
-static constexpr int ROWS_BOX = 130;       // pixel rows per staged box
-static constexpr int ROWS_ABOX = 2176;     // bytes per box slot (130 x 16 rounded up to 128)
-static constexpr int CONV_RING = 5;        // A-operand stages in flight (a tile and two thirds)
+static constexpr int ROWS_BOXW = 130;      // staged columns: 128 outputs and a halo column each side
+static constexpr int ROWS_RING = 2;        // tile stages in flight
 static constexpr int ROWS_THREADS = 320;   // producer, MMA, eight epilogue warps
 static constexpr int ROWS_EPI_WARPS = 8;
 
@@ -222,16 +225,18 @@ template <int CIN, int COUT>
 struct RowsCfg {
     static constexpr int MT = conv_rows_mt<CIN, COUT>();
     static constexpr int NCH = CIN / 8;                                 // 16-byte chunks per pixel
-    static constexpr int ASLOT = MT * NCH * ROWS_ABOX;                  // one tap row of a tile
+    static constexpr int BOXB = 16 * ROWS_BOXW * (MT + 2);              // one chunk's box
+    static constexpr int CPL = (BOXB + 127) / 128 * 128;                // chunk plane stride
+    static constexpr int ASLOT = (NCH * CPL + 1023) / 1024 * 1024;      // one tile
     static constexpr int BT = (COUT * CIN * 2 + 1023) / 1024 * 1024;    // one tap's weights
     static constexpr int NC = MT * COUT;                                // columns per accumulator
     static constexpr uint32_t TCOLS = 2 * NC <= 32 ? 32 : (2 * NC <= 64 ? 64 : (2 * NC <= 128 ? 128 : (2 * NC <= 256 ? 256 : 512)));
-    static constexpr unsigned ATX = MT * NCH * ROWS_BOX * 16;
+    static constexpr unsigned ATX = NCH * BOXB;
     static constexpr unsigned BTX = 9 * COUT * CIN * 2;
-    static constexpr size_t SMEM = 9 * (size_t)BT + CONV_RING * (size_t)ASLOT + 1024;
+    static constexpr size_t SMEM = 9 * (size_t)BT + ROWS_RING * (size_t)ASLOT + 1024;
     static_assert(CIN == 16 || CIN == 32, "row boxes serve 16 or 32 input channels");
-    static_assert(ASLOT % 1024 == 0 && BT % 1024 == 0, "operand tiles start 1024-byte aligned");
-    static_assert(2 * NC <= 512 && ROWS_ABOX % 128 == 0 && ROWS_ABOX >= ROWS_BOX * 16, "layout");
+    static_assert(MT % 2 == 0, "two epilogue warps per lane quarter take alternate rows");
+    static_assert(2 * NC <= 512 && CPL < (1 << 18), "layout");
 };
 
 template <int CIN, int COUT>
@@ -241,16 +246,17 @@ __global__ void __launch_bounds__(ROWS_THREADS) k_conv_rows(const __grid_constan
     using R = RowsCfg<CIN, COUT>;
     constexpr int MT = R::MT, NCH = R::NCH;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    __shared__ __align__(8) uint64_t full[CONV_RING], empty[CONV_RING], tfull[2], tempty[2], wfull, done;
+    __shared__ __align__(8) uint64_t full[ROWS_RING], empty[ROWS_RING], tfull[2], tempty[2], wfull, done;
     __shared__ uint32_t tmem_base;
     __shared__ volatile int abort_;
     unsigned char *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
     unsigned char *sw = smem, *ring = smem + 9 * R::BT;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int ntiles = cdiv_dev(a.P, 128 * MT);
+    const int HP = a.H + 2;                               // padded rows
+    const int ncb = cdiv_dev(a.Wp, 128), ntiles = cdiv_dev(HP, MT) * ncb;
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < CONV_RING; s++) {
+        for (int s = 0; s < ROWS_RING; s++) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
@@ -272,44 +278,36 @@ __global__ void __launch_bounds__(ROWS_THREADS) k_conv_rows(const __grid_constan
         mbar_expect_tx(&wfull, R::BTX);
         for (int t = 0; t < 9; t++) tma_load_2d(sw + t * R::BT, &tb, 0, (a.tap_reverse ? 8 - t : t) * COUT, &wfull);
         int s = 0;
-        for (int tile = blockIdx.x; tile < ntiles && !abort_; tile += gridDim.x) {
-            const int m0 = tile * 128 * MT;
-            for (int di = 0; di < 3; di++, s++) {
-                const int slot = s % CONV_RING;
-                if (s >= CONV_RING && !mbar_wait(&empty[slot], ((s / CONV_RING) - 1) & 1)) {
-                    atomicOr(a.status, ST_UNET_TIMEOUT);
-                    abort_ = 1;
-                    break;
-                }
-                unsigned char *sa = ring + slot * R::ASLOT;
-                mbar_expect_tx(&full[slot], R::ATX);
-                const int row0 = m0 + (di - 1) * a.Wp - 1;
-#pragma unroll
-                for (int mt = 0; mt < MT; mt++)
-#pragma unroll
-                    for (int c = 0; c < NCH; c++)
-                        tma_load_2d(sa + (mt * NCH + c) * ROWS_ABOX, &ta, 8 * c, row0 + mt * 128, &full[slot]);
+        for (int tile = blockIdx.x; tile < ntiles && !abort_; tile += gridDim.x, s++) {
+            const int r0 = (tile / ncb) * MT, c0 = (tile % ncb) * 128;
+            const int slot = s % ROWS_RING;
+            if (s >= ROWS_RING && !mbar_wait(&empty[slot], ((s / ROWS_RING) - 1) & 1)) {
+                atomicOr(a.status, ST_UNET_TIMEOUT);
+                abort_ = 1;
+                break;
             }
+            unsigned char *sa = ring + slot * R::ASLOT;
+            mbar_expect_tx(&full[slot], R::ATX);
+#pragma unroll
+            for (int c = 0; c < NCH; c++) tma_load_3d(sa + c * R::CPL, &ta, 8 * c, c0 - 1, r0 - 1, &full[slot]);
         }
         // the copies of the last ring round have landed before the CTA exits
-        for (int q = s - CONV_RING < 0 ? 0 : s - CONV_RING; q < s; q++)
-            if (!mbar_wait(&full[q % CONV_RING], (q / CONV_RING) & 1)) atomicOr(a.status, ST_UNET_TIMEOUT);
+        for (int q = s - ROWS_RING < 0 ? 0 : s - ROWS_RING; q < s; q++)
+            if (!mbar_wait(&full[q % ROWS_RING], (q / ROWS_RING) & 1)) atomicOr(a.status, ST_UNET_TIMEOUT);
         if (!mbar_wait(&wfull, 0)) atomicOr(a.status, ST_UNET_TIMEOUT);
     } else if (warp == 1 && lane == 0) {
         constexpr uint32_t idesc = idesc_bf16_f32(COUT);
         const uint32_t sb = smem_u32(sw), sring = smem_u32(ring);
         bool ok = mbar_wait(&wfull, 0);
-        int s = 0, li = 0;
+        int li = 0;
         for (int tile = blockIdx.x; ok && tile < ntiles && !abort_; tile += gridDim.x, li++) {
-            const int buf = li & 1;
+            const int buf = li & 1, slot = li % ROWS_RING;
             if (li >= 2 && !mbar_wait(&tempty[buf], ((li >> 1) - 1) & 1)) { ok = false; break; }
+            if (!mbar_wait(&full[slot], (li / ROWS_RING) & 1)) { ok = false; break; }
             tc_fence_after();
-            const uint32_t acc = tmem + (uint32_t)(buf * R::NC);
-            for (int di = 0; di < 3; di++, s++) {
-                const int slot = s % CONV_RING;
-                if (!mbar_wait(&full[slot], (s / CONV_RING) & 1)) { ok = false; break; }
-                tc_fence_after();
-                const uint32_t sa = sring + slot * R::ASLOT;
+            const uint32_t acc = tmem + (uint32_t)(buf * R::NC), sa = sring + slot * R::ASLOT;
+#pragma unroll
+            for (int dy = 0; dy < 3; dy++)
 #pragma unroll
                 for (int dx = 0; dx < 3; dx++)
 #pragma unroll
@@ -317,12 +315,11 @@ __global__ void __launch_bounds__(ROWS_THREADS) k_conv_rows(const __grid_constan
 #pragma unroll
                         for (int ks = 0; ks < CIN / 16; ks++)
                             mma_bf16(acc + (uint32_t)(mt * COUT),
-                                     smem_desc_noswz(sa + (mt * NCH + 2 * ks) * ROWS_ABOX + 16 * dx, ROWS_ABOX, 128),
-                                     smem_desc(sb + (3 * di + dx) * R::BT + 32 * ks, CIN * 2), idesc,
-                                     (di > 0 || dx > 0 || ks > 0) ? 1u : 0u);
-                mma_commit(&empty[slot]);
-            }
-            if (!ok) break;
+                                     smem_desc_noswz(sa + 2 * ks * R::CPL + ((mt + dy) * ROWS_BOXW + dx) * 16,
+                                                     R::CPL, 128),
+                                     smem_desc(sb + (3 * dy + dx) * R::BT + 32 * ks, CIN * 2), idesc,
+                                     (dy > 0 || dx > 0 || ks > 0) ? 1u : 0u);
+            mma_commit(&empty[slot]);
             mma_commit(&tfull[buf]);
         }
         if (!ok) {
@@ -334,7 +331,7 @@ __global__ void __launch_bounds__(ROWS_THREADS) k_conv_rows(const __grid_constan
         if (!mbar_wait(&done, 0)) atomicOr(a.status, ST_UNET_TIMEOUT);
     } else if (warp >= 2) {
         const int q = warp & 3;                     // tensor-memory lane quarter of this warp
-        const int half = (warp - 2) >> 2;           // sub-tiles half, half + 2, ...
+        const int half = (warp - 2) >> 2;           // output rows half, half + 2, ...
         int li = 0;
         for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, li++) {
             const int buf = li & 1;
@@ -347,11 +344,13 @@ __global__ void __launch_bounds__(ROWS_THREADS) k_conv_rows(const __grid_constan
                 break;
             }
             tc_fence_after();
-            const int m0 = tile * 128 * MT;
+            const int r0 = (tile / ncb) * MT, col = (tile % ncb) * 128 + 32 * q + lane;
 #pragma unroll 1
             for (int mt = half; mt < MT; mt += 2) {
-                const int p = m0 + mt * 128 + 32 * q + lane;
-                const bool in = p < a.P && interior_pixel(p, a);
+                const int row = r0 + mt;
+                const bool valid = row < HP && col < a.Wp;
+                const bool in = row >= 1 && row <= a.H && col >= 1 && col <= a.W;
+                const size_t p = (size_t)row * a.Wp + col;
                 uint32_t r[COUT];
 #pragma unroll
                 for (int n0 = 0; n0 < COUT; n0 += 8)
@@ -359,7 +358,7 @@ __global__ void __launch_bounds__(ROWS_THREADS) k_conv_rows(const __grid_constan
                                    r + n0);
 #pragma unroll
                 for (int n0 = 0; n0 < COUT; n0 += 8) tmem_ld_wait(r + n0);
-                if (p >= a.P) continue;
+                if (!valid) continue;
 #pragma unroll
                 for (int n0 = 0; n0 < COUT; n0 += 8) {
                     float v[8];
@@ -370,7 +369,7 @@ __global__ void __launch_bounds__(ROWS_THREADS) k_conv_rows(const __grid_constan
                         v[i] = (in ? x : 0.f);
                     }
                     if (a.mask && in) {
-                        const uint4 mk = *reinterpret_cast<const uint4 *>(a.mask + (size_t)p * COUT + n0);
+                        const uint4 mk = *reinterpret_cast<const uint4 *>(a.mask + p * COUT + n0);
                         const __nv_bfloat16 *mv = reinterpret_cast<const __nv_bfloat16 *>(&mk);
 #pragma unroll
                         for (int i = 0; i < 8; i++)
@@ -383,7 +382,7 @@ __global__ void __launch_bounds__(ROWS_THREADS) k_conv_rows(const __grid_constan
                         __nv_bfloat162 *ov = reinterpret_cast<__nv_bfloat162 *>(&o);
 #pragma unroll
                         for (int i = 0; i < 4; i++) ov[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
-                        *reinterpret_cast<uint4 *>(a.out + (size_t)p * COUT + n0) = o;
+                        *reinterpret_cast<uint4 *>(a.out + p * COUT + n0) = o;
                     }
                 }
             }
