@@ -41,9 +41,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 YEAR_S = 365.25 * 86400.0
-# DRAM bytes (read + write) per launch of the V-cycle kernels at 1025^2,
-# from one ncu capture of the headline solver (profiles/vcycle_kernels_1025.md)
-TRAFFIC = {"up0": 31.19e6, "down0": 17.35e6, "residual": 33.74e6}
+# DRAM bytes (read + write) per launch at 1025^2 from ncu captures with the
+# caches flushed before the kernel: the V-cycle kernels of the mixed solver
+# (profiles/vcycle_kernels_1025.md) and the U-Net's first 16 -> 16 channel
+# convolution (profiles/unet_conv_1025.md)
+TRAFFIC = {"up0": 31.19e6, "down0": 17.35e6, "residual": 33.74e6, "conv16": 34.03e6}
 METRIC = "simulated yr/hr at 1025² (learned+mixed vs plain FP64 MG, 1e-9 rel residual)"
 
 
@@ -64,6 +66,9 @@ def parse():
     p.add_argument("--no-learned", action="store_true", help="headline without the learned warm start")
     p.add_argument("--lr", type=float, default=1e-3)
     p.add_argument("--seed", type=int, default=1)
+    p.add_argument("--profile-run", action="store_true",
+                   help="only the headline solver's W + K steps (network trained for --train-steps "
+                        "steps first), for per-kernel profilers; prints a one-line summary")
     p.add_argument("--history", type=int, default=4,
                    help="stored solutions of the solution-history guess (0: start every solve "
                         "from the previous solution, as the reference)")
@@ -321,6 +326,17 @@ def run_ours(args):
     learned = not args.no_learned
     peaks = _peaks()
     net, tinfo = train_network(mixed_cfg) if learned else (None, {})
+    if args.profile_run:
+        simp, run = timed_run(mixed_cfg, net=net, history=H)
+        simp.close()
+        if rank == 0:
+            print(json.dumps({"profile_run": "headline solver", "learned": learned, "history": H,
+                              "steps": args.steps, "warmup": args.warmup, "ms_per_step": run["ms"] / args.steps,
+                              "vcycles_per_solve": run["vcycles"] / max(1, run["solves"]),
+                              "solves_per_step": run["solves"] / args.steps}), flush=True)
+        if net is not None:
+            net.close()
+        return 0
     clocks = Clocks(local)
     clocks.start()
     sim, head = timed_run(mixed_cfg, net=net, history=H)
@@ -398,41 +414,63 @@ def run_ours(args):
     if not args.headline_only:
         extra["ensemble"] = ensemble_run()
 
-    # Roofline of the V-cycle's kernels (the headline solver's hierarchy).
-    # Inside a solve they run in a CUDA graph, so each is timed by
-    # qd_mg_time_kernel: REPS back-to-back launches on the solver's stream
-    # between two CUDA events, on the solver's own state after the timed run.
-    # Algorithmic bytes per launch are the unfused algorithm's traffic:
+    # Roofline.  The candidates are the kernels with the largest device time
+    # in the headline step: the V-cycle's level-0 kernels and coarse tail and,
+    # with the network, its first (full-grid, 16 -> 16 channel) convolution,
+    # four of which run per inference.  Inside a solve the V-cycle kernels run
+    # in a CUDA graph, so each is timed by qd_mg_time_kernel: REPS
+    # back-to-back launches on the solver's stream between two CUDA events,
+    # on the solver's own state after the timed run; the convolution by
+    # qd_unet_time the same way.  Algorithmic bytes per launch are the
+    # unfused algorithm's traffic:
     #   down0    2 red+black sweeps x 20 B + residual/restriction 16 B per
     #            level-0 node, + 4 B per level-1 node
     #   up0      prolongation 8 B + 2 sweeps x 20 B + u64 += e 16 B per
     #            level-0 node, + 4 B per level-1 node
     #   residual FP64 u, cx, cz, diag read + FP32 rhs written: 36 B per node
-    # The dominant kernel (largest time per V-cycle) is the roofline entry.
+    #   conv16   16 BF16 channels read and written: 64 B per padded pixel
+    # Launches per step: one of each cycle kernel per V-cycle, the residual
+    # once more per solve (the guess), the convolution 4 per solve.  The
+    # dominant kernel (largest time x launches per step) is the roofline entry.
     peak = peaks.get("hbm_gbs", 6800.0)
     n0 = cfg.ni * cfg.nk
     n1 = ((cfg.ni - 1) // 2 + 1) * ((cfg.nk - 1) // 2 + 1)
-    algo = {"up0": 64.0 * n0 + 4.0 * n1, "down0": 56.0 * n0 + 4.0 * n1, "residual": 36.0 * n0}
+    pad_px = (cfg.nk + 2) * ((cfg.ni + 2 + 7) // 8 * 8)
+    algo = {"up0": 64.0 * n0 + 4.0 * n1, "down0": 56.0 * n0 + 4.0 * n1, "residual": 36.0 * n0,
+            "conv16": 64.0 * pad_px}
     names = {"up0": "k_up<float,2> level 0 (prolongation + 2 sweeps + u64 += e)",
              "down0": "k_down<float> level 0 (2 sweeps + residual + restriction)",
              "residual": "k_residual64_to32 (FP64 residual -> FP32 rhs + norm)",
-             "tail": "k_tail<float> (levels <= 65 rows, one CTA)"}
+             "tail": "k_tail<float> (levels <= 65 rows, one CTA)",
+             "conv16": "k_conv_rows<16,16> (U-Net 3x3 convolution, full grid, tcgen05)"}
     REPS = 50
     kern = {}
     for k in ("up0", "down0", "residual", "tail"):
         sim.solver.time_kernel(k, 3)                      # warm-up launches
-        us = sim.solver.time_kernel(k, REPS)
-        kern[k] = {"us": us, "kernel": names[k]}
+        kern[k] = {"us": sim.solver.time_kernel(k, REPS), "kernel": names[k]}
+    cyc_step = head["vcycles"] / args.steps
+    sol_step = head["solves"] / args.steps
+    per_step = {"up0": cyc_step, "down0": cyc_step, "residual": cyc_step + sol_step, "tail": cyc_step}
+    if net is not None:
+        net.time("conv16", 3)
+        us_c, fl_c = net.time("conv16", REPS)
+        kern["conv16"] = {"us": us_c, "kernel": names["conv16"],
+                          "tflops": fl_c / (us_c * 1e-6) / 1e12}
+        per_step["conv16"] = 4.0 * sol_step
+    for k, v in kern.items():
+        v["launches_per_step"] = per_step[k]
+        v["us_per_step"] = v["us"] * per_step[k]
+        v["share_of_step_est"] = v["us_per_step"] / (1e3 * ms_max / args.steps)
         if k in algo:
-            kern[k]["algo_bytes"] = algo[k]
-            kern[k]["achieved_gbs"] = algo[k] / (us * 1e-6) / 1e9
-    dom = max(algo, key=lambda k: kern[k]["us"])
+            v["algo_bytes"] = algo[k]
+            v["achieved_gbs"] = algo[k] / (v["us"] * 1e-6) / 1e9
+    dom = max(algo.keys() & kern.keys(), key=lambda k: kern[k]["us_per_step"])
     achieved = kern[dom]["achieved_gbs"]
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": TRAFFIC.get(dom),
                 "kernel": names[dom], "us_per_launch": kern[dom]["us"], "reps": REPS,
                 "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
-                "vcycle_kernels": kern}
+                "kernels": kern}
 
     # end to end through the C ABI with host buffers (pinned), the same steps
     e2e = None

@@ -61,12 +61,14 @@ int qd_solver_warm_start(qd_solver *s, qd_unet *u, int mode, float lr);
 /* training steps taken, and the loss of the last step */
 int qd_unet_stats(qd_unet *u, long long *train_steps, float *last_loss);
 
-/* Mean device microseconds of one inference (what = 0) or one training
- * step without the parameter update (what = 1: forward, loss, backward),
- * timed with CUDA events over `reps` back-to-back runs on the network's
- * stream on its current input and target; *flops receives the tensor-core
- * FLOPs of one run (2 * 9 * cin * cout per output pixel of every
- * convolution; in training, the data and weight gradients add two more). */
+/* Mean device microseconds of one inference (what = 0), one training step
+ * without the parameter update (what = 1: forward, loss, backward) or the
+ * first convolution alone (what = 2: 16 -> 16 channels on the full grid,
+ * the network's most frequent and longest-running kernel), timed with CUDA
+ * events over `reps` back-to-back runs on the network's stream on its
+ * current input and target; *flops receives the tensor-core FLOPs of one
+ * run (2 * 9 * cin * cout per output pixel of every convolution; in
+ * training, the data and weight gradients add two more). */
 int qd_unet_time(qd_unet *u, int what, int reps, double *us, double *flops);
 
 #ifdef __cplusplus

@@ -79,7 +79,8 @@ struct qd_unet {
     float *out32, *target32;       // P0 floats
     float *d_prev;                 // the last solve's change of u / s_bc (P0 floats): input channel 4
     float *d_loss;                 // [0] loss sum
-    float *d_scale;                // [0] s_bc, [1] s_u
+    float *d_scale;                // [0] s_bc, [1] s_u, [2] 1/s_bc, [3] 1/s_u
+    float *d_rowf;                 // per-row input channels: fault (N), far (N)
     double *d_bc_old;              // saved boundary columns: fault (N), far (N)
     double *d_u_start;             // u a solve would start from without the network (level-0 layout)
     __nv_bfloat16 *planar;         // dY planar + 3 shifted X planar copies
@@ -337,20 +338,29 @@ __global__ void k_save_bc(const double *u, int N, int K, int P, double *bc) {
     bc[N + j] = u[(long)j * P + K - 1];
 }
 
-// s_bc = max |change of the boundary data|, s_u = max |boundary data|
-__global__ void k_scales(const double *u, int N, int K, int P, const double *bc, float *scale) {
-    double sb = 0.0, su = 0.0;
+// One CTA over the boundary rows: s_bc = max |change of the boundary data|,
+// s_u = max |boundary data|, their reciprocals, and the two per-row input
+// channels (change on the fault / far column over s_bc).  Every row's
+// difference is taken in FP64 and rounded to FP32 on the integer pipes
+// (d2f_rne); scales and features are FP32 (the network's inputs are BF16).
+// scale: [0] s_bc, [1] s_u, [2] 1/s_bc, [3] 1/s_u; rowf: fault (N), far (N)
+__global__ void __launch_bounds__(1024) k_scales(const double *u, int N, int K, int P, const double *bc,
+                                                 float *scale, float *rowf) {
+    __shared__ float wb[32], wu[32], inv[2];
+    float sb = 0.f, su = 0.f;
     for (int j = threadIdx.x; j < N; j += blockDim.x) {
         const double f = u[(long)j * P], r = u[(long)j * P + K - 1];
-        sb = fmax(sb, fmax(fabs(f - bc[j]), fabs(r - bc[N + j])));
-        su = fmax(su, fmax(fabs(f), fabs(r)));
+        const float df = d2f_rne(f - bc[j]), dr = d2f_rne(r - bc[N + j]);
+        rowf[j] = df;
+        rowf[N + j] = dr;
+        sb = fmaxf(sb, fmaxf(fabsf(df), fabsf(dr)));
+        su = fmaxf(su, fmaxf(fabsf(d2f_rne(f)), fabsf(d2f_rne(r))));
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        sb = fmax(sb, __shfl_xor_sync(0xffffffffu, sb, o));
-        su = fmax(su, __shfl_xor_sync(0xffffffffu, su, o));
+        sb = fmaxf(sb, __shfl_xor_sync(0xffffffffu, sb, o));
+        su = fmaxf(su, __shfl_xor_sync(0xffffffffu, su, o));
     }
-    __shared__ double wb[32], wu[32];
     if ((threadIdx.x & 31) == 0) {
         wb[threadIdx.x >> 5] = sb;
         wu[threadIdx.x >> 5] = su;
@@ -358,15 +368,24 @@ __global__ void k_scales(const double *u, int N, int K, int P, const double *bc,
     __syncthreads();
     if (threadIdx.x == 0) {
         for (int w = 1; w < (int)(blockDim.x >> 5); w++) {
-            sb = fmax(sb, wb[w]);
-            su = fmax(su, wu[w]);
+            sb = fmaxf(sb, wb[w]);
+            su = fmaxf(su, wu[w]);
         }
-        scale[0] = (float)fmax(sb, 1e-30);
-        scale[1] = (float)fmax(su, 1e-30);
+        sb = fmaxf(sb, 1e-30f);
+        su = fmaxf(su, 1e-30f);
+        scale[0] = sb;
+        scale[1] = su;
+        scale[2] = inv[0] = 1.f / sb;
+        scale[3] = inv[1] = 1.f / su;
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < N; j += blockDim.x) {   // each thread rescales the rows it wrote
+        rowf[j] *= inv[0];
+        rowf[N + j] *= inv[0];
     }
 }
 
-__global__ void k_features(const double *u, int N, int K, int P, const double *bc, const float *scale,
+__global__ void k_features(const double *u, int N, int K, int P, const float *rowf, const float *scale,
                            const float *prev, __nv_bfloat16 *x0, UGrid g) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= g.P) return;
@@ -374,10 +393,9 @@ __global__ void k_features(const double *u, int N, int K, int P, const double *b
     float f[UNET_NIN] = {0.f, 0.f, 0.f, 0.f, 0.f};
     if (uin(r, q, g)) {
         const int j = r - 1, k = q - 1;
-        const float sb = scale[0], su = scale[1];
-        f[0] = (float)(u[(long)j * P + k] / su);
-        f[1] = (float)((u[(long)j * P] - bc[j]) / sb);
-        f[2] = (float)((u[(long)j * P + K - 1] - bc[N + j]) / sb);
+        f[0] = d2f_rne(u[(long)j * P + k]) * scale[3];
+        f[1] = rowf[j];
+        f[2] = rowf[N + j];
         f[3] = (float)k / (float)(K - 1);
         f[4] = prev[p];
     }
@@ -399,7 +417,8 @@ __global__ void k_apply(double *u, int N, int K, int P, const float *out, const 
     u[(long)j * P + k] += (double)scale[0] * (double)out[(long)(j + 1) * g.Wp + (k + 1)];
 }
 
-// training target: (u_solved - u_start) / s_bc on the interior
+// training target: (u_solved - u_start) / s_bc on the interior (the
+// difference in FP64, then FP32)
 __global__ void k_target(const double *u, const double *u0, int N, int K, int P, const float *scale,
                          float *target, UGrid g) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -408,7 +427,7 @@ __global__ void k_target(const double *u, const double *u0, int N, int K, int P,
     float t = 0.f;
     if (uin(r, q, g)) {
         const long c = (long)(r - 1) * P + (q - 1);
-        t = (float)((u[c] - u0[c]) / (double)scale[0]);
+        t = d2f_rne(u[c] - u0[c]) * scale[2];
     }
     target[p] = t;
 }
@@ -729,7 +748,7 @@ static void unet_free(qd_unet *u) {
         cudaFree(Ly.w32); cudaFree(Ly.b32); cudaFree(Ly.mw); cudaFree(Ly.vw); cudaFree(Ly.mb);
         cudaFree(Ly.vb); cudaFree(Ly.gw); cudaFree(Ly.gb); cudaFree(Ly.w); cudaFree(Ly.wt);
     }
-    cudaFree(u->out32); cudaFree(u->target32); cudaFree(u->d_prev); cudaFree(u->d_loss); cudaFree(u->d_scale);
+    cudaFree(u->out32); cudaFree(u->target32); cudaFree(u->d_prev); cudaFree(u->d_loss); cudaFree(u->d_scale); cudaFree(u->d_rowf);
     cudaFree(u->d_bc_old); cudaFree(u->d_u_start); cudaFree(u->planar); cudaFree(u->d_status);
     if (u->own_stream) cudaStreamDestroy(u->own_stream);
     delete u;
@@ -878,7 +897,8 @@ static int unet_build(qd_unet *u, unsigned long long seed) {
     u->target32 = dalloc_z<float>(u->g[0].P, &rc);
     u->d_prev = dalloc_z<float>(u->g[0].P, &rc);
     u->d_loss = dalloc_z<float>(1, &rc);
-    u->d_scale = dalloc_z<float>(2, &rc);
+    u->d_scale = dalloc_z<float>(4, &rc);
+    u->d_rowf = dalloc_z<float>(2 * (size_t)u->nk, &rc);
     u->d_status = dalloc_z<unsigned>(1, &rc);
     u->d_bc_old = dalloc_z<double>(2 * (size_t)u->nk, &rc);
     if (rc != QD_OK) set_error("U-Net allocation failed");
@@ -957,8 +977,8 @@ int warm_start_after_boundary(qd_solver *s) {
     if (!u || !u->mode) return QD_OK;
     const LevelDims &d = s->dims[0];
     const UGrid &g = u->g[0];
-    k_scales<<<1, 1024, 0, s->stream>>>(s->L64[0].u, d.N, d.K, d.P, u->d_bc_old, u->d_scale);
-    k_features<<<cdv(g.P, 256), 256, 0, s->stream>>>(s->L64[0].u, d.N, d.K, d.P, u->d_bc_old, u->d_scale,
+    k_scales<<<1, 1024, 0, s->stream>>>(s->L64[0].u, d.N, d.K, d.P, u->d_bc_old, u->d_scale, u->d_rowf);
+    k_features<<<cdv(g.P, 256), 256, 0, s->stream>>>(s->L64[0].u, d.N, d.K, d.P, u->d_rowf, u->d_scale,
                                                      u->d_prev, u->x0->p, g);
     QD_LAUNCH_CHECK(s);
     // the field the solve would start from without the network: the change
@@ -1143,12 +1163,26 @@ int qd_solver_warm_start(qd_solver *s, qd_unet *u, int mode, float lr) {
     return QD_OK;
 }
 
+// the first convolution of the forward pass alone
+static int first_conv(qd_unet *u) {
+    ULayer &Ly = u->L[0];
+    ConvArgs a = conv_args(u, u->g[Ly.lvl], Ly.cin, Ly.cout);
+    a.relu = Ly.relu;
+    a.bias = Ly.b32;
+    a.out = Ly.out->p;
+    return conv_dispatch(u, Ly.m_in, Ly.rows_fwd ? &Ly.m_in_rows : nullptr, Ly.m_w, a);
+}
+
 int qd_unet_time(qd_unet *u, int what, int reps, double *us, double *flops) {
-    if (!u || (what != 0 && what != 1) || reps < 1 || !us) return QD_ERR_ARG;
+    if (!u || what < 0 || what > 2 || reps < 1 || !us) return QD_ERR_ARG;
     double f = 0.0;
     for (const auto &Ly : u->L) {
         const UGrid &g = u->g[Ly.lvl];
         const double conv = 2.0 * 9.0 * Ly.cin * Ly.cout * (double)g.H * g.W;
+        if (what == 2) {
+            f = conv;
+            break;
+        }
         f += conv * (what ? (Ly.gin ? 3.0 : 2.0) : 1.0);
     }
     if (flops) *flops = f;
@@ -1156,7 +1190,8 @@ int qd_unet_time(qd_unet *u, int what, int reps, double *us, double *flops) {
     QD_CUDA(cudaEventCreate(&e0));
     QD_CUDA(cudaEventCreate(&e1));
     int rc = cudaEventRecord(e0, u->stream) == cudaSuccess ? QD_OK : QD_ERR_CUDA;
-    for (int i = 0; i < reps && rc == QD_OK; i++) rc = what ? loss_and_grad(u) : forward(u);
+    for (int i = 0; i < reps && rc == QD_OK; i++)
+        rc = what == 2 ? first_conv(u) : (what ? loss_and_grad(u) : forward(u));
     float ms = 0.f;
     if (rc == QD_OK && (cudaEventRecord(e1, u->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
                         cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))

@@ -81,9 +81,11 @@ class UNet:
 
     def time(self, what: str = "forward", reps: int = 10):
         """(microseconds per run, tensor-core FLOPs per run) of one inference
-        ("forward") or one training step without the update ("train")."""
+        ("forward"), one training step without the update ("train") or the
+        first, full-grid 16 -> 16 channel convolution alone ("conv16")."""
         us, fl = C.c_double(0), C.c_double(0)
-        check(self.L.qd_unet_time(self.h, 0 if what == "forward" else 1, reps, C.byref(us), C.byref(fl)))
+        code = {"forward": 0, "train": 1, "conv16": 2}[what]
+        check(self.L.qd_unet_time(self.h, code, reps, C.byref(us), C.byref(fl)))
         return us.value, fl.value
 
     def stats(self):
