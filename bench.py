@@ -69,6 +69,8 @@ def parse():
     p.add_argument("--profile-run", action="store_true",
                    help="only the headline solver's W + K steps (network trained for --train-steps "
                         "steps first), for per-kernel profilers; prints a one-line summary")
+    p.add_argument("--no-autotune", action="store_true",
+                   help="keep the default smoother schedule and tiles in the runs with the history guess")
     p.add_argument("--history", type=int, default=4,
                    help="stored solutions of the solution-history guess (0: start every solve "
                         "from the previous solution, as the reference)")
@@ -219,6 +221,7 @@ def run_ours(args):
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     T = args.train_steps
     H = args.history
+    TUNE = not args.no_autotune
 
     def barrier():
         if world > 1:
@@ -244,12 +247,14 @@ def run_ours(args):
         tsim.close()
         return net, {"train_samples": n, "last_loss": loss, "train_instance_seed": tcfg.seed}
 
-    def timed_run(mg, host_io=False, net=None, history=0):
+    def timed_run(mg, host_io=False, net=None, history=0, tune=False):
         """W untimed warm-up steps from steady sliding, then K steps each
         bracketed by CUDA events on the solver's stream (L2 flushed before
         each); with `history` >= 2 every stage solve starts from the
         solution-history guess, and with `net` from the network's correction
-        of that guess.  host_io: every step goes through the C ABI with host
+        of that guess; `tune`: qd_autotune on the run's own state after the
+        warm-up steps (outside the timed region).  host_io: every step goes
+        through the C ABI with host
         buffers -- state and u uploaded from pinned memory before, read back
         after (the e2e measurement)."""
         sim = api.Simulation(prob, mg)
@@ -258,6 +263,7 @@ def run_ours(args):
             net.attach(sim.solver, warmstart.MODE_PREDICT)
         sim.start()
         sim.step(args.warmup)
+        tuning = sim.solver.autotune(3) if tune else None
         stream = torch.cuda.ExternalStream(sim.solver.stream_ptr())
         s0 = sim.state(with_u=False)
         ms, step_ms = 0.0, []
@@ -304,7 +310,7 @@ def run_ours(args):
                      "t0": s0["t"], "t_end": s1["t"],
                      "launches": s1["kernel_launches"] - s0["kernel_launches"],
                      "vcycles": s1["vcycles"] - s0["vcycles"], "solves": s1["solves"] - s0["solves"],
-                     "attempts": s1["attempts"] - s0["attempts"]}
+                     "attempts": s1["attempts"] - s0["attempts"], "autotune": tuning}
 
     def job_value(run):
         """whole-job simulated yr/hr: years of all replicas / slowest rank's hours"""
@@ -327,7 +333,7 @@ def run_ours(args):
     peaks = _peaks()
     net, tinfo = train_network(mixed_cfg) if learned else (None, {})
     if args.profile_run:
-        simp, run = timed_run(mixed_cfg, net=net, history=H)
+        simp, run = timed_run(mixed_cfg, net=net, history=H, tune=TUNE)
         simp.close()
         if rank == 0:
             print(json.dumps({"profile_run": "headline solver", "learned": learned, "history": H,
@@ -339,13 +345,13 @@ def run_ours(args):
         return 0
     clocks = Clocks(local)
     clocks.start()
-    sim, head = timed_run(mixed_cfg, net=net, history=H)
+    sim, head = timed_run(mixed_cfg, net=net, history=H, tune=TUNE)
     clk = clocks.stop()
     ms_max = reduce_max(head["ms"])
     value = job_value(head)
     extra = {}
     if learned:
-        simm, mixed = timed_run(mixed_cfg, history=H)
+        simm, mixed = timed_run(mixed_cfg, history=H, tune=TUNE)
         simm.close()
         extra["mixed_no_learned"] = summary(mixed)
         us_f, fl_f = net.time("forward", 10)
@@ -475,7 +481,7 @@ def run_ours(args):
     # end to end through the C ABI with host buffers (pinned), the same steps
     e2e = None
     if not args.no_e2e:
-        sim_e, io = timed_run(mixed_cfg, host_io=True, net=net, history=H)
+        sim_e, io = timed_run(mixed_cfg, host_io=True, net=net, history=H, tune=TUNE)
         sim_e.close()
         e2e = {"value": job_value(io), "unit": "sim_yr/hr",
                "h2d_bytes_per_step": 8 * (4 * prob.nz + prob.ni * prob.nk),
@@ -492,6 +498,10 @@ def run_ours(args):
 
     if rank == 0:
         guess = f"solution-history guess (last {H} solutions)" if H >= 2 else "previous-solution start"
+        tn = head["autotune"]
+        sched = (tn["nu_pre"], tn["nu_post"]) if tn else (cfg.mg.nu_pre, cfg.mg.nu_post)
+        if tn:
+            guess += f", autotuned tiles ({tn['box_down']}/{tn['box_up']}-column boxes)"
         mode = (f"learned warm start on the {guess} + FP32 cycles in FP64 refinement" if learned
                 else f"{guess} + FP32 cycles in FP64 refinement")
         line = {
@@ -501,12 +511,13 @@ def run_ours(args):
             "dtype": "f64+f32+bf16" if learned else "f64+f32", "data": "synthetic",
             "config": {"workload": f"{cfg.name}: {cfg.ni}x{cfg.nk} earthquake cycle, accepted RK43 steps "
                                    f"{args.warmup + 1}..{args.warmup + args.steps} from steady sliding",
-                       "mg": f"{cfg.mg.n_levels} levels V({cfg.mg.nu_pre},{cfg.mg.nu_post}), "
+                       "mg": f"{cfg.mg.n_levels} levels V({sched[0]},{sched[1]}), "
                              f"rel {cfg.mg.tol:g}, {mode}, exact coarsest solve, surface-row prolongation",
                        "parallelism": f"replicas x{world}", "l2": "flushed before every timed step"},
             "sim_years_timed": head["yrs"], "t_start_s": head["t0"], "t_end_s": head["t_end"],
             "vcycles_per_solve": head["vcycles"] / max(1, head["solves"]),
             "attempts_per_step": head["attempts"] / args.steps,
+            "autotune": head["autotune"],
             **extra,
             "plain_fp64": None if plain is None else {
                 "value": plain_value, "ms_per_step": plain["ms"] / args.steps,

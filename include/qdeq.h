@@ -253,6 +253,26 @@ int qd_rk43_set_state(qd_solver *s, const double *Slip, const double *psi,
                       const double *V, const double *dpsi, double t, double dt,
                       double errA0, double errA1, int it);
 
+/* Autotuner.  Times every candidate smoother schedule (nu_pre, nu_post in
+ * {1,1 2,2 3,3 4,4 1,2 2,1 2,3 3,2}) and pair of tile box widths of the
+ * descending and ascending tile kernels ({64, 96, 128} columns each) on
+ * `reps` solves of the solver's current boundary data from a zero interior
+ * to its tolerance, keeps the fastest (options and tiles), and restores u and
+ * the solve counters.  The reference's schedule is fixed (odeSolver.cpp:2-4).
+ * n_levels, precision and the tolerance are not changed.  out may be NULL. */
+typedef struct qd_tuning {
+    int nu_pre, nu_post;       /* the schedule picked                         */
+    int box_up, box_down;      /* the tile box widths picked (columns)        */
+    double us_best;            /* its mean time per solve                     */
+    double us_initial;         /* the same for the settings before tuning     */
+    int cycles_best, cycles_initial;   /* V-cycles of those solves            */
+    int candidates;            /* settings that converged and were timed      */
+} qd_tuning;
+int qd_autotune(qd_solver *s, int reps, qd_tuning *out);
+/* Staged box widths of the tile kernels (multiples of 16 in 32..256; 0: the
+ * default 64).  qd_autotune sets them; this sets them directly. */
+int qd_set_tiles(qd_solver *s, int box_up, int box_down);
+
 /* Initial guess of the RK43 driver's stage solves from the solution history
  * (no counterpart in the reference, which starts every solve from the last
  * solution, odeSolver.cpp:669-677).  With m >= 2 the solver keeps its last m

@@ -56,6 +56,8 @@ EXPORTS = [
     ("qd_rk43_set_state", C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp, C.c_double, C.c_double,
                                     C.c_double, C.c_double, C.c_int]),
     ("qd_set_solution_history", C.c_int, [C.c_void_p, C.c_int]),
+    ("qd_autotune", C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    ("qd_set_tiles", C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     ("qd_solution_history_fit", C.c_int, [C.c_void_p, _dp, _ip]),
     ("qd_load_initial_u", C.c_int, [C.c_char_p, C.c_int, C.c_int, _dp]),
     ("qd_save_initial_u", C.c_int, [C.c_char_p, C.c_int, C.c_int, _dp]),
@@ -94,6 +96,12 @@ class Stats(C.Structure):
     _fields_ = [("solves", C.c_longlong), ("vcycles", C.c_longlong), ("attempts", C.c_longlong),
                 ("steps", C.c_longlong), ("newton_iters", C.c_longlong),
                 ("kernel_launches", C.c_longlong)]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("nu_pre", C.c_int), ("nu_post", C.c_int), ("box_up", C.c_int), ("box_down", C.c_int),
+                ("us_best", C.c_double), ("us_initial", C.c_double), ("cycles_best", C.c_int),
+                ("cycles_initial", C.c_int), ("candidates", C.c_int)]
 
 
 class QdError(RuntimeError):

@@ -17,7 +17,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import MgOptions, Rk43Params, Stats, check
+from ._lib import MgOptions, Rk43Params, Stats, Tuning, check
 from .config import MGConfig
 
 _dp = C.POINTER(C.c_double)
@@ -207,6 +207,17 @@ class Solver:
         last m solutions that best matches the new boundary data (m < 2: off,
         the previous solution as the reference)."""
         check(self.L.qd_set_solution_history(self.h, int(m)))
+
+    def autotune(self, reps=3):
+        """Time the candidate smoother schedules and tile box widths on this
+        solver's problem (solves from a zero interior to its tolerance), keep
+        the fastest, restore u; returns the qd_tuning fields."""
+        t = Tuning()
+        check(self.L.qd_autotune(self.h, int(reps), C.byref(t)))
+        return {f: getattr(t, f) for f, _ in Tuning._fields_}
+
+    def set_tiles(self, box_up=0, box_down=0):
+        check(self.L.qd_set_tiles(self.h, int(box_up), int(box_down)))
 
     def solution_history_fit(self):
         """(coefficients in use, boundary misfit / change) of the last fit."""

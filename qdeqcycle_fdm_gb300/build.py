@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libqdeq_gb300.so")
-SOURCES = ["capi.cu", "mg.cu", "mg_fused.cu", "fault.cu", "medium.cu", "dropin.cpp", "noalloc.cu", "mg_graph.cu", "unet.cu", "io.cu", "history.cu"]
+SOURCES = ["capi.cu", "mg.cu", "mg_fused.cu", "fault.cu", "medium.cu", "dropin.cpp", "noalloc.cu", "mg_graph.cu", "unet.cu", "io.cu", "history.cu", "autotune.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr"]

@@ -413,8 +413,8 @@ struct TileGeom {
     size_t smem;
 };
 
-static constexpr int kBoxW = 64;       // k_up boxes: one pass of 32 lanes per row
-static constexpr int kDownBoxW = 64;   // k_down boxes (80 measured slower at 1025^2: 24.1 vs 22.6 us)
+static constexpr int kBoxW = 64;       // default k_up boxes: one pass of 32 lanes per row
+static constexpr int kDownBoxW = 64;   // default k_down boxes (qd_autotune may pick others)
 static constexpr int kWaveCtas = 150;
 
 static size_t two_cta_smem() { return std::min<size_t>(smem_limit(), 112 * 1024); }
@@ -466,13 +466,13 @@ static size_t up_smem(const TileGeom &t, bool has_f, bool prolong) {
     return b;
 }
 
-// widest TW with W <= kBoxW, then the tallest TH that fits two CTAs per SM
+// widest TW with W <= box, then the tallest TH that fits two CTAs per SM
 // and still gives about a wave of CTAs
 template <typename T>
-static TileGeom pick_up(int N, int K, int H, bool has_f, bool prolong) {
+static TileGeom pick_up(int N, int K, int H, bool has_f, bool prolong, int box) {
     const int A = TileCfg<T>::kAlign;
-    int tw = std::max(A, (kBoxW - 2 * H) / A * A);
-    while (tw > A && up_geom(N, K, 8, tw, H, A).W > kBoxW) tw -= A;
+    int tw = std::max(A, (box - 2 * H) / A * A);
+    while (tw > A && up_geom(N, K, 8, tw, H, A).W > box) tw -= A;
     TileGeom best{};
     bool found = false;
     for (int th = 64; th >= 8; th /= 2) {
@@ -489,10 +489,10 @@ static TileGeom pick_up(int N, int K, int H, bool has_f, bool prolong) {
 }
 
 template <typename T>
-static TileGeom pick_down(int Nc, int Kc, int N, int K, int S, bool has_f) {
+static TileGeom pick_down(int Nc, int Kc, int N, int K, int S, bool has_f, int box) {
     const int A = TileCfg<T>::kAlign;
-    int cw = std::max(2, (kDownBoxW - 2 * S - 3) / 2);
-    while (cw > 2 && down_geom(Nc, Kc, N, K, 8, cw, S, A).W > kDownBoxW) cw--;
+    int cw = std::max(2, (box - 2 * S - 3) / 2);
+    while (cw > 2 && down_geom(Nc, Kc, N, K, 8, cw, S, A).W > box) cw--;
     TileGeom best{};
     for (int ch = 32; ch >= 4; ch /= 2) {
         TileGeom t = down_geom(Nc, Kc, N, K, ch, cw, S, A);
@@ -509,7 +509,7 @@ static int launch_down(qd_solver *s, Level<T> *Ls, int l, int S, int zero_u) {
     const LvArgs<T> g = lv(s, Ls, l), c = lv(s, Ls, l + 1);
     // the residual goes into f, or into the dinv slot on the FP64 level 0
     const bool has_f = g.f != nullptr;
-    const TileGeom t = pick_down<T>(c.N, c.K, g.N, g.K, S, has_f);
+    const TileGeom t = pick_down<T>(c.N, c.K, g.N, g.K, S, has_f, s->box_down ? s->box_down : kDownBoxW);
     const int BH = t.BH, W = t.W, CH = t.TH, CW = t.TW, ntj = t.ntj, ntk = t.ntk;
     const size_t smem = t.smem;
     if (BH > 256 || W > 256 || smem > smem_limit()) {
@@ -531,7 +531,7 @@ static int launch_up(qd_solver *s, Level<T> *Ls, int l, int S, int prolong, int 
     const LvArgs<T> g = lv(s, Ls, l);
     const LvArgs<T> c = (l + 1 < s->nlev) ? lv(s, Ls, l + 1) : g;
     const int R1 = MODE == 1 ? 1 : 0;
-    const TileGeom t = pick_up<T>(g.N, g.K, S + R1, g.f != nullptr, prolong != 0);
+    const TileGeom t = pick_up<T>(g.N, g.K, S + R1, g.f != nullptr, prolong != 0, s->box_up ? s->box_up : kBoxW);
     const int BH = t.BH, W = t.W, TH = t.TH, TW = t.TW, ntj = t.ntj, ntk = t.ntk;
     const size_t smem = t.smem;
     if (BH > 256 || W > 256 || smem > smem_limit()) {
@@ -595,6 +595,21 @@ int encode_tiled_2d(CUtensorMap *map, const void *base, int dtype, int esz, long
         set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
         return QD_ERR_CUDA;
     }
+    return QD_OK;
+}
+
+// staged box widths of the tile kernels (multiples of 16 columns, 32..256;
+// 0 restores the default); the solve graph is rebuilt on the next solve
+int tiles_set(qd_solver *s, int box_up, int box_down) {
+    auto ok = [](int b) { return b == 0 || (b >= 32 && b <= 256 && b % 16 == 0); };
+    if (!ok(box_up) || !ok(box_down)) {
+        set_error("tile box widths must be 0 or multiples of 16 in 32..256");
+        return QD_ERR_ARG;
+    }
+    QD_CUDA(cudaStreamSynchronize(s->stream));
+    s->box_up = box_up;
+    s->box_down = box_down;
+    solve_graph_free(s);
     return QD_OK;
 }
 

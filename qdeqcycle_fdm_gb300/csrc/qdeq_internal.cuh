@@ -154,6 +154,7 @@ struct qd_solver {
     void *history;         // ring of earlier solutions for the initial guess (history.cu), or null
     void *snapshot;        // the snapshot writer in flight (io.cu), or null
     int tail_l0;           // first level of the coarse tail
+    int box_up, box_down;  // staged tile box widths of k_up / k_down (0: the default 64)
     void *solve_graph;     // the instantiated multigrid graph (mg_graph.cu)
     qd::SolveState *d_solve, *h_solve;
     int n_partial;
@@ -186,6 +187,7 @@ int vcycle64_norm(qd_solver *s, int *nblocks);
 int vcycle32_into64(qd_solver *s);
 void tma_cache_free(qd_solver *s);
 int tail_image_build(qd_solver *s);
+int tiles_set(qd_solver *s, int box_up, int box_down);
 int time_kernel(qd_solver *s, int which, int reps, double *us);
 // mg.cu: level-0 norms into d_scal[slot] (to32: FP64 residual -> FP32 rhs)
 int level0_norm(qd_solver *s, int to32, int slot);
@@ -224,6 +226,8 @@ int history_push(qd_solver *s);
 void history_reset(qd_solver *s);
 void history_free(qd_solver *s);
 int history_last_fit(qd_solver *s, double *out, int *nd);
+// autotune.cu
+int autotune(qd_solver *s, int reps, qd_tuning *out);
 // io.cu
 void snapshot_free(qd_solver *s);
 }  // namespace qd
