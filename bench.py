@@ -388,7 +388,8 @@ def run_ours(args):
         cfgs = [config.ensemble_instance(n, i) for i, n in enumerate(sizes)]
         probs = [problem.build_problem(c) for c in cfgs]
         out = {"instances": "12 x 257^2 + 6 x 513^2 + 2 x 1025^2 (config-4 parameter draws)",
-               "steps_timed": ksteps, "warmup": 3, "history": H}
+               "steps_timed": ksteps, "warmup": 3, "history": H,
+               "autotune": "per instance" if TUNE else None}
         for mode in ("batched", "sequential"):
             sims = [api.Simulation(p, c.mg) for p, c in zip(probs, cfgs)]
             for x in sims:
@@ -399,6 +400,9 @@ def run_ours(args):
             else:
                 for x in sims:
                     x.step(3)
+            if TUNE:
+                for x in sims:
+                    x.solver.autotune(2)          # on each instance's own state, untimed
             t0 = [x.solver.rk43_state()["t"] for x in sims]
             torch.cuda.synchronize()
             w0 = time.perf_counter()
