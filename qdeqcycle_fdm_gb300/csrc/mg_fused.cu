@@ -614,7 +614,7 @@ int tiles_set(qd_solver *s, int box_up, int box_down) {
 }
 
 int encode_tiled_3d(CUtensorMap *map, const void *base, int dtype, int esz, long d0, long d1, long d2,
-                    long stride1_bytes, long stride2_bytes, int box0, int box1, int box2) {
+                    long stride1_bytes, long stride2_bytes, int box0, int box1, int box2, int swizzle) {
     static EncodeTiledFn fn = nullptr;
     if (!fn) {
         void *p = nullptr;
@@ -627,9 +627,12 @@ int encode_tiled_3d(CUtensorMap *map, const void *base, int dtype, int esz, long
         }
         fn = (EncodeTiledFn)p;
     }
+    const int sw_bytes = swizzle == CU_TENSOR_MAP_SWIZZLE_128B ? 128
+                         : swizzle == CU_TENSOR_MAP_SWIZZLE_64B ? 64
+                         : swizzle == CU_TENSOR_MAP_SWIZZLE_32B ? 32 : 0;
     if (!base || ((uintptr_t)base & 15) || stride1_bytes % 16 || stride2_bytes % 16 || ((long)box0 * esz) % 16 ||
         box0 < 1 || box0 > 256 || box1 < 1 || box1 > 256 || box2 < 1 || box2 > 256 || d0 < 1 || d1 < 1 ||
-        d2 < 1) {
+        d2 < 1 || (sw_bytes && (long)box0 * esz > sw_bytes)) {
         set_error("tensor map %ldx%ldx%ld box %dx%dx%d violates the TMA rules", d0, d1, d2, box0, box1, box2);
         return QD_ERR_ARG;
     }
@@ -638,7 +641,7 @@ int encode_tiled_3d(CUtensorMap *map, const void *base, int dtype, int esz, long
     const cuuint32_t box[3] = {(cuuint32_t)box0, (cuuint32_t)box1, (cuuint32_t)box2};
     const cuuint32_t es[3] = {1, 1, 1};
     const CUresult r = fn(map, (CUtensorMapDataType)dtype, 3, const_cast<void *>(base), dims, strides, box, es,
-                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, (CUtensorMapSwizzle)swizzle,
                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
         set_error("cuTensorMapEncodeTiled (3-D) failed (%d)", (int)r);

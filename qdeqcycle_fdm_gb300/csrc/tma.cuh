@@ -87,6 +87,6 @@ int encode_tiled_2d(CUtensorMap *map, const void *base, int dtype, int esz, long
                     long pitch_bytes, int box_w, int box_h, int swizzle);
 // unswizzled 3-D map: d0 innermost; strides of dimensions 1 and 2 in bytes
 int encode_tiled_3d(CUtensorMap *map, const void *base, int dtype, int esz, long d0, long d1, long d2,
-                    long stride1_bytes, long stride2_bytes, int box0, int box1, int box2);
+                    long stride1_bytes, long stride2_bytes, int box0, int box1, int box2, int swizzle);
 
 }  // namespace qd

@@ -447,12 +447,12 @@ static int map_act(CUtensorMap *m, const UTensor &t, const UGrid &g) {
                            swz(KB * 2));
 }
 
-// A operand of k_conv_rows: the tensor as (channel, column, row) with
-// unswizzled boxes of 8 channels x 130 columns x (mt + 2) rows, mt the
-// convolution's tile height
+// A operand of k_conv_rows: the tensor as (channel, column, row) with boxes
+// of all C channels x 130 columns x (mt + 2) rows, mt the convolution's tile
+// height, swizzled to the pixel row (32 or 64 bytes)
 static int map_act_rows(CUtensorMap *m, const UTensor &t, const UGrid &g, int mt) {
     return encode_tiled_3d(m, t.p, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, t.C, g.Wp, g.H + 2, (long)t.C * 2,
-                           (long)g.Wp * t.C * 2, 8, ROWS_BOXW, mt + 2);
+                           (long)g.Wp * t.C * 2, t.C, ROWS_BOXW, mt + 2, swz(t.C * 2));
 }
 
 // tile height of k_conv_rows for cin -> cout channels (0: not a row-box case)

@@ -188,15 +188,16 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv_fwd(const __grid_constant
 }
 
 // k_conv_rows: the 3x3 convolution for 16 or 32 input channels, persistent,
-// on 2-D tiles of MT image rows x 128 columns of the padded grid.  A pixel
-// row of the operand is 32 or 64 bytes, too narrow for efficient swizzled
-// boxes; here the activation is staged unswizzled in 16-byte channel chunks:
-// per chunk one 3-D box of 8 channels x 130 columns x (MT + 2) rows (the
-// tile with a one-pixel halo), so that
-//   * the operand of output row mt at tap (dy, dx) is the box's row mt + dy
-//     started dx columns in -- a 16-byte multiple added to the descriptor's
-//     start address (core matrices are 8 columns x 16 bytes, rows 16 bytes
-//     apart; the K-adjacent chunk is the next chunk plane);
+// on 2-D tiles of MT image rows x 128 columns of the padded grid.  The
+// activation is staged as one 3-D TMA box of all CIN channels x 130 columns
+// x (MT + 2) rows (the tile with a one-pixel halo): pixel rows of 32 or 64
+// bytes with the matching 32- or 64-byte swizzle, so that
+//   * the operand of output row mt at tap (dy, dx) is the box's pixel
+//     (mt + dy) * 130 + dx onwards -- a whole number of pixel rows added to
+//     the descriptor's start address (base offset 0): the TMA writes and the
+//     MMA reads apply the swizzle to the absolute shared-memory address, so
+//     a start part-way into the pattern reads the rows as they were written
+//     (the same holds for the 32-byte K offsets within a swizzled row);
 //   * the three tap rows of neighbouring output rows share staged rows, so a
 //     tile stages (MT + 2) / (3 MT) of what one box per tap row would.
 // Each CTA walks the tiles with stride gridDim.x:
@@ -224,19 +225,18 @@ static constexpr int ROWS_EPI_WARPS = 8;
 template <int CIN, int COUT>
 struct RowsCfg {
     static constexpr int MT = conv_rows_mt<CIN, COUT>();
-    static constexpr int NCH = CIN / 8;                                 // 16-byte chunks per pixel
-    static constexpr int BOXB = 16 * ROWS_BOXW * (MT + 2);              // one chunk's box
-    static constexpr int CPL = (BOXB + 127) / 128 * 128;                // chunk plane stride
-    static constexpr int ASLOT = (NCH * CPL + 1023) / 1024 * 1024;      // one tile
+    static constexpr int ROWB = CIN * 2;                                // bytes per staged pixel (= swizzle span)
+    static constexpr int BOXB = ROWB * ROWS_BOXW * (MT + 2);            // the tile's box
+    static constexpr int ASLOT = (BOXB + 1023) / 1024 * 1024;           // one tile
     static constexpr int BT = (COUT * CIN * 2 + 1023) / 1024 * 1024;    // one tap's weights
     static constexpr int NC = MT * COUT;                                // columns per accumulator
     static constexpr uint32_t TCOLS = 2 * NC <= 32 ? 32 : (2 * NC <= 64 ? 64 : (2 * NC <= 128 ? 128 : (2 * NC <= 256 ? 256 : 512)));
-    static constexpr unsigned ATX = NCH * BOXB;
+    static constexpr unsigned ATX = BOXB;
     static constexpr unsigned BTX = 9 * COUT * CIN * 2;
     static constexpr size_t SMEM = 9 * (size_t)BT + ROWS_RING * (size_t)ASLOT + 1024;
     static_assert(CIN == 16 || CIN == 32, "row boxes serve 16 or 32 input channels");
     static_assert(MT % 2 == 0, "two epilogue warps per lane quarter take alternate rows");
-    static_assert(2 * NC <= 512 && CPL < (1 << 18), "layout");
+    static_assert(2 * NC <= 512, "layout");
 };
 
 template <int CIN, int COUT>
@@ -244,7 +244,7 @@ __global__ void __launch_bounds__(ROWS_THREADS) k_conv_rows(const __grid_constan
                                                             const __grid_constant__ CUtensorMap tb,
                                                             ConvArgs a) {
     using R = RowsCfg<CIN, COUT>;
-    constexpr int MT = R::MT, NCH = R::NCH;
+    constexpr int MT = R::MT;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t full[ROWS_RING], empty[ROWS_RING], tfull[2], tempty[2], wfull, done;
     __shared__ uint32_t tmem_base;
@@ -288,8 +288,7 @@ __global__ void __launch_bounds__(ROWS_THREADS) k_conv_rows(const __grid_constan
             }
             unsigned char *sa = ring + slot * R::ASLOT;
             mbar_expect_tx(&full[slot], R::ATX);
-#pragma unroll
-            for (int c = 0; c < NCH; c++) tma_load_3d(sa + c * R::CPL, &ta, 8 * c, c0 - 1, r0 - 1, &full[slot]);
+            tma_load_3d(sa, &ta, 0, c0 - 1, r0 - 1, &full[slot]);
         }
         // the copies of the last ring round have landed before the CTA exits
         for (int q = s - ROWS_RING < 0 ? 0 : s - ROWS_RING; q < s; q++)
@@ -315,8 +314,7 @@ __global__ void __launch_bounds__(ROWS_THREADS) k_conv_rows(const __grid_constan
 #pragma unroll
                         for (int ks = 0; ks < CIN / 16; ks++)
                             mma_bf16(acc + (uint32_t)(mt * COUT),
-                                     smem_desc_noswz(sa + 2 * ks * R::CPL + ((mt + dy) * ROWS_BOXW + dx) * 16,
-                                                     R::CPL, 128),
+                                     smem_desc(sa + ((mt + dy) * ROWS_BOXW + dx) * R::ROWB + 32 * ks, R::ROWB),
                                      smem_desc(sb + (3 * dy + dx) * R::BT + 32 * ks, CIN * 2), idesc,
                                      (dy > 0 || dx > 0 || ks > 0) ? 1u : 0u);
             mma_commit(&empty[slot]);
