@@ -55,7 +55,7 @@ struct ULayer {
     float *w32, *b32, *mw, *vw, *mb, *vb, *gw, *gb;
     __nv_bfloat16 *w, *wt;             // [9][cout][cin], [9][cin][cout]
     CUtensorMap m_in, m_w, m_gout, m_wt;   // A/B operands of forward and data gradient
-    CUtensorMap m_in_rows, m_gout_rows;    // A operands as 8-channel row boxes (16/32 channels)
+    CUtensorMap m_in_rows, m_gout_rows;    // A operands as pixel-row boxes of k_conv_rows
     bool rows_fwd, rows_dgrad;             // which of the two have them
 };
 
@@ -461,6 +461,7 @@ static int rows_mt(int cin, int cout) {
     if (cin == ci && cout == co) return conv_rows_mt<ci, co>();
     QD_MT_CASE(16, 16) QD_MT_CASE(16, 32) QD_MT_CASE(16, 64)
     QD_MT_CASE(32, 16) QD_MT_CASE(32, 32) QD_MT_CASE(32, 64)
+    QD_MT_CASE(64, 32) QD_MT_CASE(64, 64)
 #undef QD_MT_CASE
     return 0;
 }
@@ -540,7 +541,7 @@ static int conv_rows_launch(qd_unet *u, const CUtensorMap &ta, const CUtensorMap
     return QD_OK;
 }
 
-// ta_rows: the row-box map of the A operand (16 or 32 channels), or null
+// ta_rows: the row-box map of the A operand (16, 32 or 64 channels), or null
 static int conv_dispatch(qd_unet *u, const CUtensorMap &ta, const CUtensorMap *ta_rows, const CUtensorMap &tb,
                          const ConvArgs &a) {
     if (ta_rows) {
@@ -548,6 +549,7 @@ static int conv_dispatch(qd_unet *u, const CUtensorMap &ta, const CUtensorMap *t
     if (a.Cin == ci && a.Cout == co) return conv_rows_launch<ci, co>(u, *ta_rows, tb, a);
         QD_ROWS_CASE(16, 16) QD_ROWS_CASE(16, 32) QD_ROWS_CASE(16, 64)
         QD_ROWS_CASE(32, 16) QD_ROWS_CASE(32, 32) QD_ROWS_CASE(32, 64)
+        QD_ROWS_CASE(64, 32) QD_ROWS_CASE(64, 64)
 #undef QD_ROWS_CASE
     }
     const int KB = a.Cin < 64 ? a.Cin : 64;

@@ -187,11 +187,11 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv_fwd(const __grid_constant
     if (warp == 2) tmem_free(tmem, TCOLS);
 }
 
-// k_conv_rows: the 3x3 convolution for 16 or 32 input channels, persistent,
+// k_conv_rows: the 3x3 convolution for 16, 32 or 64 input channels, persistent,
 // on 2-D tiles of MT image rows x 128 columns of the padded grid.  The
 // activation is staged as one 3-D TMA box of all CIN channels x 130 columns
-// x (MT + 2) rows (the tile with a one-pixel halo): pixel rows of 32 or 64
-// bytes with the matching 32- or 64-byte swizzle, so that
+// x (MT + 2) rows (the tile with a one-pixel halo): pixel rows of 32, 64 or
+// 128 bytes with the matching swizzle, so that
 //   * the operand of output row mt at tap (dy, dx) is the box's pixel
 //     (mt + dy) * 130 + dx onwards -- a whole number of pixel rows added to
 //     the descriptor's start address (base offset 0): the TMA writes and the
@@ -215,7 +215,7 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv_fwd(const __grid_constant
 // memory is freed.
 template <int CIN, int COUT>
 __host__ __device__ constexpr int conv_rows_mt() {
-    return CIN == 16 ? (COUT <= 32 ? 8 : 4) : (COUT <= 32 ? 4 : 4);
+    return CIN == 16 ? (COUT <= 32 ? 8 : 4) : (CIN == 32 ? 4 : 2);
 }
 static constexpr int ROWS_BOXW = 130;      // staged columns: 128 outputs and a halo column each side
 static constexpr int ROWS_RING = 2;        // tile stages in flight
@@ -234,7 +234,7 @@ struct RowsCfg {
     static constexpr unsigned ATX = BOXB;
     static constexpr unsigned BTX = 9 * COUT * CIN * 2;
     static constexpr size_t SMEM = 9 * (size_t)BT + ROWS_RING * (size_t)ASLOT + 1024;
-    static_assert(CIN == 16 || CIN == 32, "row boxes serve 16 or 32 input channels");
+    static_assert(CIN == 16 || CIN == 32 || CIN == 64, "pixel rows of 32, 64 or 128 bytes");
     static_assert(MT % 2 == 0, "two epilogue warps per lane quarter take alternate rows");
     static_assert(2 * NC <= 512, "layout");
 };
