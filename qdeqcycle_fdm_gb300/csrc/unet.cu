@@ -27,6 +27,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <utility>
 #include <vector>
 
 #include "qdeq_internal.cuh"
@@ -38,6 +39,24 @@ namespace qd {
 static constexpr int UNET_NIN = 5;   // input channels in use (of the 16 staged)
 
 __host__ __device__ static inline int cdv(long a, long b) { return (int)((a + b - 1) / b); }
+
+// kernel launch, with programmatic stream serialization when pdl is set (the
+// kernel then waits for its predecessor itself, with pdl_wait)
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_k(bool pdl, void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                            cudaStream_t st, Args &&...args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
 
 struct UGrid {
     int H, W, Wp, P;
@@ -92,6 +111,7 @@ struct qd_unet {
     double last_loss;
     float lr;
     int mode;                      // 0 off, 1 train, 2 predict
+    bool pdl;                      // launch with programmatic stream serialization (inside forward())
 };
 
 namespace qd {
@@ -137,6 +157,8 @@ __device__ __forceinline__ void axpy8(F8 &y, float a, const F8 &x) {
 
 // 2x2 mean pool, fine level f -> coarse level c
 __global__ void k_pool(const __nv_bfloat16 *in, __nv_bfloat16 *out, UGrid f, UGrid c, int C) {
+    pdl_trigger();
+    pdl_wait();
     const int C8 = C >> 3, idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= c.P * C8) return;
     const int p = idx / C8, ch = (idx - p * C8) * 8;
@@ -173,6 +195,8 @@ __global__ void k_pool_bwd(const __nv_bfloat16 *gout, __nv_bfloat16 *gin, UGrid 
 
 // bilinear up-sampling, coarse c -> fine f
 __global__ void k_up(const __nv_bfloat16 *in, __nv_bfloat16 *out, UGrid c, UGrid f, int C) {
+    pdl_trigger();
+    pdl_wait();
     const int C8 = C >> 3, idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= f.P * C8) return;
     const int p = idx / C8, ch = (idx - p * C8) * 8;
@@ -225,6 +249,8 @@ __global__ void k_up_bwd(const __nv_bfloat16 *gout, __nv_bfloat16 *gin, UGrid c,
 
 // the element kernels below take n = pixels * channels (a multiple of 8)
 __global__ void k_add(const __nv_bfloat16 *a, const __nv_bfloat16 *b, __nv_bfloat16 *out, long n) {
+    pdl_trigger();
+    pdl_wait();
     const long i = 8L * (blockIdx.x * (long)blockDim.x + threadIdx.x);
     if (i >= n) return;
     F8 x = ld8(a + i);
@@ -484,7 +510,8 @@ static int conv_launch(qd_unet *u, const CUtensorMap &ta, const CUtensorMap &tb,
                                      (int)smem));
         raised = true;
     }
-    k_conv_fwd<KB, COUT><<<cdv(a.P, 128 * MT), CONV_THREADS, smem, u->stream>>>(ta, tb, a);
+    QD_CUDA(launch_k(u->pdl, k_conv_fwd<KB, COUT>, dim3(cdv(a.P, 128 * MT)), dim3(CONV_THREADS), smem, u->stream,
+                     ta, tb, a));
     QD_CUDA(cudaPeekAtLastError());
     return QD_OK;
 }
@@ -536,7 +563,7 @@ static int conv_rows_launch(qd_unet *u, const CUtensorMap &ta, const CUtensorMap
     }
     const int tiles = cdv(a.H + 2, R::MT) * cdv(a.Wp, 128);
     const int grid = std::min(tiles, per_sm * sm_count());
-    k_conv_rows<CIN, COUT><<<grid, ROWS_THREADS, R::SMEM, u->stream>>>(ta, tb, a);
+    QD_CUDA(launch_k(u->pdl, k_conv_rows<CIN, COUT>, dim3(grid), dim3(ROWS_THREADS), R::SMEM, u->stream, ta, tb, a));
     QD_CUDA(cudaPeekAtLastError());
     return QD_OK;
 }
@@ -590,8 +617,21 @@ static ConvArgs conv_args(const qd_unet *u, const UGrid &g, int cin, int cout) {
 #define EW_GRID(n) cdv((long)(n), 256), 256, 0, u->stream
 #define EW8_GRID(n) cdv((long)(n) / 8, 256), 256, 0, u->stream   // eight channels per thread
 
-// forward through every layer; the head writes out32
+// forward through every layer; the head writes out32.  Its kernels are
+// launched with programmatic stream serialization: each one's set-up
+// overlaps the previous one's tail, and it waits for the previous one's
+// results (pdl_wait) before it touches them.  The first waits on whatever
+// preceded the forward pass; the next kernel after it, launched normally,
+// waits for its completion.
+static int forward_ops(qd_unet *u);
 static int forward(qd_unet *u) {
+    u->pdl = true;
+    const int rc = forward_ops(u);
+    u->pdl = false;
+    return rc;
+}
+
+static int forward_ops(qd_unet *u) {
     for (const UOp &op : u->ops) {
         if (op.k == OP_CONV) {
             ULayer &Ly = u->L[op.layer];
@@ -603,13 +643,16 @@ static int forward(qd_unet *u) {
             QD_TRY(conv_dispatch(u, Ly.m_in, Ly.rows_fwd ? &Ly.m_in_rows : nullptr, Ly.m_w, a));
         } else if (op.k == OP_POOL) {
             const long n = (long)u->g[op.out->lvl].P * op.out->C;
-            k_pool<<<EW8_GRID(n)>>>(op.a->p, op.out->p, u->g[op.a->lvl], u->g[op.out->lvl], op.a->C);
+            QD_CUDA(launch_k(true, k_pool, dim3(cdv(n / 8, 256)), dim3(256), 0, u->stream, op.a->p, op.out->p,
+                             u->g[op.a->lvl], u->g[op.out->lvl], op.a->C));
         } else if (op.k == OP_UP) {
             const long n = (long)u->g[op.out->lvl].P * op.out->C;
-            k_up<<<EW8_GRID(n)>>>(op.a->p, op.out->p, u->g[op.a->lvl], u->g[op.out->lvl], op.a->C);
+            QD_CUDA(launch_k(true, k_up, dim3(cdv(n / 8, 256)), dim3(256), 0, u->stream, op.a->p, op.out->p,
+                             u->g[op.a->lvl], u->g[op.out->lvl], op.a->C));
         } else {
             const long n = (long)u->g[op.out->lvl].P * op.out->C;
-            k_add<<<EW8_GRID(n)>>>(op.a->p, op.b->p, op.out->p, n);
+            QD_CUDA(launch_k(true, k_add, dim3(cdv(n / 8, 256)), dim3(256), 0, u->stream,
+                             (const __nv_bfloat16 *)op.a->p, (const __nv_bfloat16 *)op.b->p, op.out->p, n));
         }
         QD_CUDA(cudaPeekAtLastError());
     }

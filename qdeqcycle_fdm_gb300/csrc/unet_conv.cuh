@@ -101,6 +101,8 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv_fwd(const __grid_constant
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = tmem_base;
+    pdl_trigger();
+    pdl_wait();          // the set-up above overlapped the previous kernel's tail
 
     if (warp == 0 && lane == 0) {
         // producer: MT activation tiles and one weight tile per K step
@@ -273,6 +275,8 @@ __global__ void __launch_bounds__(ROWS_THREADS) k_conv_rows(const __grid_constan
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = tmem_base;
+    pdl_trigger();
+    pdl_wait();          // the set-up above overlapped the previous kernel's tail
 
     if (warp == 0 && lane == 0) {
         mbar_expect_tx(&wfull, R::BTX);
