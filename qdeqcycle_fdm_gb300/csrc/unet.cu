@@ -193,35 +193,50 @@ __global__ void k_pool_bwd(const __nv_bfloat16 *gout, __nv_bfloat16 *gin, UGrid 
     st8(gin + (long)p * C + ch, g);
 }
 
-// bilinear up-sampling, coarse c -> fine f
+// bilinear up-sampling, coarse c -> fine f: one thread per coarse node and
+// eight channels writes the 2 x 2 fine block the node starts (the block is
+// clipped at the last fine row and column).  The fine border pixels are not
+// written: the tensor is zeroed at allocation and only this kernel writes it.
 __global__ void k_up(const __nv_bfloat16 *in, __nv_bfloat16 *out, UGrid c, UGrid f, int C) {
     pdl_trigger();
     pdl_wait();
-    const int C8 = C >> 3, idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= f.P * C8) return;
-    const int p = idx / C8, ch = (idx - p * C8) * 8;
-    const int r = p / f.Wp, q = p - r * f.Wp;
-    F8 v = {};
-    if (uin(r, q, f)) {
-        const int y = r - 1, x = q - 1, yc = y >> 1, xc = x >> 1, fy = y & 1, fx = x & 1;
-        const __nv_bfloat16 *b = in + ((long)(yc + 1) * c.Wp + (xc + 1)) * C + ch;
-        const long dn = (long)c.Wp * C;
-        if (!fy && !fx) {
-            v = ld8(b);
-        } else if (fy && !fx) {
-            axpy8(v, 0.5f, ld8(b));
-            axpy8(v, 0.5f, ld8(b + dn));
-        } else if (!fy && fx) {
-            axpy8(v, 0.5f, ld8(b));
-            axpy8(v, 0.5f, ld8(b + C));
-        } else {
-            axpy8(v, 0.25f, ld8(b));
-            axpy8(v, 0.25f, ld8(b + dn));
-            axpy8(v, 0.25f, ld8(b + C));
-            axpy8(v, 0.25f, ld8(b + dn + C));
+    const int C8 = C >> 3;
+    const long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (idx >= (long)c.H * c.W * C8) return;
+    const long cell = idx / C8;
+    const int ch = (int)(idx - cell * C8) * 8;
+    const int yc = (int)(cell / c.W), xc = (int)(cell - (long)yc * c.W);
+    const bool hy = 2 * yc + 1 < f.H, hx = 2 * xc + 1 < f.W;
+    const __nv_bfloat16 *b = in + ((long)(yc + 1) * c.Wp + (xc + 1)) * C + ch;
+    const long dn = (long)c.Wp * C, fdn = (long)f.Wp * C;
+    const F8 a = ld8(b);
+    const F8 bx = hx ? ld8(b + C) : a, by = hy ? ld8(b + dn) : a;
+    __nv_bfloat16 *o = out + ((long)(2 * yc + 1) * f.Wp + (2 * xc + 1)) * C + ch;
+    st8(o, a);
+    F8 v;
+    if (hx) {
+#pragma unroll
+        for (int i = 0; i < 8; i++) v.v[i] = 0.5f * a.v[i] + 0.5f * bx.v[i];
+        st8(o + C, v);
+    }
+    if (hy) {
+#pragma unroll
+        for (int i = 0; i < 8; i++) v.v[i] = 0.5f * a.v[i] + 0.5f * by.v[i];
+        st8(o + fdn, v);
+        if (hx) {
+            const F8 bxy = ld8(b + dn + C);
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                float t = 0.f;
+                t += 0.25f * a.v[i];
+                t += 0.25f * by.v[i];
+                t += 0.25f * bx.v[i];
+                t += 0.25f * bxy.v[i];
+                v.v[i] = t;
+            }
+            st8(o + fdn + C, v);
         }
     }
-    st8(out + (long)p * C + ch, v);
 }
 
 // gradient of k_up (its transpose), written into gin (coarse)
@@ -646,9 +661,10 @@ static int forward_ops(qd_unet *u) {
             QD_CUDA(launch_k(true, k_pool, dim3(cdv(n / 8, 256)), dim3(256), 0, u->stream, op.a->p, op.out->p,
                              u->g[op.a->lvl], u->g[op.out->lvl], op.a->C));
         } else if (op.k == OP_UP) {
-            const long n = (long)u->g[op.out->lvl].P * op.out->C;
-            QD_CUDA(launch_k(true, k_up, dim3(cdv(n / 8, 256)), dim3(256), 0, u->stream, op.a->p, op.out->p,
-                             u->g[op.a->lvl], u->g[op.out->lvl], op.a->C));
+            const UGrid &gc = u->g[op.a->lvl];
+            const long n = (long)gc.H * gc.W * (op.a->C / 8);
+            QD_CUDA(launch_k(true, k_up, dim3(cdv(n, 256)), dim3(256), 0, u->stream, op.a->p, op.out->p, gc,
+                             u->g[op.out->lvl], op.a->C));
         } else {
             const long n = (long)u->g[op.out->lvl].P * op.out->C;
             QD_CUDA(launch_k(true, k_add, dim3(cdv(n / 8, 256)), dim3(256), 0, u->stream,
