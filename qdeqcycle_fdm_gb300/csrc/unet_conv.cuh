@@ -251,8 +251,14 @@ __global__ void __launch_bounds__(ROWS_THREADS) k_conv_rows(const __grid_constan
     __shared__ __align__(8) uint64_t full[ROWS_RING], empty[ROWS_RING], tfull[2], tempty[2], wfull, done;
     __shared__ uint32_t tmem_base;
     __shared__ volatile int abort_;
+    __shared__ float sbias[COUT];
+    constexpr int RB = COUT <= 16 ? 2 : 1;   // output rows per tensor-memory wait in the epilogue
+    static_assert((MT / 2) % RB == 0, "each epilogue warp's rows come in whole batches");
     unsigned char *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
     unsigned char *sw = smem, *ring = smem + 9 * R::BT;
+    // the bias is a parameter of the layer: no kernel the forward pass
+    // overlaps with writes it
+    for (int i = threadIdx.x; i < COUT; i += blockDim.x) sbias[i] = a.bias ? a.bias[i] : 0.f;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int HP = a.H + 2;                               // padded rows
     const int ncb = cdiv_dev(a.Wp, 128), ntiles = cdiv_dev(HP, MT) * ncb;
@@ -347,44 +353,52 @@ __global__ void __launch_bounds__(ROWS_THREADS) k_conv_rows(const __grid_constan
             }
             tc_fence_after();
             const int r0 = (tile / ncb) * MT, col = (tile % ncb) * 128 + 32 * q + lane;
+            // RB of this warp's output rows (half, half + 2, ...) per tensor-memory wait
 #pragma unroll 1
-            for (int mt = half; mt < MT; mt += 2) {
-                const int row = r0 + mt;
-                const bool valid = row < HP && col < a.Wp;
-                const bool in = row >= 1 && row <= a.H && col >= 1 && col <= a.W;
-                const size_t p = (size_t)row * a.Wp + col;
-                uint32_t r[COUT];
+            for (int m0 = half; m0 < MT; m0 += 2 * RB) {
+                uint32_t r[RB][COUT];
 #pragma unroll
-                for (int n0 = 0; n0 < COUT; n0 += 8)
-                    tmem_ld8_issue(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(buf * R::NC + mt * COUT + n0),
-                                   r + n0);
+                for (int j = 0; j < RB; j++)
 #pragma unroll
-                for (int n0 = 0; n0 < COUT; n0 += 8) tmem_ld_wait(r + n0);
-                if (!valid) continue;
+                    for (int n0 = 0; n0 < COUT; n0 += 8)
+                        tmem_ld8_issue(tmem + ((uint32_t)(32 * q) << 16) +
+                                           (uint32_t)(buf * R::NC + (m0 + 2 * j) * COUT + n0),
+                                       r[j] + n0);
 #pragma unroll
-                for (int n0 = 0; n0 < COUT; n0 += 8) {
-                    float v[8];
+                for (int j = 0; j < RB; j++)
 #pragma unroll
-                    for (int i = 0; i < 8; i++) {
-                        float x = __uint_as_float(r[n0 + i]) + (a.bias ? a.bias[n0 + i] : 0.f);
-                        if (a.relu) x = fmaxf(x, 0.f);
-                        v[i] = (in ? x : 0.f);
-                    }
-                    if (a.mask && in) {
-                        const uint4 mk = *reinterpret_cast<const uint4 *>(a.mask + p * COUT + n0);
-                        const __nv_bfloat16 *mv = reinterpret_cast<const __nv_bfloat16 *>(&mk);
+                    for (int n0 = 0; n0 < COUT; n0 += 8) tmem_ld_wait(r[j] + n0);
 #pragma unroll
-                        for (int i = 0; i < 8; i++)
-                            if (!(__bfloat162float(mv[i]) > 0.f)) v[i] = 0.f;
-                    }
-                    if (a.out_f32) {
-                        if (n0 == 0) a.out_f32[p] = v[0];
-                    } else {
-                        uint4 o;
-                        __nv_bfloat162 *ov = reinterpret_cast<__nv_bfloat162 *>(&o);
+                for (int j = 0; j < RB; j++) {
+                    const int row = r0 + m0 + 2 * j;
+                    if (!(row < HP && col < a.Wp)) continue;
+                    const bool in = row >= 1 && row <= a.H && col >= 1 && col <= a.W;
+                    const size_t p = (size_t)row * a.Wp + col;
 #pragma unroll
-                        for (int i = 0; i < 4; i++) ov[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
-                        *reinterpret_cast<uint4 *>(a.out + p * COUT + n0) = o;
+                    for (int n0 = 0; n0 < COUT; n0 += 8) {
+                        float v[8];
+#pragma unroll
+                        for (int i = 0; i < 8; i++) {
+                            float x = __uint_as_float(r[j][n0 + i]) + sbias[n0 + i];
+                            if (a.relu) x = fmaxf(x, 0.f);
+                            v[i] = (in ? x : 0.f);
+                        }
+                        if (a.mask && in) {
+                            const uint4 mk = *reinterpret_cast<const uint4 *>(a.mask + p * COUT + n0);
+                            const __nv_bfloat16 *mv = reinterpret_cast<const __nv_bfloat16 *>(&mk);
+#pragma unroll
+                            for (int i = 0; i < 8; i++)
+                                if (!(__bfloat162float(mv[i]) > 0.f)) v[i] = 0.f;
+                        }
+                        if (a.out_f32) {
+                            if (n0 == 0) a.out_f32[p] = v[0];
+                        } else {
+                            uint4 o;
+                            __nv_bfloat162 *ov = reinterpret_cast<__nv_bfloat162 *>(&o);
+#pragma unroll
+                            for (int i = 0; i < 4; i++) ov[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+                            *reinterpret_cast<uint4 *>(a.out + p * COUT + n0) = o;
+                        }
                     }
                 }
             }
