@@ -84,9 +84,13 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv_fwd(const __grid_constant
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t full[CONV_STAGES], empty[CONV_STAGES], done;
     __shared__ uint32_t tmem_base;
+    __shared__ float sbias[COUT];
     unsigned char *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int m0 = blockIdx.x * 128 * MT;
+    // the bias is a parameter of the layer: no kernel the forward pass
+    // overlaps with writes it
+    for (int i = threadIdx.x; i < COUT; i += blockDim.x) sbias[i] = a.bias ? a.bias[i] : 0.f;
     const int nkb = a.Cin / KB, nsteps = 9 * nkb;
 
     if (threadIdx.x == 0) {
@@ -158,7 +162,7 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv_fwd(const __grid_constant
             if (p >= a.P || !ok) continue;
 #pragma unroll
             for (int i = 0; i < 8; i++) {
-                float x = v[i] + (a.bias ? a.bias[n0 + i] : 0.f);
+                float x = v[i] + sbias[n0 + i];
                 if (a.relu) x = fmaxf(x, 0.f);
                 v[i] = x;
             }
