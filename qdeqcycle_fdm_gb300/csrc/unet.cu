@@ -173,8 +173,9 @@ __global__ void k_pool(const __nv_bfloat16 *in, __nv_bfloat16 *out, UGrid f, UGr
                     axpy8(v, 1.f, ld8(in + ((long)(y0 + a + 1) * f.Wp + (x0 + b + 1)) * C + ch));
                     n++;
                 }
+        const float w = n == 4 ? 0.25f : (n == 2 ? 0.5f : 1.f);   // exact: the mean of 1, 2 or 4 nodes
 #pragma unroll
-        for (int i = 0; i < 8; i++) v.v[i] /= (float)n;
+        for (int i = 0; i < 8; i++) v.v[i] *= w;
     }
     st8(out + (long)p * C + ch, v);
 }
