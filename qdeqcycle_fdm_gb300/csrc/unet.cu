@@ -515,23 +515,6 @@ static int map_w(CUtensorMap *m, const __nv_bfloat16 *w, int rows, int K) {
                            swz(KB * 2));
 }
 
-template <int KB, int COUT>
-static int conv_launch(qd_unet *u, const CUtensorMap &ta, const CUtensorMap &tb, const ConvArgs &a) {
-    constexpr int MT = conv_mt<KB, COUT>();
-    constexpr int STAGE = ((MT * 128 * KB * 2 + COUT * KB * 2) + 1023) / 1024 * 1024;
-    const size_t smem = (size_t)CONV_STAGES * STAGE + 1024;
-    static bool raised = false;
-    if (!raised) {
-        QD_CUDA(cudaFuncSetAttribute(k_conv_fwd<KB, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem));
-        raised = true;
-    }
-    QD_CUDA(launch_k(u->pdl, k_conv_fwd<KB, COUT>, dim3(cdv(a.P, 128 * MT)), dim3(CONV_THREADS), smem, u->stream,
-                     ta, tb, a));
-    QD_CUDA(cudaPeekAtLastError());
-    return QD_OK;
-}
-
 static int sm_count() {
     static int n = 0;
     if (!n) {
@@ -542,6 +525,32 @@ static int sm_count() {
     }
     return n;
 }
+
+template <int KB, int COUT, int MT_>
+static int conv_launch_mt(qd_unet *u, const CUtensorMap &ta, const CUtensorMap &tb, const ConvArgs &a) {
+    constexpr int MT = MT_ ? MT_ : conv_mt<KB, COUT>();
+    constexpr int STAGE = ((MT * 128 * KB * 2 + COUT * KB * 2) + 1023) / 1024 * 1024;
+    const size_t smem = (size_t)CONV_STAGES * STAGE + 1024;
+    static bool raised = false;
+    if (!raised) {
+        QD_CUDA(cudaFuncSetAttribute(k_conv_fwd<KB, COUT, MT_>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+        raised = true;
+    }
+    QD_CUDA(launch_k(u->pdl, k_conv_fwd<KB, COUT, MT_>, dim3(cdv(a.P, 128 * MT)), dim3(CONV_THREADS), smem,
+                     u->stream, ta, tb, a));
+    QD_CUDA(cudaPeekAtLastError());
+    return QD_OK;
+}
+
+// one sub-tile per CTA where MT-tile CTAs would leave SMs idle
+template <int KB, int COUT>
+static int conv_launch(qd_unet *u, const CUtensorMap &ta, const CUtensorMap &tb, const ConvArgs &a) {
+    constexpr int MT = conv_mt<KB, COUT>();
+    if (MT > 1 && cdv(a.P, 128 * MT) < sm_count()) return conv_launch_mt<KB, COUT, 1>(u, ta, tb, a);
+    return conv_launch_mt<KB, COUT, 0>(u, ta, tb, a);
+}
+
 
 // CTAs of a kernel that fit on one SM at once, from its attributes: shared
 // memory (static + dynamic + the 1 KB the driver reserves per CTA),

@@ -71,11 +71,13 @@ __host__ __device__ constexpr int conv_mt() {
     return (128 / KB) < (256 / COUT) ? (128 / KB) : (256 / COUT);
 }
 
-template <int KB, int COUT>
+// MT_: sub-tiles per CTA (0: conv_mt's choice; 1 for grids too small to
+// fill the GPU with MT-tile CTAs)
+template <int KB, int COUT, int MT_ = 0>
 __global__ void __launch_bounds__(CONV_THREADS) k_conv_fwd(const __grid_constant__ CUtensorMap ta,
                                                            const __grid_constant__ CUtensorMap tb,
                                                            ConvArgs a) {
-    constexpr int MT = conv_mt<KB, COUT>();
+    constexpr int MT = MT_ ? MT_ : conv_mt<KB, COUT>();
     constexpr int ROWB = KB * 2;                        // bytes per operand row
     constexpr int ATILE = 128 * ROWB, ABYTES = MT * ATILE, BBYTES = COUT * ROWB;
     constexpr int STAGE = ((ABYTES + BBYTES) + 1023) / 1024 * 1024;
