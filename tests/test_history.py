@@ -60,9 +60,10 @@ def test_history_guess_keeps_oracle_parity():
     assert np.max(np.abs(g["V"][k] - c["V"][k]) / c["V"][k]) < 1e-10
     assert rel(g["Ts"][k] + prob.tau0[k], c["Ts"][k] + prob.tau0[k]) < 1e-10
     assert rel(g["U"], c["U"]) < 1e-10
-    # the last solve is the step's refresh solve, whose boundary data equal
-    # the last stage's (a_6j = b_j): nothing is left to fit there, and a fit
-    # is only ever kept when it does not increase the misfit
+    # the last solve is the step's refresh solve: its new slip carries the
+    # last stage's slip rate (weight b_6 = 1/4), a direction no stored
+    # solution's boundary contains, so its fit removes little; a fit is only
+    # ever kept when it does not increase the misfit
     coef, misfit = gpu.solver.solution_history_fit()
     assert len(coef) == 5 and 0.0 <= misfit <= 1.0
     gpu.close()
