@@ -223,10 +223,10 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv_fwd(const __grid_constant
 // memory is freed.
 template <int CIN, int COUT>
 __host__ __device__ constexpr int conv_rows_mt() {
-    return CIN == 16 ? (COUT <= 32 ? 8 : 4) : (CIN == 32 ? 4 : 2);
+    return CIN == 16 ? 4 : (CIN == 32 ? 4 : 2);
 }
 static constexpr int ROWS_BOXW = 130;      // staged columns: 128 outputs and a halo column each side
-static constexpr int ROWS_RING = 2;        // tile stages in flight
+static constexpr int ROWS_RING = 2;        // tile stages in flight (default)
 static constexpr int ROWS_THREADS = 320;   // producer, MMA, eight epilogue warps
 static constexpr int ROWS_EPI_WARPS = 8;
 
@@ -237,11 +237,12 @@ struct RowsCfg {
     static constexpr int BOXB = ROWB * ROWS_BOXW * (MT + 2);            // the tile's box
     static constexpr int ASLOT = (BOXB + 1023) / 1024 * 1024;           // one tile
     static constexpr int BT = (COUT * CIN * 2 + 1023) / 1024 * 1024;    // one tap's weights
+    static constexpr int RING = CIN == 16 ? 4 : ROWS_RING;              // tile stages in flight (measured)
     static constexpr int NC = MT * COUT;                                // columns per accumulator
     static constexpr uint32_t TCOLS = 2 * NC <= 32 ? 32 : (2 * NC <= 64 ? 64 : (2 * NC <= 128 ? 128 : (2 * NC <= 256 ? 256 : 512)));
     static constexpr unsigned ATX = BOXB;
     static constexpr unsigned BTX = 9 * COUT * CIN * 2;
-    static constexpr size_t SMEM = 9 * (size_t)BT + ROWS_RING * (size_t)ASLOT + 1024;
+    static constexpr size_t SMEM = 9 * (size_t)BT + RING * (size_t)ASLOT + 1024;
     static_assert(CIN == 16 || CIN == 32 || CIN == 64, "pixel rows of 32, 64 or 128 bytes");
     static_assert(MT % 2 == 0, "two epilogue warps per lane quarter take alternate rows");
     static_assert(2 * NC <= 512, "layout");
@@ -254,7 +255,7 @@ __global__ void __launch_bounds__(ROWS_THREADS) k_conv_rows(const __grid_constan
     using R = RowsCfg<CIN, COUT>;
     constexpr int MT = R::MT;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    __shared__ __align__(8) uint64_t full[ROWS_RING], empty[ROWS_RING], tfull[2], tempty[2], wfull, done;
+    __shared__ __align__(8) uint64_t full[R::RING], empty[R::RING], tfull[2], tempty[2], wfull, done;
     __shared__ uint32_t tmem_base;
     __shared__ volatile int abort_;
     __shared__ float sbias[COUT];
@@ -270,7 +271,7 @@ __global__ void __launch_bounds__(ROWS_THREADS) k_conv_rows(const __grid_constan
     const int ncb = cdiv_dev(a.Wp, 128), ntiles = cdiv_dev(HP, MT) * ncb;
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < ROWS_RING; s++) {
+        for (int s = 0; s < R::RING; s++) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
@@ -296,8 +297,8 @@ __global__ void __launch_bounds__(ROWS_THREADS) k_conv_rows(const __grid_constan
         int s = 0;
         for (int tile = blockIdx.x; tile < ntiles && !abort_; tile += gridDim.x, s++) {
             const int r0 = (tile / ncb) * MT, c0 = (tile % ncb) * 128;
-            const int slot = s % ROWS_RING;
-            if (s >= ROWS_RING && !mbar_wait(&empty[slot], ((s / ROWS_RING) - 1) & 1)) {
+            const int slot = s % R::RING;
+            if (s >= R::RING && !mbar_wait(&empty[slot], ((s / R::RING) - 1) & 1)) {
                 atomicOr(a.status, ST_UNET_TIMEOUT);
                 abort_ = 1;
                 break;
@@ -307,8 +308,8 @@ __global__ void __launch_bounds__(ROWS_THREADS) k_conv_rows(const __grid_constan
             tma_load_3d(sa, &ta, 0, c0 - 1, r0 - 1, &full[slot]);
         }
         // the copies of the last ring round have landed before the CTA exits
-        for (int q = s - ROWS_RING < 0 ? 0 : s - ROWS_RING; q < s; q++)
-            if (!mbar_wait(&full[q % ROWS_RING], (q / ROWS_RING) & 1)) atomicOr(a.status, ST_UNET_TIMEOUT);
+        for (int q = s - R::RING < 0 ? 0 : s - R::RING; q < s; q++)
+            if (!mbar_wait(&full[q % R::RING], (q / R::RING) & 1)) atomicOr(a.status, ST_UNET_TIMEOUT);
         if (!mbar_wait(&wfull, 0)) atomicOr(a.status, ST_UNET_TIMEOUT);
     } else if (warp == 1 && lane == 0) {
         constexpr uint32_t idesc = idesc_bf16_f32(COUT);
@@ -316,9 +317,9 @@ __global__ void __launch_bounds__(ROWS_THREADS) k_conv_rows(const __grid_constan
         bool ok = mbar_wait(&wfull, 0);
         int li = 0;
         for (int tile = blockIdx.x; ok && tile < ntiles && !abort_; tile += gridDim.x, li++) {
-            const int buf = li & 1, slot = li % ROWS_RING;
+            const int buf = li & 1, slot = li % R::RING;
             if (li >= 2 && !mbar_wait(&tempty[buf], ((li >> 1) - 1) & 1)) { ok = false; break; }
-            if (!mbar_wait(&full[slot], (li / ROWS_RING) & 1)) { ok = false; break; }
+            if (!mbar_wait(&full[slot], (li / R::RING) & 1)) { ok = false; break; }
             tc_fence_after();
             const uint32_t acc = tmem + (uint32_t)(buf * R::NC), sa = sring + slot * R::ASLOT;
 #pragma unroll
