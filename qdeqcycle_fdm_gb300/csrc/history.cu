@@ -349,6 +349,12 @@ int history_push(qd_solver *s) {
     return QD_OK;
 }
 
+// true when the next stage solve will start from a fitted guess
+bool history_will_guess(qd_solver *s) {
+    const History *H = hist(s);
+    return H && H->n >= 2;
+}
+
 // host copy of the last fit: coefficients [HIST_ND] and the misfit ratio
 int history_last_fit(qd_solver *s, double *out, int *nd) {
     History *H = hist(s);

@@ -235,26 +235,26 @@ __global__ void __launch_bounds__(BX * BY)
 }
 
 // residual norm^2 of the zero-interior guess: only the columns next to the
-// Dirichlet data see a non-zero residual (f = 0 on level 0)
+// Dirichlet data see a non-zero residual (f = 0 on level 0).  One block: each
+// thread sums its rows, the block reduces in a fixed order into *out.
 template <typename T>
-__global__ void k_r0(View<T> v, double *partial) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(1024) k_r0(View<T> v, double *out) {
     double sq = 0.0;
-    if (j < v.N) {
+    for (int j = threadIdx.x; j < v.N; j += blockDim.x) {
         const long row = (long)j * v.P;
         const int K = v.K;
         if (K - 2 == 1) {
             const double r = -((double)v.cx[row] * v.u[row] + (double)v.cx[row + 1] * v.u[row + 2]) *
                              (double)v.inv_h2;
-            sq = r * r;
+            sq += r * r;
         } else if (K - 2 > 1) {
             const double r1 = -(double)v.cx[row] * (double)v.u[row] * (double)v.inv_h2;
             const double r2 = -(double)v.cx[row + K - 2] * (double)v.u[row + K - 1] * (double)v.inv_h2;
-            sq = r1 * r1 + r2 * r2;
+            sq += r1 * r1 + r2 * r2;
         }
     }
     sq = block_sum(sq);
-    if (threadIdx.x == 0) partial[blockIdx.x] = sq;
+    if (threadIdx.x == 0) *out = sq;
 }
 
 // ---------------------------------------------------------------------------
@@ -484,10 +484,7 @@ int level0_norm(qd_solver *s, int to32, int slot) {
 
 int r0_norm(qd_solver *s, int slot) {
     View<double> v = make_view(s, s->L64, 0);
-    const int nb = cdiv(v.N, 256);
-    k_r0<double><<<nb, 256, 0, s->stream>>>(v, s->d_partial);
-    QD_LAUNCH_CHECK(s);
-    k_final_sum<<<1, 1024, 0, s->stream>>>(s->d_partial, nb, s->d_scal + slot);
+    k_r0<double><<<1, 1024, 0, s->stream>>>(v, s->d_scal + slot);
     QD_LAUNCH_CHECK(s);
     return QD_OK;
 }

@@ -1035,6 +1035,7 @@ namespace qd {
 int warm_start_before_boundary(qd_solver *s) {
     qd_unet *u = static_cast<qd_unet *>(s->unet);
     if (!u || !u->mode) return QD_OK;
+    if (history_will_guess(s)) return QD_OK;   // the fit writes the boundary data its guess implies
     const LevelDims &d = s->dims[0];
     k_save_bc<<<cdv(d.N, 256), 256, 0, s->stream>>>(s->L64[0].u, d.N, d.K, d.P, u->d_bc_old);
     QD_LAUNCH_CHECK(s);
