@@ -274,11 +274,9 @@ def run_ours(args):
                 return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
 
             hU = pinned((nz, nx))
-            hU[:] = sim.solver.download_u()
+            sim.solver.download_u(out=hU)
             hv = {k: pinned(nz) for k in ("Slip", "psi", "V", "dpsi", "Ts")}
-            st = sim.solver.rk43_state()
-            for k in hv:
-                hv[k][:] = st[k]
+            st = sim.solver.rk43_state(out=hv)
         barrier()
         for _ in range(args.steps):
             flush.fill_(1.0)
@@ -291,15 +289,12 @@ def run_ours(args):
                                           st["errA"][0], st["errA"][1], st["it"])
                 sim.solver.upload_u(hU)
                 sim.solver.rk43_step(1)
-                st = sim.solver.rk43_state()
-                hU[:] = sim.solver.download_u()
+                st = sim.solver.rk43_state(out=hv)
+                sim.solver.download_u(out=hU)
             else:
                 sim.step(1)
             e1.record(stream)
             e1.synchronize()
-            if host_io:
-                for k in hv:
-                    hv[k][:] = st[k]
             step_ms.append(e0.elapsed_time(e1))
             ms += step_ms[-1]
         barrier()

@@ -109,8 +109,10 @@ class Solver:
     def upload_u(self, U):
         check(self.L.qd_upload_u(self.h, _p(np.ascontiguousarray(U))))
 
-    def download_u(self):
-        U = np.zeros((self.nz, self.nx))
+    def download_u(self, out=None):
+        """The ghosted nz x nx field; `out`: a C-contiguous float64 array of
+        that shape to write into (e.g. pinned host memory)."""
+        U = np.zeros((self.nz, self.nx)) if out is None else out
         check(self.L.qd_download_u(self.h, _p(U)))
         return U
 
@@ -188,8 +190,10 @@ class Solver:
         check(self.L.qd_rk43_step(self.h, n, C.byref(done)))
         return done.value
 
-    def rk43_state(self):
-        out = {k: np.zeros(self.nz) for k in ("Slip", "psi", "V", "Ts", "dpsi")}
+    def rk43_state(self, out=None):
+        """State after the last accepted step; `out`: a dict of nz float64
+        arrays (Slip, psi, V, Ts, dpsi) to write into."""
+        out = {k: np.zeros(self.nz) for k in ("Slip", "psi", "V", "Ts", "dpsi")} if out is None else out
         check(self.L.qd_rk43_get_state(self.h, _p(out["Slip"]), _p(out["psi"]), _p(out["V"]),
                                        _p(out["Ts"]), _p(out["dpsi"])))
         d = np.zeros(4)

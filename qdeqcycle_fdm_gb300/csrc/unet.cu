@@ -1076,11 +1076,16 @@ int warm_start_after_solve(qd_solver *s) {
     k_target<<<cdv(g.P, 256), 256, 0, s->stream>>>(s->L64[0].u, u->d_u_start, d.N, d.K, d.P, u->d_scale,
                                                    u->target32, g);
     QD_LAUNCH_CHECK(s);
-    QD_CUDA(cudaMemcpyAsync(u->d_prev, u->target32, sizeof(float) * (size_t)g.P, cudaMemcpyDeviceToDevice,
-                            s->stream));
-    if (u->mode != 1) return QD_OK;
-    QD_TRY(loss_and_grad(u));
-    return adam(u);
+    if (u->mode == 1) {
+        QD_TRY(loss_and_grad(u));
+        QD_TRY(adam(u));
+    }
+    // the solved change is the next solve's input channel 4: the buffers
+    // trade places (stream order keeps the next writer after every reader)
+    float *t = u->d_prev;
+    u->d_prev = u->target32;
+    u->target32 = t;
+    return QD_OK;
 }
 
 // where the solution-history guess leaves the boundary data its combination
