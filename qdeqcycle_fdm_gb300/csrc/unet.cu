@@ -37,6 +37,7 @@
 namespace qd {
 
 static constexpr int UNET_NIN = 5;   // input channels in use (of the 16 staged)
+static constexpr int UNET_BIAS_BLOCKS = 1024;   // blocks of the bias-gradient sums
 
 __host__ __device__ static inline int cdv(long a, long b) { return (int)((a + b - 1) / b); }
 
@@ -103,6 +104,7 @@ struct qd_unet {
     double *d_bc_old;              // saved boundary columns: fault (N), far (N)
     double *d_u_start;             // u a solve would start from without the network (level-0 layout)
     __nv_bfloat16 *planar;         // dY planar + 3 shifted X planar copies
+    float *parts;                  // per-CTA partial sums of a weight or bias gradient
     size_t planar_elems;
     unsigned *d_status;
     cudaStream_t stream;           // the stream the net runs on (the solver's while attached)
@@ -302,17 +304,24 @@ __global__ void k_planar(const __nv_bfloat16 *in, __nv_bfloat16 *out, int P, int
     out[idx] = (s >= 0 && s < P) ? in[(long)s * C + c] : __float2bfloat16_rn(0.f);
 }
 
-// per-channel sum of g over the pixels (bias gradient), atomically added
-__global__ void k_bias_grad(const __nv_bfloat16 *g, float *gb, int P, int C) {
-    __shared__ float acc[128];
-    for (int c = threadIdx.x; c < C; c += blockDim.x) acc[c] = 0.f;
-    __syncthreads();
+// per-channel sum of g over a block's share of the pixels (bias gradient):
+// thread (lane l, channel c) of the block sums pixels p0 + l, p0 + l + L, ...
+// in order, the lanes are then added in order; part[block][c]
+__global__ void __launch_bounds__(256) k_bias_grad(const __nv_bfloat16 *g, float *part, int P, int C) {
+    __shared__ float acc[256];
+    const int L = blockDim.x / C, c = threadIdx.x % C, l = threadIdx.x / C;
     const int per = cdv(P, gridDim.x);
     const int p0 = blockIdx.x * per, p1 = min(P, p0 + per);
-    for (long i = (long)p0 * C + threadIdx.x; i < (long)p1 * C; i += blockDim.x)
-        atomicAdd(&acc[i % C], __bfloat162float(g[i]));
+    float s = 0.f;
+    if (l < L)
+        for (int p = p0 + l; p < p1; p += L) s += __bfloat162float(g[(long)p * C + c]);
+    acc[threadIdx.x] = s;
     __syncthreads();
-    for (int c = threadIdx.x; c < C; c += blockDim.x) atomicAdd(&gb[c], acc[c]);
+    if (threadIdx.x < C) {
+        float t = 0.f;
+        for (int k = 0; k < L; k++) t += acc[k * C + threadIdx.x];
+        part[(size_t)blockIdx.x * C + threadIdx.x] = t;
+    }
 }
 
 // Adam on one layer's FP32 master weights and biases, then the BF16 copies
@@ -703,9 +712,14 @@ static int wgrad_layer(qd_unet *u, ULayer &Ly) {
     WgradArgs a;
     a.Cin = CIN; a.Cout = Ly.cout; a.Wp = g.Wp; a.P = g.P;
     a.chunk = 64 * 32;
-    a.dW = Ly.gw;
+    a.part = u->parts;
     a.status = u->d_status;
-    return wgrad_launch<CIN>(u, m, a, cdv(g.P, a.chunk));
+    const int nchunks = cdv(g.P, a.chunk);
+    QD_TRY(wgrad_launch<CIN>(u, m, a, nchunks));
+    const int n = 9 * Ly.cout * CIN;
+    k_sum_parts<<<cdv(n, 256), 256, 0, u->stream>>>(u->parts, nchunks, n, Ly.gw);
+    QD_CUDA(cudaPeekAtLastError());
+    return QD_OK;
 }
 
 // gradient of the loss already in head_gout; every layer's gw/gb
@@ -724,7 +738,9 @@ static int backward(qd_unet *u) {
             const UGrid &g = u->g[Ly.lvl];
             const long n = (long)g.P * Ly.cout;
             if (Ly.relu) k_relu_bwd<<<EW8_GRID(n)>>>(Ly.gout->p, Ly.out->p, n);
-            k_bias_grad<<<std::min(cdv(g.P, 256), 1024), 256, 0, u->stream>>>(Ly.gout->p, Ly.gb, g.P, Ly.cout);
+            const int nb = std::min(cdv(g.P, 256), UNET_BIAS_BLOCKS);
+            k_bias_grad<<<nb, 256, 0, u->stream>>>(Ly.gout->p, u->parts, g.P, Ly.cout);
+            k_sum_parts<<<1, 128, 0, u->stream>>>(u->parts, nb, Ly.cout, Ly.gb);
             QD_CUDA(cudaPeekAtLastError());
             switch (Ly.cin) {
                 case 16: QD_TRY(wgrad_layer<16>(u, Ly)); break;
@@ -819,7 +835,7 @@ static void unet_free(qd_unet *u) {
         cudaFree(Ly.w32); cudaFree(Ly.b32); cudaFree(Ly.mw); cudaFree(Ly.vw); cudaFree(Ly.mb);
         cudaFree(Ly.vb); cudaFree(Ly.gw); cudaFree(Ly.gb); cudaFree(Ly.w); cudaFree(Ly.wt);
     }
-    cudaFree(u->out32); cudaFree(u->target32); cudaFree(u->d_prev); cudaFree(u->d_loss); cudaFree(u->d_scale); cudaFree(u->d_rowf);
+    cudaFree(u->out32); cudaFree(u->target32); cudaFree(u->d_prev); cudaFree(u->d_loss); cudaFree(u->d_scale); cudaFree(u->d_rowf); cudaFree(u->parts);
     cudaFree(u->d_bc_old); cudaFree(u->d_u_start); cudaFree(u->planar); cudaFree(u->d_status);
     if (u->own_stream) cudaStreamDestroy(u->own_stream);
     delete u;
@@ -964,6 +980,12 @@ static int unet_build(qd_unet *u, unsigned long long seed) {
     for (auto &Ly : u->L) need = std::max(need, (size_t)u->g[Ly.lvl].P * (128 + 3 * (size_t)Ly.cin));
     u->planar = dalloc_z<__nv_bfloat16>(need, &rc);
     u->planar_elems = need;
+    // partial sums of the weight and bias gradients
+    size_t nparts = 0;
+    for (auto &Ly : u->L)
+        nparts = std::max({nparts, (size_t)cdv(u->g[Ly.lvl].P, 64 * 32) * 9 * Ly.cout * Ly.cin,
+                           (size_t)UNET_BIAS_BLOCKS * Ly.cout});
+    u->parts = dalloc_z<float>(nparts, &rc);
     u->out32 = dalloc_z<float>(u->g[0].P, &rc);
     u->target32 = dalloc_z<float>(u->g[0].P, &rc);
     u->d_prev = dalloc_z<float>(u->g[0].P, &rc);

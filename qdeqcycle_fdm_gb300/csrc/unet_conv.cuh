@@ -25,7 +25,8 @@
 // k_conv_wgrad: dW[t][co][ci] = sum_p dY[p, co] * X[p + shift_t, ci] with
 //   pixel-contiguous (planar) copies of dY and X: M = Cout rows (padded to
 //   128 by the TMA zero fill), N = Cin, K = a chunk of pixels; one CTA per
-//   (chunk, tap) adds its partial product into dW with FP32 atomics.
+//   (chunk, tap) writes its partial product to part[chunk][t][co][ci], and
+//   k_sum_parts adds the chunks in order: training is deterministic.
 //   The X copies are pre-shifted by dx in {-1, 0, 1}, so the remaining tap
 //   shift dy*Wp is a multiple of 8 pixels (16 bytes): a legal TMA x origin.
 //
@@ -423,7 +424,7 @@ __global__ void __launch_bounds__(ROWS_THREADS) k_conv_rows(const __grid_constan
 struct WgradArgs {
     int Cin, Cout, Wp, P;
     int chunk;                // pixels per CTA (a multiple of 64)
-    float *dW;                // [9][Cout][Cin] FP32, accumulated
+    float *part;              // [chunks][9][Cout][Cin] FP32 partial products
     unsigned *status;
 };
 
@@ -502,14 +503,23 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv_wgrad(const __grid_consta
     for (int n0 = 0; n0 < CIN; n0 += 8) {
         float v[8];
         tmem_ld8(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)n0, v);
-        if (!ok || co >= a.Cout) continue;
-        float *dst = a.dW + ((size_t)t * a.Cout + co) * a.Cin + n0;
-#pragma unroll
-        for (int i = 0; i < 8; i++) atomicAdd(dst + i, v[i]);
+        if (co >= a.Cout) continue;
+        float4 *dst = reinterpret_cast<float4 *>(a.part + (((size_t)blockIdx.x * 9 + t) * a.Cout + co) * a.Cin + n0);
+        dst[0] = ok ? make_float4(v[0], v[1], v[2], v[3]) : make_float4(0.f, 0.f, 0.f, 0.f);
+        dst[1] = ok ? make_float4(v[4], v[5], v[6], v[7]) : make_float4(0.f, 0.f, 0.f, 0.f);
     }
     tc_fence_before();
     __syncthreads();
     if (warp == 2) tmem_free(tmem, TCOLS);
+}
+
+// out[i] = sum over k < nparts of part[k * n + i], in order of k
+__global__ void k_sum_parts(const float *__restrict__ part, int nparts, int n, float *out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float s = 0.f;
+    for (int k = 0; k < nparts; k++) s += part[(size_t)k * n + i];
+    out[i] = s;
 }
 
 }  // namespace qd
