@@ -57,6 +57,8 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--config", default="config1")
     p.add_argument("--cpu-sample-s", type=float, default=20.0)
+    p.add_argument("--ref-budget-s", type=float, default=60.0,
+                   help="--impl reference: stop timing after the step that passes this many seconds")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--headline-only", action="store_true",
@@ -185,7 +187,7 @@ def run_reference(args):
     oracle.build(ref=False)
     cfg = config.CONFIGS[args.config]()
     prob = problem.build_problem(cfg, homogenize=lambda ni, nk, mu: oracle.set_medium(ni, nk, mu)[1])
-    r = run_cpu(prob, args.warmup, args.steps)
+    r = run_cpu(prob, args.warmup, args.steps, budget_s=args.ref_budget_s)
     line = {
         "impl": "reference", "metric": METRIC, "value": r["value"], "unit": "sim_yr/hr",
         "n_gpus": args.gpus, "steps": r["steps"], "warmup": args.warmup,
