@@ -73,6 +73,9 @@ def parse():
                         "steps first), for per-kernel profilers; prints a one-line summary")
     p.add_argument("--no-autotune", action="store_true",
                    help="keep the default smoother schedule and tiles in the runs with the history guess")
+    p.add_argument("--unet-level", type=int, default=1, choices=[0, 1],
+                   help="multigrid level whose grid the U-Net runs on (1: every other node, its "
+                        "prediction prolongated bilinearly)")
     p.add_argument("--history", type=int, default=4,
                    help="stored solutions of the solution-history guess (0: start every solve "
                         "from the previous solution, as the reference)")
@@ -223,6 +226,11 @@ def run_ours(args):
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     T = args.train_steps
     H = args.history
+
+    def unet_n(n):
+        """network nodes per side: the solver's level-0 grid, or its level-1
+        grid with the prediction prolongated bilinearly"""
+        return n if args.unet_level == 0 else (n - 1) // 2 + 1
     TUNE = not args.no_autotune
 
     def barrier():
@@ -240,7 +248,7 @@ def run_ours(args):
         tprob = problem.build_problem(tcfg)
         tsim = api.Simulation(tprob, mg)
         tsim.solver.set_solution_history(H)
-        net = warmstart.UNet(tprob.nk, tprob.ni, seed=args.seed)
+        net = warmstart.UNet(unet_n(tprob.nk), unet_n(tprob.ni), seed=args.seed)
         net.attach(tsim.solver, warmstart.MODE_TRAIN, args.lr)
         tsim.start()
         tsim.step(T)
@@ -356,6 +364,8 @@ def run_ours(args):
         bf = peaks.get("bf16_tflops", 1900.0)
         extra["warm_start"] = {
             "network": "U-Net 4 levels 16/32/64/128 ch, 3x3 conv, BF16 in / FP32 accumulate (tcgen05)",
+            "network_grid": f"{unet_n(prob.nk)}x{unet_n(prob.ni)} (multigrid level {args.unet_level}"
+                            + (", prediction prolongated bilinearly)" if args.unet_level else ")"),
             "train_steps": T, **tinfo, "lr": args.lr,
             "inference_us": us_f, "inference_tflops": fl_f / (us_f * 1e-6) / 1e12,
             "train_step_us": us_t, "train_tflops": fl_t / (us_t * 1e-6) / 1e12,

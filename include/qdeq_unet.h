@@ -51,10 +51,14 @@ int qd_unet_loss_grad_host(qd_unet *u, const float *x, const float *target, floa
 /* one Adam step (beta 0.9 / 0.999) with learning rate lr on (x, target) */
 int qd_unet_train_step_host(qd_unet *u, const float *x, const float *target, float lr, float *loss);
 
-/* Attach the network to a solver of the same grid: mode 1 trains online
- * (one Adam step per stage solve on the change the solve made, the solve
- * itself starting from the unmodified field), mode 2 predicts (the solve
- * starts from u + prediction), mode 0 detaches.  While attached the
+/* Attach the network to a solver of the same grid, or of twice its
+ * resolution (2n-1 nodes per side for an n-node network: the network then
+ * sees every other level-0 node -- the multigrid's level-1 grid -- and its
+ * prediction is prolongated bilinearly with the multigrid's weights; about
+ * a quarter of the cost of a full-resolution network).  Mode 1 trains
+ * online (one Adam step per stage solve on the change the solve made, the
+ * solve itself starting from the unmodified field), mode 2 predicts (the
+ * solve starts from u + prediction), mode 0 detaches.  While attached the
  * network runs on the solver's stream; destroying the solver detaches it. */
 int qd_solver_warm_start(qd_solver *s, qd_unet *u, int mode, float lr);
 

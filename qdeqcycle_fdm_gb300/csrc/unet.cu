@@ -113,6 +113,7 @@ struct qd_unet {
     double last_loss;
     float lr;
     int mode;                      // 0 off, 1 train, 2 predict
+    int stride;                    // solver level-0 nodes per network pixel (1, or 2: the level-1 grid)
     bool pdl;                      // launch with programmatic stream serialization (inside forward())
 };
 
@@ -436,14 +437,17 @@ __global__ void __launch_bounds__(1024) k_scales(const double *u, int N, int K, 
     }
 }
 
+// input channels at network pixel (r, q): the solver's level-0 node
+// (st (r-1), st (q-1)) -- every node (st = 1) or every other one (st = 2,
+// the network on the multigrid's level-1 grid)
 __global__ void k_features(const double *u, int N, int K, int P, const float *rowf, const float *scale,
-                           const float *prev, __nv_bfloat16 *x0, UGrid g) {
+                           const float *prev, __nv_bfloat16 *x0, UGrid g, int st) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= g.P) return;
     const int r = p / g.Wp, q = p - r * g.Wp;
     float f[UNET_NIN] = {0.f, 0.f, 0.f, 0.f, 0.f};
     if (uin(r, q, g)) {
-        const int j = r - 1, k = q - 1;
+        const int j = st * (r - 1), k = st * (q - 1);
         f[0] = d2f_rne(u[(long)j * P + k]) * scale[3];
         f[1] = rowf[j];
         f[2] = rowf[N + j];
@@ -461,23 +465,37 @@ __global__ void k_features(const double *u, int N, int K, int P, const float *ro
     dst[1] = hi;
 }
 
-// u += s_bc * out on the interior columns
-__global__ void k_apply(double *u, int N, int K, int P, const float *out, const float *scale, UGrid g) {
+// u += s_bc * out on the interior columns; with st = 2 the network's
+// output on the level-1 grid is prolongated bilinearly (the multigrid's
+// prolongation weights: the coincident node, or the mean of the 2 or 4
+// neighbouring level-1 nodes)
+__global__ void k_apply(double *u, int N, int K, int P, const float *out, const float *scale, UGrid g, int st) {
     const int j = blockIdx.y, k = blockIdx.x * blockDim.x + threadIdx.x + 1;
     if (j >= N || k > K - 2) return;
-    u[(long)j * P + k] += (double)scale[0] * (double)out[(long)(j + 1) * g.Wp + (k + 1)];
+    float v;
+    if (st == 1) {
+        v = out[(long)(j + 1) * g.Wp + (k + 1)];
+    } else {
+        const int jc = j >> 1, kc = k >> 1, fy = j & 1, fx = k & 1;
+        const float *o = out + (long)(jc + 1) * g.Wp + (kc + 1);
+        if (!fy && !fx) v = o[0];
+        else if (fy && !fx) v = 0.5f * o[0] + 0.5f * o[g.Wp];
+        else if (!fy && fx) v = 0.5f * o[0] + 0.5f * o[1];
+        else v = 0.25f * (o[0] + o[1] + o[g.Wp] + o[g.Wp + 1]);
+    }
+    u[(long)j * P + k] += (double)scale[0] * (double)v;
 }
 
 // training target: (u_solved - u_start) / s_bc on the interior (the
 // difference in FP64, then FP32)
 __global__ void k_target(const double *u, const double *u0, int N, int K, int P, const float *scale,
-                         float *target, UGrid g) {
+                         float *target, UGrid g, int st) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= g.P) return;
     const int r = p / g.Wp, q = p - r * g.Wp;
     float t = 0.f;
     if (uin(r, q, g)) {
-        const long c = (long)(r - 1) * P + (q - 1);
+        const long c = (long)st * (r - 1) * P + (long)st * (q - 1);
         t = d2f_rne(u[c] - u0[c]) * scale[2];
     }
     target[p] = t;
@@ -991,9 +1009,9 @@ static int unet_build(qd_unet *u, unsigned long long seed) {
     u->d_prev = dalloc_z<float>(u->g[0].P, &rc);
     u->d_loss = dalloc_z<float>(1, &rc);
     u->d_scale = dalloc_z<float>(4, &rc);
-    u->d_rowf = dalloc_z<float>(2 * (size_t)u->nk, &rc);
+    u->d_rowf = dalloc_z<float>(2 * (2 * (size_t)u->nk - 1), &rc);   // level-0 rows of a solver twice as fine
     u->d_status = dalloc_z<unsigned>(1, &rc);
-    u->d_bc_old = dalloc_z<double>(2 * (size_t)u->nk, &rc);
+    u->d_bc_old = dalloc_z<double>(2 * (2 * (size_t)u->nk - 1), &rc);
     if (rc != QD_OK) set_error("U-Net allocation failed");
     QD_CUDA(cudaStreamSynchronize(u->stream));
     return rc;
@@ -1073,7 +1091,7 @@ int warm_start_after_boundary(qd_solver *s) {
     const UGrid &g = u->g[0];
     k_scales<<<1, 1024, 0, s->stream>>>(s->L64[0].u, d.N, d.K, d.P, u->d_bc_old, u->d_scale, u->d_rowf);
     k_features<<<cdv(g.P, 256), 256, 0, s->stream>>>(s->L64[0].u, d.N, d.K, d.P, u->d_rowf, u->d_scale,
-                                                     u->d_prev, u->x0->p, g);
+                                                     u->d_prev, u->x0->p, g, u->stride);
     QD_LAUNCH_CHECK(s);
     // the field the solve would start from without the network: the change
     // the solve then makes is the training target and the next input
@@ -1082,7 +1100,7 @@ int warm_start_after_boundary(qd_solver *s) {
     if (u->mode == 2) {
         QD_TRY(forward(u));
         k_apply<<<dim3(cdv(d.K, 256), d.N), 256, 0, s->stream>>>(s->L64[0].u, d.N, d.K, d.P, u->out32,
-                                                                 u->d_scale, g);
+                                                                 u->d_scale, g, u->stride);
         QD_LAUNCH_CHECK(s);
     }
     return QD_OK;
@@ -1096,7 +1114,7 @@ int warm_start_after_solve(qd_solver *s) {
     const LevelDims &d = s->dims[0];
     const UGrid &g = u->g[0];
     k_target<<<cdv(g.P, 256), 256, 0, s->stream>>>(s->L64[0].u, u->d_u_start, d.N, d.K, d.P, u->d_scale,
-                                                   u->target32, g);
+                                                   u->target32, g, u->stride);
     QD_LAUNCH_CHECK(s);
     if (u->mode == 1) {
         QD_TRY(loss_and_grad(u));
@@ -1237,10 +1255,15 @@ int qd_solver_warm_start(qd_solver *s, qd_unet *u, int mode, float lr) {
         set_error("qd_solver_warm_start: bad arguments");
         return QD_ERR_ARG;
     }
+    int stride = 1;
     if (u && (u->nk != s->nk || u->ni != s->ni)) {
-        set_error("qd_solver_warm_start: network grid %dx%d differs from the solver's %dx%d", u->nk, u->ni,
-                  s->nk, s->ni);
-        return QD_ERR_ARG;
+        if (2 * u->nk - 1 == s->nk && 2 * u->ni - 1 == s->ni) {
+            stride = 2;   // the network on the solver's level-1 grid
+        } else {
+            set_error("qd_solver_warm_start: network grid %dx%d is neither the solver's %dx%d nor its level-1 grid",
+                      u->nk, u->ni, s->nk, s->ni);
+            return QD_ERR_ARG;
+        }
     }
     QD_CUDA(cudaStreamSynchronize(s->stream));
     if (s->unet && s->unet != u) {
@@ -1256,6 +1279,7 @@ int qd_solver_warm_start(qd_solver *s, qd_unet *u, int mode, float lr) {
     if (!u->d_u_start) QD_CUDA(cudaMalloc(&u->d_u_start, sizeof(double) * (size_t)s->dims[0].N * s->dims[0].P));
     if (s->unet != u) QD_CUDA(cudaMemset(u->d_prev, 0, sizeof(float) * (size_t)u->g[0].P));   // a new run
     u->stream = s->stream;   // the net runs on the solver's stream while attached
+    u->stride = stride;
     u->mode = mode;
     u->lr = mode == 1 ? lr : u->lr;
     s->unet = u;

@@ -162,3 +162,47 @@ def test_online_training_is_deterministic():
         net.close()
     assert params[0].size > 0 and np.any(params[0] != 0)
     assert np.array_equal(params[0], params[1])
+
+
+def test_warm_start_on_the_level1_grid():
+    """A network on the solver's level-1 grid (33 x 33 for a 65 x 65 solver):
+    its inputs are every other level-0 node and its prediction is
+    prolongated bilinearly.  It trains on the solver's own solves, the run
+    still follows the plain run (the multigrid solves to its tolerance from
+    the predicted field), and the prediction does not cost V-cycles."""
+    import dataclasses
+    from qdeqcycle_fdm_gb300 import api, config, problem
+    cfg = config.small(65)
+    mg = dataclasses.replace(cfg.mg, precision=1, surface_prolong=1, coarse_solve=1, tol=1e-9)
+    prob = problem.build_problem(cfg)
+    T, K = 60, 30
+
+    def cycles(a, b):
+        return (b["vcycles"] - a["vcycles"]) / max(1, b["solves"] - a["solves"])
+
+    plain = api.Simulation(prob, mg)
+    plain.start()
+    plain.step(T)
+    p0 = plain.state(with_u=False)
+    plain.step(K)
+    p1 = plain.state(with_u=False)
+    plain.close()
+
+    net = warmstart.UNet(33, 33, seed=1)
+    sim = api.Simulation(prob, mg)
+    net.attach(sim.solver, warmstart.MODE_TRAIN, 1e-3)
+    sim.start()
+    sim.step(T)
+    w0 = sim.state(with_u=False)
+    steps, loss = net.stats()
+    net.attach(sim.solver, warmstart.MODE_PREDICT)
+    sim.step(K)
+    w1 = sim.state(with_u=False)
+    sim.close()
+    net.close()
+    c_plain, c_ws = cycles(p0, p1), cycles(w0, w1)
+    print(f"\nlevel-1 warm start: {steps} training steps, V-cycles per solve {c_ws:.3f} (plain {c_plain:.3f})")
+    assert steps == w0["solves"] and np.isfinite(loss)
+    for k in ("Slip", "psi"):
+        assert rel(w1[k], p1[k]) < 1e-5, (k, rel(w1[k], p1[k]))
+    assert c_ws <= c_plain, (c_ws, c_plain)
