@@ -41,11 +41,13 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 YEAR_S = 365.25 * 86400.0
-# DRAM bytes (read + write) per launch at 1025^2 from ncu captures with the
-# caches flushed before the kernel: the V-cycle kernels of the mixed solver
-# (profiles/vcycle_kernels_1025.md) and the U-Net's first 16 -> 16 channel
-# convolution (profiles/unet_conv_1025.md)
-TRAFFIC = {"up0": 31.19e6, "down0": 17.35e6, "residual": 33.74e6, "conv16": 34.03e6}
+# DRAM bytes (read + write) per launch from ncu captures with the caches
+# flushed before the kernel: the V-cycle kernels of the mixed solver at
+# 1025^2 (profiles/vcycle_kernels_1025.md) and the U-Net's first 16 -> 16
+# channel convolution on the network's grid (profiles/unet_conv_1025.md),
+# keyed by the network's nodes per side
+TRAFFIC = {"up0": 31.19e6, "down0": 17.35e6, "residual": 33.74e6}
+TRAFFIC_CONV16 = {513: 8.62e6, 1025: 34.03e6}
 METRIC = "simulated yr/hr at 1025² (learned+mixed vs plain FP64 MG, 1e-9 rel residual)"
 
 
@@ -445,21 +447,23 @@ def run_ours(args):
     #   up0      prolongation 8 B + 2 sweeps x 20 B + u64 += e 16 B per
     #            level-0 node, + 4 B per level-1 node
     #   residual FP64 u, cx, cz, diag read + FP32 rhs written: 36 B per node
-    #   conv16   16 BF16 channels read and written: 64 B per padded pixel
+    #   conv16   16 BF16 channels read and written: 64 B per padded pixel of
+    #            the network's grid
     # Launches per step: one of each cycle kernel per V-cycle, the residual
     # once more per solve (the guess), the convolution 4 per solve.  The
     # dominant kernel (largest time x launches per step) is the roofline entry.
     peak = peaks.get("hbm_gbs", 6800.0)
     n0 = cfg.ni * cfg.nk
     n1 = ((cfg.ni - 1) // 2 + 1) * ((cfg.nk - 1) // 2 + 1)
-    pad_px = (cfg.nk + 2) * ((cfg.ni + 2 + 7) // 8 * 8)
+    # the network's padded grid (H+2 rows x W+2 columns rounded up to 8)
+    pad_px = (unet_n(cfg.nk) + 2) * ((unet_n(cfg.ni) + 2 + 7) // 8 * 8)
     algo = {"up0": 64.0 * n0 + 4.0 * n1, "down0": 56.0 * n0 + 4.0 * n1, "residual": 36.0 * n0,
             "conv16": 64.0 * pad_px}
     names = {"up0": "k_up<float,2> level 0 (prolongation + 2 sweeps + u64 += e)",
              "down0": "k_down<float> level 0 (2 sweeps + residual + restriction)",
              "residual": "k_residual64_to32 (FP64 residual -> FP32 rhs + norm)",
              "tail": "k_tail<float> (levels <= 65 rows, one CTA)",
-             "conv16": "k_conv_rows<16,16> (U-Net 3x3 convolution, full grid, tcgen05)"}
+             "conv16": f"k_conv_rows<16,16> (U-Net 3x3 convolution, {unet_n(cfg.nk)}x{unet_n(cfg.ni)} grid, tcgen05)"}
     REPS = 50
     kern = {}
     for k in ("up0", "down0", "residual", "tail"):
@@ -483,8 +487,9 @@ def run_ours(args):
             v["achieved_gbs"] = algo[k] / (v["us"] * 1e-6) / 1e9
     dom = max(algo.keys() & kern.keys(), key=lambda k: kern[k]["us_per_step"])
     achieved = kern[dom]["achieved_gbs"]
+    traffic = TRAFFIC_CONV16.get(unet_n(cfg.nk)) if dom == "conv16" else TRAFFIC.get(dom)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": TRAFFIC.get(dom),
+                "frac": achieved / peak, "traffic": traffic,
                 "kernel": names[dom], "us_per_launch": kern[dom]["us"], "reps": REPS,
                 "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
                 "kernels": kern}
