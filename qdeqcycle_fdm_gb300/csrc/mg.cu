@@ -185,7 +185,7 @@ static constexpr int RES_RPT = 4;
 template <bool HAS_F>
 __global__ void __launch_bounds__(BX * BY)
     k_residual64_to32(View<double> v, const double *__restrict__ diag, float *f32, double *partial,
-                      unsigned *count, double *out) {
+                      unsigned *count, double *out, Decide dc) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j0 = blockIdx.y * (BY * RES_RPT) + threadIdx.y;
     const float nih2 = -(float)v.inv_h2;
@@ -231,6 +231,32 @@ __global__ void __launch_bounds__(BX * BY)
     if (tid == 0) {
         *out = t;
         *count = 0;
+    }
+    if (dc.mode == 1) {
+        // ||r0||^2 of the zero-interior guess (as k_r0), then the first decision
+        double r0 = 0.0;
+        if (dc.rel) {
+            for (int j = tid; j < v.N; j += blockDim.x * blockDim.y) {
+                const long row = (long)j * v.P;
+                if (v.K - 2 == 1) {
+                    const double r = -(v.cx[row] * v.u[row] + v.cx[row + 1] * v.u[row + 2]) * v.inv_h2;
+                    r0 += r * r;
+                } else if (v.K - 2 > 1) {
+                    const double r1 = -v.cx[row] * v.u[row] * v.inv_h2;
+                    const double r2 = -v.cx[row + v.K - 2] * v.u[row + v.K - 1] * v.inv_h2;
+                    r0 += r1 * r1 + r2 * r2;
+                }
+            }
+            r0 = block_sum(r0);
+        }
+        if (tid == 0) {
+            if (dc.rel) out[1] = r0;
+            const int go = solve_begin_dev(out, dc.st, dc.rel, dc.tol, dc.n_kernels);
+            if (dc.in_graph) cudaGraphSetConditional(dc.h, go ? 1u : 0u);
+        }
+    } else if (dc.mode == 2 && tid == 0) {
+        const int go = solve_check_dev(out, dc.st, dc.max_cycles, dc.n_kernels);
+        if (dc.in_graph) cudaGraphSetConditional(dc.h, go ? 1u : 0u);
     }
 }
 
@@ -458,6 +484,21 @@ static int smooth_t(qd_solver *s, Level<T> *Ls, int l, int nsweeps) {
 
 // ||r||^2 of level 0 into d_scal[slot]; for mixed precision also writes the
 // FP32 correction right-hand side.
+// the mixed solver's level-0 residual with a decision fused into its last
+// block (norm into d_scal[0], ||r0||^2 into d_scal[1] for mode 1)
+int level0_norm_decide(qd_solver *s, const Decide &dc) {
+    View<double> v = make_view(s, s->L64, 0);
+    dim3 blk(BX, BY), grd(cdiv(v.K, BX), cdiv(v.N, BY * RES_RPT));
+    if (v.f)
+        k_residual64_to32<true><<<grd, blk, 0, s->stream>>>(v, s->L64[0].diag, s->L32[0].f, s->d_partial,
+                                                             s->d_count, s->d_scal, dc);
+    else
+        k_residual64_to32<false><<<grd, blk, 0, s->stream>>>(v, s->L64[0].diag, s->L32[0].f, s->d_partial,
+                                                              s->d_count, s->d_scal, dc);
+    QD_LAUNCH_CHECK(s);
+    return QD_OK;
+}
+
 int level0_norm(qd_solver *s, int to32, int slot) {
     View<double> v = make_view(s, s->L64, 0);
     if (to32) {
@@ -465,11 +506,11 @@ int level0_norm(qd_solver *s, int to32, int slot) {
         if (v.f)
             k_residual64_to32<true><<<grd, blk, 0, s->stream>>>(v, s->L64[0].diag, s->L32[0].f,
                                                                  s->d_partial, s->d_count,
-                                                                 s->d_scal + slot);
+                                                                 s->d_scal + slot, Decide{});
         else
             k_residual64_to32<false><<<grd, blk, 0, s->stream>>>(v, s->L64[0].diag, s->L32[0].f,
                                                                   s->d_partial, s->d_count,
-                                                                  s->d_scal + slot);
+                                                                  s->d_scal + slot, Decide{});
         QD_LAUNCH_CHECK(s);
         return QD_OK;
     }

@@ -8,6 +8,9 @@
 //              -> k_solve_begin: threshold, first "continue?" decision
 //   WHILE      body: one V-cycle -> ||r|| -> k_solve_check: next decision
 //
+// In mixed precision the prologue and the body's check are folded into the
+// last block of the FP64 residual's reduction (one kernel each).
+//
 // The loop condition is a graph conditional handle that the check kernels
 // set on the device (cudaGraphSetConditional), so no host round trip
 // happens inside a solve.  The loop stops when ||r|| <= threshold, when the
@@ -37,42 +40,14 @@ struct SolveGraph {
 // loop condition (otherwise the host reads st->go)
 __global__ void k_solve_begin(cudaGraphConditionalHandle h, const double *scal, SolveState *st,
                               int rel, double tol, int n_kernels, int in_graph) {
-    const double r0 = rel ? sqrt(scal[1]) : 0.0;
-    const double thr = rel ? (r0 > 0.0 ? tol * r0 : tol) : tol;
-    const double delta = sqrt(scal[0]);
-    st->r0 = r0;
-    st->thr = thr;
-    st->delta = delta;
-    st->cycles = 0;
-    st->total_solves++;
-    st->kernels += (unsigned long long)n_kernels;
-    int go = !(delta <= thr);
-    if (go && !isfinite(delta)) {
-        st->flag |= 1;
-        go = 0;
-    }
-    st->go = go;
+    const int go = solve_begin_dev(scal, st, rel, tol, n_kernels);
     if (in_graph) cudaGraphSetConditional(h, go ? 1u : 0u);
 }
 
 // n_kernels: kernels of one loop iteration, this one included
 __global__ void k_solve_check(cudaGraphConditionalHandle h, const double *scal, SolveState *st,
                               int max_cycles, int n_kernels, int in_graph) {
-    const double delta = sqrt(scal[0]);
-    st->delta = delta;
-    st->cycles++;
-    st->total_cycles++;
-    st->kernels += (unsigned long long)n_kernels;
-    int go = !(delta <= st->thr);
-    if (go && !isfinite(delta)) {
-        st->flag |= 1;
-        go = 0;
-    }
-    if (go && max_cycles > 0 && st->cycles >= max_cycles) {
-        st->flag |= 2;
-        go = 0;
-    }
-    st->go = go;
+    const int go = solve_check_dev(scal, st, max_cycles, n_kernels);
     if (in_graph) cudaGraphSetConditional(h, go ? 1u : 0u);
 }
 
@@ -92,11 +67,23 @@ void solve_graph_free(qd_solver *s) {
     s->solve_graph = nullptr;
 }
 
-// the body of one loop iteration: a V-cycle and the norm of the new residual
-static int capture_cycle(qd_solver *s) {
+// the body of one loop iteration: a V-cycle and the norm of the new
+// residual; in mixed precision the norm's last block also takes the loop's
+// decision (*fused set), otherwise k_solve_check follows
+static int capture_cycle(qd_solver *s, cudaGraphConditionalHandle h, int in_graph, long long launches0,
+                         bool *fused) {
+    *fused = false;
     if (s->opt.precision == QD_PREC_MIXED) {
         QD_TRY(vcycle32_into64(s));          // FP32 cycle on A e = r, then u += e
-        QD_TRY(level0_norm(s, 1, 0));        // FP64 residual -> FP32 rhs, norm
+        Decide dc{};
+        dc.mode = 2;
+        dc.max_cycles = s->opt.max_cycles;
+        dc.n_kernels = (int)(s->launches - launches0) + 1;
+        dc.in_graph = in_graph;
+        dc.h = h;
+        dc.st = s->d_solve;
+        QD_TRY(level0_norm_decide(s, dc));   // FP64 residual -> FP32 rhs, norm, decision
+        *fused = true;
     } else {
         int nb = 0;
         QD_TRY(vcycle64_norm(s, &nb));       // the last kernel leaves norm partials
@@ -110,6 +97,31 @@ static int capture_cycle(qd_solver *s) {
     return QD_OK;
 }
 
+// the solve's prologue: ||r0|| (relative tolerance), ||r|| of the guess and
+// the first decision; in mixed precision one kernel (the residual's last
+// block computes ||r0|| and decides), in FP64 k_r0, the norm and
+// k_solve_begin.  n_kernels counts the prologue's kernels.
+static int prologue(qd_solver *s, cudaGraphConditionalHandle h, int in_graph, long long launches0) {
+    const int rel = s->opt.tol_mode == QD_TOL_REL;
+    if (s->opt.precision == QD_PREC_MIXED) {
+        Decide dc{};
+        dc.mode = 1;
+        dc.rel = rel;
+        dc.tol = s->opt.tol;
+        dc.n_kernels = (int)(s->launches - launches0) + 1;
+        dc.in_graph = in_graph;
+        dc.h = h;
+        dc.st = s->d_solve;
+        return level0_norm_decide(s, dc);
+    }
+    if (rel) QD_TRY(r0_norm(s, 1));
+    QD_TRY(level0_norm(s, 0, 0));
+    k_solve_begin<<<1, 1, 0, s->stream>>>(h, s->d_scal, s->d_solve, rel, s->opt.tol,
+                                          (int)(s->launches - launches0) + 1, in_graph);
+    QD_LAUNCH_CHECK(s);
+    return QD_OK;
+}
+
 static int end_capture(qd_solver *s, cudaGraph_t *g, int rc) {
     cudaGraph_t out = nullptr;
     const cudaError_t e = cudaStreamEndCapture(s->stream, &out);
@@ -120,7 +132,6 @@ static int end_capture(qd_solver *s, cudaGraph_t *g, int rc) {
 }
 
 static int build(qd_solver *s, SolveGraph *sg) {
-    const int rel = s->opt.tol_mode == QD_TOL_REL;
     QD_CUDA(cudaGraphCreate(&sg->graph, 0));
     cudaGraphConditionalHandle h;
     QD_CUDA(cudaGraphConditionalHandleCreate(&h, sg->graph, 0, cudaGraphCondAssignDefault));
@@ -130,14 +141,7 @@ static int build(qd_solver *s, SolveGraph *sg) {
     const long long launches0 = s->launches;
     QD_CUDA(cudaStreamBeginCaptureToGraph(s->stream, sg->graph, nullptr, nullptr, 0,
                                           cudaStreamCaptureModeRelaxed));
-    int rc = QD_OK;
-    if (rel) rc = r0_norm(s, 1);
-    if (rc == QD_OK) rc = level0_norm(s, s->opt.precision == QD_PREC_MIXED, 0);
-    if (rc == QD_OK) {
-        const int n = (int)(s->launches - launches0) + 1;
-        k_solve_begin<<<1, 1, 0, s->stream>>>(h, s->d_scal, s->d_solve, rel, s->opt.tol, n, 1);
-        if (cudaPeekAtLastError() != cudaSuccess) rc = QD_ERR_CUDA;
-    }
+    int rc = prologue(s, h, 1, launches0);
     s->launches = launches0;
     QD_TRY(end_capture(s, nullptr, rc));
     // the prologue is a chain: its one leaf is the loop's dependency
@@ -161,8 +165,9 @@ static int build(qd_solver *s, SolveGraph *sg) {
     cudaGraph_t body = cp.conditional.phGraph_out[0];
     QD_CUDA(cudaStreamBeginCaptureToGraph(s->stream, body, nullptr, nullptr, 0,
                                           cudaStreamCaptureModeRelaxed));
-    rc = capture_cycle(s);
-    if (rc == QD_OK) {
+    bool fused = false;
+    rc = capture_cycle(s, h, 1, launches0, &fused);
+    if (rc == QD_OK && !fused) {
         const int n = (int)(s->launches - launches0) + 1;
         k_solve_check<<<1, 1, 0, s->stream>>>(h, s->d_scal, s->d_solve, s->opt.max_cycles, n, 1);
         if (cudaPeekAtLastError() != cudaSuccess) rc = QD_ERR_CUDA;
@@ -187,22 +192,20 @@ static bool eager_solve() {
 }
 
 static int solve_eager(qd_solver *s) {
-    const int rel = s->opt.tol_mode == QD_TOL_REL;
     const long long launches0 = s->launches;
-    if (rel) QD_TRY(r0_norm(s, 1));
-    QD_TRY(level0_norm(s, s->opt.precision == QD_PREC_MIXED, 0));
-    k_solve_begin<<<1, 1, 0, s->stream>>>(0, s->d_scal, s->d_solve, rel, s->opt.tol,
-                                          (int)(s->launches - launches0) + 1, 0);
-    QD_LAUNCH_CHECK(s);
+    QD_TRY(prologue(s, 0, 0, launches0));
     s->launches = launches0;       // counted on the device, as in the graph
     for (;;) {
         SolveState st;
         QD_TRY(solve_state_read(s, &st));
         if (!st.go) return QD_OK;
-        QD_TRY(capture_cycle(s));
-        k_solve_check<<<1, 1, 0, s->stream>>>(0, s->d_scal, s->d_solve, s->opt.max_cycles,
-                                              (int)(s->launches - launches0) + 1, 0);
-        QD_LAUNCH_CHECK(s);
+        bool fused = false;
+        QD_TRY(capture_cycle(s, 0, 0, launches0, &fused));
+        if (!fused) {
+            k_solve_check<<<1, 1, 0, s->stream>>>(0, s->d_scal, s->d_solve, s->opt.max_cycles,
+                                                  (int)(s->launches - launches0) + 1, 0);
+            QD_LAUNCH_CHECK(s);
+        }
         s->launches = launches0;
     }
 }

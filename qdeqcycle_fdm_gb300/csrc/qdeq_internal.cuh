@@ -98,6 +98,59 @@ struct SolveState {
     unsigned long long kernels;           // kernels the solve graphs ran
 };
 
+// The solve loop's decisions, shared by the stand-alone decision kernels and
+// the reductions that fuse them: after the prologue's norms (scal[0] =
+// ||r||^2 of the guess, scal[1] = ||r0||^2 for the relative tolerance) and
+// after each cycle.  Both return "run another cycle"; the caller sets the
+// graph's loop condition from it.
+__device__ inline int solve_begin_dev(const double *scal, SolveState *st, int rel, double tol, int n_kernels) {
+    const double r0 = rel ? sqrt(scal[1]) : 0.0;
+    const double thr = rel ? (r0 > 0.0 ? tol * r0 : tol) : tol;
+    const double delta = sqrt(scal[0]);
+    st->r0 = r0;
+    st->thr = thr;
+    st->delta = delta;
+    st->cycles = 0;
+    st->total_solves++;
+    st->kernels += (unsigned long long)n_kernels;
+    int go = !(delta <= thr);
+    if (go && !isfinite(delta)) {
+        st->flag |= 1;
+        go = 0;
+    }
+    st->go = go;
+    return go;
+}
+
+__device__ inline int solve_check_dev(const double *scal, SolveState *st, int max_cycles, int n_kernels) {
+    const double delta = sqrt(scal[0]);
+    st->delta = delta;
+    st->cycles++;
+    st->total_cycles++;
+    st->kernels += (unsigned long long)n_kernels;
+    int go = !(delta <= st->thr);
+    if (go && !isfinite(delta)) {
+        st->flag |= 1;
+        go = 0;
+    }
+    if (go && max_cycles > 0 && st->cycles >= max_cycles) {
+        st->flag |= 2;
+        go = 0;
+    }
+    st->go = go;
+    return go;
+}
+
+// a decision fused into the last block of the level-0 FP64 residual
+// reduction (mixed precision): mode 1 also computes ||r0||^2 and takes the
+// first decision, mode 2 the decision after a cycle; mode 0 none
+struct Decide {
+    int mode, rel, max_cycles, n_kernels, in_graph;
+    double tol;
+    cudaGraphConditionalHandle h;
+    SolveState *st;
+};
+
 // binary64 -> binary32 with round-to-nearest-even, on the integer pipes.
 // GB300's FP64 pipe also executes the hardware F2F conversion, and that pipe
 // bounds the mixed-precision residual kernel; this routine follows the IEEE
@@ -191,6 +244,7 @@ int tiles_set(qd_solver *s, int box_up, int box_down);
 int time_kernel(qd_solver *s, int which, int reps, double *us);
 // mg.cu: level-0 norms into d_scal[slot] (to32: FP64 residual -> FP32 rhs)
 int level0_norm(qd_solver *s, int to32, int slot);
+int level0_norm_decide(qd_solver *s, const Decide &dc);
 int convert_f64_f32(const double *in, float *out, int n);
 int r0_norm(qd_solver *s, int slot);
 void tail_image_free(qd_solver *s);
