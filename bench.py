@@ -442,10 +442,11 @@ def run_ours(args):
     # on the solver's own state after the timed run; the convolution by
     # qd_unet_time the same way.  Algorithmic bytes per launch are the
     # unfused algorithm's traffic:
-    #   down0    2 red+black sweeps x 20 B + residual/restriction 16 B per
+    #   down0    nu_pre red+black sweeps x 20 B + residual/restriction 16 B
+    #            per level-0 node, + 4 B per level-1 node
+    #   up0      prolongation 8 B + nu_post sweeps x 20 B + u64 += e 16 B per
     #            level-0 node, + 4 B per level-1 node
-    #   up0      prolongation 8 B + 2 sweeps x 20 B + u64 += e 16 B per
-    #            level-0 node, + 4 B per level-1 node
+    #            (nu_pre, nu_post: the schedule the run used, tuned or not)
     #   residual FP64 u, cx, cz, diag read + FP32 rhs written: 36 B per node
     #   conv16   16 BF16 channels read and written: 64 B per padded pixel of
     #            the network's grid
@@ -457,10 +458,13 @@ def run_ours(args):
     n1 = ((cfg.ni - 1) // 2 + 1) * ((cfg.nk - 1) // 2 + 1)
     # the network's padded grid (H+2 rows x W+2 columns rounded up to 8)
     pad_px = (unet_n(cfg.nk) + 2) * ((unet_n(cfg.ni) + 2 + 7) // 8 * 8)
-    algo = {"up0": 64.0 * n0 + 4.0 * n1, "down0": 56.0 * n0 + 4.0 * n1, "residual": 36.0 * n0,
+    tn = head["autotune"]
+    nu_pre, nu_post = (tn["nu_pre"], tn["nu_post"]) if tn else (cfg.mg.nu_pre, cfg.mg.nu_post)
+    algo = {"up0": (24.0 + 20.0 * nu_post) * n0 + 4.0 * n1, "down0": (16.0 + 20.0 * nu_pre) * n0 + 4.0 * n1,
+            "residual": 36.0 * n0,
             "conv16": 64.0 * pad_px}
-    names = {"up0": "k_up<float,2> level 0 (prolongation + 2 sweeps + u64 += e)",
-             "down0": "k_down<float> level 0 (2 sweeps + residual + restriction)",
+    names = {"up0": f"k_up<float,2> level 0 (prolongation + {nu_post} sweep(s) + u64 += e)",
+             "down0": f"k_down<float> level 0 ({nu_pre} sweep(s) + residual + restriction)",
              "residual": "k_residual64_to32 (FP64 residual -> FP32 rhs + norm)",
              "tail": "k_tail<float> (levels <= 65 rows, one CTA)",
              "conv16": f"k_conv_rows<16,16> (U-Net 3x3 convolution, {unet_n(cfg.nk)}x{unet_n(cfg.ni)} grid, tcgen05)"}
