@@ -13,7 +13,7 @@
 //     32*(w%4) .. 32*(w%4)+31.
 // Operands are K-major tiles in shared memory written by TMA with the
 // matching swizzle: rows of SW bytes (32, 64 or 128), eight-row groups of
-// 8*SW bytes, tile bases 1024-byte aligned.
+// 8*SW bytes, tile bases 1024-byte aligned (an MMA may start on any row).
 #pragma once
 
 #include <stdint.h>
@@ -52,8 +52,11 @@ __host__ __device__ constexpr uint32_t sw_layout_type(int row_bytes) {
 
 // Shared-memory matrix descriptor: start address, leading-dimension offset
 // (unused for swizzled K-major tiles, set to 16 B), stride between 8-row
-// groups (8 * row_bytes), descriptor version 1, base offset 0 (tiles are
-// 1024-byte aligned), swizzle layout.
+// groups (8 * row_bytes), descriptor version 1, base offset 0, swizzle
+// layout.  The MMA applies the swizzle to the absolute shared-memory
+// address, as the TMA does when it writes a 1024-byte-aligned tile, so a
+// start on any row of the tile (or 32 bytes into a row, for the K steps)
+// reads the rows as written.
 __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, int row_bytes) {
     uint64_t d = 0;
     d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
@@ -61,19 +64,6 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, int row_bytes) {
     d |= (uint64_t)((8u * (uint32_t)row_bytes) >> 4) << 32;
     d |= (uint64_t)1 << 46;
     d |= (uint64_t)sw_layout_type(row_bytes) << 61;
-    return d;
-}
-
-// Unswizzled K-major operand: core matrices of 8 rows x 16 bytes (rows 16
-// bytes apart), sbo bytes between 8-row groups along M/N and lbo bytes
-// between the 16-byte column chunks along K.  Any 16-byte-aligned start
-// address is valid, so a tile may start one row further down.
-__device__ __forceinline__ uint64_t smem_desc_noswz(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-    uint64_t d = 0;
-    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
-    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
-    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
-    d |= (uint64_t)1 << 46;
     return d;
 }
 
