@@ -75,7 +75,11 @@ def parse():
                         "steps first), for per-kernel profilers; prints a one-line summary")
     p.add_argument("--no-autotune", action="store_true",
                    help="keep the default smoother schedule and tiles in the runs with the history guess")
-    p.add_argument("--unet-level", type=int, default=1, choices=[0, 1],
+    p.add_argument("--net-gate", type=float, default=0.0,
+                   help="the network corrects a stage solve's guess when the guess's residual exceeds "
+                        "this multiple of the solve's threshold (0: when one V-cycle at the solver's "
+                        "measured reduction per cycle would not reach it)")
+    p.add_argument("--unet-level", type=int, default=1, choices=[0, 1, 2],
                    help="multigrid level whose grid the U-Net runs on (1: every other node, its "
                         "prediction prolongated bilinearly)")
     p.add_argument("--history", type=int, default=4,
@@ -232,7 +236,7 @@ def run_ours(args):
     def unet_n(n):
         """network nodes per side: the solver's level-0 grid, or its level-1
         grid with the prediction prolongated bilinearly"""
-        return n if args.unet_level == 0 else (n - 1) // 2 + 1
+        return (n - 1) // (1 << args.unet_level) + 1
     TUNE = not args.no_autotune
 
     def barrier():
@@ -273,6 +277,7 @@ def run_ours(args):
         sim.solver.set_solution_history(history)
         if net is not None:
             net.attach(sim.solver, warmstart.MODE_PREDICT)
+            warmstart.UNet.set_gate(sim.solver, args.net_gate)
         sim.start()
         sim.step(args.warmup)
         tuning = sim.solver.autotune(3) if tune else None
@@ -317,6 +322,7 @@ def run_ours(args):
                      "t0": s0["t"], "t_end": s1["t"],
                      "launches": s1["kernel_launches"] - s0["kernel_launches"],
                      "vcycles": s1["vcycles"] - s0["vcycles"], "solves": s1["solves"] - s0["solves"],
+                     "net_solves": s1["net_solves"] - s0["net_solves"],
                      "attempts": s1["attempts"] - s0["attempts"], "autotune": tuning}
 
     def job_value(run):
@@ -346,7 +352,9 @@ def run_ours(args):
             print(json.dumps({"profile_run": "headline solver", "learned": learned, "history": H,
                               "steps": args.steps, "warmup": args.warmup, "ms_per_step": run["ms"] / args.steps,
                               "vcycles_per_solve": run["vcycles"] / max(1, run["solves"]),
-                              "solves_per_step": run["solves"] / args.steps}), flush=True)
+                              "solves_per_step": run["solves"] / args.steps,
+                              "network_corrected_solves": run["net_solves"] / max(1, run["solves"])}),
+                  flush=True)
         if net is not None:
             net.close()
         return 0
@@ -536,6 +544,7 @@ def run_ours(args):
                        "parallelism": f"replicas x{world}", "l2": "flushed before every timed step"},
             "sim_years_timed": head["yrs"], "t_start_s": head["t0"], "t_end_s": head["t_end"],
             "vcycles_per_solve": head["vcycles"] / max(1, head["solves"]),
+            "network_corrected_solves": head["net_solves"] / max(1, head["solves"]) if learned else None,
             "attempts_per_step": head["attempts"] / args.steps,
             "autotune": head["autotune"],
             **extra,

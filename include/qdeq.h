@@ -93,6 +93,9 @@ typedef struct qd_stats {
     long long steps;         /* accepted RK43 steps                          */
     long long newton_iters;  /* Newton iterations, summed over nodes         */
     long long kernel_launches; /* kernels this library launched              */
+    long long net_solves;    /* solves whose guess the attached network
+                                corrected (prediction mode: only solves
+                                whose guess missed the tolerance)          */
 } qd_stats;
 
 const char *qd_version(void);

@@ -51,16 +51,33 @@ int qd_unet_loss_grad_host(qd_unet *u, const float *x, const float *target, floa
 /* one Adam step (beta 0.9 / 0.999) with learning rate lr on (x, target) */
 int qd_unet_train_step_host(qd_unet *u, const float *x, const float *target, float lr, float *loss);
 
-/* Attach the network to a solver of the same grid, or of twice its
- * resolution (2n-1 nodes per side for an n-node network: the network then
- * sees every other level-0 node -- the multigrid's level-1 grid -- and its
- * prediction is prolongated bilinearly with the multigrid's weights; about
- * a quarter of the cost of a full-resolution network).  Mode 1 trains
+/* Attach the network to a solver of the same grid, or of twice or four
+ * times its resolution (2n-1 or 4n-3 nodes per side for an n-node network:
+ * the network then sees every other or every fourth level-0 node -- the
+ * multigrid's level-1 or level-2 grid -- and its prediction is interpolated
+ * bilinearly; each halving of the resolution cuts the cost about four
+ * times).  Mode 1 trains
  * online (one Adam step per stage solve on the change the solve made, the
- * solve itself starting from the unmodified field), mode 2 predicts (the
- * solve starts from u + prediction), mode 0 detaches.  While attached the
- * network runs on the solver's stream; destroying the solver detaches it. */
+ * solve itself starting from the unmodified field), mode 2 predicts, mode 0
+ * detaches.  In mode 2 each stage solve first measures the residual of its
+ * guess; when that misses the solve's threshold by more than the gate
+ * (qd_solver_warm_start_gate) the solve adds the network's prediction,
+ * scaled by the step that minimises the energy norm of the guess's error
+ * (so the corrected guess is never worse in that norm), and iterates from
+ * there; otherwise the network is left out.  The decision is taken on the
+ * device, inside the solve's CUDA graph.  While attached the network runs
+ * on the solver's stream; destroying the solver detaches it. */
 int qd_solver_warm_start(qd_solver *s, qd_unet *u, int mode, float lr);
+
+/* The gate of mode 2: the network corrects a solve's guess only when the
+ * guess's residual norm exceeds ratio x the solve's threshold (ratio >= 1).
+ * ratio 0 (the default): when one V-cycle would not reach the threshold from
+ * the guess -- the ratio is 1 / rho, rho the solver's running geometric
+ * mean of the residual reduction per V-cycle (measured on the device; 1
+ * until a cycle has run).  A guess one cycle from the threshold takes that
+ * cycle whatever the network adds, so the network is kept for the guesses
+ * where it can save one. */
+int qd_solver_warm_start_gate(qd_solver *s, double ratio);
 
 /* training steps taken, and the loss of the last step */
 int qd_unet_stats(qd_unet *u, long long *train_steps, float *last_loss);

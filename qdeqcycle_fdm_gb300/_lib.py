@@ -75,6 +75,7 @@ EXPORTS = [
     ("qd_unet_loss_grad_host", C.c_int, [C.c_void_p, _fp, _fp, _fp, _fp]),
     ("qd_unet_train_step_host", C.c_int, [C.c_void_p, _fp, _fp, C.c_float, _fp]),
     ("qd_solver_warm_start", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_float]),
+    ("qd_solver_warm_start_gate", C.c_int, [C.c_void_p, C.c_double]),
     ("qd_unet_stats", C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), _fp]),
     ("qd_unet_time", C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp]),
 ]
@@ -95,7 +96,7 @@ class Rk43Params(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("solves", C.c_longlong), ("vcycles", C.c_longlong), ("attempts", C.c_longlong),
                 ("steps", C.c_longlong), ("newton_iters", C.c_longlong),
-                ("kernel_launches", C.c_longlong)]
+                ("kernel_launches", C.c_longlong), ("net_solves", C.c_longlong)]
 
 
 class Tuning(C.Structure):

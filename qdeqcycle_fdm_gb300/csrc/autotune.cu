@@ -9,8 +9,9 @@
 // solver's current boundary data from a zero interior (the guess-independent
 // reference point of the relative tolerance) to the solver's tolerance, with
 // CUDA events around the solve graph on the solver's stream; the fastest is
-// kept.  u and the solve counters are restored afterwards, so tuning leaves
-// the simulation state as it found it.  The reference has no tuner: its
+// kept.  An attached network is left out of the timed solves (the tuner
+// times the multigrid).  u and the solve counters are restored afterwards,
+// so tuning leaves the simulation state as it found it.  The reference has no tuner: its
 // schedule is fixed at V(32,32) on 6 levels (odeSolver.cpp:2-4).
 #include <math.h>
 
@@ -106,6 +107,11 @@ int autotune(qd_solver *s, int reps, qd_tuning *out) {
             }
 
     Saved sv;
+    s->net_paused = true;
+    struct Resume {
+        qd_solver *s;
+        ~Resume() { s->net_paused = false; }
+    } resume{s};
     QD_CUDA(cudaMalloc(&sv.u, sizeof(double) * (size_t)d.N * d.P));
     QD_CUDA(cudaMemcpyAsync(sv.u, s->L64[0].u, sizeof(double) * (size_t)d.N * d.P, cudaMemcpyDeviceToDevice,
                             s->stream));

@@ -227,6 +227,7 @@ int qd_solver_create(int ni, int nk, double dh, const double *mu_equi, const dou
     *out = nullptr;
     QD_TRY(check_opts(opt));
     qd_solver *s = new qd_solver();
+    s->net_ratio = 0.0;   // the measured one-cycle gate
     memset((void *)s, 0, sizeof(*s));
     s->ni = ni; s->nk = nk; s->nx = ni + 2; s->nz = nk + 2; s->dh = dh;
     s->opt = *opt;
@@ -301,6 +302,7 @@ int qd_get_stats(qd_solver *s, qd_stats *st) {
     st->attempts = s->attempts;
     // host-issued kernels plus the kernels the solve graphs ran on the device
     st->steps = s->steps; st->kernel_launches = s->launches + (long long)ss.kernels;
+    st->net_solves = (long long)ss.net_solves;
     std::vector<int> it(s->nz);
     QD_CUDA(cudaMemcpy(it.data(), s->F.iters, s->nz * sizeof(int), cudaMemcpyDeviceToHost));
     long long sum = 0;

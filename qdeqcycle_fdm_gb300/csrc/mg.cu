@@ -251,8 +251,11 @@ __global__ void __launch_bounds__(BX * BY)
         }
         if (tid == 0) {
             if (dc.rel) out[1] = r0;
-            const int go = solve_begin_dev(out, dc.st, dc.rel, dc.tol, dc.n_kernels);
-            if (dc.in_graph) cudaGraphSetConditional(dc.h, go ? 1u : 0u);
+            const int go = solve_begin_dev(out, dc.st, dc.rel, dc.tol, dc.n_kernels, dc.phase, dc.net_ratio);
+            if (dc.in_graph) {
+                cudaGraphSetConditional(dc.h, go ? 1u : 0u);
+                if (dc.phase == 1) cudaGraphSetConditional(dc.h_net, dc.st->net ? 1u : 0u);
+            }
         }
     } else if (dc.mode == 2 && tid == 0) {
         const int go = solve_check_dev(out, dc.st, dc.max_cycles, dc.n_kernels);
@@ -479,6 +482,103 @@ static int smooth_t(qd_solver *s, Level<T> *Ls, int l, int nsweeps) {
             QD_LAUNCH_CHECK(s);
         }
     }
+    return QD_OK;
+}
+
+// The energy-optimal step along a correction of the guess.  With u0 the
+// guess, d = u - u0 the correction already added to u (zero on the boundary
+// columns), A x = lap(x) / h^2 the level-0 operator of the residual kernels
+// (negative definite) and r0 = f - A u0 = A e (e: the guess's error),
+// alpha = (d . r0) / (d . A d) minimises the error's energy norm
+// (e - alpha d)^T (-A) (e - alpha d) -- the Galerkin step of a one-vector
+// subspace -- so the corrected guess u0 + alpha d never has a larger error
+// in that norm than u0 (alpha = 1 for an exact correction, 0 when d . A d
+// is not negative).  The residual norm, which weights the correction's
+// high-frequency content, is not the measure: a prediction that is right in
+// the smooth components and noisy in the rough ones still saves V-cycles.
+// k_mr_dots: both sums per block, the last block adds the partials in a
+// fixed order and writes alpha; k_mr_update: u = u0 + alpha d.
+template <bool HAS_F>
+__global__ void __launch_bounds__(BX * BY)
+    k_mr_dots(View<double> v, const double *__restrict__ diag, const double *__restrict__ u0, double *partial,
+              unsigned *count, double *alpha) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j0 = blockIdx.y * (BY * RES_RPT) + threadIdx.y;
+    double ra = 0.0, aa = 0.0;
+    if (k >= 1 && k <= v.K - 2) {
+        const double *__restrict__ u = v.u;
+#pragma unroll
+        for (int i = 0; i < RES_RPT; i++) {
+            const int j = j0 + i * BY;
+            if (j < v.N) {
+                const long c = (long)j * v.P + k;
+                const long up = (j == 0) ? v.P : -(long)v.P;
+                const long dn = (j == v.N - 1) ? -(long)v.P : v.P;
+                const double a0 = u0[c - 1], a1 = u0[c + 1], a2 = u0[c + up], a3 = u0[c + dn], a4 = u0[c];
+                const double lap0 = v.cx[c - 1] * a0 + v.cx[c] * a1 + v.cz[c] * a2 + v.cz[c + v.P] * a3 - diag[c] * a4;
+                const double lapd = v.cx[c - 1] * (u[c - 1] - a0) + v.cx[c] * (u[c + 1] - a1) +
+                                    v.cz[c] * (u[c + up] - a2) + v.cz[c + v.P] * (u[c + dn] - a3) -
+                                    diag[c] * (u[c] - a4);
+                const double r0 = HAS_F ? v.f[c] - lap0 * v.inv_h2 : -lap0 * v.inv_h2;
+                const double dc = u[c] - a4;
+                ra = fma(dc, r0, ra);                 // d . r0
+                aa = fma(dc, lapd * v.inv_h2, aa);    // d . A d (< 0)
+            }
+        }
+    }
+    ra = block_sum(ra);
+    aa = block_sum(aa);
+    __shared__ bool last;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const unsigned nblk = gridDim.x * gridDim.y;
+    if (tid == 0) {
+        const unsigned b = blockIdx.y * gridDim.x + blockIdx.x;
+        partial[2 * b] = ra;
+        partial[2 * b + 1] = aa;
+        __threadfence();
+        last = atomicAdd(count, 1u) == nblk - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    ra = 0.0;
+    aa = 0.0;
+    for (unsigned i = tid; i < nblk; i += blockDim.x * blockDim.y) {
+        ra += __ldcg(partial + 2 * i);
+        aa += __ldcg(partial + 2 * i + 1);
+    }
+    ra = block_sum(ra);
+    aa = block_sum(aa);
+    if (tid == 0) {
+        const double al = ra / aa;
+        *alpha = (aa < 0.0 && isfinite(al)) ? al : 0.0;
+        *count = 0;
+    }
+}
+
+__global__ void k_mr_update(double *u, const double *u0, int N, int K, int P, const double *alpha) {
+    const int j = blockIdx.y, k = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (j >= N || k > K - 2) return;
+    const long c = (long)j * P + k;
+    const double a = *alpha;
+    u[c] = a == 0.0 ? u0[c] : u0[c] + a * (u[c] - u0[c]);   // alpha 0 also drops a non-finite correction
+}
+
+int mr_step(qd_solver *s, const double *u0) {
+    View<double> v = make_view(s, s->L64, 0);
+    dim3 blk(BX, BY), grd(cdiv(v.K, BX), cdiv(v.N, BY * RES_RPT));
+    if (2 * (long)grd.x * grd.y > s->n_partial) {
+        set_error("minimal-residual step: %u blocks exceed the partial buffer", grd.x * grd.y);
+        return QD_ERR_ARG;
+    }
+    double *alpha = s->d_scal + 3;
+    if (v.f)
+        k_mr_dots<true><<<grd, blk, 0, s->stream>>>(v, s->L64[0].diag, u0, s->d_partial, s->d_count, alpha);
+    else
+        k_mr_dots<false><<<grd, blk, 0, s->stream>>>(v, s->L64[0].diag, u0, s->d_partial, s->d_count, alpha);
+    QD_LAUNCH_CHECK(s);
+    k_mr_update<<<dim3(cdiv(v.K, 256), v.N), 256, 0, s->stream>>>(v.u, u0, v.N, v.K, v.P, alpha);
+    QD_LAUNCH_CHECK(s);
     return QD_OK;
 }
 

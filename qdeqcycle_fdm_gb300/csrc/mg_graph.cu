@@ -6,6 +6,9 @@
 //
 //   prologue   [||r0|| for the relative tolerance] -> ||r|| of the guess
 //              -> k_solve_begin: threshold, first "continue?" decision
+//   [IF        with a network in prediction mode attached, and only when
+//              the guess misses the tolerance: the network's correction
+//              of the guess, then the prologue again on the corrected one]
 //   WHILE      body: one V-cycle -> ||r|| -> k_solve_check: next decision
 //
 // In mixed precision the prologue and the body's check are folded into the
@@ -34,14 +37,21 @@ struct SolveGraph {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     qd_mg_options opt;
+    bool net = false;   // built with the network's conditional correction
+    double net_ratio = 0.0;
 };
 
 // n_kernels: kernels of the prologue, this one included; in_graph: set the
 // loop condition (otherwise the host reads st->go)
-__global__ void k_solve_begin(cudaGraphConditionalHandle h, const double *scal, SolveState *st,
-                              int rel, double tol, int n_kernels, int in_graph) {
-    const int go = solve_begin_dev(scal, st, rel, tol, n_kernels);
-    if (in_graph) cudaGraphSetConditional(h, go ? 1u : 0u);
+// (phase: see solve_begin_dev; phase 1 also sets h_net)
+__global__ void k_solve_begin(cudaGraphConditionalHandle h, cudaGraphConditionalHandle h_net, const double *scal,
+                              SolveState *st, int rel, double tol, int n_kernels, int in_graph, int phase,
+                              double net_ratio) {
+    const int go = solve_begin_dev(scal, st, rel, tol, n_kernels, phase, net_ratio);
+    if (in_graph) {
+        cudaGraphSetConditional(h, go ? 1u : 0u);
+        if (phase == 1) cudaGraphSetConditional(h_net, st->net ? 1u : 0u);
+    }
 }
 
 // n_kernels: kernels of one loop iteration, this one included
@@ -100,26 +110,40 @@ static int capture_cycle(qd_solver *s, cudaGraphConditionalHandle h, int in_grap
 // the solve's prologue: ||r0|| (relative tolerance), ||r|| of the guess and
 // the first decision; in mixed precision one kernel (the residual's last
 // block computes ||r0|| and decides), in FP64 k_r0, the norm and
-// k_solve_begin.  n_kernels counts the prologue's kernels.
-static int prologue(qd_solver *s, cudaGraphConditionalHandle h, int in_graph, long long launches0) {
+// k_solve_begin.  n_kernels counts the prologue's kernels and `extra`
+// kernels launched before it; phase as for solve_begin_dev.
+static int prologue(qd_solver *s, cudaGraphConditionalHandle h, cudaGraphConditionalHandle h_net, int in_graph,
+                    long long launches0, int extra, int phase) {
     const int rel = s->opt.tol_mode == QD_TOL_REL;
     if (s->opt.precision == QD_PREC_MIXED) {
         Decide dc{};
         dc.mode = 1;
         dc.rel = rel;
         dc.tol = s->opt.tol;
-        dc.n_kernels = (int)(s->launches - launches0) + 1;
+        dc.n_kernels = (int)(s->launches - launches0) + 1 + extra;
         dc.in_graph = in_graph;
+        dc.phase = phase;
+        dc.net_ratio = s->net_ratio;
         dc.h = h;
+        dc.h_net = h_net;
         dc.st = s->d_solve;
         return level0_norm_decide(s, dc);
     }
     if (rel) QD_TRY(r0_norm(s, 1));
     QD_TRY(level0_norm(s, 0, 0));
-    k_solve_begin<<<1, 1, 0, s->stream>>>(h, s->d_scal, s->d_solve, rel, s->opt.tol,
-                                          (int)(s->launches - launches0) + 1, in_graph);
+    k_solve_begin<<<1, 1, 0, s->stream>>>(h, h_net, s->d_scal, s->d_solve, rel, s->opt.tol,
+                                          (int)(s->launches - launches0) + 1 + extra, in_graph, phase,
+                                          s->net_ratio);
     QD_LAUNCH_CHECK(s);
     return QD_OK;
+}
+
+// the network's correction of the guess and the prologue again (the body
+// of the graph's IF node, or its eager form)
+static int corrected_prologue(qd_solver *s, cudaGraphConditionalHandle h, int in_graph, long long launches0) {
+    int nk = 0;
+    QD_TRY(warm_start_predict(s, &nk));
+    return prologue(s, h, 0, in_graph, launches0, nk, 2);
 }
 
 static int end_capture(qd_solver *s, cudaGraph_t *g, int rc) {
@@ -133,18 +157,21 @@ static int end_capture(qd_solver *s, cudaGraph_t *g, int rc) {
 
 static int build(qd_solver *s, SolveGraph *sg) {
     QD_CUDA(cudaGraphCreate(&sg->graph, 0));
-    cudaGraphConditionalHandle h;
+    cudaGraphConditionalHandle h, h_net = 0;
     QD_CUDA(cudaGraphConditionalHandleCreate(&h, sg->graph, 0, cudaGraphCondAssignDefault));
+    sg->net = warm_start_predicting(s);
+    sg->net_ratio = s->net_ratio;
+    if (sg->net) QD_CUDA(cudaGraphConditionalHandleCreate(&h_net, sg->graph, 0, cudaGraphCondAssignDefault));
     // prologue, captured into the top-level graph
     // captured launches are counted on the device each time they run, so the
     // host counter is restored after each capture
     const long long launches0 = s->launches;
     QD_CUDA(cudaStreamBeginCaptureToGraph(s->stream, sg->graph, nullptr, nullptr, 0,
                                           cudaStreamCaptureModeRelaxed));
-    int rc = prologue(s, h, 1, launches0);
+    int rc = prologue(s, h, h_net, 1, launches0, 0, sg->net ? 1 : 0);
     s->launches = launches0;
     QD_TRY(end_capture(s, nullptr, rc));
-    // the prologue is a chain: its one leaf is the loop's dependency
+    // the prologue is a chain: its one leaf is the next node's dependency
     size_t n = 0;
     QD_CUDA(cudaGraphGetNodes(sg->graph, nullptr, &n));
     std::vector<cudaGraphNode_t> nodes(n);
@@ -154,6 +181,24 @@ static int build(qd_solver *s, SolveGraph *sg) {
         size_t nout = 0;
         QD_CUDA(cudaGraphNodeGetDependentNodes(nd, nullptr, nullptr, &nout));
         if (nout == 0) leaf = nd;
+    }
+    if (sg->net) {
+        // IF the guess misses the tolerance: the network's correction and
+        // the prologue on the corrected guess (which re-sets the loop's
+        // condition)
+        cudaGraphNodeParams ip = {};
+        ip.type = cudaGraphNodeTypeConditional;
+        ip.conditional.handle = h_net;
+        ip.conditional.type = cudaGraphCondTypeIf;
+        ip.conditional.size = 1;
+        cudaGraphNode_t gate;
+        QD_CUDA(cudaGraphAddNode(&gate, sg->graph, leaf ? &leaf : nullptr, nullptr, leaf ? 1 : 0, &ip));
+        QD_CUDA(cudaStreamBeginCaptureToGraph(s->stream, ip.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                              cudaStreamCaptureModeRelaxed));
+        rc = corrected_prologue(s, h, 1, launches0);
+        s->launches = launches0;
+        QD_TRY(end_capture(s, nullptr, rc));
+        leaf = gate;
     }
     cudaGraphNodeParams cp = {};
     cp.type = cudaGraphNodeTypeConditional;
@@ -193,8 +238,17 @@ static bool eager_solve() {
 
 static int solve_eager(qd_solver *s) {
     const long long launches0 = s->launches;
-    QD_TRY(prologue(s, 0, 0, launches0));
+    const bool net = warm_start_predicting(s);
+    QD_TRY(prologue(s, 0, 0, 0, launches0, 0, net ? 1 : 0));
     s->launches = launches0;       // counted on the device, as in the graph
+    if (net) {
+        SolveState st;
+        QD_TRY(solve_state_read(s, &st));
+        if (st.net) {
+            QD_TRY(corrected_prologue(s, 0, 0, launches0));
+            s->launches = launches0;
+        }
+    }
     for (;;) {
         SolveState st;
         QD_TRY(solve_state_read(s, &st));
@@ -214,7 +268,8 @@ static int solve_eager(qd_solver *s) {
 int mg_solve_async(qd_solver *s) {
     if (eager_solve()) return solve_eager(s);
     SolveGraph *sg = static_cast<SolveGraph *>(s->solve_graph);
-    if (sg && !same_opts(sg->opt, s->opt)) {
+    if (sg && (!same_opts(sg->opt, s->opt) || sg->net != warm_start_predicting(s) ||
+               sg->net_ratio != s->net_ratio)) {
         solve_graph_free(s);
         sg = nullptr;
     }

@@ -96,14 +96,52 @@ struct SolveState {
     int go;                               // the last "run another cycle" decision
     unsigned long long total_cycles, total_solves;
     unsigned long long kernels;           // kernels the solve graphs ran
+    int net;                              // the network corrected the last solve's guess
+    unsigned long long net_solves;        // solves whose guess the network corrected
+    double log_rho;                       // running mean of log(||r|| after / before a V-cycle)
+    unsigned long long rho_samples;       // cycles in that mean
 };
+
+// ---- programmatic dependent launch ----------------------------------------
+// A kernel launched with programmatic stream serialization (launch_pdl) may
+// be scheduled while the kernel before it drains, which hides the launch
+// latency between dependent kernels.  Such a kernel calls pdl_trigger (let
+// the next kernel start launching) and pdl_wait (block until the previous
+// kernel has completed and its memory operations are visible) before it
+// touches anything the previous kernel produced or reads.  Both are no-ops
+// in a kernel launched without the attribute.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+static inline cudaError_t launch_pdl(bool pdl, void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                                     cudaStream_t st, Args &&...args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kern, static_cast<Args &&>(args)...);
+}
 
 // The solve loop's decisions, shared by the stand-alone decision kernels and
 // the reductions that fuse them: after the prologue's norms (scal[0] =
 // ||r||^2 of the guess, scal[1] = ||r0||^2 for the relative tolerance) and
 // after each cycle.  Both return "run another cycle"; the caller sets the
 // graph's loop condition from it.
-__device__ inline int solve_begin_dev(const double *scal, SolveState *st, int rel, double tol, int n_kernels) {
+// phase 0: a solve's only first decision; 1: the first decision of a solve
+// whose guess the network corrects when ||r|| of the guess exceeds
+// net_ratio x the threshold (st->net); net_ratio 0: by more than one
+// V-cycle's measured reduction, i.e. when one cycle would not reach the
+// threshold (ratio 1 / rho, rho = exp(log_rho), while no cycle has been
+// measured ratio 1); 2: the decision after that correction (the same solve)
+__device__ inline int solve_begin_dev(const double *scal, SolveState *st, int rel, double tol, int n_kernels,
+                                      int phase, double net_ratio = 1.0) {
     const double r0 = rel ? sqrt(scal[1]) : 0.0;
     const double thr = rel ? (r0 > 0.0 ? tol * r0 : tol) : tol;
     const double delta = sqrt(scal[0]);
@@ -111,7 +149,8 @@ __device__ inline int solve_begin_dev(const double *scal, SolveState *st, int re
     st->thr = thr;
     st->delta = delta;
     st->cycles = 0;
-    st->total_solves++;
+    if (phase == 2) st->net_solves++;
+    else st->total_solves++;
     st->kernels += (unsigned long long)n_kernels;
     int go = !(delta <= thr);
     if (go && !isfinite(delta)) {
@@ -119,11 +158,25 @@ __device__ inline int solve_begin_dev(const double *scal, SolveState *st, int re
         go = 0;
     }
     st->go = go;
+    if (phase == 0) st->net = 0;
+    else if (phase == 1) {
+        const double ratio = net_ratio > 0.0 ? net_ratio : (st->rho_samples ? exp(-st->log_rho) : 1.0);
+        st->net = go && !(delta <= ratio * thr);
+    }
     return go;
 }
 
 __device__ inline int solve_check_dev(const double *scal, SolveState *st, int max_cycles, int n_kernels) {
     const double delta = sqrt(scal[0]);
+    // the cycle's reduction factor, into the running mean of its log
+    // (weight 1/8 after the first eight; factors clamped to [1e-6, 1])
+    const double red = delta / st->delta;
+    if (st->delta > 0.0 && isfinite(red)) {
+        const double l = log(fmin(fmax(red, 1e-6), 1.0));
+        const double w = st->rho_samples < 8 ? 1.0 / (double)(st->rho_samples + 1) : 0.125;
+        st->log_rho += w * (l - st->log_rho);
+        st->rho_samples++;
+    }
     st->delta = delta;
     st->cycles++;
     st->total_cycles++;
@@ -143,11 +196,12 @@ __device__ inline int solve_check_dev(const double *scal, SolveState *st, int ma
 
 // a decision fused into the last block of the level-0 FP64 residual
 // reduction (mixed precision): mode 1 also computes ||r0||^2 and takes the
-// first decision, mode 2 the decision after a cycle; mode 0 none
+// first decision (phase as for solve_begin_dev; phase 1 also sets h_net to
+// the decision), mode 2 the decision after a cycle; mode 0 none
 struct Decide {
-    int mode, rel, max_cycles, n_kernels, in_graph;
-    double tol;
-    cudaGraphConditionalHandle h;
+    int mode, rel, max_cycles, n_kernels, in_graph, phase;
+    double tol, net_ratio;
+    cudaGraphConditionalHandle h, h_net;
     SolveState *st;
 };
 
@@ -204,6 +258,8 @@ struct qd_solver {
     void *tma_cache;       // tensor maps of the tile kernels (mg_fused.cu)
     void *d_tail_img[2];   // coarse-tail coefficient images, FP32 [0] and FP64 [1]
     void *unet;            // attached warm-start network (unet.cu), or null
+    bool net_paused;       // solves leave the attached network out (the autotuner's timing)
+    double net_ratio;      // the network corrects guesses with ||r|| > net_ratio x threshold
     void *history;         // ring of earlier solutions for the initial guess (history.cu), or null
     void *snapshot;        // the snapshot writer in flight (io.cu), or null
     int tail_l0;           // first level of the coarse tail
@@ -211,7 +267,7 @@ struct qd_solver {
     void *solve_graph;     // the instantiated multigrid graph (mg_graph.cu)
     qd::SolveState *d_solve, *h_solve;
     int n_partial;
-    double *d_scal;        // device scalars: [0] ||r||^2, [1] ||r0||^2, [2] totErr
+    double *d_scal;        // device scalars: [0] ||r||^2, [1] ||r0||^2, [2] totErr, [3] the step of mr_step
     double *h_scal;        // pinned mirror
     qd::DevStatus *d_status;
     qd::DevStatus *h_status;
@@ -245,6 +301,9 @@ int time_kernel(qd_solver *s, int which, int reps, double *us);
 // mg.cu: level-0 norms into d_scal[slot] (to32: FP64 residual -> FP32 rhs)
 int level0_norm(qd_solver *s, int to32, int slot);
 int level0_norm_decide(qd_solver *s, const Decide &dc);
+// u = u0 + alpha (u - u0) with the alpha that minimises the energy norm of
+// the level-0 error (the guess u0's correction u - u0 scaled optimally)
+int mr_step(qd_solver *s, const double *u0);
 int convert_f64_f32(const double *in, float *out, int n);
 int r0_norm(qd_solver *s, int slot);
 void tail_image_free(qd_solver *s);
@@ -271,6 +330,14 @@ int set_medium_gpu(int ni, int nk, const double *mu_node, double *mu_equi);
 int warm_start_before_boundary(qd_solver *s);
 int warm_start_after_boundary(qd_solver *s);
 int warm_start_after_solve(qd_solver *s);
+// true while a network in prediction mode is attached: each solve then
+// corrects its guess with warm_start_predict when the guess misses the
+// tolerance (a conditional node of the solve graph)
+bool warm_start_predicting(qd_solver *s);
+// the network's correction of the guess in u (enqueued on the solver's
+// stream, capturable); *kernels: the kernels it launched that s->launches
+// does not count
+int warm_start_predict(qd_solver *s, int *kernels);
 void warm_start_detach(qd_solver *s);
 double *warm_start_bc_buffer(qd_solver *s);
 // history.cu: initial guess from the solution history

@@ -130,15 +130,6 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float v[8]) {
     for (int i = 0; i < 8; i++) v[i] = __uint_as_float(r[i]);
 }
 
-// ---- programmatic dependent launch ----------------------------------------
-// A kernel launched with programmatic stream serialization may start while
-// the kernel before it drains.  pdl_trigger lets the next kernel start
-// launching; pdl_wait blocks until the previous kernel has completed and its
-// memory operations are visible.  Both are no-ops in a kernel launched
-// without the attribute.
-__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
-__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-
 // ---- plain mbarrier arrive (for barriers a thread, not a copy, completes) --
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");

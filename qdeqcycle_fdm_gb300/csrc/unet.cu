@@ -41,24 +41,6 @@ static constexpr int UNET_BIAS_BLOCKS = 1024;   // blocks of the bias-gradient s
 
 __host__ __device__ static inline int cdv(long a, long b) { return (int)((a + b - 1) / b); }
 
-// kernel launch, with programmatic stream serialization when pdl is set (the
-// kernel then waits for its predecessor itself, with pdl_wait)
-template <typename... KArgs, typename... Args>
-static cudaError_t launch_k(bool pdl, void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem,
-                            cudaStream_t st, Args &&...args) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = grid;
-    cfg.blockDim = block;
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = pdl ? 1 : 0;
-    return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
-}
-
 struct UGrid {
     int H, W, Wp, P;
 };
@@ -113,7 +95,7 @@ struct qd_unet {
     double last_loss;
     float lr;
     int mode;                      // 0 off, 1 train, 2 predict
-    int stride;                    // solver level-0 nodes per network pixel (1, or 2: the level-1 grid)
+    int stride;                    // solver level-0 nodes per network pixel (1; 2 or 4: the level-1 or -2 grid)
     bool pdl;                      // launch with programmatic stream serialization (inside forward())
 };
 
@@ -438,8 +420,8 @@ __global__ void __launch_bounds__(1024) k_scales(const double *u, int N, int K, 
 }
 
 // input channels at network pixel (r, q): the solver's level-0 node
-// (st (r-1), st (q-1)) -- every node (st = 1) or every other one (st = 2,
-// the network on the multigrid's level-1 grid)
+// (st (r-1), st (q-1)) -- every node (st = 1), every other one (st = 2, the
+// network on the multigrid's level-1 grid) or every fourth (st = 4, level 2)
 __global__ void k_features(const double *u, int N, int K, int P, const float *rowf, const float *scale,
                            const float *prev, __nv_bfloat16 *x0, UGrid g, int st) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -465,36 +447,50 @@ __global__ void k_features(const double *u, int N, int K, int P, const float *ro
     dst[1] = hi;
 }
 
-// u += s_bc * out on the interior columns; with st = 2 the network's
-// output on the level-1 grid is prolongated bilinearly (the multigrid's
-// prolongation weights: the coincident node, or the mean of the 2 or 4
-// neighbouring level-1 nodes)
-__global__ void k_apply(double *u, int N, int K, int P, const float *out, const float *scale, UGrid g, int st) {
-    const int j = blockIdx.y, k = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    if (j >= N || k > K - 2) return;
+// u0 = u on every column (the field the solve would have started from),
+// then u += s_bc * out on the interior columns; with st = 2 or 4 the
+// network's output on the level-1 or level-2 grid is interpolated
+// bilinearly (for st = 2 these are the multigrid's prolongation weights:
+// the coincident node, or the mean of the 2 or 4 neighbouring nodes)
+__global__ void k_apply(double *u, double *u0, int N, int K, int P, const float *out, const float *scale, UGrid g,
+                        int st) {
+    const int j = blockIdx.y, k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= N || k > K - 1) return;
+    const long c = (long)j * P + k;
+    const double uc = u[c];
+    u0[c] = uc;
+    if (k == 0 || k == K - 1) return;
     float v;
     if (st == 1) {
         v = out[(long)(j + 1) * g.Wp + (k + 1)];
     } else {
-        const int jc = j >> 1, kc = k >> 1, fy = j & 1, fx = k & 1;
+        // (jc, kc): the coarse node at or before (j, k); the weights of the
+        // next coarse row / column are fy / fx (zero on a coincident node,
+        // whose neighbour is then not read)
+        const int jc = j / st, kc = k / st;
+        const float fy = (float)(j - jc * st) / (float)st, fx = (float)(k - kc * st) / (float)st;
         const float *o = out + (long)(jc + 1) * g.Wp + (kc + 1);
-        if (!fy && !fx) v = o[0];
-        else if (fy && !fx) v = 0.5f * o[0] + 0.5f * o[g.Wp];
-        else if (!fy && fx) v = 0.5f * o[0] + 0.5f * o[1];
-        else v = 0.25f * (o[0] + o[1] + o[g.Wp] + o[g.Wp + 1]);
+        const float r0 = fx > 0.f ? (1.f - fx) * o[0] + fx * o[1] : o[0];
+        if (fy > 0.f) {
+            const float r1 = fx > 0.f ? (1.f - fx) * o[g.Wp] + fx * o[g.Wp + 1] : o[g.Wp];
+            v = (1.f - fy) * r0 + fy * r1;
+        } else {
+            v = r0;
+        }
     }
-    u[(long)j * P + k] += (double)scale[0] * (double)v;
+    u[c] = uc + (double)scale[0] * (double)v;
 }
 
 // training target: (u_solved - u_start) / s_bc on the interior (the
-// difference in FP64, then FP32)
+// difference in FP64, then FP32); zero when `ss` says the network did not
+// run on this solve (its guess met the tolerance: the solve changed nothing)
 __global__ void k_target(const double *u, const double *u0, int N, int K, int P, const float *scale,
-                         float *target, UGrid g, int st) {
+                         float *target, UGrid g, int st, const SolveState *ss) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= g.P) return;
     const int r = p / g.Wp, q = p - r * g.Wp;
     float t = 0.f;
-    if (uin(r, q, g)) {
+    if (uin(r, q, g) && (!ss || ss->net)) {
         const long c = (long)st * (r - 1) * P + (long)st * (q - 1);
         t = d2f_rne(u[c] - u0[c]) * scale[2];
     }
@@ -564,7 +560,7 @@ static int conv_launch_mt(qd_unet *u, const CUtensorMap &ta, const CUtensorMap &
                                      (int)smem));
         raised = true;
     }
-    QD_CUDA(launch_k(u->pdl, k_conv_fwd<KB, COUT, MT_>, dim3(cdv(a.P, 128 * MT)), dim3(CONV_THREADS), smem,
+    QD_CUDA(launch_pdl(u->pdl, k_conv_fwd<KB, COUT, MT_>, dim3(cdv(a.P, 128 * MT)), dim3(CONV_THREADS), smem,
                      u->stream, ta, tb, a));
     QD_CUDA(cudaPeekAtLastError());
     return QD_OK;
@@ -615,7 +611,7 @@ static int conv_rows_launch(qd_unet *u, const CUtensorMap &ta, const CUtensorMap
     }
     const int tiles = cdv(a.H + 2, R::MT) * cdv(a.Wp, 128);
     const int grid = std::min(tiles, per_sm * sm_count());
-    QD_CUDA(launch_k(u->pdl, k_conv_rows<CIN, COUT>, dim3(grid), dim3(ROWS_THREADS), R::SMEM, u->stream, ta, tb, a));
+    QD_CUDA(launch_pdl(u->pdl, k_conv_rows<CIN, COUT>, dim3(grid), dim3(ROWS_THREADS), R::SMEM, u->stream, ta, tb, a));
     QD_CUDA(cudaPeekAtLastError());
     return QD_OK;
 }
@@ -695,16 +691,16 @@ static int forward_ops(qd_unet *u) {
             QD_TRY(conv_dispatch(u, Ly.m_in, Ly.rows_fwd ? &Ly.m_in_rows : nullptr, Ly.m_w, a));
         } else if (op.k == OP_POOL) {
             const long n = (long)u->g[op.out->lvl].P * op.out->C;
-            QD_CUDA(launch_k(true, k_pool, dim3(cdv(n / 8, 256)), dim3(256), 0, u->stream, op.a->p, op.out->p,
+            QD_CUDA(launch_pdl(true, k_pool, dim3(cdv(n / 8, 256)), dim3(256), 0, u->stream, op.a->p, op.out->p,
                              u->g[op.a->lvl], u->g[op.out->lvl], op.a->C));
         } else if (op.k == OP_UP) {
             const UGrid &gc = u->g[op.a->lvl];
             const long n = (long)gc.H * gc.W * (op.a->C / 8);
-            QD_CUDA(launch_k(true, k_up, dim3(cdv(n, 256)), dim3(256), 0, u->stream, op.a->p, op.out->p, gc,
+            QD_CUDA(launch_pdl(true, k_up, dim3(cdv(n, 256)), dim3(256), 0, u->stream, op.a->p, op.out->p, gc,
                              u->g[op.out->lvl], op.a->C));
         } else {
             const long n = (long)u->g[op.out->lvl].P * op.out->C;
-            QD_CUDA(launch_k(true, k_add, dim3(cdv(n / 8, 256)), dim3(256), 0, u->stream,
+            QD_CUDA(launch_pdl(true, k_add, dim3(cdv(n / 8, 256)), dim3(256), 0, u->stream,
                              (const __nv_bfloat16 *)op.a->p, (const __nv_bfloat16 *)op.b->p, op.out->p, n));
         }
         QD_CUDA(cudaPeekAtLastError());
@@ -1009,9 +1005,11 @@ static int unet_build(qd_unet *u, unsigned long long seed) {
     u->d_prev = dalloc_z<float>(u->g[0].P, &rc);
     u->d_loss = dalloc_z<float>(1, &rc);
     u->d_scale = dalloc_z<float>(4, &rc);
-    u->d_rowf = dalloc_z<float>(2 * (2 * (size_t)u->nk - 1), &rc);   // level-0 rows of a solver twice as fine
+    // per level-0 row of the finest solver the network attaches to (four
+    // times as fine: the network on its level-2 grid)
+    u->d_rowf = dalloc_z<float>(2 * (4 * (size_t)u->nk - 3), &rc);
     u->d_status = dalloc_z<unsigned>(1, &rc);
-    u->d_bc_old = dalloc_z<double>(2 * (2 * (size_t)u->nk - 1), &rc);
+    u->d_bc_old = dalloc_z<double>(2 * (4 * (size_t)u->nk - 3), &rc);
     if (rc != QD_OK) set_error("U-Net allocation failed");
     QD_CUDA(cudaStreamSynchronize(u->stream));
     return rc;
@@ -1082,27 +1080,56 @@ int warm_start_before_boundary(qd_solver *s) {
     return QD_OK;
 }
 
-// after the new boundary data are in u: features; predict (mode 2) or keep
-// the starting field for the training target (mode 1)
-int warm_start_after_boundary(qd_solver *s) {
-    qd_unet *u = static_cast<qd_unet *>(s->unet);
-    if (!u || !u->mode) return QD_OK;
+// the input channels of the guess now in u (k_scales, k_features)
+static int features(qd_solver *s, qd_unet *u) {
     const LevelDims &d = s->dims[0];
     const UGrid &g = u->g[0];
     k_scales<<<1, 1024, 0, s->stream>>>(s->L64[0].u, d.N, d.K, d.P, u->d_bc_old, u->d_scale, u->d_rowf);
+    QD_LAUNCH_CHECK(s);
     k_features<<<cdv(g.P, 256), 256, 0, s->stream>>>(s->L64[0].u, d.N, d.K, d.P, u->d_rowf, u->d_scale,
                                                      u->d_prev, u->x0->p, g, u->stride);
     QD_LAUNCH_CHECK(s);
-    // the field the solve would start from without the network: the change
-    // the solve then makes is the training target and the next input
+    return QD_OK;
+}
+
+// after the new boundary data are in u, in training mode: the features, and
+// the starting field for the training target (the change the solve then
+// makes is the target and the next input).  In prediction mode the solve
+// itself calls warm_start_predict, and only when its guess misses the
+// tolerance.
+int warm_start_after_boundary(qd_solver *s) {
+    qd_unet *u = static_cast<qd_unet *>(s->unet);
+    if (!u || u->mode != 1) return QD_OK;
+    const LevelDims &d = s->dims[0];
+    QD_TRY(features(s, u));
     QD_CUDA(cudaMemcpyAsync(u->d_u_start, s->L64[0].u, sizeof(double) * (size_t)d.N * d.P,
                             cudaMemcpyDeviceToDevice, s->stream));
-    if (u->mode == 2) {
-        QD_TRY(forward(u));
-        k_apply<<<dim3(cdv(d.K, 256), d.N), 256, 0, s->stream>>>(s->L64[0].u, d.N, d.K, d.P, u->out32,
-                                                                 u->d_scale, g, u->stride);
-        QD_LAUNCH_CHECK(s);
+    return QD_OK;
+}
+
+bool warm_start_predicting(qd_solver *s) {
+    const qd_unet *u = static_cast<const qd_unet *>(s->unet);
+    return u && u->mode == 2 && !s->net_paused;
+}
+
+// features, the forward pass and u0 = u, u += prediction (k_apply); all on
+// the solver's stream, so the solve graph captures them into its IF node
+int warm_start_predict(qd_solver *s, int *kernels) {
+    qd_unet *u = static_cast<qd_unet *>(s->unet);
+    *kernels = 0;
+    if (!u || u->mode != 2) return QD_OK;
+    if (u->stream != s->stream) {
+        set_error("warm start: the network is attached to another solver");
+        return QD_ERR_ARG;
     }
+    const LevelDims &d = s->dims[0];
+    QD_TRY(features(s, u));
+    QD_TRY(forward(u));
+    k_apply<<<dim3(cdv(d.K, 256), d.N), 256, 0, s->stream>>>(s->L64[0].u, u->d_u_start, d.N, d.K, d.P, u->out32,
+                                                             u->d_scale, u->g[0], u->stride);
+    QD_LAUNCH_CHECK(s);
+    QD_TRY(mr_step(s, u->d_u_start));   // the prediction's energy-optimal scale: never a larger error
+    *kernels = (int)u->ops.size();   // the forward pass's, one per op (not in s->launches)
     return QD_OK;
 }
 
@@ -1114,7 +1141,8 @@ int warm_start_after_solve(qd_solver *s) {
     const LevelDims &d = s->dims[0];
     const UGrid &g = u->g[0];
     k_target<<<cdv(g.P, 256), 256, 0, s->stream>>>(s->L64[0].u, u->d_u_start, d.N, d.K, d.P, u->d_scale,
-                                                   u->target32, g, u->stride);
+                                                   u->target32, g, u->stride,
+                                                   u->mode == 2 ? s->d_solve : nullptr);
     QD_LAUNCH_CHECK(s);
     if (u->mode == 1) {
         QD_TRY(loss_and_grad(u));
@@ -1139,6 +1167,7 @@ double *warm_start_bc_buffer(qd_solver *s) {
 void warm_start_detach(qd_solver *s) {
     qd_unet *u = static_cast<qd_unet *>(s->unet);
     if (!u) return;
+    solve_graph_free(s);
     cudaFree(u->d_u_start);
     u->d_u_start = nullptr;
     u->stream = u->own_stream;
@@ -1259,9 +1288,11 @@ int qd_solver_warm_start(qd_solver *s, qd_unet *u, int mode, float lr) {
     if (u && (u->nk != s->nk || u->ni != s->ni)) {
         if (2 * u->nk - 1 == s->nk && 2 * u->ni - 1 == s->ni) {
             stride = 2;   // the network on the solver's level-1 grid
+        } else if (4 * u->nk - 3 == s->nk && 4 * u->ni - 3 == s->ni && s->opt.n_levels >= 3) {
+            stride = 4;   // on its level-2 grid
         } else {
-            set_error("qd_solver_warm_start: network grid %dx%d is neither the solver's %dx%d nor its level-1 grid",
-                      u->nk, u->ni, s->nk, s->ni);
+            set_error("qd_solver_warm_start: network grid %dx%d is not the solver's %dx%d grid, nor its level-1 "
+                      "or level-2 grid", u->nk, u->ni, s->nk, s->ni);
             return QD_ERR_ARG;
         }
     }
@@ -1278,11 +1309,21 @@ int qd_solver_warm_start(qd_solver *s, qd_unet *u, int mode, float lr) {
     QD_CUDA(cudaStreamSynchronize(u->stream));
     if (!u->d_u_start) QD_CUDA(cudaMalloc(&u->d_u_start, sizeof(double) * (size_t)s->dims[0].N * s->dims[0].P));
     if (s->unet != u) QD_CUDA(cudaMemset(u->d_prev, 0, sizeof(float) * (size_t)u->g[0].P));   // a new run
+    solve_graph_free(s);     // the solve graph holds the attached network's kernels
     u->stream = s->stream;   // the net runs on the solver's stream while attached
     u->stride = stride;
     u->mode = mode;
     u->lr = mode == 1 ? lr : u->lr;
     s->unet = u;
+    return QD_OK;
+}
+
+int qd_solver_warm_start_gate(qd_solver *s, double ratio) {
+    if (!s || !(ratio == 0.0 || ratio >= 1.0) || !isfinite(ratio)) {
+        set_error("qd_solver_warm_start_gate: ratio must be 0 or finite and >= 1");
+        return QD_ERR_ARG;
+    }
+    s->net_ratio = ratio;
     return QD_OK;
 }
 

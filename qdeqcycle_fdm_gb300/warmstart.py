@@ -79,6 +79,14 @@ class UNet:
         MODE_PREDICT or MODE_OFF)."""
         check(self.L.qd_solver_warm_start(solver.h, self.h if mode else None, mode, lr))
 
+    @staticmethod
+    def set_gate(solver, ratio: float) -> None:
+        """Prediction mode's gate: the network corrects a solve's guess only
+        when the guess's residual exceeds ratio x the solve's threshold;
+        ratio 0 (the default): when one V-cycle, at the solver's measured
+        reduction per cycle, would not reach the threshold."""
+        check(solver.L.qd_solver_warm_start_gate(solver.h, float(ratio)))
+
     def time(self, what: str = "forward", reps: int = 10):
         """(microseconds per run, tensor-core FLOPs per run) of one inference
         ("forward"), one training step without the update ("train") or the

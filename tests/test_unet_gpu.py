@@ -138,6 +138,60 @@ def test_warm_start_coupled_to_the_solver():
         assert rel(w1[k], p1[k]) < 1e-5, (k, rel(w1[k], p1[k]))
     assert abs(w1["t"] - p1["t"]) <= 1e-6 * p1["t"]
     assert c_ws < 0.95 * c_plain, (c_ws, c_plain)
+    # from the previous solution nearly every stage solve misses the
+    # tolerance, so the network corrects nearly every guess
+    assert w1["net_solves"] - w0["net_solves"] >= 0.5 * (w1["solves"] - w0["solves"])
+
+
+def test_prediction_runs_only_where_the_guess_misses():
+    """In prediction mode a solve applies the network only when its guess
+    misses the tolerance (a conditional node of the solve graph, decided on
+    the device).  With random weights (a poor, non-zero prediction): a solve
+    from an already converged u takes no cycle, leaves the network out and u
+    bit for bit; a solve from a perturbed u (boundary columns included, so
+    that the network's boundary-change inputs and output scale are not zero)
+    runs the network once, ends in another field than the same solve without
+    the network (the correction was applied) and still meets the tolerance
+    and the same solution."""
+    import dataclasses
+    from qdeqcycle_fdm_gb300 import api, config, problem
+    cfg = config.small(65)
+    mg = dataclasses.replace(cfg.mg, precision=1, surface_prolong=1, coarse_solve=1, tol=1e-9)
+    prob = problem.build_problem(cfg)
+    net = warmstart.UNet(65, 65, seed=2)
+    rng = np.random.default_rng(0)
+    net.set_params(rng.normal(scale=0.05, size=net.num_params).astype(np.float32))
+    sim = api.Simulation(prob, mg)
+    net.attach(sim.solver, warmstart.MODE_PREDICT)
+    sim.start()
+    sim.step(2)
+    s = sim.solver
+    s.ode_solve()
+    U0 = s.download_u()
+    n0 = s.stats()["net_solves"]
+    cyc, rn, r0 = s.ode_solve()
+    assert cyc == 0 and rn <= 1e-9 * r0
+    assert s.stats()["net_solves"] == n0
+    assert np.array_equal(s.download_u(), U0)
+
+    U = U0.copy()
+    U[1:-1, 1:-1] += 1e-3 * np.max(np.abs(U0)) * rng.standard_normal(U[1:-1, 1:-1].shape)
+    s.upload_u(U)
+    cyc, rn, r0 = s.ode_solve()
+    assert cyc >= 1 and rn <= 1e-9 * r0
+    assert s.stats()["net_solves"] == n0 + 1
+    got = s.download_u()
+
+    plain = api.Solver(prob.ni, prob.nk, prob.dh, prob.mu_equi, prob.mu_node, mg)
+    plain.upload_u(U)
+    cyc_p, rn_p, r0_p = plain.ode_solve()
+    ref = plain.download_u()
+    plain.close()
+    sim.close()
+    net.close()
+    assert rn_p <= 1e-9 * r0_p
+    assert not np.array_equal(got, ref)
+    assert rel(got, ref) < 1e-5
 
 
 def test_online_training_is_deterministic():
@@ -164,18 +218,21 @@ def test_online_training_is_deterministic():
     assert np.array_equal(params[0], params[1])
 
 
-def test_warm_start_on_the_level1_grid():
-    """A network on the solver's level-1 grid (33 x 33 for a 65 x 65 solver):
-    its inputs are every other level-0 node and its prediction is
-    prolongated bilinearly.  It trains on the solver's own solves, the run
-    still follows the plain run (the multigrid solves to its tolerance from
-    the predicted field), and the prediction does not cost V-cycles."""
+@pytest.mark.parametrize("n,level", [(65, 1), (129, 2)])
+def test_warm_start_on_a_coarse_grid(n, level):
+    """A 33 x 33 network on the solver's level-1 grid (65 x 65 solver) or
+    level-2 grid (129 x 129): its inputs are every other or every fourth
+    level-0 node and its prediction is interpolated bilinearly.  It trains
+    on the solver's own solves, the run still follows the plain run (the
+    multigrid solves to its tolerance from the corrected guess), and the
+    prediction does not cost V-cycles."""
     import dataclasses
     from qdeqcycle_fdm_gb300 import api, config, problem
-    cfg = config.small(65)
+    cfg = config.small(n)
     mg = dataclasses.replace(cfg.mg, precision=1, surface_prolong=1, coarse_solve=1, tol=1e-9)
     prob = problem.build_problem(cfg)
     T, K = 60, 30
+    m = (n - 1) // (1 << level) + 1
 
     def cycles(a, b):
         return (b["vcycles"] - a["vcycles"]) / max(1, b["solves"] - a["solves"])
@@ -188,7 +245,7 @@ def test_warm_start_on_the_level1_grid():
     p1 = plain.state(with_u=False)
     plain.close()
 
-    net = warmstart.UNet(33, 33, seed=1)
+    net = warmstart.UNet(m, m, seed=1)
     sim = api.Simulation(prob, mg)
     net.attach(sim.solver, warmstart.MODE_TRAIN, 1e-3)
     sim.start()
@@ -201,8 +258,10 @@ def test_warm_start_on_the_level1_grid():
     sim.close()
     net.close()
     c_plain, c_ws = cycles(p0, p1), cycles(w0, w1)
-    print(f"\nlevel-1 warm start: {steps} training steps, V-cycles per solve {c_ws:.3f} (plain {c_plain:.3f})")
+    print(f"\nlevel-{level} warm start: {steps} training steps, V-cycles per solve {c_ws:.3f} "
+          f"(plain {c_plain:.3f}), network on {w1['net_solves'] - w0['net_solves']} solves")
     assert steps == w0["solves"] and np.isfinite(loss)
+    assert w1["net_solves"] > w0["net_solves"]
     for k in ("Slip", "psi"):
         assert rel(w1[k], p1[k]) < 1e-5, (k, rel(w1[k], p1[k]))
     assert c_ws <= c_plain, (c_ws, c_plain)
