@@ -459,8 +459,9 @@ def run_ours(args):
     #   conv16   16 BF16 channels read and written: 64 B per padded pixel of
     #            the network's grid
     # Launches per step: one of each cycle kernel per V-cycle, the residual
-    # once more per solve (the guess), the convolution 4 per solve.  The
-    # dominant kernel (largest time x launches per step) is the roofline entry.
+    # once more per solve (the guess) and once more per solve the network
+    # corrected, the convolution 4 per corrected solve.  The dominant kernel
+    # (largest time x launches per step) is the roofline entry.
     peak = peaks.get("hbm_gbs", 6800.0)
     n0 = cfg.ni * cfg.nk
     n1 = ((cfg.ni - 1) // 2 + 1) * ((cfg.nk - 1) // 2 + 1)
@@ -483,13 +484,15 @@ def run_ours(args):
         kern[k] = {"us": sim.solver.time_kernel(k, REPS), "kernel": names[k]}
     cyc_step = head["vcycles"] / args.steps
     sol_step = head["solves"] / args.steps
-    per_step = {"up0": cyc_step, "down0": cyc_step, "residual": cyc_step + sol_step, "tail": cyc_step}
+    net_step = head["net_solves"] / args.steps
+    per_step = {"up0": cyc_step, "down0": cyc_step, "residual": cyc_step + sol_step + net_step,
+                "tail": cyc_step}
     if net is not None:
         net.time("conv16", 3)
         us_c, fl_c = net.time("conv16", REPS)
         kern["conv16"] = {"us": us_c, "kernel": names["conv16"],
                           "tflops": fl_c / (us_c * 1e-6) / 1e12}
-        per_step["conv16"] = 4.0 * sol_step
+        per_step["conv16"] = 4.0 * net_step
     for k, v in kern.items():
         v["launches_per_step"] = per_step[k]
         v["us_per_step"] = v["us"] * per_step[k]

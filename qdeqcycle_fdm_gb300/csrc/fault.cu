@@ -94,10 +94,14 @@ __device__ __forceinline__ double log_sinh(double y) {
 // shrinking bracket.
 __device__ double newton_v(double Ts, double Tn, double tau0, double a, double eta, double psi,
                            double V0, double Vseed, int *iters, unsigned int *flags) {
-    double x = asinh(0.5 * Vseed / V0 * exp(psi / a));
+    // the seed's x; a zero seed (the reference's, every stage after the
+    // first) gives x = +0 without the exponential and asinh while e^{psi/a}
+    // is finite, the same value the full expression gives
+    const double pa = psi / a;
+    double x = (Vseed == 0.0 && pa < 709.0) ? 0.0 : asinh(0.5 * Vseed / V0 * exp(pa));
     const double fa = a * fabs(Tn);
     const double fb = Ts + tau0;
-    const double A = 2.0 * eta * V0 * exp(-psi / a);
+    const double A = 2.0 * eta * V0 * exp(-pa);
     double lo, hi;
     if (fb >= 0.0) { lo = 0.0; hi = fb / fa; } else { lo = fb / fa; hi = 0.0; }
     if (!(x >= lo && x <= hi)) x = 0.5 * (lo + hi);
@@ -181,6 +185,8 @@ __device__ __forceinline__ void report(DevStatus *st, unsigned int flags, int no
 // :1610) and setBoundary's two Dirichlet columns (:1162-1172).
 // stage 1 copies y (the start and the post-accept refresh, :1430,1606-1614).
 __global__ void k_stage_boundary(FaultArgs A, int stage, double t, double dt, double ratio) {
+    pdl_trigger();
+    pdl_wait();
     const int k = blockIdx.x * blockDim.x + threadIdx.x + 1;
     if (k > A.nk) return;
     const FaultState &F = A.F;
@@ -204,6 +210,8 @@ __global__ void k_stage_boundary(FaultArgs A, int stage, double t, double dt, do
 
 // stress -> Newton -> aging law for one stage (odeSolver.cpp:1498-1500)
 __global__ void k_fault_stage(FaultArgs A, int stage) {
+    pdl_trigger();
+    pdl_wait();
     const int k = blockIdx.x * blockDim.x + threadIdx.x + 1;
     if (k > A.nk) return;
     const FaultState &F = A.F;
@@ -249,6 +257,7 @@ __global__ void k_dpsi(FaultArgs A, const double *psi, const double *V, double *
 
 // y3 / y4 (odeSolver.cpp:1569-1593) and computeError (:1211-1238); one block.
 __global__ void k_error(FaultArgs A, double dt, double *out) {
+    pdl_wait();
     __shared__ double s1[1024], s2[1024];
     const FaultState &F = A.F;
     double e1 = 0.0, e2 = 0.0;
@@ -331,8 +340,13 @@ void fault_free(qd_solver *s) {
     s->F = FaultState();
 }
 
+// The stage chain's kernels (boundary, history fit and guess, fault stage,
+// error estimate) are launched with programmatic stream serialization: each
+// waits for its predecessor (pdl_wait) before touching its data, and the
+// launch latency between them overlaps the predecessor's tail.
 int launch_stage_boundary(qd_solver *s, int stage, double ratio, const double *, const double *) {
-    k_stage_boundary<<<nblk(s->nk, 128), 128, 0, s->stream>>>(fargs(s), stage, s->t, s->dt, ratio);
+    QD_CUDA(launch_pdl(true, k_stage_boundary, dim3(nblk(s->nk, 128)), dim3(128), 0, s->stream, fargs(s), stage,
+                       s->t, s->dt, ratio));
     QD_LAUNCH_CHECK(s);
     return QD_OK;
 }
@@ -343,13 +357,14 @@ int launch_stage_boundary(qd_solver *s, int stage, double ratio, const double *,
 static constexpr int kNewtonBlock = 32;
 
 int launch_fault(qd_solver *s, int stage, int) {
-    k_fault_stage<<<nblk(s->nk, kNewtonBlock), kNewtonBlock, 0, s->stream>>>(fargs(s), stage);
+    QD_CUDA(launch_pdl(true, k_fault_stage, dim3(nblk(s->nk, kNewtonBlock)), dim3(kNewtonBlock), 0, s->stream,
+                       fargs(s), stage));
     QD_LAUNCH_CHECK(s);
     return QD_OK;
 }
 
 int launch_error(qd_solver *s) {
-    k_error<<<1, 1024, 0, s->stream>>>(fargs(s), s->dt, s->d_scal + 2);
+    QD_CUDA(launch_pdl(true, k_error, dim3(1), dim3(1024), 0, s->stream, fargs(s), s->dt, s->d_scal + 2));
     QD_LAUNCH_CHECK(s);
     return QD_OK;
 }

@@ -22,10 +22,13 @@
 // Device data: a ring of m level-0 FP64 fields (the last m solutions, N x P
 // each) and their boundary columns packed as [fault rows 0..N-1, far rows
 // 0..N-1].  Sixteen CTAs form the normal equations of the fit (at most 7
-// unknowns); the last one scales them to a unit diagonal, adds a 1e-12
-// ridge, solves by Cholesky and keeps the fit only if its misfit is below
-// the unfitted change; a grid then writes the guess into the interior
-// columns as a weighted sum of the stored fields.
+// unknowns; one boundary value per thread, so that the strided loads of the
+// boundary columns overlap); the last one scales them to a unit diagonal,
+// adds a 1e-12 ridge, solves by Cholesky and keeps the fit only if its
+// misfit is below the unfitted change; a grid then writes the guess into
+// the interior columns as a weighted sum of the stored fields.  Both
+// kernels use programmatic dependent launch.  (One CTA of 512 threads, four
+// values per thread and no cross-CTA hand-off, measured 8 us slower.)
 #include <math.h>
 
 #include <algorithm>
@@ -69,12 +72,14 @@ struct FitArgs {
     unsigned *count;
 };
 
-// Normal equations of the fit over the 2N boundary values, split over
-// FIT_CTAS blocks; the last block to finish sums the block partials in a
-// fixed order (deterministic) and solves.  Accumulators per boundary value:
+// Normal equations of the fit over the 2N boundary values; with more than
+// one block the last block to finish sums the block partials in a fixed
+// order (deterministic) and solves.  Accumulators per boundary value:
 // G = D^T D (upper triangle), b = D^T t, |t|^2.
 template <int ND>
 __global__ void __launch_bounds__(FIT_THREADS) k_hist_fit(FitArgs F) {
+    pdl_trigger();
+    pdl_wait();
     constexpr int NT = ND * (ND + 1) / 2, NA = NT + ND + 1;
     __shared__ double red[FIT_THREADS / 32][NA];
     __shared__ double sums[NA];
@@ -106,25 +111,35 @@ __global__ void __launch_bounds__(FIT_THREADS) k_hist_fit(FitArgs F) {
         if (lane == 0) red[warp][i] = x;
     }
     __syncthreads();
-    if (threadIdx.x < NA) {
-        double x = 0.0;
-        for (int w = 0; w < FIT_THREADS / 32; w++) x += red[w][threadIdx.x];
-        F.partial[blockIdx.x * NA + threadIdx.x] = x;
+    if (gridDim.x == 1) {
+        if (threadIdx.x < NA) {
+            double x = 0.0;
+            for (int w = 0; w < FIT_THREADS / 32; w++) x += red[w][threadIdx.x];
+            sums[threadIdx.x] = x;
+        }
+        __syncthreads();
+        if (threadIdx.x != 0) return;
+    } else {
+        if (threadIdx.x < NA) {
+            double x = 0.0;
+            for (int w = 0; w < FIT_THREADS / 32; w++) x += red[w][threadIdx.x];
+            F.partial[blockIdx.x * NA + threadIdx.x] = x;
+        }
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) is_last = atomicAdd(F.count, 1u) == gridDim.x - 1;
+        __syncthreads();
+        if (!is_last) return;
+        __threadfence();
+        if (threadIdx.x < NA) {
+            double x = 0.0;
+            for (int b = 0; b < (int)gridDim.x; b++) x += __ldcg(F.partial + b * NA + threadIdx.x);
+            sums[threadIdx.x] = x;
+        }
+        __syncthreads();
+        if (threadIdx.x != 0) return;
+        *F.count = 0;                               // ready for the next fit
     }
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) is_last = atomicAdd(F.count, 1u) == gridDim.x - 1;
-    __syncthreads();
-    if (!is_last) return;
-    __threadfence();
-    if (threadIdx.x < NA) {
-        double x = 0.0;
-        for (int b = 0; b < (int)gridDim.x; b++) x += __ldcg(F.partial + b * NA + threadIdx.x);
-        sums[threadIdx.x] = x;
-    }
-    __syncthreads();
-    if (threadIdx.x != 0) return;
-    *F.count = 0;                                   // ready for the next fit
 
     // unit-diagonal scaling, 1e-12 ridge, Cholesky
     double G[ND][ND], b[ND], sc[ND], L[ND][ND], y[ND], c[ND];
@@ -195,6 +210,7 @@ struct ApplyArgs {
 // One row per blockIdx.y, two nodes per thread.
 template <int ND>
 __global__ void k_hist_apply(ApplyArgs A) {
+    pdl_wait();
     const int row = blockIdx.y, col = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     if (col >= A.K) return;
     double c[ND], wa = 1.0;
@@ -213,7 +229,8 @@ __global__ void k_hist_apply(ApplyArgs A) {
         v.y = fma(c[k], sk.y, v.y);
     }
     double2 *dst = reinterpret_cast<double2 *>(A.u + e);
-    double2 o = *dst;
+    // only a pair holding a boundary column (or the padding) keeps part of u
+    double2 o = (col >= 1 && col + 1 <= A.K - 2) ? v : *dst;
     if (col >= 1 && col <= A.K - 2) o.x = v.x;
     if (col + 1 <= A.K - 2) o.y = v.y;
     *dst = o;
@@ -319,9 +336,9 @@ int history_guess(qd_solver *s, double *implied_bc) {
     switch (nd) {
 #define QD_HIST_CASE(n)                                                       \
     case n:                                                                   \
-        k_hist_fit<n><<<fit_ctas, FIT_THREADS, 0, s->stream>>>(F);            \
+        QD_CUDA(launch_pdl(true, k_hist_fit<n>, dim3(fit_ctas), dim3(FIT_THREADS), 0, s->stream, F)); \
         QD_LAUNCH_CHECK(s);                                                   \
-        k_hist_apply<n><<<agrid, 128, 0, s->stream>>>(A);                     \
+        QD_CUDA(launch_pdl(true, k_hist_apply<n>, agrid, dim3(128), 0, s->stream, A)); \
         QD_LAUNCH_CHECK(s);                                                   \
         break;
         QD_HIST_CASE(1) QD_HIST_CASE(2) QD_HIST_CASE(3) QD_HIST_CASE(4)

@@ -486,6 +486,8 @@ __global__ void k_apply(double *u, double *u0, int N, int K, int P, const float 
 // run on this solve (its guess met the tolerance: the solve changed nothing)
 __global__ void k_target(const double *u, const double *u0, int N, int K, int P, const float *scale,
                          float *target, UGrid g, int st, const SolveState *ss) {
+    pdl_trigger();
+    pdl_wait();
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= g.P) return;
     const int r = p / g.Wp, q = p - r * g.Wp;
@@ -1140,9 +1142,9 @@ int warm_start_after_solve(qd_solver *s) {
     if (!u || !u->mode) return QD_OK;
     const LevelDims &d = s->dims[0];
     const UGrid &g = u->g[0];
-    k_target<<<cdv(g.P, 256), 256, 0, s->stream>>>(s->L64[0].u, u->d_u_start, d.N, d.K, d.P, u->d_scale,
-                                                   u->target32, g, u->stride,
-                                                   u->mode == 2 ? s->d_solve : nullptr);
+    QD_CUDA(launch_pdl(true, k_target, dim3(cdv(g.P, 256)), dim3(256), 0, s->stream, (const double *)s->L64[0].u,
+                       (const double *)u->d_u_start, d.N, d.K, d.P, (const float *)u->d_scale, u->target32, g,
+                       u->stride, (const SolveState *)(u->mode == 2 ? s->d_solve : nullptr)));
     QD_LAUNCH_CHECK(s);
     if (u->mode == 1) {
         QD_TRY(loss_and_grad(u));
