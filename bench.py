@@ -75,6 +75,8 @@ def parse():
                         "steps first), for per-kernel profilers; prints a one-line summary")
     p.add_argument("--no-autotune", action="store_true",
                    help="keep the default smoother schedule and tiles in the runs with the history guess")
+    p.add_argument("--schedule", default=None,
+                   help="nu_pre,nu_post of the fast runs (implies --no-autotune)")
     p.add_argument("--net-gate", type=float, default=0.0,
                    help="the network corrects a stage solve's guess when the guess's residual exceeds "
                         "this multiple of the solve's threshold (0: when one V-cycle at the solver's "
@@ -237,7 +239,7 @@ def run_ours(args):
         """network nodes per side: the solver's level-0 grid, or its level-1
         grid with the prediction prolongated bilinearly"""
         return (n - 1) // (1 << args.unet_level) + 1
-    TUNE = not args.no_autotune
+    TUNE = not args.no_autotune and args.schedule is None
 
     def barrier():
         if world > 1:
@@ -339,6 +341,9 @@ def run_ours(args):
 
     mixed_cfg = config.MGConfig(**{**cfg.mg.__dict__, "precision": 1, "surface_prolong": 1,
                                    "coarse_solve": 1})
+    if args.schedule:
+        nu = [int(v) for v in args.schedule.split(",")]
+        mixed_cfg = config.MGConfig(**{**mixed_cfg.__dict__, "nu_pre": nu[0], "nu_post": nu[1]})
     fp64_cfg = config.MGConfig(**{**cfg.mg.__dict__, "precision": 0, "surface_prolong": 0})
     fp64s_cfg = config.MGConfig(**{**cfg.mg.__dict__, "precision": 0, "surface_prolong": 1,
                                    "coarse_solve": 1})
@@ -353,7 +358,8 @@ def run_ours(args):
                               "steps": args.steps, "warmup": args.warmup, "ms_per_step": run["ms"] / args.steps,
                               "vcycles_per_solve": run["vcycles"] / max(1, run["solves"]),
                               "solves_per_step": run["solves"] / args.steps,
-                              "network_corrected_solves": run["net_solves"] / max(1, run["solves"])}),
+                              "network_corrected_solves": run["net_solves"] / max(1, run["solves"]),
+                              "autotune": run["autotune"]}),
                   flush=True)
         if net is not None:
             net.close()
@@ -468,7 +474,7 @@ def run_ours(args):
     # the network's padded grid (H+2 rows x W+2 columns rounded up to 8)
     pad_px = (unet_n(cfg.nk) + 2) * ((unet_n(cfg.ni) + 2 + 7) // 8 * 8)
     tn = head["autotune"]
-    nu_pre, nu_post = (tn["nu_pre"], tn["nu_post"]) if tn else (cfg.mg.nu_pre, cfg.mg.nu_post)
+    nu_pre, nu_post = (tn["nu_pre"], tn["nu_post"]) if tn else (mixed_cfg.nu_pre, mixed_cfg.nu_post)
     algo = {"up0": (24.0 + 20.0 * nu_post) * n0 + 4.0 * n1, "down0": (16.0 + 20.0 * nu_pre) * n0 + 4.0 * n1,
             "residual": 36.0 * n0,
             "conv16": 64.0 * pad_px}
@@ -530,7 +536,7 @@ def run_ours(args):
     if rank == 0:
         guess = f"solution-history guess (last {H} solutions)" if H >= 2 else "previous-solution start"
         tn = head["autotune"]
-        sched = (tn["nu_pre"], tn["nu_post"]) if tn else (cfg.mg.nu_pre, cfg.mg.nu_post)
+        sched = (tn["nu_pre"], tn["nu_post"]) if tn else (mixed_cfg.nu_pre, mixed_cfg.nu_post)
         if tn:
             guess += f", autotuned tiles ({tn['box_down']}/{tn['box_up']}-column boxes)"
         mode = (f"learned warm start on the {guess} + FP32 cycles in FP64 refinement" if learned

@@ -259,9 +259,12 @@ int qd_rk43_set_state(qd_solver *s, const double *Slip, const double *psi,
 /* Autotuner.  Times every candidate smoother schedule (nu_pre, nu_post in
  * {1,1 2,2 3,3 4,4 1,2 2,1 2,3 3,2}) and pair of tile box widths of the
  * descending and ascending tile kernels ({64, 96, 128} columns each) on
- * `reps` solves of the solver's current boundary data from a zero interior
- * to its tolerance, keeps the fastest (options and tiles), and restores u and
- * the solve counters.  The reference's schedule is fixed (odeSolver.cpp:2-4).
+ * `reps` solves to the solver's tolerance, keeps the fastest (options and
+ * tiles), and restores u and the solve counters.  The timed solves are the
+ * run's own kind: with a solution history holding at least three solutions,
+ * its last stored solve replayed from the guess of the solutions before it
+ * (when that solve takes a V-cycle); otherwise the current boundary data
+ * from a zero interior.  The reference's schedule is fixed (odeSolver.cpp:2-4).
  * n_levels, precision and the tolerance are not changed.  out may be NULL. */
 typedef struct qd_tuning {
     int nu_pre, nu_post;       /* the schedule picked                         */
@@ -270,6 +273,8 @@ typedef struct qd_tuning {
     double us_initial;         /* the same for the settings before tuning     */
     int cycles_best, cycles_initial;   /* V-cycles of those solves            */
     int candidates;            /* settings that converged and were timed      */
+    int replayed;              /* 1: timed on the replayed history solve,
+                                  0: on solves from a zero interior          */
 } qd_tuning;
 int qd_autotune(qd_solver *s, int reps, qd_tuning *out);
 /* Staged box widths of the tile kernels (multiples of 16 in 32..256; 0: the

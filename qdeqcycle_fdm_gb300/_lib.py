@@ -102,7 +102,7 @@ class Stats(C.Structure):
 class Tuning(C.Structure):
     _fields_ = [("nu_pre", C.c_int), ("nu_post", C.c_int), ("box_up", C.c_int), ("box_down", C.c_int),
                 ("us_best", C.c_double), ("us_initial", C.c_double), ("cycles_best", C.c_int),
-                ("cycles_initial", C.c_int), ("candidates", C.c_int)]
+                ("cycles_initial", C.c_int), ("candidates", C.c_int), ("replayed", C.c_int)]
 
 
 class QdError(RuntimeError):

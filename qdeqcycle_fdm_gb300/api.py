@@ -214,8 +214,10 @@ class Solver:
 
     def autotune(self, reps=3):
         """Time the candidate smoother schedules and tile box widths on this
-        solver's problem (solves from a zero interior to its tolerance), keep
-        the fastest, restore u; returns the qd_tuning fields."""
+        solver's problem (the last stored solve replayed from the solution
+        history's guess when the history holds three solutions, else solves
+        from a zero interior; to its tolerance), keep the fastest, restore u;
+        returns the qd_tuning fields."""
         t = Tuning()
         check(self.L.qd_autotune(self.h, int(reps), C.byref(t)))
         return {f: getattr(t, f) for f, _ in Tuning._fields_}

@@ -5,11 +5,19 @@
 // level) and a pair of staged tile box widths for the descending (k_down)
 // and ascending (k_up) tile kernels; the box width sets the tile width and,
 // through the shared-memory budget of two CTAs per SM, the tile height and
-// the halo overhead.  Each candidate is timed on `reps` solves of the
-// solver's current boundary data from a zero interior (the guess-independent
-// reference point of the relative tolerance) to the solver's tolerance, with
-// CUDA events around the solve graph on the solver's stream; the fastest is
-// kept.  An attached network is left out of the timed solves (the tuner
+// the halo overhead.  Each candidate is timed on `reps` solves to the
+// solver's tolerance, with CUDA events around the solve graph on the
+// solver's stream; the fastest is kept.  The solves are those the run
+// makes: with a solution history of at least three solutions, the last
+// stored solve replayed from the history guess of the solutions before it
+// (history_replay_guess: a starting residual like the run's own, which a
+// solve clears in about one V-cycle, so per-cycle cost ranks the
+// candidates), as long as that solve takes a V-cycle with the starting
+// settings (one that starts within the tolerance times no cycle and ranks
+// nothing); otherwise the solver's current boundary data from a zero
+// interior (the guess-independent reference point of the relative
+// tolerance, several V-cycles, where the convergence rate weighs in).  An
+// attached network is left out of the timed solves (the tuner
 // times the multigrid).  u and the solve counters are restored afterwards,
 // so tuning leaves the simulation state as it found it.  The reference has no tuner: its
 // schedule is fixed at V(32,32) on 6 levels (odeSolver.cpp:2-4).
@@ -47,15 +55,21 @@ int restore_u(qd_solver *s, const Saved &sv) {
     return QD_OK;
 }
 
-// mean microseconds of one solve from a zero interior with the solver's
-// current settings; QD_OK with *us = +inf when the setting is not usable
-int time_solves(qd_solver *s, const Saved &sv, int reps, cudaEvent_t e0, cudaEvent_t e1, double *us,
-                int *cycles) {
+// the starting field of a timed solve (see the head of the file)
+int start_field(qd_solver *s, const Saved &sv, bool replay) {
+    if (replay) return history_replay_guess(s);
+    QD_TRY(restore_u(s, sv));
+    return zero_interior(s);
+}
+
+// mean microseconds of one solve with the solver's current settings; QD_OK
+// with *us = +inf when the setting is not usable
+int time_solves(qd_solver *s, const Saved &sv, bool replay, int reps, cudaEvent_t e0, cudaEvent_t e1,
+                double *us, int *cycles) {
     *us = INFINITY;
     *cycles = -1;
     // one untimed solve: builds the graph and checks that the setting converges
-    QD_TRY(restore_u(s, sv));
-    QD_TRY(zero_interior(s));
+    QD_TRY(start_field(s, sv, replay));
     int cyc = 0;
     double rn = 0.0;
     int rc = mg_solve(s, &cyc, &rn, nullptr);
@@ -63,8 +77,7 @@ int time_solves(qd_solver *s, const Saved &sv, int reps, cudaEvent_t e0, cudaEve
     QD_TRY(rc);
     double total = 0.0;
     for (int r = 0; r < reps; r++) {
-        QD_TRY(restore_u(s, sv));
-        QD_TRY(zero_interior(s));
+        QD_TRY(start_field(s, sv, replay));
         QD_CUDA(cudaEventRecord(e0, s->stream));
         QD_TRY(mg_solve_async(s));
         QD_CUDA(cudaEventRecord(e1, s->stream));
@@ -121,6 +134,17 @@ int autotune(qd_solver *s, int reps, qd_tuning *out) {
         set_error("autotune: event creation failed");
         rc = QD_ERR_CUDA;
     }
+    // replay the last stored solve where the history holds one and the
+    // replayed solve takes a cycle
+    bool replay = rc == QD_OK && history_replay_guess(s) == QD_OK;
+    if (replay) {
+        int cyc = 0;
+        double rn = 0.0;
+        const int r = mg_solve(s, &cyc, &rn, nullptr);
+        if (r == QD_OK) replay = cyc > 0;
+        else if (r == QD_ERR_NOT_CONVERGED) replay = false;
+        else rc = r;
+    }
     double best_us = INFINITY, init_us = INFINITY;
     int best_cyc = -1, init_cyc = -1, timed = 0;
     Candidate best = initial;
@@ -129,7 +153,7 @@ int autotune(qd_solver *s, int reps, qd_tuning *out) {
         if (rc != QD_OK) break;
         double us = INFINITY;
         int cyc = -1;
-        rc = time_solves(s, sv, reps, e0, e1, &us, &cyc);
+        rc = time_solves(s, sv, replay, reps, e0, e1, &us, &cyc);
         if (rc != QD_OK) break;
         if (isfinite(us)) timed++;
         if (i == 0) {
@@ -167,6 +191,7 @@ int autotune(qd_solver *s, int reps, qd_tuning *out) {
         out->cycles_best = best_cyc;
         out->cycles_initial = init_cyc;
         out->candidates = timed;
+        out->replayed = replay ? 1 : 0;
     }
     return QD_OK;
 }

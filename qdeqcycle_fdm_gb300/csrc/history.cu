@@ -308,17 +308,16 @@ static int history_slots(const History *H, int *a, int oth[HIST_ND]) {
     return nd;
 }
 
-// after the stage's boundary data are in u: replace the interior by the
-// fitted combination (no-op with fewer than two stored solutions)
-int history_guess(qd_solver *s, double *implied_bc) {
-    History *H = hist(s);
-    if (!H || H->n < 2) return QD_OK;
+// the fit of the boundary data in u by the stored solutions a (anchor) and
+// oth[0..nd), and the guess it gives in u's interior
+static int guess_from(qd_solver *s, History *H, int a, const int *oth, int nd, double *implied_bc) {
     const LevelDims &d = s->dims[0];
     FitArgs F{};
     F.u = s->L64[0].u;
     F.bc = H->bc;
     F.N = d.N; F.K = d.K; F.P = d.P;
-    const int nd = history_slots(H, &F.a, F.oth);
+    F.a = a;
+    for (int k = 0; k < HIST_ND; k++) F.oth[k] = k < nd ? oth[k] : 0;
     F.coef = H->coef;
     F.partial = H->partial;
     F.count = H->count;
@@ -348,8 +347,35 @@ int history_guess(qd_solver *s, double *implied_bc) {
             set_error("solution history: %d stored solutions", H->n);
             return QD_ERR_STATE;
     }
+    return QD_OK;
+}
+
+// after the stage's boundary data are in u: replace the interior by the
+// fitted combination (no-op with fewer than two stored solutions)
+int history_guess(qd_solver *s, double *implied_bc) {
+    History *H = hist(s);
+    if (!H || H->n < 2) return QD_OK;
+    int a, oth[HIST_ND];
+    const int nd = history_slots(H, &a, oth);
+    QD_TRY(guess_from(s, H, a, oth, nd, implied_bc));
     H->guesses++;
     return QD_OK;
+}
+
+// The last stored solve once more: u = the newest stored solution (its
+// boundary data and, as the answer, its interior), then the guess the
+// other stored solutions give for it, as the solve had started from with
+// one stored solution fewer.  The ring is left as it is.  QD_ERR_STATE
+// with fewer than three stored solutions.
+int history_replay_guess(qd_solver *s) {
+    History *H = hist(s);
+    if (!H || H->n < 3) return QD_ERR_STATE;
+    int a, oth[HIST_ND];
+    const int nd = history_slots(H, &a, oth);
+    const LevelDims &d = s->dims[0];
+    QD_CUDA(cudaMemcpyAsync(s->L64[0].u, H->u + (size_t)a * H->field, sizeof(double) * (size_t)d.N * d.P,
+                            cudaMemcpyDeviceToDevice, s->stream));
+    return guess_from(s, H, oth[0], oth + 1, nd - 1, nullptr);
 }
 
 // after a stage solve: store the solution

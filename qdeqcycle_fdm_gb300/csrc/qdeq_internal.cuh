@@ -348,6 +348,7 @@ void history_reset(qd_solver *s);
 void history_free(qd_solver *s);
 int history_last_fit(qd_solver *s, double *out, int *nd);
 bool history_will_guess(qd_solver *s);
+int history_replay_guess(qd_solver *s);
 // autotune.cu
 int autotune(qd_solver *s, int reps, qd_tuning *out);
 // io.cu

@@ -4,7 +4,8 @@
     V-cycles match the oracle to 1e-12, as with the default tiles;
   * tuning leaves the simulation as it found it (u bit for bit, the solve
     counters), keeps a setting at least as fast as the one it started from,
-    and the run continues with it.
+    and the run continues with it; with a solution history it times the
+    replayed last solve, which starts one V-cycle or so from the tolerance.
 """
 import numpy as np
 import pytest
@@ -69,7 +70,34 @@ def test_autotune_restores_the_state_and_keeps_the_faster_setting():
     assert t["us_best"] <= t["us_initial"]
     assert (t["nu_pre"], t["nu_post"]) in {(1, 1), (2, 2), (3, 3), (4, 4), (1, 2), (2, 1), (2, 3), (3, 2)}
     assert t["box_up"] in (64, 96, 128) and t["box_down"] in (64, 96, 128)
-    assert t["cycles_best"] >= 1
+    assert t["cycles_best"] >= 1 and t["replayed"] == 0
     sim.step(5)                      # the run goes on with the tuned setting
+    assert sim.state(with_u=False)["steps"] == 10
+    sim.close()
+
+
+def test_autotune_replays_the_history_solve():
+    cfg = config.small(257, mu_profile="layered", amb_perturb=0.05)
+    prob = problem.build_problem(cfg)
+    import dataclasses
+    mg = dataclasses.replace(cfg.mg, precision=1, surface_prolong=1, coarse_solve=1, tol=1e-9)
+    sim = api.Simulation(prob, mg)
+    sim.solver.set_solution_history(4)
+    sim.start()
+    sim.step(5)
+    # a tolerance the replayed solve does not start within, so that it takes
+    # cycles (a replay that takes none ranks nothing and is not used)
+    sim.solver.set_options(dataclasses.replace(mg, tol=1e-12))
+    before = sim.state()
+    t = sim.solver.autotune(2)
+    after = sim.state()
+    assert t["replayed"] == 1
+    assert np.array_equal(before["U"], after["U"])
+    for k in ("solves", "vcycles", "steps", "attempts"):
+        assert before[k] == after[k], k
+    # the replayed solve starts from a history guess: a few cycles, against
+    # the many of a solve from a zero interior
+    assert 1 <= t["cycles_best"] <= 5 and t["us_best"] <= t["us_initial"]
+    sim.step(5)
     assert sim.state(with_u=False)["steps"] == 10
     sim.close()
