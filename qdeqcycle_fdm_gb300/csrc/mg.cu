@@ -186,6 +186,8 @@ template <bool HAS_F>
 __global__ void __launch_bounds__(BX * BY)
     k_residual64_to32(View<double> v, const double *__restrict__ diag, float *f32, double *partial,
                       unsigned *count, double *out, Decide dc) {
+    pdl_trigger();
+    pdl_wait();   // launched with programmatic serialization: the previous kernel's data first
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j0 = blockIdx.y * (BY * RES_RPT) + threadIdx.y;
     const float nih2 = -(float)v.inv_h2;
@@ -590,11 +592,11 @@ int level0_norm_decide(qd_solver *s, const Decide &dc) {
     View<double> v = make_view(s, s->L64, 0);
     dim3 blk(BX, BY), grd(cdiv(v.K, BX), cdiv(v.N, BY * RES_RPT));
     if (v.f)
-        k_residual64_to32<true><<<grd, blk, 0, s->stream>>>(v, s->L64[0].diag, s->L32[0].f, s->d_partial,
-                                                             s->d_count, s->d_scal, dc);
+        QD_CUDA(launch_pdl(true, k_residual64_to32<true>, grd, blk, 0, s->stream, v, (const double *)s->L64[0].diag,
+                           s->L32[0].f, s->d_partial, s->d_count, s->d_scal, dc));
     else
-        k_residual64_to32<false><<<grd, blk, 0, s->stream>>>(v, s->L64[0].diag, s->L32[0].f, s->d_partial,
-                                                              s->d_count, s->d_scal, dc);
+        QD_CUDA(launch_pdl(true, k_residual64_to32<false>, grd, blk, 0, s->stream, v,
+                           (const double *)s->L64[0].diag, s->L32[0].f, s->d_partial, s->d_count, s->d_scal, dc));
     QD_LAUNCH_CHECK(s);
     return QD_OK;
 }

@@ -182,6 +182,8 @@ __device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned b
 
 template <typename T, bool ALLS>
 __global__ void __launch_bounds__(NT_TAIL) k_tail(TailArgs<T> a) {
+    pdl_trigger();
+    pdl_wait();   // launched with programmatic serialization: the previous kernel's data first
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bar;
     __shared__ TV<T> V[QD_MAXLEV];   // per-level views, read by every thread
@@ -519,8 +521,8 @@ static int launch_down(qd_solver *s, Level<T> *Ls, int l, int S, int zero_u) {
     const TileMaps *maps = nullptr;
     QD_TRY(tile_maps<T>(s, Ls, l, W, BH, &maps));
     QD_TRY(set_smem(k_down<T>, smem));
-    k_down<T><<<dim3(ntk, ntj), NT, smem, s->stream>>>(g, c, *maps, CH, CW, ntj, ntk, S, zero_u,
-                                                       &s->d_status->flags);
+    QD_CUDA(launch_pdl(true, k_down<T>, dim3(ntk, ntj), dim3(NT), smem, s->stream, g, c, *maps, CH, CW, ntj, ntk,
+                       S, zero_u, &s->d_status->flags));
     QD_LAUNCH_CHECK(s);
     return QD_OK;
 }
@@ -545,9 +547,9 @@ static int launch_up(qd_solver *s, Level<T> *Ls, int l, int S, int prolong, int 
     const TileMaps *maps = nullptr;
     QD_TRY(tile_maps<T>(s, Ls, l, W, BH, &maps));
     QD_TRY(set_smem(k_up<T, MODE>, smem));
-    k_up<T, MODE><<<dim3(ntk, ntj), NT, smem, s->stream>>>(g, c, *maps, TH, TW, ntj, ntk, S, prolong,
-                                                         s->opt.surface_prolong, zero_u, s->d_partial,
-                                                         u64, P64, &s->d_status->flags);
+    QD_CUDA(launch_pdl(true, k_up<T, MODE>, dim3(ntk, ntj), dim3(NT), smem, s->stream, g, c, *maps, TH, TW, ntj,
+                       ntk, S, prolong, s->opt.surface_prolong, zero_u, s->d_partial, u64, P64,
+                       &s->d_status->flags));
     QD_LAUNCH_CHECK(s);
     if (nblocks) *nblocks = ntj * ntk;
     return QD_OK;
@@ -720,10 +722,10 @@ static int launch_tail(qd_solver *s, Level<T> *Ls, int lt) {
     const size_t smem = prefix + work + kSmemSlack;
     if (prefix == img) {   // every array in shared memory
         QD_TRY(set_smem(k_tail<T, true>, smem));
-        k_tail<T, true><<<1, NT_TAIL, smem, s->stream>>>(ta);
+        QD_CUDA(launch_pdl(true, k_tail<T, true>, dim3(1), dim3(NT_TAIL), smem, s->stream, ta));
     } else {
         QD_TRY(set_smem(k_tail<T, false>, smem));
-        k_tail<T, false><<<1, NT_TAIL, smem, s->stream>>>(ta);
+        QD_CUDA(launch_pdl(true, k_tail<T, false>, dim3(1), dim3(NT_TAIL), smem, s->stream, ta));
     }
     QD_LAUNCH_CHECK(s);
     return QD_OK;

@@ -179,6 +179,8 @@ template <typename T>
 __global__ void __launch_bounds__(NT, 2)
     k_down(LvArgs<T> g, LvArgs<T> c, const __grid_constant__ TileMaps maps, int CH, int CW, int ntj,
            int ntk, int S, int zero_u, unsigned *status) {
+    pdl_trigger();
+    pdl_wait();   // launched with programmatic serialization: the previous kernel's data first
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bar;
     unsigned char *smem = align_smem128(smem_raw);
@@ -247,6 +249,8 @@ __global__ void __launch_bounds__(NT, 2)
     k_up(LvArgs<T> g, LvArgs<T> c, const __grid_constant__ TileMaps maps, int TH, int TW, int ntj,
          int ntk, int S, int prolong, int surface, int zero_u, double *partial, double *u64, int P64,
          unsigned *status) {
+    pdl_trigger();
+    pdl_wait();   // launched with programmatic serialization: the previous kernel's data first
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bar;
     unsigned char *smem = align_smem128(smem_raw);
