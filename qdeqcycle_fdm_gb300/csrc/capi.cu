@@ -108,9 +108,10 @@ static int stage(qd_solver *s, int st, double ratio) {
     QD_TRY(history_guess(s, warm_start_bc_buffer(s)));   // no-op unless enabled
     QD_TRY(warm_start_after_boundary(s));
     QD_TRY(mg_solve_async(s));
-    QD_TRY(history_push(s));
     QD_TRY(warm_start_after_solve(s));
-    return launch_fault(s, st, 0);
+    CopyJob push;
+    QD_TRY(history_push_job(s, &push));   // stored by the fault stage's extra blocks
+    return launch_fault(s, st, push);
 }
 
 static int rk_start(qd_solver *s) {

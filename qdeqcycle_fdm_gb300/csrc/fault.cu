@@ -208,10 +208,45 @@ __global__ void k_stage_boundary(FaultArgs A, int stage, double t, double dt, do
     row[A.K - 1] = 0.50 * F.Vini * (t + ratio * dt) + F.SlipShift[k];
 }
 
-// stress -> Newton -> aging law for one stage (odeSolver.cpp:1498-1500)
-__global__ void k_fault_stage(FaultArgs A, int stage) {
+// Blocks past the fault nodes' copy the solved u into a history slot: the
+// Newton chains leave the SMs nearly idle, so the copy rides along instead
+// of taking a launch of its own.  Rows are dealt round-robin to the copy
+// blocks, 16-byte pairs across the block's threads, four pairs in flight
+// per thread.  The pitch P is even, so every pair is 16-byte aligned.
+__device__ __forceinline__ void copy_rows(const CopyJob &J, int blk, int nblk) {
+    constexpr int U = 4;
+    const int step = 2 * (int)blockDim.x;
+    for (int row = blk; row < J.N; row += nblk) {
+        const size_t r0 = (size_t)row * J.P;
+        for (int c0 = 2 * (int)threadIdx.x; c0 < J.P; c0 += U * step) {
+            double2 v[U];
+#pragma unroll
+            for (int i = 0; i < U; i++) {
+                const int c = c0 + i * step;
+                if (c < J.P) v[i] = *reinterpret_cast<const double2 *>(J.src + r0 + c);
+            }
+#pragma unroll
+            for (int i = 0; i < U; i++) {
+                const int c = c0 + i * step;
+                if (c >= J.P) break;
+                *reinterpret_cast<double2 *>(J.dst + r0 + c) = v[i];
+                if (c == 0) J.bc[row] = v[i].x;
+                if (c == J.K - 1) J.bc[J.N + row] = v[i].x;
+                if (c + 1 == J.K - 1) J.bc[J.N + row] = v[i].y;
+            }
+        }
+    }
+}
+
+// stress -> Newton -> aging law for one stage (odeSolver.cpp:1498-1500);
+// blocks fault_blocks.. store u into the solution history (job)
+__global__ void k_fault_stage(FaultArgs A, int stage, CopyJob job, int fault_blocks) {
     pdl_trigger();
     pdl_wait();
+    if ((int)blockIdx.x >= fault_blocks) {
+        copy_rows(job, (int)blockIdx.x - fault_blocks, (int)gridDim.x - fault_blocks);
+        return;
+    }
     const int k = blockIdx.x * blockDim.x + threadIdx.x + 1;
     if (k > A.nk) return;
     const FaultState &F = A.F;
@@ -356,9 +391,14 @@ int launch_stage_boundary(qd_solver *s, int stage, double ratio, const double *,
 // packing four warps onto each of nk/128 SMs' FP64 pipes.
 static constexpr int kNewtonBlock = 32;
 
-int launch_fault(qd_solver *s, int stage, int) {
-    QD_CUDA(launch_pdl(true, k_fault_stage, dim3(nblk(s->nk, kNewtonBlock)), dim3(kNewtonBlock), 0, s->stream,
-                       fargs(s), stage));
+// copy blocks of the fault-stage launch: eight 32-thread blocks per SM
+static constexpr int kCopyBlocks = 1216;
+
+int launch_fault(qd_solver *s, int stage, const CopyJob &job) {
+    const int fb = nblk(s->nk, kNewtonBlock);
+    const int cb = job.src ? kCopyBlocks : 0;
+    QD_CUDA(launch_pdl(true, k_fault_stage, dim3(fb + cb), dim3(kNewtonBlock), 0, s->stream, fargs(s), stage, job,
+                       fb));
     QD_LAUNCH_CHECK(s);
     return QD_OK;
 }

@@ -241,18 +241,6 @@ __global__ void k_hist_apply(ApplyArgs A) {
     }
 }
 
-// copy the solved u into a ring slot and pack its boundary columns
-__global__ void k_hist_push(const double *u, double *dst, double *bc, int N, int K, int P) {
-    const int row = blockIdx.y, col = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
-    if (col >= P) return;
-    const size_t e = (size_t)row * P + col;
-    const double2 v = *reinterpret_cast<const double2 *>(u + e);
-    *reinterpret_cast<double2 *>(dst + e) = v;
-    if (col == 0) bc[row] = v.x;
-    if (col == K - 1) bc[N + row] = v.x;
-    if (col + 1 == K - 1) bc[N + row] = v.y;
-}
-
 void history_free(qd_solver *s) {
     History *H = hist(s);
     if (!H) return;
@@ -378,15 +366,20 @@ int history_replay_guess(qd_solver *s) {
     return guess_from(s, H, oth[0], oth + 1, nd - 1, nullptr);
 }
 
-// after a stage solve: store the solution
-int history_push(qd_solver *s) {
+// after a stage solve: the copy of the solution into the ring, for the
+// fault stage's launch to carry out (launch_fault)
+int history_push_job(qd_solver *s, CopyJob *job) {
+    *job = CopyJob{};
     History *H = hist(s);
     if (!H) return QD_OK;
     const LevelDims &d = s->dims[0];
     const int slot = H->head;
-    k_hist_push<<<dim3((d.P / 2 + 127) / 128, d.N), 128, 0, s->stream>>>(
-        s->L64[0].u, H->u + (size_t)slot * H->field, H->bc + (size_t)slot * 2 * d.N, d.N, d.K, d.P);
-    QD_LAUNCH_CHECK(s);
+    job->src = s->L64[0].u;
+    job->dst = H->u + (size_t)slot * H->field;
+    job->bc = H->bc + (size_t)slot * 2 * d.N;
+    job->N = d.N;
+    job->K = d.K;
+    job->P = d.P;
     H->head = (H->head + 1) % H->m;
     if (H->n < H->m) H->n++;
     return QD_OK;

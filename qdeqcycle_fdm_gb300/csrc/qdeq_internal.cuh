@@ -317,7 +317,17 @@ int fault_alloc(qd_solver *s);
 void fault_free(qd_solver *s);
 int launch_stage_boundary(qd_solver *s, int stage, double ratio, const double *slip_dev,
                           const double *psi_dev);
-int launch_fault(qd_solver *s, int stage, int compute_stress_only);
+// a copy of the solved level-0 u into a slot of the solution history
+// (history_push_job), run by extra CTAs of the fault-stage kernel
+struct CopyJob {
+    const double *src = nullptr;   // null: no copy
+    double *dst = nullptr;         // N x P field
+    double *bc = nullptr;          // its boundary columns, [fault rows, far rows]
+    int N = 0, K = 0, P = 0;
+};
+// the stage's stress, Newton and aging law (k_fault_stage); with job.src
+// set the same launch also stores u into the solution history
+int launch_fault(qd_solver *s, int stage, const CopyJob &job);
 int launch_error(qd_solver *s);
 int launch_commit(qd_solver *s);
 int launch_stress(qd_solver *s);
@@ -343,7 +353,10 @@ double *warm_start_bc_buffer(qd_solver *s);
 // history.cu: initial guess from the solution history
 int history_set(qd_solver *s, int m);
 int history_guess(qd_solver *s, double *implied_bc);
-int history_push(qd_solver *s);
+// after a stage solve: the store of the solution into the ring as a copy
+// job for the next kernel that takes one (the ring's slot is claimed now);
+// job->src stays null without a history
+int history_push_job(qd_solver *s, CopyJob *job);
 void history_reset(qd_solver *s);
 void history_free(qd_solver *s);
 int history_last_fit(qd_solver *s, double *out, int *nd);
