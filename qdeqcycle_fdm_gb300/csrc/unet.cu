@@ -1290,7 +1290,7 @@ int qd_solver_warm_start(qd_solver *s, qd_unet *u, int mode, float lr) {
     if (u && (u->nk != s->nk || u->ni != s->ni)) {
         if (2 * u->nk - 1 == s->nk && 2 * u->ni - 1 == s->ni) {
             stride = 2;   // the network on the solver's level-1 grid
-        } else if (4 * u->nk - 3 == s->nk && 4 * u->ni - 3 == s->ni && s->opt.n_levels >= 3) {
+        } else if (4 * u->nk - 3 == s->nk && 4 * u->ni - 3 == s->ni) {
             stride = 4;   // on its level-2 grid
         } else {
             set_error("qd_solver_warm_start: network grid %dx%d is not the solver's %dx%d grid, nor its level-1 "
