@@ -7,8 +7,10 @@
 //   prologue   [||r0|| for the relative tolerance] -> ||r|| of the guess
 //              -> k_solve_begin: threshold, first "continue?" decision
 //   [IF        with a network in prediction mode attached, and only when
-//              the guess misses the tolerance: the network's correction
-//              of the guess, then the prologue again on the corrected one]
+//              the guess misses the tolerance by more than the gate (one
+//              V-cycle's measured reduction by default): the network's
+//              correction of the guess, then the prologue again on the
+//              corrected one]
 //   WHILE      body: one V-cycle -> ||r|| -> k_solve_check: next decision
 //
 // In mixed precision the prologue and the body's check are folded into the
@@ -183,9 +185,9 @@ static int build(qd_solver *s, SolveGraph *sg) {
         if (nout == 0) leaf = nd;
     }
     if (sg->net) {
-        // IF the guess misses the tolerance: the network's correction and
-        // the prologue on the corrected guess (which re-sets the loop's
-        // condition)
+        // IF the guess misses the tolerance by more than the gate: the
+        // network's correction and the prologue on the corrected guess
+        // (which re-sets the loop's condition)
         cudaGraphNodeParams ip = {};
         ip.type = cudaGraphNodeTypeConditional;
         ip.conditional.handle = h_net;

@@ -483,7 +483,8 @@ __global__ void k_apply(double *u, double *u0, int N, int K, int P, const float 
 
 // training target: (u_solved - u_start) / s_bc on the interior (the
 // difference in FP64, then FP32); zero when `ss` says the network did not
-// run on this solve (its guess met the tolerance: the solve changed nothing)
+// run on this solve (u_start is then not this solve's starting field: the
+// gate keeps it only when the network corrects the guess)
 __global__ void k_target(const double *u, const double *u0, int N, int K, int P, const float *scale,
                          float *target, UGrid g, int st, const SolveState *ss) {
     pdl_trigger();
