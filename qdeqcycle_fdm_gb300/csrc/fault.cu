@@ -109,8 +109,11 @@ __device__ double newton_v(double Ts, double Tn, double tau0, double a, double e
     int it = 0;
     bool done = false, phase2 = false;
     while (it < itmax) {
-        const double fy = A * sinh(x) + fa * x - fb;
-        const double df = A * cosh(x) + fa;
+        // sinh(0) = 0 and cosh(0) = 1 exactly: the first step from the
+        // reference's zero seed needs neither function
+        const bool x0 = x == 0.0;
+        const double fy = A * (x0 ? 0.0 : sinh(x)) + fa * x - fb;
+        const double df = A * (x0 ? 1.0 : cosh(x)) + fa;
         const double d = -fy / (df + 1e-100);
         const double xn = x + d;
         if (!isnan(fy)) {
