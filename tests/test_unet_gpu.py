@@ -163,6 +163,12 @@ def test_prediction_runs_only_where_the_guess_misses():
     net.set_params(rng.normal(scale=0.05, size=net.num_params).astype(np.float32))
     sim = api.Simulation(prob, mg)
     net.attach(sim.solver, warmstart.MODE_PREDICT)
+    from qdeqcycle_fdm_gb300._lib import QdError
+    for bad in (0.5, -1.0, float("nan"), float("inf")):
+        with pytest.raises(QdError):
+            warmstart.UNet.set_gate(sim.solver, bad)
+    warmstart.UNet.set_gate(sim.solver, 30.0)
+    warmstart.UNet.set_gate(sim.solver, 0.0)      # back to the measured one-cycle gate
     sim.start()
     sim.step(2)
     s = sim.solver
