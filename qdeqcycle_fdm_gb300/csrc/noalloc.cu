@@ -20,9 +20,13 @@ namespace qd {
 namespace {
 
 constexpr int NA_BX = 32, NA_BY = 8;           // the solver's residual block shape
-// 129 x 513 blocks of 32 x 8 cover a 4097 x 4097 grid; the last slot holds
-// the total.  69,633 doubles = 544 KB per GPU.
-constexpr int NOALLOC_MAX_PARTIALS = 69632;
+// The largest grid is 4097 x 4097 nodes (rows and columns each checked):
+// ceil(4097 / 32) = 129 block columns x ceil(4097 / 8) = 513 block rows =
+// 66,177 partial sums, and one more slot for the total: 66,178 doubles =
+// 529,424 bytes (517 KB) per GPU.
+constexpr int NOALLOC_MAX_N = 4097;
+constexpr int NOALLOC_MAX_PARTIALS = ((NOALLOC_MAX_N + NA_BX - 1) / NA_BX) * ((NOALLOC_MAX_N + NA_BY - 1) / NA_BY);
+static_assert(NOALLOC_MAX_PARTIALS == 66177, "129 x 513 blocks");
 
 static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_MAX_PARTIALS + 1];
 
@@ -76,7 +80,10 @@ __global__ void k_noalloc_total(const double *partial, int n, double *out) {
 }
 
 // The array's device address for the current device, looked up once per
-// device (host code cannot use the symbol itself as a device pointer).
+// device (host code cannot use the symbol itself as a device pointer) and
+// kept for the life of the process.  A cudaDeviceReset reloads the module,
+// which may move the array, so calls after a reset of a device that already
+// ran this entry point are not supported.
 int scratch_for_current_device(double **out) {
     int dev = 0;
     QD_CUDA(cudaGetDevice(&dev));
@@ -104,13 +111,13 @@ extern "C" int qd_residual_norm_noalloc(const double *u, const double *cx, const
         set_error("qd_residual_norm_noalloc: bad arguments (nk=%d ni=%d pitch=%d)", nk, ni, pitch);
         return QD_ERR_ARG;
     }
-    const int gx = (ni + NA_BX - 1) / NA_BX, gy = (nk + NA_BY - 1) / NA_BY;
-    const long nb = (long)gx * gy;
-    if (nb > NOALLOC_MAX_PARTIALS) {
-        set_error("qd_residual_norm_noalloc: a %d x %d grid needs %ld partial sums; the static "
-                  "scratch holds %d (grids up to 4097 x 4097)", nk, ni, nb, NOALLOC_MAX_PARTIALS);
+    if (nk > NOALLOC_MAX_N || ni > NOALLOC_MAX_N) {
+        set_error("qd_residual_norm_noalloc: a %d x %d grid is larger than the static scratch "
+                  "allows (at most %d rows and %d columns)", nk, ni, NOALLOC_MAX_N, NOALLOC_MAX_N);
         return QD_ERR_ARG;
     }
+    const int gx = (ni + NA_BX - 1) / NA_BX, gy = (nk + NA_BY - 1) / NA_BY;
+    const long nb = (long)gx * gy;     // <= NOALLOC_MAX_PARTIALS by the check above
     double *scratch = nullptr;
     QD_TRY(scratch_for_current_device(&scratch));
     cudaStream_t st = static_cast<cudaStream_t>(stream);

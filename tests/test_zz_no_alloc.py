@@ -67,6 +67,9 @@ def test_noalloc_rejects_grids_beyond_its_scratch(gpu_lib):
     L = _lib.load()
     out = C.c_double(0.0)
     dummy = C.c_void_p(8)      # never dereferenced: the size check comes first
-    rc = L.qd_residual_norm_noalloc(dummy, dummy, dummy, 8193, 8193, 8224, 1.0, None, C.byref(out))
-    assert rc == _lib.QD_ERR_ARG
-    assert b"4097" in L.qd_last_error()
+    # too many rows and columns; and a grid whose block count would fit but
+    # whose columns exceed 4097
+    for nk, ni, pitch in ((8193, 8193, 8224), (4097, 4300, 4320), (5000, 129, 160)):
+        rc = L.qd_residual_norm_noalloc(dummy, dummy, dummy, nk, ni, pitch, 1.0, None, C.byref(out))
+        assert rc == _lib.QD_ERR_ARG, (nk, ni)
+        assert b"4097" in L.qd_last_error()
