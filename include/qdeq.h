@@ -49,6 +49,12 @@ extern "C" {
 #define QD_PREC_MIXED 1         /* FP32 V-cycles inside FP64 iterative
                                    refinement; FP64 residual and update      */
 
+/* Ceiling on the V-cycles of one solve run as a CUDA graph when max_cycles
+ * is <= 0: the graph's loop is decided on the device, where no host check
+ * could stop a solve whose tolerance is out of reach (an absolute tolerance
+ * below the round-off floor of a large grid, or a refinement that stalls). */
+#define QD_SOLVE_GRAPH_MAX_CYCLES 10000
+
 typedef struct qd_solver qd_solver;
 
 /* Multigrid schedule.  The reference hard-codes n_levels = 6, V(32,32) with
@@ -62,7 +68,10 @@ typedef struct qd_mg_options {
     int tol_mode;     /* QD_TOL_ABS or QD_TOL_REL                            */
     double tol;
     int max_cycles;   /* V-cycles per solve before QD_ERR_NOT_CONVERGED
-                         (<= 0: no cap, as the reference)                    */
+                         (<= 0: no cap in the host-driven loop, as the
+                         reference; a solve run as a CUDA graph, the
+                         default, loops on the device and stops after
+                         QD_SOLVE_GRAPH_MAX_CYCLES instead)                 */
     int precision;    /* QD_PREC_FP64 or QD_PREC_MIXED                       */
     int surface_prolong; /* 0: as prolongate_kernel (odeSolver.cpp:1034), the
                          last row (the free surface) gets no coarse-grid
@@ -114,6 +123,19 @@ void qd_default_options(qd_mg_options *opt);
 int qd_solver_create(int ni, int nk, double dh, const double *mu_equi,
                      const double *mu_node, const qd_mg_options *opt,
                      qd_solver **out);
+/* The same on a grid stretched in depth (no counterpart in the reference,
+ * whose grid is uniform, coord.cpp:18,27): z = z(zeta) with the
+ * computational coordinate zeta uniform, spacing dh like x, and the
+ * operator div(mu grad u) in its conservative mapped form
+ *   J d/dx(mu du/dx) + d/dzeta((mu / J) du/dzeta),   J = dz/dzeta,
+ * i.e. x-face moduli mu J and z-face moduli mu / J on the uniform
+ * computational grid.  jrow: J at every staggered row of mu_equi (2nz-1
+ * values: even rows at nodes, odd rows at faces, the ghost rows mirrored),
+ * all positive; NULL gives qd_solver_create.  The fault stress (a derivative
+ * in x) and everything else are unchanged. */
+int qd_solver_create_mapped(int ni, int nk, double dh, const double *mu_equi,
+                            const double *mu_node, const double *jrow,
+                            const qd_mg_options *opt, qd_solver **out);
 int qd_solver_destroy(qd_solver *s);
 int qd_solver_set_options(qd_solver *s, const qd_mg_options *opt);
 int qd_get_stats(qd_solver *s, qd_stats *st);
@@ -166,6 +188,18 @@ int qd_mg_residual_norm(qd_solver *s, double *rnorm);
 #define QD_KERNEL_TAIL     3   /* single-CTA coarse tail */
 int qd_mg_time_kernel(qd_solver *s, int kernel, int reps, double *us);
 
+/* Test hook for the bounded waits of the shared-memory staging pipelines
+ * (every mbarrier wait of the multigrid tile kernels and the U-Net's
+ * convolutions gives up after a fixed number of polls instead of spinning
+ * forever): one kernel on the solver's stream waits on an mbarrier that
+ * nothing completes, gives up after `polls` polls (1 .. 4,194,304, the
+ * pipelines' own limit), records the timeout in the solver's status word and
+ * returns.  The call then reports it as a solver call does after a staging
+ * wait gave up: QD_ERR_CUDA, with qd_last_error() naming the staging.  The
+ * CUDA context stays usable; the status word stays set until the next
+ * qd_rk43_start.  No counterpart in the reference. */
+int qd_probe_bounded_wait(qd_solver *s, int polls);
+
 /* The binary64 -> binary32 rounding (to nearest, ties to even) that the
  * mixed-precision residual kernel performs on the device's integer pipes,
  * applied to n host values (a device round trip), so that tests can hold it
@@ -182,9 +216,9 @@ int qd_convert_f64_to_f32(const double *in, float *out, int n);
  * are DEVICE arrays the caller owns, with a row pitch of `pitch` doubles;
  * dh is the grid spacing; the work runs on `stream` (a cudaStream_t; NULL
  * for the default stream) and *rnorm (host) receives the norm.
- * The block partial sums live in a file-scope device array of 69,633
- * doubles (544 KB) that every GPU using this library keeps until the
- * process exits; grids beyond 4097 x 4097 nodes are rejected with
+ * The block partial sums live in a file-scope device array of 66,178
+ * doubles (517 KB) that every GPU using this library keeps until the
+ * process exits; grids of more than 4097 rows or 4097 columns are rejected with
  * QD_ERR_ARG.  The first call on each device looks up that array's device
  * address, so make it before any stream capture.  All calls share the
  * array: calls that overlap on the GPU (two streams, two host threads)
@@ -234,6 +268,19 @@ int qd_cal_dpsi(qd_solver *s, const double *psi, const double *V, double *dpsi);
 int qd_rk43_start(qd_solver *s, const qd_rk43_params *p, const double *Slip,
                   const double *psi);
 int qd_rk43_step(qd_solver *s, int nsteps, int *steps_done);
+/* Restart from the fault state alone (a compact checkpoint: Slip and psi,
+ * nz arrays, and the loop's scalars t, dt, errA0, errA1 and the accepted
+ * step count it): the state an accepted step leaves behind is Slip, psi,
+ * t, dt and the error history, and everything else follows from them.  Sets
+ * the boundary data from Slip at t, solves from the device u as it stands
+ * (upload a guess first, e.g. the last known u or zero), then takes the
+ * stress, Newton (from the zero seed) and aging law -- the refresh solve of
+ * a commit (odeSolver.cpp:1605-1619) -- and keeps dt; the next qd_rk43_step
+ * continues from there.  The solution history is cleared.  No counterpart
+ * in the reference, which always starts from t = 0. */
+int qd_rk43_resume(qd_solver *s, const qd_rk43_params *p, const double *Slip,
+                   const double *psi, double t, double dt, double errA0,
+                   double errA1, int it);
 /* Batched ensemble: advance n independent, started solvers (any grids and
  * parameters, each with its own adaptive dt) by nsteps accepted steps each,
  * interleaving their GPU work: every instance's attempt (stages 2-6 and the

@@ -64,8 +64,10 @@ def lib():
         L.qo_sim_set_U.argtypes = [C.c_void_p, _dp]
         L.qo_sim_set_surface_prolong.argtypes = [C.c_void_p, C.c_int]
         L.qo_sim_set_coarse_solve.argtypes = [C.c_void_p, C.c_int]
+        L.qo_sim_set_metric.argtypes = [C.c_void_p, _dp]
         L.qo_sim_start.argtypes = [C.c_void_p]
         L.qo_sim_step.argtypes = [C.c_void_p]
+        L.qo_sim_resume.argtypes = [C.c_void_p, _dp, _dp] + [C.c_double] * 4 + [C.c_int]
         L.qo_sim_get.argtypes = [C.c_void_p] + [_dp] * 6
         L.qo_sim_scalars.argtypes = [C.c_void_p, _dp, C.POINTER(C.c_longlong)]
         L.qo_sim_set_scalars.argtypes = [C.c_void_p] + [C.c_double] * 4 + [C.c_int]
@@ -119,7 +121,8 @@ class _QoMg(C.Structure):
     _fields_ = [("n_levels", C.c_int), ("nu_pre", C.c_int), ("nu_post", C.c_int),
                 ("nu_coarse", C.c_int), ("N", C.c_int * 16), ("K", C.c_int * 16),
                 ("fc", C.c_int * 16), ("DH", C.c_double * 16), ("nx", C.c_int),
-                ("mu", _dp), ("res", _dp * 16), ("res2", _dp * 16), ("err2", _dp * 16),
+                ("mu", _dp), ("mux", _dp), ("muz", _dp), ("own_x", _dp), ("own_z", _dp),
+                ("res", _dp * 16), ("res2", _dp * 16), ("err2", _dp * 16),
                 ("delta", _dp), ("rowsum", _dp), ("surface_prolong", C.c_int),
                 ("coarse_solve", C.c_int)]
 
@@ -128,7 +131,7 @@ class Multigrid:
     """The reference's multigrid (odeSolver.cpp:652-1147) on the CPU."""
 
     def __init__(self, ni, nk, dh, mu_equi, n_levels=6, nu_pre=32, nu_post=32, nu_coarse=32,
-                 surface_prolong=0, coarse_solve=0):
+                 surface_prolong=0, coarse_solve=0, jrow=None):
         L = lib()
         self._mu = np.ascontiguousarray(mu_equi, dtype=np.float64)
         self.m = _QoMg()
@@ -138,6 +141,9 @@ class Multigrid:
             raise ValueError("bad multigrid configuration")
         self.m.surface_prolong = int(surface_prolong)
         self.m.coarse_solve = int(coarse_solve)
+        if jrow is not None:
+            self._jrow = np.ascontiguousarray(jrow, dtype=np.float64)
+            L.qo_mg_set_metric(C.byref(self.m), nk, _p(self._jrow))
         self.ni, self.nk = ni, nk
         self.shapes = [(self.m.N[l], self.m.K[l]) for l in range(n_levels)]
 
@@ -263,6 +269,10 @@ class Simulation:
         L.qo_sim_set_U(self.h, _p(np.ascontiguousarray(prob.U)))
         L.qo_sim_set_surface_prolong(self.h, int(surface_prolong))
         L.qo_sim_set_coarse_solve(self.h, int(coarse_solve))
+        jrow = getattr(prob, "jrow", None)
+        if jrow is not None:          # a grid stretched in depth
+            self._keep.append(np.ascontiguousarray(jrow, dtype=np.float64))
+            L.qo_sim_set_metric(self.h, _p(self._keep[-1]))
 
     def __del__(self):
         try:
@@ -292,3 +302,73 @@ class Simulation:
 
     def set_scalars(self, t, dt, errA0, errA1, it):
         lib().qo_sim_set_scalars(self.h, t, dt, errA0, errA1, it)
+
+    def set_params(self, tmax, ini_dt, mindt, maxdt, totTol, maxNumSteps):
+        lib().qo_sim_set_params(self.h, tmax, ini_dt, mindt, maxdt, totTol, int(maxNumSteps))
+
+    def set_U(self, U):
+        lib().qo_sim_set_U(self.h, _p(np.ascontiguousarray(U, dtype=np.float64)))
+
+    def resume(self, ck, U=None):
+        """Restart from a fault-state checkpoint (a dict with Slip, psi, t, dt,
+        errA0, errA1, it): the refresh solve from U (default: the current U)
+        and the fault update that end an accepted step."""
+        if U is not None:
+            self.set_U(U)
+        return lib().qo_sim_resume(self.h, _p(np.ascontiguousarray(ck["Slip"], dtype=np.float64)),
+                                   _p(np.ascontiguousarray(ck["psi"], dtype=np.float64)),
+                                   float(ck["t"]), float(ck["dt"]), float(ck["errA0"]),
+                                   float(ck["errA1"]), int(ck["it"]))
+
+
+# --------------------------------------------------------------------------
+# the reference's own GPU multigrid (refgpu.c over _ref/ref_kernels.cubin)
+# --------------------------------------------------------------------------
+_REFGPU_PATH = os.path.join(_HERE, "_build", "librefgpu.so")
+_SOLVE_HOOK = C.CFUNCTYPE(C.c_int, C.c_void_p, _dp, C.c_int, C.c_int, _dp)
+
+
+def refgpu_available() -> bool:
+    return os.path.exists(_REFGPU_PATH) and os.path.exists(REF_KERNELS_CUBIN)
+
+
+class RefGpuMultigrid:
+    """The reference's multigrid() on the GPU: its unmodified kernels with
+    the host sequencing restated in C (odeSolver.cpp:652-755, 1101-1147):
+    6 levels, V(32,32), u up and down every solve, a blocking norm per
+    V-cycle.  attach(sim) makes an oracle Simulation call it for every
+    elliptic solve, so the RK43 loop runs as the reference program does:
+    host code around GPU multigrid.  rel = 1 stops at tol * ||r0|| (the
+    relative tolerance of the solvers it is compared with), rel = 0 at the
+    reference's absolute tol."""
+
+    def __init__(self, prob, rel=1, tol=1e-9):
+        L = C.CDLL(_REFGPU_PATH)
+        L.rg_create.restype = C.c_void_p
+        L.rg_create.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_double, _dp, C.c_int, C.c_double,
+                                C.c_char_p, C.c_int]
+        L.rg_free.argtypes = [C.c_void_p]
+        L.rg_stats.argtypes = [C.c_void_p, C.POINTER(C.c_longlong)]
+        self.L = L
+        self._mu = np.ascontiguousarray(prob.mu_equi, dtype=np.float64)
+        err = C.create_string_buffer(256)
+        self.h = L.rg_create(REF_KERNELS_CUBIN.encode(), prob.ni, prob.nk, prob.dh, _p(self._mu), int(rel),
+                             float(tol), err, 256)
+        if not self.h:
+            raise RuntimeError(f"reference GPU multigrid: {err.value.decode()}")
+        self.hook = C.cast(L.rg_solve, C.c_void_p).value
+
+    def attach(self, sim):
+        fn = lib().qo_sim_set_solve_hook
+        fn.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        fn(sim.h, self.hook, self.h)
+
+    def stats(self):
+        v = (C.c_longlong * 2)()
+        self.L.rg_stats(self.h, v)
+        return {"solves": v[0], "vcycles": v[1]}
+
+    def close(self):
+        if self.h:
+            self.L.rg_free(self.h)
+            self.h = None

@@ -57,6 +57,8 @@ int qo_mg_init(qo_mg *m, int ni, int nk, double dh, const double *mu_equi,
     m->nu_coarse = nu_coarse;
     m->nx = ni + 2 * LEND;
     m->mu = mu_equi;
+    m->mux = mu_equi;
+    m->muz = mu_equi;
     int n = nk, k = ni;
     double h = dh;
     m->N[0] = n; m->K[0] = k; m->fc[0] = 1; m->DH[0] = dh;
@@ -75,7 +77,30 @@ int qo_mg_init(qo_mg *m, int ni, int nk, double dh, const double *mu_equi,
     return 0;
 }
 
+/* A grid stretched in depth: the x-face moduli times J and the z-face
+ * moduli over J, J = dz/dzeta given per staggered row of mu_equi (the
+ * conservative mapped form J d/dx(mu du/dx) + d/dzeta((mu/J) du/dzeta) on
+ * the uniform computational grid).  The reference's grid is uniform
+ * (coord.cpp:18,27); this is the project's own discretisation. */
+void qo_mg_set_metric(qo_mg *m, int nk, const double *jrow) {
+    free(m->own_x); free(m->own_z);
+    m->own_x = m->own_z = NULL;
+    m->mux = m->muz = m->mu;
+    if (!jrow) return;
+    const long W = 2L * m->nx - 1, R = 2L * (nk + 2 * LEND) - 1;
+    m->own_x = (double *)malloc((size_t)(W * R) * sizeof(double));
+    m->own_z = (double *)malloc((size_t)(W * R) * sizeof(double));
+    for (long r = 0; r < R; r++)
+        for (long c = 0; c < W; c++) {
+            m->own_x[r * W + c] = m->mu[r * W + c] * jrow[r];
+            m->own_z[r * W + c] = m->mu[r * W + c] / jrow[r];
+        }
+    m->mux = m->own_x;
+    m->muz = m->own_z;
+}
+
 void qo_mg_free(qo_mg *m) {
+    free(m->own_x); free(m->own_z);
     for (int i = 0; i < QO_MAXLEV; i++) {
         free(m->res[i]); free(m->res2[i]); free(m->err2[i]);
     }
@@ -110,7 +135,7 @@ static inline void mu_index(const qo_mg *m, int level, int j, int k,
 void qo_rbgs(const qo_mg *m, double *u, const double *f, int level, int phase) {
     const int N = m->N[level], K = m->K[level];
     const double DH2 = m->DH[level] * m->DH[level];
-    const double *mu = m->mu;
+    const double *mx = m->mux, *mz = m->muz;   /* x-face / z-face moduli */
 #pragma omp parallel for schedule(static)
     for (int j = 0; j < N; j++) {
         const int kstart = ((j + 1) % 2 == phase) ? 1 : 2;
@@ -123,28 +148,28 @@ void qo_rbgs(const qo_mg *m, double *u, const double *f, int level, int phase) {
             if (j == 0) {
                 const double nb = u[c + K];
                 if (level == 0) {   /* :792-800 */
-                    val = (RELAX / (mu[i1] + mu[i2] + mu[i3] + mu[i4])) *
-                              (mu[i1] * uW + mu[i2] * uE + mu[i3] * nb + mu[i4] * nb - DH2 * fv) +
+                    val = (RELAX / (mx[i1] + mx[i2] + mz[i3] + mz[i4])) *
+                              (mx[i1] * uW + mx[i2] * uE + mz[i3] * nb + mz[i4] * nb - DH2 * fv) +
                           (1.00 - RELAX) * uc;
                 } else {            /* :830-838 */
-                    val = (RELAX / (mu[i1] + mu[i2] + mu[i4] + mu[i4])) *
-                              (mu[i1] * uW + mu[i2] * uE + mu[i4] * nb + mu[i4] * nb - DH2 * fv) +
+                    val = (RELAX / (mx[i1] + mx[i2] + mz[i4] + mz[i4])) *
+                              (mx[i1] * uW + mx[i2] * uE + mz[i4] * nb + mz[i4] * nb - DH2 * fv) +
                           (1.00 - RELAX) * uc;
                 }
             } else if (j == N - 1) {
                 const double nb = u[c - K];
                 if (level == 0) {   /* :801-809 */
-                    val = (RELAX / (mu[i1] + mu[i2] + mu[i3] + mu[i4])) *
-                              (mu[i1] * uW + mu[i2] * uE + mu[i3] * nb + mu[i4] * nb - DH2 * fv) +
+                    val = (RELAX / (mx[i1] + mx[i2] + mz[i3] + mz[i4])) *
+                              (mx[i1] * uW + mx[i2] * uE + mz[i3] * nb + mz[i4] * nb - DH2 * fv) +
                           (1.00 - RELAX) * uc;
                 } else {            /* :839-847 */
-                    val = (RELAX / (mu[i1] + mu[i2] + mu[i3] + mu[i3])) *
-                              (mu[i1] * uW + mu[i2] * uE + mu[i3] * nb + mu[i3] * nb - DH2 * fv) +
+                    val = (RELAX / (mx[i1] + mx[i2] + mz[i3] + mz[i3])) *
+                              (mx[i1] * uW + mx[i2] * uE + mz[i3] * nb + mz[i3] * nb - DH2 * fv) +
                           (1.00 - RELAX) * uc;
                 }
             } else {                /* :810-818, :848-856 */
-                val = (RELAX / (mu[i1] + mu[i2] + mu[i3] + mu[i4])) *
-                          (mu[i1] * uW + mu[i2] * uE + mu[i3] * u[c - K] + mu[i4] * u[c + K] - DH2 * fv) +
+                val = (RELAX / (mx[i1] + mx[i2] + mz[i3] + mz[i4])) *
+                          (mx[i1] * uW + mx[i2] * uE + mz[i3] * u[c - K] + mz[i4] * u[c + K] - DH2 * fv) +
                       (1.00 - RELAX) * uc;
             }
             u[c] = val;
@@ -157,7 +182,7 @@ void qo_rbgs(const qo_mg *m, double *u, const double *f, int level, int phase) {
 void qo_residual(const qo_mg *m, double *r, const double *u, const double *f, int level) {
     const int N = m->N[level], K = m->K[level];
     const double DH2 = m->DH[level] * m->DH[level];
-    const double *mu = m->mu;
+    const double *mx = m->mux, *mz = m->muz;   /* x-face / z-face moduli */
 #pragma omp parallel for schedule(static)
     for (int j = 0; j < N; j++) {
         for (int k = 1; k < K - 1; k++) {
@@ -169,24 +194,24 @@ void qo_residual(const qo_mg *m, double *r, const double *u, const double *f, in
             if (j == 0) {
                 const double nb = u[c + K];
                 if (level == 0) {
-                    val = fv - (mu[i1] * uW + mu[i2] * uE + mu[i3] * nb + mu[i4] * nb -
-                                (mu[i1] + mu[i2] + mu[i3] + mu[i4]) * uc) / DH2;
+                    val = fv - (mx[i1] * uW + mx[i2] * uE + mz[i3] * nb + mz[i4] * nb -
+                                (mx[i1] + mx[i2] + mz[i3] + mz[i4]) * uc) / DH2;
                 } else {
-                    val = fv - (mu[i1] * uW + mu[i2] * uE + mu[i4] * nb + mu[i4] * nb -
-                                (mu[i1] + mu[i2] + mu[i4] + mu[i4]) * uc) / DH2;
+                    val = fv - (mx[i1] * uW + mx[i2] * uE + mz[i4] * nb + mz[i4] * nb -
+                                (mx[i1] + mx[i2] + mz[i4] + mz[i4]) * uc) / DH2;
                 }
             } else if (j == N - 1) {
                 const double nb = u[c - K];
                 if (level == 0) {
-                    val = fv - (mu[i1] * uW + mu[i2] * uE + mu[i3] * nb + mu[i4] * nb -
-                                (mu[i1] + mu[i2] + mu[i3] + mu[i4]) * uc) / DH2;
+                    val = fv - (mx[i1] * uW + mx[i2] * uE + mz[i3] * nb + mz[i4] * nb -
+                                (mx[i1] + mx[i2] + mz[i3] + mz[i4]) * uc) / DH2;
                 } else {
-                    val = fv - (mu[i1] * uW + mu[i2] * uE + mu[i3] * nb + mu[i3] * nb -
-                                (mu[i1] + mu[i2] + mu[i3] + mu[i3]) * uc) / DH2;
+                    val = fv - (mx[i1] * uW + mx[i2] * uE + mz[i3] * nb + mz[i3] * nb -
+                                (mx[i1] + mx[i2] + mz[i3] + mz[i3]) * uc) / DH2;
                 }
             } else {
-                val = fv - (mu[i1] * uW + mu[i2] * uE + mu[i3] * u[c - K] + mu[i4] * u[c + K] -
-                            (mu[i1] + mu[i2] + mu[i3] + mu[i4]) * uc) / DH2;
+                val = fv - (mx[i1] * uW + mx[i2] * uE + mz[i3] * u[c - K] + mz[i4] * u[c + K] -
+                            (mx[i1] + mx[i2] + mz[i3] + mz[i4]) * uc) / DH2;
             }
             r[c] = val;
         }
@@ -272,7 +297,7 @@ void qo_smooth(const qo_mg *m, double *u, const double *f, int level, int nsweep
 static void qo_coarse_solve(const qo_mg *m, double *u, const double *f, int level) {
     const int N = m->N[level], K = m->K[level], KI = K - 2, n = N * KI;
     const double DH2 = m->DH[level] * m->DH[level];
-    const double *mu = m->mu;
+    const double *mx = m->mux, *mz = m->muz;   /* x-face / z-face moduli */
     double *A = (double *)calloc((size_t)n * (n + 1), sizeof(double));
 #define AA(r, c) A[(size_t)(r) * (n + 1) + (c)]
     for (int j = 0; j < N; j++)
@@ -280,14 +305,14 @@ static void qo_coarse_solve(const qo_mg *m, double *u, const double *f, int leve
             long i1, i2, i3, i4;
             mu_index(m, level, j, k, &i1, &i2, &i3, &i4);
             double mN, mS;
-            if (j == 0) { mN = (level == 0) ? mu[i3] : mu[i4]; mS = mu[i4]; }
-            else if (j == N - 1) { mN = mu[i3]; mS = (level == 0) ? mu[i4] : mu[i3]; }
-            else { mN = mu[i3]; mS = mu[i4]; }
+            if (j == 0) { mN = (level == 0) ? mz[i3] : mz[i4]; mS = mz[i4]; }
+            else if (j == N - 1) { mN = mz[i3]; mS = (level == 0) ? mz[i4] : mz[i3]; }
+            else { mN = mz[i3]; mS = mz[i4]; }
             const int row = j * KI + (k - 1);
             const int jn = (j == 0) ? 1 : j - 1, js = (j == N - 1) ? N - 2 : j + 1;
-            AA(row, row) -= (mu[i1] + mu[i2] + mN + mS) / DH2;
-            if (k - 1 >= 1) AA(row, row - 1) += mu[i1] / DH2;
-            if (k + 1 <= KI) AA(row, row + 1) += mu[i2] / DH2;
+            AA(row, row) -= (mx[i1] + mx[i2] + mN + mS) / DH2;
+            if (k - 1 >= 1) AA(row, row - 1) += mx[i1] / DH2;
+            if (k + 1 <= KI) AA(row, row + 1) += mx[i2] / DH2;
             AA(row, jn * KI + (k - 1)) += mN / DH2;
             AA(row, js * KI + (k - 1)) += mS / DH2;
             AA(row, n) = f[(long)j * K + k];
@@ -790,7 +815,14 @@ struct qo_sim {
     double tol;
     long long solves, vcycles, attempts, newton_iters;
     int status;
+    qo_solve_hook hook;     /* replaces qo_multigrid in sim_solve when set */
+    void *hook_ctx;
 };
+
+void qo_sim_set_solve_hook(qo_sim *s, qo_solve_hook fn, void *ctx) {
+    s->hook = fn;
+    s->hook_ctx = ctx;
+}
 
 static double *dz(size_t n) { return (double *)calloc(n, sizeof(double)); }
 
@@ -852,6 +884,7 @@ void qo_sim_set_params(qo_sim *s, double tmax, double ini_dt, double mindt,
 }
 
 void qo_sim_set_surface_prolong(qo_sim *s, int v) { s->mg.surface_prolong = v; }
+void qo_sim_set_metric(qo_sim *s, const double *jrow) { qo_mg_set_metric(&s->mg, s->nk, jrow); }
 void qo_sim_set_coarse_solve(qo_sim *s, int v) { s->mg.coarse_solve = v; }
 
 void qo_sim_set_U(qo_sim *s, const double *U) {
@@ -862,7 +895,8 @@ void qo_sim_set_U(qo_sim *s, const double *U) {
 static int sim_solve(qo_sim *s) {
     qo_pack(s->ni, s->nk, s->U, s->u);
     double rn;
-    const int cyc = qo_multigrid(&s->mg, s->u, s->f, s->tol_mode, s->tol, s->max_cycles, &rn, NULL);
+    const int cyc = s->hook ? s->hook(s->hook_ctx, s->u, s->ni, s->nk, &rn)
+                            : qo_multigrid(&s->mg, s->u, s->f, s->tol_mode, s->tol, s->max_cycles, &rn, NULL);
     qo_unpack(s->ni, s->nk, s->u, s->U);
     qo_extend_crew(s->ni, s->nk, s->U);
     s->solves++;
@@ -890,6 +924,30 @@ int qo_sim_start(qo_sim *s) {
         s->kslip[1][k] = s->Slip[k];
         s->kpsi[1][k] = s->psi[k];
     }
+    qo_set_boundary(s->ni, s->nk, s->U, s->kslip[1], s->SlipShift, s->Vini, s->t, 0.0, s->dt);
+    sim_solve(s);
+    return sim_fault(s, s->kpsi[1], s->fV[1], s->fdpsi[1]);
+}
+
+/* Restart from the fault state an accepted step leaves behind (Slip, psi,
+ * t, dt, the error history, the step count): zero Newton seeds as after the
+ * commit (odeSolver.cpp:1605-1614), then the commit's refresh solve and
+ * fault update (:1615-1619) from the current U as the guess. */
+int qo_sim_resume(qo_sim *s, const double *Slip, const double *psi, double t, double dt,
+                  double errA0, double errA1, int it) {
+    const size_t nzb = (size_t)s->nz * sizeof(double);
+    memcpy(s->Slip, Slip, nzb);
+    memcpy(s->psi, psi, nzb);
+    for (int st = 1; st <= 6; st++) {
+        memset(s->kslip[st], 0, nzb); memset(s->kpsi[st], 0, nzb);
+        memset(s->fV[st], 0, nzb); memset(s->fdpsi[st], 0, nzb);
+    }
+    for (int k = 1; k <= s->nk; k++) {
+        s->kslip[1][k] = s->Slip[k];
+        s->kpsi[1][k] = s->psi[k];
+    }
+    s->t = t; s->dt = dt; s->errA[0] = errA0; s->errA[1] = errA1; s->it = it;
+    s->status = 0;
     qo_set_boundary(s->ni, s->nk, s->U, s->kslip[1], s->SlipShift, s->Vini, s->t, 0.0, s->dt);
     sim_solve(s);
     return sim_fault(s, s->kpsi[1], s->fV[1], s->fdpsi[1]);

@@ -34,6 +34,9 @@ typedef struct qo_mg {
     double DH[QO_MAXLEV];
     int nx;                 /* K0 + 2*LEND: half-grid width is 2*nx-1         */
     const double *mu;       /* mu_equi (borrowed)                             */
+    const double *mux, *muz;  /* the moduli the x- and z-faces read: mu, or
+                               mu J and mu / J on a stretched grid          */
+    double *own_x, *own_z;  /* their storage when a metric is set            */
     double *res[QO_MAXLEV], *res2[QO_MAXLEV], *err2[QO_MAXLEV];
     double *delta;          /* level-0 residual buffer (delta_res)            */
     double *rowsum;         /* per-row partial sums for a deterministic norm  */
@@ -44,6 +47,9 @@ typedef struct qo_mg {
 int  qo_mg_init(qo_mg *m, int ni, int nk, double dh, const double *mu_equi,
                 int n_levels, int nu_pre, int nu_post, int nu_coarse);
 void qo_mg_free(qo_mg *m);
+/* Depth metric J = dz/dzeta per staggered row of mu_equi (2(nk+2)-1 values;
+ * NULL: uniform). */
+void qo_mg_set_metric(qo_mg *m, int nk, const double *jrow);
 
 /* single kernels, restated (odeSolver.cpp:757-1043) */
 void qo_rbgs(const qo_mg *m, double *u, const double *f, int level, int phase);
@@ -120,9 +126,23 @@ void qo_sim_set_params(qo_sim *s, double tmax, double ini_dt, double mindt,
                        double maxdt, double totTol, int maxNumSteps);
 void qo_sim_set_U(qo_sim *s, const double *U);       /* ghosted nx*nz */
 void qo_sim_set_surface_prolong(qo_sim *s, int v);
+void qo_sim_set_metric(qo_sim *s, const double *jrow);
 void qo_sim_set_coarse_solve(qo_sim *s, int v);
 /* The pre-loop part of RK43 (odeSolver.cpp:1363, 1428-1439). */
 int  qo_sim_start(qo_sim *s);
+/* The elliptic solve of ode_solve() by another implementation: called with
+ * the packed compact u (nk rows x ni columns, host memory; columns 0 and
+ * ni-1 the Dirichlet data) in place of qo_multigrid, it solves u in place
+ * and returns the V-cycles it took (and the final norm in *rnorm).  Used to
+ * run the reference's own GPU multigrid kernels under this RK43 loop, as
+ * the reference's ode_solve() does (odeSolver.cpp:605-720). */
+typedef int (*qo_solve_hook)(void *ctx, double *u, int ni, int nk, double *rnorm);
+void qo_sim_set_solve_hook(qo_sim *s, qo_solve_hook fn, void *ctx);
+/* Restart from the fault state alone (Slip, psi and the loop's scalars):
+ * the refresh solve and fault update that end an accepted step
+ * (odeSolver.cpp:1605-1619), from the current U as the guess. */
+int  qo_sim_resume(qo_sim *s, const double *Slip, const double *psi, double t,
+                   double dt, double errA0, double errA1, int it);
 /* One pass of the outer while-loop body (odeSolver.cpp:1462-1636). */
 int  qo_sim_step(qo_sim *s);
 /* Full state read-back.  Any pointer may be NULL.  V is f1.V_f. */

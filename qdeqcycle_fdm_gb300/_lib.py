@@ -26,6 +26,8 @@ EXPORTS = [
     ("qd_default_options", None, [C.c_void_p]),
     ("qd_solver_create", C.c_int, [C.c_int, C.c_int, C.c_double, _dp, _dp, C.c_void_p,
                                    C.POINTER(C.c_void_p)]),
+    ("qd_solver_create_mapped", C.c_int, [C.c_int, C.c_int, C.c_double, _dp, _dp, _dp, C.c_void_p,
+                                          C.POINTER(C.c_void_p)]),
     ("qd_solver_destroy", C.c_int, [C.c_void_p]),
     ("qd_solver_set_options", C.c_int, [C.c_void_p, C.c_void_p]),
     ("qd_get_stats", C.c_int, [C.c_void_p, C.c_void_p]),
@@ -50,6 +52,9 @@ EXPORTS = [
     ("qd_cal_dpsi", C.c_int, [C.c_void_p, _dp, _dp, _dp]),
     ("qd_rk43_start", C.c_int, [C.c_void_p, C.c_void_p, _dp, _dp]),
     ("qd_rk43_step", C.c_int, [C.c_void_p, C.c_int, _ip]),
+    ("qd_rk43_resume", C.c_int, [C.c_void_p, C.c_void_p, _dp, _dp, C.c_double, C.c_double, C.c_double,
+                                 C.c_double, C.c_int]),
+    ("qd_probe_bounded_wait", C.c_int, [C.c_void_p, C.c_int]),
     ("qd_ensemble_step", C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_int, _ip]),
     ("qd_rk43_get_state", C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp, _dp]),
     ("qd_rk43_get_scalars", C.c_int, [C.c_void_p, _dp, _ip]),

@@ -73,14 +73,17 @@ def set_medium(ni: int, nk: int, mu_node: np.ndarray) -> np.ndarray:
 class Solver:
     """One device-resident solver: multigrid hierarchy + fault state."""
 
-    def __init__(self, ni, nk, dh, mu_equi, mu_node, mg: MGConfig):
+    def __init__(self, ni, nk, dh, mu_equi, mu_node, mg: MGConfig, jrow=None):
+        """jrow: the depth metric of a stretched grid, J per staggered row of
+        mu_equi (problem.depth_metric); None: the uniform grid."""
         self.L = _lib.load()
         self.ni, self.nk, self.nx, self.nz = ni, nk, ni + 2, nk + 2
         self.h = C.c_void_p()
         opt = mg_options(mg)
-        check(self.L.qd_solver_create(ni, nk, dh, _p(np.ascontiguousarray(mu_equi)),
-                                      _p(np.ascontiguousarray(mu_node)), C.byref(opt),
-                                      C.byref(self.h)))
+        jr = None if jrow is None else _p(np.ascontiguousarray(jrow, dtype=np.float64))
+        check(self.L.qd_solver_create_mapped(ni, nk, dh, _p(np.ascontiguousarray(mu_equi)),
+                                             _p(np.ascontiguousarray(mu_node)), jr, C.byref(opt),
+                                             C.byref(self.h)))
 
     def close(self):
         if self.h:
@@ -185,6 +188,24 @@ class Solver:
                        int(min(prob.maxNumSteps, 2**31 - 1)))
         check(self.L.qd_rk43_start(self.h, C.byref(p), _p(prob.Slip), _p(prob.psi)))
 
+    def rk43_resume(self, prob, ck, params=None):
+        """Restart from a fault-state checkpoint (Slip, psi, t, dt, errA0,
+        errA1, it): the commit's refresh solve from the device u as it stands
+        and the fault update.  `params`: (tmax, ini_dt, mindt, maxdt, totTol,
+        maxNumSteps) overriding the problem's."""
+        if params is None:
+            params = (prob.tmax, prob.ini_dt, prob.mindt, prob.maxdt, prob.totTol,
+                      int(min(prob.maxNumSteps, 2**31 - 1)))
+        p = Rk43Params(*params)
+        check(self.L.qd_rk43_resume(self.h, C.byref(p), _p(np.ascontiguousarray(ck["Slip"], dtype=np.float64)),
+                                    _p(np.ascontiguousarray(ck["psi"], dtype=np.float64)), float(ck["t"]),
+                                    float(ck["dt"]), float(ck["errA0"]), float(ck["errA1"]), int(ck["it"])))
+
+    def probe_bounded_wait(self, polls):
+        """qd_probe_bounded_wait: the return code and qd_last_error()."""
+        rc = self.L.qd_probe_bounded_wait(self.h, int(polls))
+        return rc, self.L.qd_last_error().decode(errors="replace")
+
     def rk43_step(self, n=1):
         done = C.c_int(0)
         check(self.L.qd_rk43_step(self.h, n, C.byref(done)))
@@ -252,12 +273,20 @@ class Simulation:
 
     def __init__(self, prob, mg: MGConfig, with_tau0=True):
         self.prob = prob
-        self.solver = Solver(prob.ni, prob.nk, prob.dh, prob.mu_equi, prob.mu_node, mg)
+        self.solver = Solver(prob.ni, prob.nk, prob.dh, prob.mu_equi, prob.mu_node, mg,
+                             jrow=getattr(prob, "jrow", None))
         self.solver.fault_setup(prob, with_tau0=with_tau0)
         self.solver.upload_u(prob.U)
 
     def start(self):
         self.solver.rk43_start(self.prob)
+        return 0
+
+    def resume(self, ck, U=None, params=None):
+        """Restart from a fault-state checkpoint; U (ghosted) is the refresh
+        solve's guess (default: the problem's initial U)."""
+        self.solver.upload_u(self.prob.U if U is None else U)
+        self.solver.rk43_resume(self.prob, ck, params)
         return 0
 
     def step(self, n=1):

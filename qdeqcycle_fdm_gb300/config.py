@@ -55,6 +55,13 @@ class ProblemConfig:
     V0: float = 1e-6
     Vp: float = 1e-9
     amb_perturb: float = 0.0   # uniform +-fraction perturbation of a-b per node
+    # depth stretching (1: the reference's uniform grid): the row spacing is
+    # stretch_ratio times larger below a tanh transition centred at
+    # stretch_depth_km, of width stretch_width in the normalised depth
+    # coordinate (see problem.depth_metric)
+    stretch_ratio: float = 1.0
+    stretch_depth_km: float = 21.0
+    stretch_width: float = 0.01
     seed: int = 12345
     prestress: bool = True     # tau0 so that V = Vp at t = 0 with u = 0
     # time stepping (SetParams.cpp:14-17)
@@ -93,6 +100,17 @@ def config1() -> ProblemConfig:
                          amb_perturb=0.05, years=500.0,
                          mg=MGConfig(n_levels=8, nu_pre=2, nu_post=2, nu_coarse=32,
                                      tol_mode=1, tol=1e-9, max_cycles=200))
+
+
+def config2() -> ProblemConfig:
+    """4097x4097 stretched in depth: 4x finer rows over the 0-20 km fault
+    zone (tanh transition centred at 21 km), config 0's friction with
+    Dc = 2 mm, homogeneous mu = 30 GPa; FP32 V(2,2) cycles inside FP64
+    refinement to a 1e-9 relative residual, 10 levels, 100 years."""
+    return ProblemConfig(name="config2_4097", ni=4097, nk=4097, mu_profile="uniform", Dc_m=0.002,
+                         years=100.0, stretch_ratio=4.0,
+                         mg=MGConfig(n_levels=10, nu_pre=2, nu_post=2, nu_coarse=32, tol_mode=1, tol=1e-9,
+                                     max_cycles=200, precision=1, surface_prolong=1, coarse_solve=1))
 
 
 def config1_mixed() -> ProblemConfig:
@@ -139,4 +157,4 @@ def ensemble_instance(n: int, index: int, base_seed: int = 777) -> ProblemConfig
                                      tol=1e-9, max_cycles=200, precision=1, surface_prolong=1,
                                      coarse_solve=1))
 
-CONFIGS = {"config0": config0, "config1": config1, "config1_mixed": config1_mixed}
+CONFIGS = {"config0": config0, "config1": config1, "config1_mixed": config1_mixed, "config2": config2}

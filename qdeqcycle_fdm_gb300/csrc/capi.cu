@@ -5,12 +5,15 @@
 // device; the only device-to-host traffic per attempt is the error estimate,
 // and per V-cycle the residual norm.
 #include <math.h>
+
+#include <cmath>
 #include <stdarg.h>
 #include <string.h>
 
 #include <vector>
 
 #include "qdeq_internal.cuh"
+#include "tma.cuh"
 
 namespace qd {
 
@@ -71,23 +74,28 @@ static int solve_flag_error(const SolveState &st) {
     return QD_OK;
 }
 
+// Failures the device kernels recorded in the status word: a bounded wait
+// that gave up, or a Newton solve with no finite root (where the reference
+// exit(0)s, fault.cpp:211-225)
+static int status_flag_error(const DevStatus &d) {
+    if (d.flags & ST_TMA_TIMEOUT) {
+        set_error("a multigrid kernel's shared-memory staging did not complete (flags %u)", d.flags);
+        return QD_ERR_CUDA;
+    }
+    if (d.flags & (ST_NEWTON_NAN | ST_NEWTON_CAP)) {
+        set_error("Newton for slip rate failed at fault node %d (flags %u)", d.bad_node, d.flags);
+        return QD_ERR_NEWTON;
+    }
+    return QD_OK;
+}
+
 static int check_status(qd_solver *s) {
     QD_CUDA(cudaMemcpyAsync(s->h_status, s->d_status, sizeof(DevStatus), cudaMemcpyDeviceToHost,
                             s->stream));
     SolveState st;
     QD_TRY(solve_state_read(s, &st));   // synchronises the stream
     QD_TRY(solve_flag_error(st));
-    if (s->h_status->flags & ST_TMA_TIMEOUT) {
-        set_error("a multigrid kernel's shared-memory staging did not complete (flags %u)",
-                  s->h_status->flags);
-        return QD_ERR_CUDA;
-    }
-    if (s->h_status->flags & (ST_NEWTON_NAN | ST_NEWTON_CAP)) {
-        set_error("Newton for slip rate failed at fault node %d (flags %u)", s->h_status->bad_node,
-                  s->h_status->flags);
-        return QD_ERR_NEWTON;
-    }
-    return QD_OK;
+    return status_flag_error(*s->h_status);
 }
 
 static int reset_status(qd_solver *s) {
@@ -128,11 +136,17 @@ static int rk_start(qd_solver *s) {
 // enqueue work (step_begin, attempt_enqueue, commit_enqueue) and phases that
 // wait for it (attempt_finish, commit_finish), so that several solvers can
 // interleave their GPU work (qd_ensemble_step).
+struct RkTableau {
+    double c[7], b[7], hb[7], a[7][7];
+};
 static const double *rk_c() {
-    static double c[7], b[7], hb[7], a[7][7];
-    static bool init = false;
-    if (!init) { rk_tableau(c, b, hb, a); init = true; }
-    return c;
+    // built once, thread-safely (function-local static), for every solver
+    static const RkTableau t = [] {
+        RkTableau x;
+        rk_tableau(x.c, x.b, x.hb, x.a);
+        return x;
+    }();
+    return t.c;
 }
 
 static int step_begin(qd_solver *s) {
@@ -151,12 +165,18 @@ static int attempt_enqueue(qd_solver *s) {
     QD_CUDA(cudaMemcpyAsync(s->h_scal + 2, s->d_scal + 2, sizeof(double), cudaMemcpyDeviceToHost,
                             s->stream));
     QD_CUDA(cudaMemcpyAsync(s->h_solve, s->d_solve, sizeof(SolveState), cudaMemcpyDeviceToHost, s->stream));
+    QD_CUDA(cudaMemcpyAsync(s->h_status, s->d_status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s->stream));
     return QD_OK;
 }
 
-// the attempt's one synchronisation; *retry: reduce dt and attempt again
+// the attempt's one synchronisation; *retry: reduce dt and attempt again.
+// A failed solve or Newton solve ends the step at the attempt that met it
+// (the reference exits in NRsearch at the first NaN, fault.cpp:211-225).
 static int attempt_finish(qd_solver *s, int attemptCount, double *totErr, int *retry) {
     QD_CUDA(cudaStreamSynchronize(s->stream));
+    // a Newton failure first: its NaN reaches the next stage's boundary data
+    // and makes that solve fail too
+    QD_TRY(status_flag_error(*s->h_status));
     QD_TRY(solve_flag_error(*s->h_solve));
     *totErr = s->h_scal[2];
     *retry = 0;
@@ -221,10 +241,21 @@ void qd_default_options(qd_mg_options *o) {
 
 int qd_solver_create(int ni, int nk, double dh, const double *mu_equi, const double *mu_node,
                      const qd_mg_options *opt, qd_solver **out) {
+    return qd_solver_create_mapped(ni, nk, dh, mu_equi, mu_node, nullptr, opt, out);
+}
+
+int qd_solver_create_mapped(int ni, int nk, double dh, const double *mu_equi, const double *mu_node,
+                            const double *jrow, const qd_mg_options *opt, qd_solver **out) {
     if (!out || !mu_equi || !mu_node || ni < 3 || nk < 3 || !(dh > 0.0)) {
         set_error("qd_solver_create: bad arguments");
         return QD_ERR_ARG;
     }
+    if (jrow)
+        for (int r = 0; r < 2 * (nk + 2) - 1; r++)
+            if (!(jrow[r] > 0.0) || !std::isfinite(jrow[r])) {
+                set_error("qd_solver_create_mapped: the depth metric must be positive and finite (row %d)", r);
+                return QD_ERR_ARG;
+            }
     *out = nullptr;
     QD_TRY(check_opts(opt));
     qd_solver *s = new qd_solver();
@@ -245,7 +276,7 @@ int qd_solver_create(int ni, int nk, double dh, const double *mu_equi, const dou
         qd_solver_destroy(s);
         return QD_ERR_CUDA;
     }
-    rc = mg_alloc(s, mu_equi);
+    rc = mg_alloc(s, mu_equi, jrow);
     if (rc == QD_OK) rc = fault_alloc(s);
     if (rc == QD_OK) {
         std::vector<double> mu0(s->nz, 0.0);
@@ -403,6 +434,15 @@ int qd_mg_time_kernel(qd_solver *s, int kernel, int reps, double *us) {
     return time_kernel(s, kernel, reps, us);
 }
 
+int qd_probe_bounded_wait(qd_solver *s, int polls) {
+    if (!s || polls < 1 || polls > (int)TMA_WAIT_LIMIT) {
+        set_error("qd_probe_bounded_wait: bad arguments (polls %d)", polls);
+        return QD_ERR_ARG;
+    }
+    QD_TRY(wait_probe(s, (unsigned)polls));
+    return check_status(s);
+}
+
 int qd_fault_setup(qd_solver *s, const double *a, const double *b, const double *eta,
                    const double *Tau_n0, const double *SlipShift, const double *tau0, double f0,
                    double V0, double L, double Vini) {
@@ -499,6 +539,36 @@ int qd_rk43_start(qd_solver *s, const qd_rk43_params *p, const double *Slip, con
     s->errA[0] = s->errA[1] = 0.0;
     history_reset(s);
     return rk_start(s);
+}
+
+int qd_rk43_resume(qd_solver *s, const qd_rk43_params *p, const double *Slip, const double *psi, double t,
+                   double dt, double errA0, double errA1, int it) {
+    if (!s || !p || !Slip || !psi || !(dt > 0.0) || it < 0) {
+        set_error("qd_rk43_resume: bad arguments");
+        return QD_ERR_ARG;
+    }
+    if (!s->fault_ready) { set_error("qd_rk43_resume: no fault set up"); return QD_ERR_STATE; }
+    if (p->maxNumSteps == 0) { set_error("max number of steps == 0"); return QD_ERR_ARG; }
+    s->P = *p;
+    const size_t n = s->nz * sizeof(double);
+    QD_CUDA(cudaMemcpy(s->F.Slip, Slip, n, cudaMemcpyHostToDevice));
+    QD_CUDA(cudaMemcpy(s->F.psi, psi, n, cudaMemcpyHostToDevice));
+    for (int st = 1; st <= 6; st++) {     // zero Newton seeds, as after a commit (:1605-1614)
+        QD_CUDA(cudaMemset(s->F.fV[st], 0, n));
+        QD_CUDA(cudaMemset(s->F.fdpsi[st], 0, n));
+    }
+    s->t = t;
+    s->it = it;
+    s->errA[0] = errA0;
+    s->errA[1] = errA1;
+    history_reset(s);
+    QD_TRY(reset_status(s));
+    QD_TRY(solve_state_clear_flag(s));
+    s->dt = dt;
+    QD_TRY(stage(s, 1, 0.0));     // the refresh solve and fault update of a commit (:1615-1619)
+    QD_TRY(check_status(s));
+    s->started = 1;
+    return QD_OK;
 }
 
 int qd_ensemble_step(qd_solver **ss, int n, int nsteps, int *steps_done) {

@@ -79,28 +79,41 @@ __global__ void k_final_sum(const double *partial, int n, double *out) {
 
 // ---------------------------------------------------------------------------
 // coefficient set-up from the reference's staggered mu_equi
+//
+// With a depth metric (a grid stretched in depth, z = z(zeta) on a uniform
+// computational coordinate zeta of spacing dh), the operator is
+//   J d/dx(mu du/dx) + d/dzeta((mu / J) du/dzeta),   J = dz/dzeta,
+// the conservative form of div(mu grad u) multiplied by J: the same 5-point
+// stencil on the uniform (x, zeta) grid with x-face moduli mu J (J at the
+// face's row) and z-face moduli mu / J (J at the face).  jrow holds J per
+// staggered row of mu_equi (node rows even, face rows odd, the ghost rows
+// mirrored), so each coefficient takes the metric of the mu_equi row it is
+// read from; null: the reference's uniform grid.
 // ---------------------------------------------------------------------------
-__global__ void k_build_faces(const double *__restrict__ mu, long W, int level, int fc, int N,
-                              int K, int P, double *cx, double *cz) {
+__global__ void k_build_faces(const double *__restrict__ mu, const double *__restrict__ jrow, long W,
+                              int level, int fc, int N, int K, int P, double *cx, double *cz) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (k >= K || j > N) return;
     if (j < N && k < K - 1) {
-        long idx;
-        if (level == 0)
-            idx = ((k + 1) * 2 + 1) + (long)((j + 1) * 2) * W;            // index2, :787
-        else
-            idx = ((k * 2 + 1) * fc / 2 + 1) * 2 + (long)((j * fc + 1) * 2) * W;   // :825
-        cx[(long)j * P + k] = mu[idx];
+        long row, col;
+        if (level == 0) {
+            col = (k + 1) * 2 + 1; row = (long)(j + 1) * 2;                    // index2, :787
+        } else {
+            col = ((k * 2 + 1) * fc / 2 + 1) * 2; row = (long)(j * fc + 1) * 2;  // :825
+        }
+        const double m = mu[col + row * W];
+        cx[(long)j * P + k] = jrow ? m * jrow[row] : m;
     }
-    long idz;
+    long row;
     if (level == 0) {
-        idz = (k + 1) * 2 + (long)(2 * j + 1) * W;                        // index3 of row j, :788
+        row = 2 * j + 1;                                                  // index3 of row j, :788
     } else {
         const int jj = (j == 0) ? 1 : (j == N ? N - 1 : j);                // :830-847 quirk
-        idz = (k * fc + 1) * 2 + (long)(((jj * 2 - 1) * fc / 2 + 1) * 2) * W;      // :826
+        row = (long)((jj * 2 - 1) * fc / 2 + 1) * 2;                      // :826
     }
-    cz[(long)j * P + k] = mu[idz];
+    const double m = mu[(k * fc + 1) * 2 + row * W];
+    cz[(long)j * P + k] = jrow ? m / jrow[row] : m;
 }
 
 __global__ void k_build_dinv(int N, int K, int P, const double *cx, const double *cz,
@@ -302,7 +315,7 @@ static T *dalloc(size_t n, int *rc) {
     return p;
 }
 
-int mg_alloc(qd_solver *s, const double *mu_equi_host) {
+int mg_alloc(qd_solver *s, const double *mu_equi_host, const double *jrow_host) {
     const int nl = s->opt.n_levels;
     if (nl < 1 || nl > QD_MAXLEV) {
         set_error("n_levels %d out of range 1..%d", nl, QD_MAXLEV);
@@ -363,11 +376,18 @@ int mg_alloc(qd_solver *s, const double *mu_equi_host) {
     if (rc != QD_OK) return rc;
     QD_CUDA(cudaMemcpyAsync(d_mu, mu_equi_host, nmu * sizeof(double), cudaMemcpyHostToDevice,
                             s->stream));
+    double *d_j = nullptr;
+    if (jrow_host) {
+        const size_t nj = 2 * (size_t)s->nz - 1;
+        d_j = dalloc<double>(nj, &rc);
+        if (rc != QD_OK) return rc;
+        QD_CUDA(cudaMemcpyAsync(d_j, jrow_host, nj * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+    }
     const long W = 2L * s->nx - 1;
     for (int l = 0; l < nl; l++) {
         const LevelDims &d = s->dims[l];
         dim3 blk(BX, BY), grd(cdiv(d.K, BX), cdiv(d.N + 1, BY));
-        k_build_faces<<<grd, blk, 0, s->stream>>>(d_mu, W, l, 1 << l, d.N, d.K, d.P, s->L64[l].cx,
+        k_build_faces<<<grd, blk, 0, s->stream>>>(d_mu, d_j, W, l, 1 << l, d.N, d.K, d.P, s->L64[l].cx,
                                                   s->L64[l].cz);
         QD_LAUNCH_CHECK(s);
         k_build_dinv<<<grd, blk, 0, s->stream>>>(d.N, d.K, d.P, s->L64[l].cx, s->L64[l].cz,
@@ -377,6 +397,7 @@ int mg_alloc(qd_solver *s, const double *mu_equi_host) {
     }
     QD_CUDA(cudaStreamSynchronize(s->stream));
     cudaFree(d_mu);
+    cudaFree(d_j);
     QD_TRY(build_coarse_inverse(s));
     return tail_image_build(s);
 }

@@ -393,6 +393,7 @@ static int tile_maps(qd_solver *s, Level<T> *Ls, int l, int W, int BH, const Til
     e.maps.W = W; e.maps.BH = BH;
     const LevelDims &d = s->dims[l];
     QD_TRY(make_tensor_map_2d(&e.maps.u, Ls[l].u, fp64, d.K, d.N, d.P, W, BH));
+    QD_TRY(make_tensor_map_2d(&e.maps.ur, Ls[l].r, fp64, d.K, d.N, d.P, W, BH));
     QD_TRY(make_tensor_map_2d(&e.maps.cx, Ls[l].cx, fp64, d.K, d.N, d.P, W, BH));
     QD_TRY(make_tensor_map_2d(&e.maps.cz, Ls[l].cz, fp64, d.K, d.N + 1, d.P, W, BH + 1));
     if (Ls[l].f) QD_TRY(make_tensor_map_2d(&e.maps.f, Ls[l].f, fp64, d.K, d.N, d.P, W, BH));
@@ -506,8 +507,16 @@ static TileGeom pick_down(int Nc, int Kc, int N, int K, int S, bool has_f, int b
     return best;
 }
 
+// Where a level's current field lives: u, or its scratch r.  Every tile
+// kernel reads one and writes the other (see mg_tile.cuh).
 template <typename T>
-static int launch_down(qd_solver *s, Level<T> *Ls, int l, int S, int zero_u) {
+static T *field(Level<T> *Ls, int l, bool in_r) { return in_r ? Ls[l].r : Ls[l].u; }
+
+// pre-smoothing + residual + restriction on level l: loads u from r when
+// *in_r (ignored with zero_u), writes the smoothed field to the other array
+// and flips *in_r
+template <typename T>
+static int launch_down(qd_solver *s, Level<T> *Ls, int l, int S, int zero_u, bool *in_r) {
     const LvArgs<T> g = lv(s, Ls, l), c = lv(s, Ls, l + 1);
     // the residual goes into f, or into the dinv slot on the FP64 level 0
     const bool has_f = g.f != nullptr;
@@ -522,14 +531,19 @@ static int launch_down(qd_solver *s, Level<T> *Ls, int l, int S, int zero_u) {
     QD_TRY(tile_maps<T>(s, Ls, l, W, BH, &maps));
     QD_TRY(set_smem(k_down<T>, smem));
     QD_CUDA(launch_pdl(true, k_down<T>, dim3(ntk, ntj), dim3(NT), smem, s->stream, g, c, *maps, CH, CW, ntj, ntk,
-                       S, zero_u, &s->d_status->flags));
+                       S, zero_u, (int)*in_r, field(Ls, l, !*in_r), &s->d_status->flags));
     QD_LAUNCH_CHECK(s);
+    *in_r = !*in_r;
     return QD_OK;
 }
 
+// prolongation (prolong = 1, the coarse correction read from r when
+// coarse_in_r) + S half-sweeps on level l: loads u from r when *in_r,
+// writes the other array and flips *in_r (MODE 2: adds into u64 instead
+// and leaves *in_r); MODE 1 also leaves the residual norm partials
 template <typename T, int MODE>
-static int launch_up(qd_solver *s, Level<T> *Ls, int l, int S, int prolong, int zero_u,
-                     double *u64 = nullptr, int P64 = 0, int *nblocks = nullptr) {
+static int launch_up(qd_solver *s, Level<T> *Ls, int l, int S, int prolong, int zero_u, bool *in_r,
+                     bool coarse_in_r = false, double *u64 = nullptr, int P64 = 0, int *nblocks = nullptr) {
     const LvArgs<T> g = lv(s, Ls, l);
     const LvArgs<T> c = (l + 1 < s->nlev) ? lv(s, Ls, l + 1) : g;
     const int R1 = MODE == 1 ? 1 : 0;
@@ -547,10 +561,12 @@ static int launch_up(qd_solver *s, Level<T> *Ls, int l, int S, int prolong, int 
     const TileMaps *maps = nullptr;
     QD_TRY(tile_maps<T>(s, Ls, l, W, BH, &maps));
     QD_TRY(set_smem(k_up<T, MODE>, smem));
+    const T *cu = (l + 1 < s->nlev) ? field(Ls, l + 1, coarse_in_r) : nullptr;
     QD_CUDA(launch_pdl(true, k_up<T, MODE>, dim3(ntk, ntj), dim3(NT), smem, s->stream, g, c, *maps, TH, TW, ntj,
-                       ntk, S, prolong, s->opt.surface_prolong, zero_u, s->d_partial, u64, P64,
-                       &s->d_status->flags));
+                       ntk, S, prolong, s->opt.surface_prolong, zero_u, (int)*in_r, field(Ls, l, !*in_r), cu,
+                       s->d_partial, u64, P64, &s->d_status->flags));
     QD_LAUNCH_CHECK(s);
+    if (MODE != 2) *in_r = !*in_r;
     if (nblocks) *nblocks = ntj * ntk;
     return QD_OK;
 }
@@ -664,17 +680,24 @@ void tma_cache_free(qd_solver *s) {
     s->tma_cache = nullptr;
 }
 
-// nsweeps red+black sweeps on level l as tile passes of at most SMAX
-// half-sweeps (the first pass may start from a zero guess)
+// passes of at most SMAX half-sweeps (whole sweeps) for nsweeps sweeps;
+// one more when `even` and their number is odd (a pass then carries fewer)
+static int pass_count(int nsweeps, bool even) {
+    int n = (2 * nsweeps + SMAX - 1) / SMAX;
+    if (even && (n & 1)) n++;
+    return n;
+}
+
+// nsweeps red+black sweeps on level l as `npass` tile passes of whole
+// sweeps (the first pass may start from a zero guess); each pass reads one
+// of u, r and writes the other
 template <typename T>
-static int smooth_passes(qd_solver *s, Level<T> *Ls, int l, int nsweeps, int zero_u) {
-    int left = 2 * nsweeps;
-    bool first = true;
-    while (left > 0) {
-        const int S = std::min(SMAX, left);
-        QD_TRY((launch_up<T, 0>(s, Ls, l, S, 0, first ? zero_u : 0)));
-        first = false;
-        left -= S;
+static int smooth_passes(qd_solver *s, Level<T> *Ls, int l, int nsweeps, int npass, int zero_u, bool *in_r) {
+    int left = nsweeps;
+    for (int p = 0; p < npass; p++) {
+        const int sw = (left + (npass - p) - 1) / (npass - p);   // spread evenly, at most SMAX / 2
+        QD_TRY((launch_up<T, 0>(s, Ls, l, 2 * sw, 0, p == 0 ? zero_u : 0, in_r)));
+        left -= sw;
     }
     return QD_OK;
 }
@@ -736,50 +759,62 @@ static int launch_tail(qd_solver *s, Level<T> *Ls, int lt) {
 template <typename T, int MODE0>
 static int vcycle_fused(qd_solver *s, Level<T> *Ls, int zero0, int *nblocks) {
     const int nl = s->nlev;
-    if (nl == 1) return smooth_passes<T>(s, Ls, 0, s->opt.nu_coarse, zero0);
+    bool in_r[QD_MAXLEV] = {};      // where each level's field lives (u or its scratch r)
+    if (nl == 1) {
+        // an even number of passes leaves the field in u
+        QD_TRY(smooth_passes<T>(s, Ls, 0, s->opt.nu_coarse, pass_count(s->opt.nu_coarse, true), zero0, &in_r[0]));
+        return QD_OK;
+    }
     const int lt = first_tail_level<T>(s);
+    const int pre = std::max(0, s->opt.nu_pre - SMAX / 2);    // sweeps before the fused k_down
+    const int post = std::max(0, s->opt.nu_post - SMAX / 2);  // sweeps after the fused k_up
+    // level 0 of the FP64 hierarchy must end in u (it is the solution): the
+    // passes there, plus k_down and k_up, must be an even number of flips
+    int pre0 = pass_count(pre, false), post0 = pass_count(post, false);
+    if (MODE0 == 1 && ((pre0 + post0) & 1)) post0 > 0 ? post0++ : pre0++;
     // descend through the tiled levels
     for (int l = 0; l < lt && l < nl - 1; l++) {
         const int zero = (l == 0) ? zero0 : 1;
-        const int S = 2 * s->opt.nu_pre;
-        const int Sfirst = S > SMAX ? S - SMAX : 0;
-        if (Sfirst) QD_TRY(smooth_passes<T>(s, Ls, l, Sfirst / 2, zero));
-        QD_TRY(launch_down<T>(s, Ls, l, std::min(S, SMAX), Sfirst ? 0 : zero));
+        const int np = (l == 0) ? pre0 : pass_count(pre, false);
+        if (pre) QD_TRY(smooth_passes<T>(s, Ls, l, pre, np, zero, &in_r[l]));
+        QD_TRY(launch_down<T>(s, Ls, l, std::min(2 * s->opt.nu_pre, SMAX), pre ? 0 : zero, &in_r[l]));
     }
     // coarse tail (or the coarsest level on its own)
     if (lt < nl) {
-        QD_TRY(launch_tail<T>(s, Ls, lt));
+        QD_TRY(launch_tail<T>(s, Ls, lt));            // writes u of level lt
+        in_r[lt] = false;
     } else {
         if (s->opt.coarse_solve) {
             set_error("coarse_solve needs the coarsest level in the single-CTA tail (<= 65 rows)");
             return QD_ERR_ARG;
         }
-        QD_TRY(smooth_passes<T>(s, Ls, nl - 1, s->opt.nu_coarse, 1));
+        QD_TRY(smooth_passes<T>(s, Ls, nl - 1, s->opt.nu_coarse, pass_count(s->opt.nu_coarse, false), 1,
+                                &in_r[nl - 1]));
     }
     // ascend
     for (int l = std::min(lt, nl - 1) - 1; l >= 0; l--) {
-        const int S = 2 * s->opt.nu_post;
-        const int S1 = std::min(S, SMAX);
-        const int rest = S - S1;
-        if (l == 0 && rest == 0) {
-            QD_TRY((launch_up<T, MODE0>(s, Ls, 0, S1, 1, 0, s->L64[0].u, s->dims[0].P, nblocks)));
+        const int S1 = std::min(2 * s->opt.nu_post, SMAX);
+        const int np = (l == 0) ? post0 : pass_count(post, false);
+        if (l == 0 && !post) {
+            QD_TRY((launch_up<T, MODE0>(s, Ls, 0, S1, 1, 0, &in_r[0], in_r[1], s->L64[0].u, s->dims[0].P,
+                                        nblocks)));
         } else {
-            QD_TRY((launch_up<T, 0>(s, Ls, l, S1, 1, 0)));
-            if (rest) {
+            QD_TRY((launch_up<T, 0>(s, Ls, l, S1, 1, 0, &in_r[l], in_r[l + 1])));
+            if (post) {
                 if (l == 0) {
-                    // remaining sweeps, the last pass in MODE0
-                    int left = rest;
-                    while (left > SMAX) {
-                        QD_TRY((launch_up<T, 0>(s, Ls, 0, SMAX, 0, 0)));
-                        left -= SMAX;
-                    }
-                    QD_TRY((launch_up<T, MODE0>(s, Ls, 0, left, 0, 0, s->L64[0].u, s->dims[0].P,
-                                                nblocks)));
+                    // the remaining sweeps, the last pass in MODE0
+                    if (np > 1) QD_TRY(smooth_passes<T>(s, Ls, 0, post - post / np, np - 1, 0, &in_r[0]));
+                    QD_TRY((launch_up<T, MODE0>(s, Ls, 0, 2 * (post / np), 0, 0, &in_r[0], false, s->L64[0].u,
+                                                s->dims[0].P, nblocks)));
                 } else {
-                    QD_TRY(smooth_passes<T>(s, Ls, l, rest / 2, 0));
+                    QD_TRY(smooth_passes<T>(s, Ls, l, post, np, 0, &in_r[l]));
                 }
             }
         }
+    }
+    if (MODE0 == 1 && in_r[0]) {
+        set_error("V-cycle left the level-0 field in its scratch array");
+        return QD_ERR_STATE;
     }
     return QD_OK;
 }
@@ -798,12 +833,18 @@ static int time_kernel_t(qd_solver *s, Level<T> *Ls, int which, int reps) {
     const int S = std::min(2 * s->opt.nu_pre, SMAX), S1 = std::min(2 * s->opt.nu_post, SMAX);
     for (int i = 0; i < reps; i++) {
         switch (which) {
-            case QD_KERNEL_DOWN0:
-                QD_TRY(launch_down<T>(s, Ls, 0, S, 0));
+            case QD_KERNEL_DOWN0: {
+                // as in a cycle: level-0 u (the FP64 solution, or the FP32
+                // correction) in, the smoothed field into the scratch array
+                bool in_r = false;
+                QD_TRY(launch_down<T>(s, Ls, 0, S, 0, &in_r));
                 break;
+            }
             case QD_KERNEL_UP0: {
+                // as in a cycle: the scratch array in, u (or u64 += e) out
                 int nb = 0;
-                QD_TRY((launch_up<T, MODE_UP>(s, Ls, 0, S1, 1, 0, s->L64[0].u, s->dims[0].P, &nb)));
+                bool in_r = true;
+                QD_TRY((launch_up<T, MODE_UP>(s, Ls, 0, S1, 1, 0, &in_r, false, s->L64[0].u, s->dims[0].P, &nb)));
                 break;
             }
             case QD_KERNEL_TAIL:
@@ -893,6 +934,25 @@ void tail_image_free(qd_solver *s) {
         cudaFree(s->d_tail_img[i]);
         s->d_tail_img[i] = nullptr;
     }
+}
+
+
+// The bounded wait of the staging pipelines, exercised where nothing can
+// complete it: one thread initialises an mbarrier that expects one arrival,
+// nothing arrives, and the wait gives up after `polls` polls and records
+// ST_TMA_TIMEOUT in the status word, as a tile kernel whose staging never
+// landed does.  No copy is in flight, so the kernel simply returns.
+__global__ void k_wait_probe(unsigned polls, unsigned *status) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    __syncthreads();
+    if (!mbar_wait_limit(&bar, 0, polls) && threadIdx.x == 0 && status) atomicOr(status, ST_TMA_TIMEOUT);
+}
+
+int wait_probe(qd_solver *s, unsigned polls) {
+    k_wait_probe<<<1, 32, 0, s->stream>>>(polls, &s->d_status->flags);
+    QD_LAUNCH_CHECK(s);
+    return QD_OK;
 }
 
 }  // namespace qd

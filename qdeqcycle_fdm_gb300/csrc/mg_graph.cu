@@ -79,6 +79,16 @@ void solve_graph_free(qd_solver *s) {
     s->solve_graph = nullptr;
 }
 
+// The cycle cap a solve's decision kernels apply.  The host-driven loop
+// (eager mode) honours max_cycles <= 0 as "no cap", as the reference's loop
+// (odeSolver.cpp:696) does; inside the solve graph the loop runs on the
+// device with no host check, so there an uncapped solve stops after
+// QD_SOLVE_GRAPH_MAX_CYCLES cycles and reports QD_ERR_NOT_CONVERGED.
+static int cycle_cap(const qd_solver *s, int in_graph) {
+    if (s->opt.max_cycles > 0) return s->opt.max_cycles;
+    return in_graph ? QD_SOLVE_GRAPH_MAX_CYCLES : 0;
+}
+
 // the body of one loop iteration: a V-cycle and the norm of the new
 // residual; in mixed precision the norm's last block also takes the loop's
 // decision (*fused set), otherwise k_solve_check follows
@@ -89,7 +99,7 @@ static int capture_cycle(qd_solver *s, cudaGraphConditionalHandle h, int in_grap
         QD_TRY(vcycle32_into64(s));          // FP32 cycle on A e = r, then u += e
         Decide dc{};
         dc.mode = 2;
-        dc.max_cycles = s->opt.max_cycles;
+        dc.max_cycles = cycle_cap(s, in_graph);
         dc.n_kernels = (int)(s->launches - launches0) + 1;
         dc.in_graph = in_graph;
         dc.h = h;
@@ -216,7 +226,7 @@ static int build(qd_solver *s, SolveGraph *sg) {
     rc = capture_cycle(s, h, 1, launches0, &fused);
     if (rc == QD_OK && !fused) {
         const int n = (int)(s->launches - launches0) + 1;
-        k_solve_check<<<1, 1, 0, s->stream>>>(h, s->d_scal, s->d_solve, s->opt.max_cycles, n, 1);
+        k_solve_check<<<1, 1, 0, s->stream>>>(h, s->d_scal, s->d_solve, cycle_cap(s, 1), n, 1);
         if (cudaPeekAtLastError() != cudaSuccess) rc = QD_ERR_CUDA;
     }
     s->launches = launches0;
@@ -258,7 +268,7 @@ static int solve_eager(qd_solver *s) {
         bool fused = false;
         QD_TRY(capture_cycle(s, 0, 0, launches0, &fused));
         if (!fused) {
-            k_solve_check<<<1, 1, 0, s->stream>>>(0, s->d_scal, s->d_solve, s->opt.max_cycles,
+            k_solve_check<<<1, 1, 0, s->stream>>>(0, s->d_scal, s->d_solve, cycle_cap(s, 0),
                                                   (int)(s->launches - launches0) + 1, 0);
             QD_LAUNCH_CHECK(s);
         }

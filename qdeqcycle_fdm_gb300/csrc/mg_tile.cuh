@@ -13,6 +13,14 @@
 // Tiles stage 1/diag with the other arrays: a division (or a correctly
 // rounded reciprocal) per update costs more issue slots than one more
 // shared-memory load, and the boxes are sized so two CTAs still fit per SM.
+//
+// No kernel writes the array its tiles load u from: a tile's halo overlaps
+// its neighbours' cores, and a CTA that stored its smoothed core into the
+// source array before a neighbour's TMA load landed would hand that
+// neighbour a halo already swept (a race that makes results depend on CTA
+// scheduling).  Each level has two arrays, u and the scratch r; every tile
+// kernel loads u from one (`src_r`) and writes the other (`dst`), boundary
+// columns included, so the Dirichlet data travel with the field.
 #pragma once
 
 #include "tma.cuh"
@@ -29,9 +37,10 @@ struct TileCfg {
     static constexpr int kAlign = 16 / (int)sizeof(T);   // elements per 16 bytes
 };
 
-// tensor maps of one level's arrays, boxes of W x BH (cz: W x BH+1)
+// tensor maps of one level's arrays, boxes of W x BH (cz: W x BH+1); ur is
+// the map of the level's scratch array r, the other source of u
 struct TileMaps {
-    CUtensorMap u, f, cx, cz, dv;
+    CUtensorMap u, ur, f, cx, cz, dv;
     int W, BH;
 };
 
@@ -82,7 +91,7 @@ __device__ __forceinline__ STile<T> carve(unsigned char *raw, int jL0, int kL0, 
 // right-hand side but the kernel keeps an array for it.  tile_wait returns
 // false (in every thread) if the copies did not land.
 template <typename T>
-__device__ void tile_issue(const LvArgs<T> &g, const TileMaps &m, STile<T> &t, bool zero_u,
+__device__ void tile_issue(const LvArgs<T> &g, const TileMaps &m, STile<T> &t, bool zero_u, bool src_r,
                            uint64_t *bar) {
     const int BH = m.BH, W = m.W;
     const bool load_f = t.f && g.f;
@@ -97,7 +106,7 @@ __device__ void tile_issue(const LvArgs<T> &g, const TileMaps &m, STile<T> &t, b
         if (load_f) bytes += a;
         if (TileCfg<T>::kDinv) bytes += a;
         mbar_expect_tx(bar, bytes);
-        if (!zero_u) tma_load_2d(t.u, &m.u, t.kL0, t.jL0, bar);
+        if (!zero_u) tma_load_2d(t.u, src_r ? &m.ur : &m.u, t.kL0, t.jL0, bar);
         tma_load_2d(t.cx, &m.cx, t.kL0, t.jL0, bar);
         tma_load_2d(t.cz, &m.cz, t.kL0, t.jL0, bar);
         if (load_f) tma_load_2d(t.f, &m.f, t.kL0, t.jL0, bar);
@@ -117,9 +126,9 @@ __device__ __forceinline__ bool tile_wait(uint64_t *bar, unsigned *status) {
 }
 
 template <typename T>
-__device__ bool tile_load(const LvArgs<T> &g, const TileMaps &m, STile<T> &t, bool zero_u,
+__device__ bool tile_load(const LvArgs<T> &g, const TileMaps &m, STile<T> &t, bool zero_u, bool src_r,
                           uint64_t *bar, unsigned *status) {
-    tile_issue(g, m, t, zero_u, bar);
+    tile_issue(g, m, t, zero_u, src_r, bar);
     return tile_wait(bar, status);
 }
 
@@ -178,7 +187,7 @@ __device__ static double block_sum_1d(double v) {
 template <typename T>
 __global__ void __launch_bounds__(NT, 2)
     k_down(LvArgs<T> g, LvArgs<T> c, const __grid_constant__ TileMaps maps, int CH, int CW, int ntj,
-           int ntk, int S, int zero_u, unsigned *status) {
+           int ntk, int S, int zero_u, int src_r, T *dst, unsigned *status) {
     pdl_trigger();
     pdl_wait();   // launched with programmatic serialization: the previous kernel's data first
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -194,7 +203,7 @@ __global__ void __launch_bounds__(NT, 2)
     // one) or, on the FP64 level 0 with its zero right-hand side, into dv
     const bool has_f = g.f != nullptr;
     STile<T> t = carve<T>(smem, jL0, kL0, LR, LC, maps.BH, maps.W, has_f);
-    if (!tile_load(g, maps, t, zero_u != 0, &bar, status)) return;
+    if (!tile_load(g, maps, t, zero_u != 0, src_r != 0, &bar, status)) return;
     for (int s = 0; s < S; s++) {
         tile_halfsweep(g, t, s & 1);
         __syncthreads();
@@ -227,12 +236,12 @@ __global__ void __launch_bounds__(NT, 2)
             }
         }
     }
-    {   // smoothed fine u on the owned region
+    {   // smoothed fine u on the owned region, the boundary columns with it
         const int ja = 2 * cj0, jb = min(g.N, 2 * cj1);
-        const int ka = max(1, 2 * ck0), kb = min(g.K - 1, 2 * ck1);
+        const int ka = 2 * ck0, kb = min(g.K, 2 * ck1);
         for (int j = ja + TWARP; j < jb; j += TNWARP) {
             const T *ur = t.u + (j - jL0) * t.W - kL0;
-            T *gr = g.u + (long)j * g.P;
+            T *gr = dst + (long)j * g.P;
             for (int k = ka + TLANE; k < kb; k += 32) gr[k] = ur[k];
         }
     }
@@ -247,8 +256,8 @@ __global__ void __launch_bounds__(NT, 2)
 template <typename T, int MODE>
 __global__ void __launch_bounds__(NT, 2)
     k_up(LvArgs<T> g, LvArgs<T> c, const __grid_constant__ TileMaps maps, int TH, int TW, int ntj,
-         int ntk, int S, int prolong, int surface, int zero_u, double *partial, double *u64, int P64,
-         unsigned *status) {
+         int ntk, int S, int prolong, int surface, int zero_u, int src_r, T *dst, const T *cu,
+         double *partial, double *u64, int P64, unsigned *status) {
     pdl_trigger();
     pdl_wait();   // launched with programmatic serialization: the previous kernel's data first
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -262,7 +271,7 @@ __global__ void __launch_bounds__(NT, 2)
     const int kL0 = max(0, k0 - S - R1) & ~(TileCfg<T>::kAlign - 1);
     const int LR = min(maps.BH, g.N - jL0), LC = min(maps.W, g.K - kL0);
     STile<T> t = carve<T>(smem, jL0, kL0, LR, LC, maps.BH, maps.W, g.f != nullptr);
-    tile_issue(g, maps, t, zero_u != 0, &bar);
+    tile_issue(g, maps, t, zero_u != 0, src_r != 0, &bar);
     // coarse block covering the tile, gathered while the tile copies fly
     const int jL1 = jL0 + LR, kL1 = kL0 + LC;
     const int cjA = jL0 >> 1, cjB = min(c.N - 1, ((jL1 - 1) >> 1) + 1);
@@ -271,7 +280,7 @@ __global__ void __launch_bounds__(NT, 2)
     T *E = reinterpret_cast<T *>(smem + tile_bytes<T>(maps.BH, maps.W, g.f != nullptr));
     if (prolong)
         for (int r = TWARP; r <= cjB - cjA; r += TNWARP)
-            for (int cc = TLANE; cc < EW; cc += 32) E[r * EW + cc] = c.u[(long)(cjA + r) * c.P + ckA + cc];
+            for (int cc = TLANE; cc < EW; cc += 32) E[r * EW + cc] = cu[(long)(cjA + r) * c.P + ckA + cc];
     const bool ok = tile_wait(&bar, status);
     if (!ok) {
         if (MODE == 1 && threadIdx.x == 0) partial[blockIdx.y * gridDim.x + blockIdx.x] = 0.0;
@@ -332,18 +341,18 @@ __global__ void __launch_bounds__(NT, 2)
         return;
     }
     double sq = 0.0;
+    // the write-out covers the boundary columns too (the copy carries the
+    // Dirichlet data to the other array); the residual only the interior
+    const int wa = (k0 == 0) ? 0 : ka, wb = (k1 == g.K) ? g.K - 1 : kb;
     for (int j = j0 + TWARP; j < j1; j += TNWARP) {
         const int r = j - jL0;
-        for (int k = ka + TLANE; k <= kb; k += 32) {
+        for (int k = wa + TLANE; k <= wb; k += 32) {
             const int cc = k - kL0;
-            if (MODE == 1) {
+            if (MODE == 1 && k >= ka && k <= kb) {
                 const double rv = (double)tile_residual(g, t, r, cc, j);
                 sq += rv * rv;
             }
-            if (MODE == 2)
-                u64[(long)j * P64 + k] += (double)t.u[r * t.W + cc];
-            else
-                g.u[(long)j * g.P + k] = t.u[r * t.W + cc];
+            dst[(long)j * g.P + k] = t.u[r * t.W + cc];
         }
     }
     if (MODE == 1) {

@@ -153,7 +153,10 @@ __device__ inline int solve_begin_dev(const double *scal, SolveState *st, int re
     else st->total_solves++;
     st->kernels += (unsigned long long)n_kernels;
     int go = !(delta <= thr);
-    if (go && !isfinite(delta)) {
+    // a non-finite norm of the guess or of the zero-interior residual (the
+    // relative tolerance's scale): the boundary data or the guess hold an
+    // infinity or a NaN, and no cycle can reach the tolerance
+    if (!isfinite(delta) || !isfinite(thr)) {
         st->flag |= 1;
         go = 0;
     }
@@ -284,7 +287,8 @@ struct qd_solver {
 
 namespace qd {
 // mg.cu
-int mg_alloc(qd_solver *s, const double *mu_equi_host);
+// jrow: the depth metric per staggered row of mu_equi (2nz-1 values), or null
+int mg_alloc(qd_solver *s, const double *mu_equi_host, const double *jrow_host);
 void mg_free(qd_solver *s);
 int mg_solve(qd_solver *s, int *cycles, double *rnorm, double *r0norm);
 int mg_smooth(qd_solver *s, int level, int nsweeps);
@@ -298,6 +302,8 @@ void tma_cache_free(qd_solver *s);
 int tail_image_build(qd_solver *s);
 int tiles_set(qd_solver *s, int box_up, int box_down);
 int time_kernel(qd_solver *s, int which, int reps, double *us);
+// a bounded mbarrier wait that nothing completes (gives up after `polls`)
+int wait_probe(qd_solver *s, unsigned polls);
 // mg.cu: level-0 norms into d_scal[slot] (to32: FP64 residual -> FP32 rhs)
 int level0_norm(qd_solver *s, int to32, int slot);
 int level0_norm_decide(qd_solver *s, const Decide &dc);

@@ -39,11 +39,11 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
                  : "memory");
 }
 
-// true once the phase with this parity has completed; false after
-// TMA_WAIT_LIMIT polls
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
+// true once the phase with this parity has completed; false after `limit`
+// polls
+__device__ __forceinline__ bool mbar_wait_limit(uint64_t *bar, unsigned parity, unsigned limit) {
     const uint32_t a = smem_u32(bar);
-    for (unsigned i = 0; i < TMA_WAIT_LIMIT; i++) {
+    for (unsigned i = 0; i < limit; i++) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
@@ -55,6 +55,11 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
         if (done) return true;
     }
     return false;
+}
+
+// the wait every staging pipeline uses: TMA_WAIT_LIMIT polls
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
+    return mbar_wait_limit(bar, parity, TMA_WAIT_LIMIT);
 }
 
 // 2-D tile load: box at (x, y) of the tensor into shared memory

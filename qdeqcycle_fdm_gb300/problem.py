@@ -56,11 +56,62 @@ class Problem:
     maxdt: float
     totTol: float
     maxNumSteps: int
+    jrow: Optional[np.ndarray] = None   # depth metric per staggered row (stretched grids)
 
 
 def depth_of_rows(nk: int, dh: float) -> np.ndarray:
     """Depth (m) of every ghosted row k = 0..nk+1 (coord.cpp:27)."""
     return (nk - np.arange(nk + 2, dtype=np.float64)) * dh
+
+
+def _lncosh(x):
+    a = np.abs(x)
+    return a + np.log1p(np.exp(-2.0 * a)) - np.log(2.0)
+
+
+def depth_metric(cfg: ProblemConfig):
+    """A grid stretched in depth (the reference's is uniform, coord.cpp:18,27).
+
+    In the normalised depth xi in [0, 1] (0 at the surface) the row spacing
+    grows smoothly by cfg.stretch_ratio = R across a tanh transition:
+        d(xi) = D g(xi) / g(1),   g'(xi) = 1 + (R - 1) (1 + tanh((xi - xi0) / w)) / 2,
+        g(xi) = xi + (R - 1) / 2 [xi + w (lncosh((xi - xi0) / w) - lncosh(-xi0 / w))],
+    with w = cfg.stretch_width and xi0 placing the transition's centre at
+    cfg.stretch_depth_km.  The computational coordinate zeta = D xi has the
+    same uniform spacing as x, and the metric is J = dz/dzeta = g'(xi) / g(1).
+
+    Returns (depth of every ghosted row k = 0..nk+1 in m, J at every
+    staggered row r = 0..2nz-2 of mu_equi).  Ghosted row k is compact row
+    k - 1 at xi = 1 - (k - 1) / (nk - 1); staggered row r sits at compact
+    position r / 2 - 1.  The ghost rows' J mirrors the interior's about the
+    first and last rows, as the mirrored (Neumann) rows of the operator do.
+    """
+    nk = cfg.nk
+    D = cfg.domain_m
+    R, w = cfg.stretch_ratio, cfg.stretch_width
+
+    def g(xi, xi0):
+        return xi + 0.5 * (R - 1.0) * (xi + w * (_lncosh((xi - xi0) / w) - _lncosh(-xi0 / w)))
+
+    frac = cfg.stretch_depth_km * 1e3 / D
+    lo, hi = 0.0, 1.0
+    for _ in range(200):                    # g(xi0, xi0) / g(1, xi0) = frac, by bisection
+        mid = 0.5 * (lo + hi)
+        if g(mid, mid) / g(1.0, mid) < frac:
+            lo = mid
+        else:
+            hi = mid
+    xi0 = 0.5 * (lo + hi)
+    g1 = g(1.0, xi0)
+    n1 = nk - 1
+    k = np.arange(nk + 2, dtype=np.float64)
+    depth = D * g(1.0 - (k - 1.0) / n1, xi0) / g1
+    p = np.arange(2 * (nk + 2) - 1, dtype=np.float64) / 2.0 - 1.0
+    p = np.where(p < 0.0, -p, p)
+    p = np.where(p > n1, 2.0 * n1 - p, p)
+    xi = 1.0 - p / n1
+    jrow = (1.0 + 0.5 * (R - 1.0) * (1.0 + np.tanh((xi - xi0) / w))) / g1
+    return depth, np.ascontiguousarray(jrow)
 
 
 def mu_profile(cfg: ProblemConfig, depth_m: np.ndarray) -> np.ndarray:
@@ -92,7 +143,11 @@ def build_problem(cfg: ProblemConfig,
     ni, nk = cfg.ni, cfg.nk
     nx, nz = ni + 2, nk + 2
     dh = cfg.dh
-    depth = depth_of_rows(nk, dh)
+    jrow = None
+    if cfg.stretch_ratio != 1.0:
+        depth, jrow = depth_metric(cfg)
+    else:
+        depth = depth_of_rows(nk, dh)
     mu_rows = mu_profile(cfg, depth)
     mu_node = np.ascontiguousarray(np.repeat(mu_rows[:, None], nx, axis=1))
     rho = mu_node / (cfg.cs_kms ** 2)
@@ -129,4 +184,4 @@ def build_problem(cfg: ProblemConfig,
                    mu_equi=mu_equi, a=a, b=b, eta=eta, Tau_n0=Tau_n0, SlipShift=SlipShift,
                    tau0=tau0, Slip=Slip, psi=psi, U=U, f0=cfg.f0, V0=cfg.V0, L=cfg.Dc_m,
                    Vini=cfg.Vp, tmax=cfg.years * YEAR_S, ini_dt=cfg.ini_dt, mindt=cfg.mindt,
-                   maxdt=cfg.maxdt, totTol=cfg.totTol, maxNumSteps=cfg.maxNumSteps)
+                   maxdt=cfg.maxdt, totTol=cfg.totTol, maxNumSteps=cfg.maxNumSteps, jrow=jrow)

@@ -17,13 +17,21 @@ def env():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
-def init(backend: str):
-    """Join the process group when launched with more than one rank."""
+def init(backend: str, timeout_s: float | None = None):
+    """Join the process group when launched with more than one rank.
+
+    timeout_s bounds every collective: a rank that left or hangs makes the
+    others' next collective raise after that long instead of waiting for the
+    library's default (minutes)."""
     rank, world, local = env()
     if world > 1:
         import torch.distributed as dist
         if not dist.is_initialized():
-            dist.init_process_group(backend)
+            kw = {}
+            if timeout_s is not None:
+                import datetime
+                kw["timeout"] = datetime.timedelta(seconds=timeout_s)
+            dist.init_process_group(backend, **kw)
     return rank, world, local
 
 

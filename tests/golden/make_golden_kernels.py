@@ -1,7 +1,7 @@
 """Golden vectors from the reference's own CUDA kernels (run on a GPU).
 
 Loads oracle/_ref/ref_kernels.cubin (the reference's odeSolver.cpp kernels,
-compiled unmodified by oracle/Makefile) through tests/refkernels.py, drives
+compiled unmodified by oracle/Makefile) through oracle/refkernels.py, drives
 them with the reference's host sequencing on a seeded 65 x 65 problem and
 writes ref_kernels_golden.npz (to the path given, default next to this
 script): one smooth() at level 0, one coarse-level smooth() with a non-zero
@@ -18,10 +18,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
-sys.path.insert(0, os.path.join(ROOT, "tests"))
 
 import oracle  # noqa: E402
-import refkernels  # noqa: E402
+from oracle import refkernels  # noqa: E402
 from qdeqcycle_fdm_gb300 import config, problem  # noqa: E402
 
 

@@ -73,7 +73,7 @@ def test_oracle_multigrid_matches_reference_kernels(gold):
 
 @pytest.mark.gpu
 def test_live_reference_kernels_vs_oracle_and_library(gpu_lib, oracle_lib):
-    import refkernels
+    from oracle import refkernels
     if not refkernels.available():
         pytest.skip("oracle/_ref/ref_kernels.cubin not built (needs the reference sources)")
     import sys

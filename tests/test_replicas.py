@@ -23,7 +23,7 @@ def _worker(rank, world, port, out, fail_rank):
                       WORLD_SIZE=str(world), LOCAL_RANK=str(rank))
     import torch.distributed as dist
     from qdeqcycle_fdm_gb300 import replicas
-    r, w, _ = replicas.init("gloo")
+    r, w, _ = replicas.init("gloo", timeout_s=20.0)
     assert (r, w) == (rank, world)
     if rank == fail_rank:
         dist.destroy_process_group()
@@ -61,6 +61,16 @@ def test_two_replicas_aggregate_sum_over_max():
     assert codes == [0, 0]
     for rank, units, secs, value in res:
         assert units == 30.0 and secs == 3.0 and value == 10.0
+
+
+def test_failed_rank_is_reported_to_the_survivor():
+    """A rank that leaves between steps (its process group torn down, exit
+    code 3) makes the survivor's aggregation collective raise instead of
+    hanging; the survivor reports the error and exits cleanly."""
+    res, codes = _run(2, fail_rank=1)
+    assert codes[1] == 3
+    assert codes[0] == 0
+    assert len(res) == 1 and res[0][0] == 0 and res[0][1] == "error", res
 
 
 def test_single_rank_is_identity():
