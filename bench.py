@@ -85,7 +85,13 @@ def parse():
                    help="also run the plain FP64 drop-in (the reference's algorithm) through the full "
                         "cycle (about 2.5 minutes)")
     p.add_argument("--no-hbm", action="store_true", help="skip the 4097^2 HBM roofline of the V-cycle kernels")
+    p.add_argument("--hbm-only", action="store_true",
+                   help="only the 4097^2 level-0 kernel timings (for profilers)")
+    p.add_argument("--hbm-reps", type=int, default=50)
     p.add_argument("--no-ensemble", action="store_true")
+    p.add_argument("--ensemble-only", action="store_true", help="only the ensemble measurement")
+    p.add_argument("--ensemble-full", action="store_true",
+                   help="config 4's full mix (256 instances) instead of the 20-instance miniature")
     p.add_argument("--headline-only", action="store_true",
                    help="time only the headline solver (no FP64 comparison, e2e, cycle or CPU runs)")
     p.add_argument("--train-years", type=float, default=50.0,
@@ -107,8 +113,10 @@ def parse():
     p.add_argument("--schedule", default=None, help="nu_pre,nu_post of the fast runs (no tuning of them)")
     p.add_argument("--net-gate", type=float, default=0.0,
                    help="the network corrects a stage solve's guess when the guess's residual exceeds "
-                        "this multiple of the solve's threshold (0: when one V-cycle at the solver's "
-                        "measured reduction per cycle would not reach it)")
+                        "this multiple of the solve's threshold (0: the measured rule, see --net-cost)")
+    p.add_argument("--net-cost", type=float, default=2.0,
+                   help="with --net-gate 0: the network's cost in V-cycles; it corrects guesses that would need "
+                        "more than 1 + cost cycles")
     p.add_argument("--unet-level", type=int, default=1, choices=[0, 1, 2],
                    help="multigrid level whose grid the U-Net runs on (1: every other node, its "
                         "prediction prolongated bilinearly)")
@@ -354,6 +362,8 @@ def run_ours(args):
         if net is not None:
             net.attach(sim.solver, warmstart.MODE_PREDICT)
             warmstart.UNet.set_gate(sim.solver, args.net_gate)
+            if args.net_gate == 0.0:
+                warmstart.UNet.set_cost(sim.solver, args.net_cost)
         sim.resume(ck if start is None else start, params=params)
         return sim
 
@@ -383,6 +393,8 @@ def run_ours(args):
             hv = {k: pinned(nz) for k in ("Slip", "psi", "V", "dpsi", "Ts")}
             st = sim.solver.rk43_state(out=hv)
         barrier()
+        if args.profile_run:
+            torch.cuda.profiler.start()   # ncu --profile-from-start off: capture the timed steps only
         for _ in range(args.steps):
             flush.fill_(1.0)
             torch.cuda.synchronize()
@@ -402,6 +414,8 @@ def run_ours(args):
             e1.synchronize()
             step_ms.append(e0.elapsed_time(e1))
             ms += step_ms[-1]
+        if args.profile_run:
+            torch.cuda.profiler.stop()
         barrier()
         s1 = sim.state(with_u=False)
         if net is not None:
@@ -411,6 +425,8 @@ def run_ours(args):
                      "launches": s1["kernel_launches"] - s0["kernel_launches"],
                      "vcycles": s1["vcycles"] - s0["vcycles"], "solves": s1["solves"] - s0["solves"],
                      "net_solves": s1["net_solves"] - s0["net_solves"],
+                     "net_needed": s1["net_cycles_needed"] - s0["net_cycles_needed"],
+                     "net_taken": s1["net_cycles_taken"] - s0["net_cycles_taken"],
                      "attempts": s1["attempts"] - s0["attempts"], "autotune": tuning}
 
     def job_value(run):
@@ -425,6 +441,61 @@ def run_ours(args):
                 "vcycles_per_solve": run["vcycles"] / max(1, run["solves"]),
                 "solves_per_step": run["solves"] / args.steps, "sim_years_timed": run["yrs"],
                 "span_s": [run["t0"], run["t_end"]]}
+
+    def ensemble_run(ksteps=8, full=False):
+        """Config 4's mix -- 96 x 257^2 + 96 x 513^2 + 64 x 1025^2 seeded
+        instances (each its own parameters and adaptive dt) with full=True, or
+        in miniature (12 + 6 + 2) -- advanced by qd_ensemble_step (GPU work of
+        all instances interleaved) and, for comparison (miniature only), one
+        instance after the other.  Host wall clock with the device synchronised
+        on both sides (one stream per instance).  From steady sliding, after 3
+        warm-up steps: the instances' dt ramps up from ini_dt, so the
+        instance-years of the window say little; accepted instance-steps per
+        second is the rate that does not depend on the window."""
+        sizes = ([257] * 96 + [513] * 96 + [1025] * 64) if full else ([257] * 12 + [513] * 6 + [1025] * 2)
+        cfgs = [config.ensemble_instance(n, i) for i, n in enumerate(sizes)]
+        probs = [problem.build_problem(c) for c in cfgs]
+        out = {"instances": ("96 x 257^2 + 96 x 513^2 + 64 x 1025^2" if full else
+                             "12 x 257^2 + 6 x 513^2 + 2 x 1025^2") + " (config-4 parameter draws)",
+               "steps_timed": ksteps, "warmup": 3, "history": H,
+               "autotune": "per instance" if TUNE_ENSEMBLE else None}
+        for mode in (("batched",) if full else ("batched", "sequential")):
+            sims = [api.Simulation(p, c.mg) for p, c in zip(probs, cfgs)]
+            for x in sims:
+                x.solver.set_solution_history(H)
+                x.start()
+            if mode == "batched":
+                api.ensemble_step(sims, 3)
+            else:
+                for x in sims:
+                    x.step(3)
+            if TUNE_ENSEMBLE:
+                for x in sims:
+                    x.solver.autotune(2)          # on each instance's own state, untimed
+            t0 = [x.solver.rk43_state()["t"] for x in sims]
+            torch.cuda.synchronize()
+            w0 = time.perf_counter()
+            if mode == "batched":
+                api.ensemble_step(sims, ksteps)
+            else:
+                for x in sims:
+                    x.step(ksteps)
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - w0
+            yrs = sum(x.solver.rk43_state()["t"] - a for x, a in zip(sims, t0)) / YEAR_S
+            out[mode] = {"wall_s": wall, "ms_per_ensemble_step": 1e3 * wall / ksteps,
+                         "instance_steps_per_s": len(sims) * ksteps / wall,
+                         "instance_years_per_hr": yrs / (wall / 3600.0)}
+            for x in sims:
+                x.close()
+        if not full:
+            out["batched_speedup"] = out["sequential"]["wall_s"] / out["batched"]["wall_s"]
+        return out
+
+    if args.ensemble_only:
+        if rank == 0:
+            print(json.dumps({"ensemble": ensemble_run(full=args.ensemble_full)}), flush=True)
+        return 0
 
     mixed_cfg = config.MGConfig(**{**cfg.mg.__dict__, "precision": 1, "surface_prolong": 1,
                                    "coarse_solve": 1})
@@ -568,6 +639,8 @@ def run_ours(args):
                 "host_wall_s": wall, "vcycles_per_solve": (s1["vcycles"] - s0["vcycles"]) / max(1, s1["solves"] - s0["solves"]),
                 "solves_per_step": (s1["solves"] - s0["solves"]) / nst,
                 "network_corrected_solves": (s1["net_solves"] - s0["net_solves"]) / max(1, s1["solves"] - s0["solves"]),
+                "network_cycles_needed_taken": [s1["net_cycles_needed"] - s0["net_cycles_needed"],
+                                                s1["net_cycles_taken"] - s0["net_cycles_taken"]],
                 "ruptures_seen": ruptures}
 
     cycle = None
@@ -582,51 +655,8 @@ def run_ours(args):
         if args.cycle_plain:
             cycle["plain_fp64"] = cycle_run(fp64_cfg)
 
-    def ensemble_run(ksteps=8):
-        """Config 4 in miniature: 12 x 257^2 + 6 x 513^2 + 2 x 1025^2 seeded
-        instances (each its own parameters and adaptive dt), advanced by
-        qd_ensemble_step (GPU work of all instances interleaved) and, for
-        comparison, one instance after the other.  Host wall clock with the
-        device synchronised on both sides (the instances use 20 streams)."""
-        sizes = [257] * 12 + [513] * 6 + [1025] * 2
-        cfgs = [config.ensemble_instance(n, i) for i, n in enumerate(sizes)]
-        probs = [problem.build_problem(c) for c in cfgs]
-        out = {"instances": "12 x 257^2 + 6 x 513^2 + 2 x 1025^2 (config-4 parameter draws)",
-               "steps_timed": ksteps, "warmup": 3, "history": H,
-               "autotune": "per instance" if TUNE_ENSEMBLE else None}
-        for mode in ("batched", "sequential"):
-            sims = [api.Simulation(p, c.mg) for p, c in zip(probs, cfgs)]
-            for x in sims:
-                x.solver.set_solution_history(H)
-                x.start()
-            if mode == "batched":
-                api.ensemble_step(sims, 3)
-            else:
-                for x in sims:
-                    x.step(3)
-            if TUNE_ENSEMBLE:
-                for x in sims:
-                    x.solver.autotune(2)          # on each instance's own state, untimed
-            t0 = [x.solver.rk43_state()["t"] for x in sims]
-            torch.cuda.synchronize()
-            w0 = time.perf_counter()
-            if mode == "batched":
-                api.ensemble_step(sims, ksteps)
-            else:
-                for x in sims:
-                    x.step(ksteps)
-            torch.cuda.synchronize()
-            wall = time.perf_counter() - w0
-            yrs = sum(x.solver.rk43_state()["t"] - a for x, a in zip(sims, t0)) / YEAR_S
-            out[mode] = {"wall_s": wall, "ms_per_ensemble_step": 1e3 * wall / ksteps,
-                         "instance_years_per_hr": yrs / (wall / 3600.0)}
-            for x in sims:
-                x.close()
-        out["batched_speedup"] = out["sequential"]["wall_s"] / out["batched"]["wall_s"]
-        return out
-
     if not args.headline_only and not args.no_ensemble:
-        extra["ensemble"] = ensemble_run()
+        extra["ensemble"] = ensemble_run(full=args.ensemble_full)
 
     # Roofline.  The candidates are the kernels with the largest device time
     # in the headline step: the V-cycle's level-0 kernels and coarse tail and,
@@ -752,6 +782,10 @@ def run_ours(args):
             "vcycles_per_solve": head["vcycles"] / max(1, head["solves"]),
             "solves_per_step": head["solves"] / args.steps,
             "network_corrected_solves": head["net_solves"] / max(1, head["solves"]) if learned else None,
+            "network_gate": (f"measured: corrects guesses that would need more than {1 + args.net_cost:g} V-cycles"
+                             if args.net_gate == 0.0 else f"fixed: ||r|| > {args.net_gate:g} x threshold")
+            if learned else None,
+            "network_cycles_needed_taken": [head["net_needed"], head["net_taken"]] if learned else None,
             "attempts_per_step": head["attempts"] / args.steps,
             "autotune": head["autotune"],
             "error_vs_fp64": err,
@@ -832,14 +866,22 @@ def run_config2(args):
     e0.record(stream)
     w0 = time.perf_counter()
     hi, ruptures, vmax = False, 0, 0.0
+    rck = None        # a state inside the last rupture (20 calls after its onset), for the error check
+    since = -1
     while time.perf_counter() - w0 < args.config2_wall_s:
-        done = sim.step(50)
+        done = sim.step(10)
         st = sim.solver.rk43_state()
         v = float(np.max(st["V"][k]))
         vmax = max(vmax, v)
-        ruptures += int(v > 0.1 and not hi)
+        if v > 0.1 and not hi:
+            ruptures += 1
+            since = 0
         hi = v > 0.1
-        if done < 50:
+        if since >= 0:
+            since += 1
+            if since == 20 and hi:
+                rck = (checkpoints.from_state(st), sim.solver.download_u(), v)
+        if done < 10:
             break
     e1.record(stream)
     e1.synchronize()
@@ -847,8 +889,10 @@ def run_config2(args):
     s1 = sim.state(with_u=False)
     yrs = (s1["t"] - s0["t"]) / YEAR_S
     nst = s1["it"] - s0["it"]
-    ck = checkpoints.from_state(st)
-    U = sim.solver.download_u()
+    if rck is not None:
+        ck, U, v_ck = rck
+    else:
+        ck, U, v_ck = checkpoints.from_state(st), sim.solver.download_u(), v
     sim.close()
     run = {"sim_years": yrs, "steps": nst, "ms": ms, "ms_per_step": ms / max(1, nst),
            "value": yrs / (ms / 3.6e6), "vcycles_per_solve": (s1["vcycles"] - s0["vcycles"]) / max(1, s1["solves"] - s0["solves"]),
@@ -875,7 +919,8 @@ def run_config2(args):
         return {"u": rmax(g["U"], ex["U"]), "tau": rmax(g["Ts"][k] + prob.tau0[k], ex["Ts"][k] + prob.tau0[k]),
                 "V": float(np.max(np.abs(g["V"][k] - ex["V"][k]) / ex["V"][k])),
                 "slip": rmax(g["Slip"][k], ex["Slip"][k]), "psi": rmax(g["psi"][k], ex["psi"][k])}
-    err = {"steps": 5, "dt_s": dt, "reference": "FP64 V(2,2) cycles to a 1e-12 relative residual",
+    err = {"steps": 5, "dt_s": dt, "from": f"t = {ck['t'] / YEAR_S:.4f} yr, max V {v_ck:.3g} m/s",
+           "reference": "FP64 V(2,2) cycles to a 1e-12 relative residual",
            "mixed": errs(out["mixed"]), "fp64_at_1e-9": errs(out["fp64_1e-9"])}
 
     # level-0 kernels on this grid (arrays larger than L2)
@@ -904,6 +949,25 @@ def run_config2(args):
     return 0
 
 
+def run_hbm_only(args):
+    """Only the level-0 V-cycle kernels on the 4097^2 grid (hbm_kernels), for
+    profilers: 3 warm-up and --hbm-reps timed launches of each kernel."""
+    from qdeqcycle_fdm_gb300 import api, build, config, problem
+    build.build()
+    mixed = config.MGConfig(**{**config.config1().mg.__dict__, "precision": 1, "surface_prolong": 1,
+                               "coarse_solve": 1})
+    n0, n1 = 4097 * 4097, 2049 * 2049
+
+    def algo_bytes(ni, nk):
+        return {"up0": (24.0 + 20.0 * mixed.nu_post) * n0 + 4.0 * n1,
+                "down0": (16.0 + 20.0 * mixed.nu_pre) * n0 + 4.0 * n1, "residual": 36.0 * n0}
+    names = {"down0": "k_down<float> level 0", "up0": "k_up<float,2> level 0",
+             "residual": "k_residual64_to32"}
+    peak = _peaks().get("hbm_gbs", 6800.0)
+    print(json.dumps(hbm_kernels(api, config, problem, mixed, algo_bytes, names, peak, args.hbm_reps)), flush=True)
+    return 0
+
+
 def _peaks():
     try:
         return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -917,6 +981,8 @@ def main():
         return run_reference(args)
     if args.config == "config2":
         return run_config2(args)
+    if args.hbm_only:
+        return run_hbm_only(args)
     return run_ours(args)
 
 

@@ -105,6 +105,10 @@ typedef struct qd_stats {
     long long net_solves;    /* solves whose guess the attached network
                                 corrected (prediction mode: only solves
                                 whose guess missed the tolerance)          */
+    double net_cycles_needed; /* over those solves: the V-cycles their
+                                guesses would have needed (from the
+                                measured reduction per cycle) ...          */
+    double net_cycles_taken;  /* ... and the V-cycles they took            */
 } qd_stats;
 
 const char *qd_version(void);

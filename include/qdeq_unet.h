@@ -71,13 +71,19 @@ int qd_solver_warm_start(qd_solver *s, qd_unet *u, int mode, float lr);
 
 /* The gate of mode 2: the network corrects a solve's guess only when the
  * guess's residual norm exceeds ratio x the solve's threshold (ratio >= 1).
- * ratio 0 (the default): when one V-cycle would not reach the threshold from
- * the guess -- the ratio is 1 / rho, rho the solver's running geometric
- * mean of the residual reduction per V-cycle (measured on the device; 1
- * until a cycle has run).  A guess one cycle from the threshold takes that
- * cycle whatever the network adds, so the network is kept for the guesses
- * where it can save one. */
+ * ratio 0 (the default): the measured rule -- when the guess would need more
+ * than 1 + c V-cycles to reach the threshold, c the network's cost in
+ * V-cycles (qd_solver_warm_start_cost, default 2); the ratio is then
+ * rho^-(1 + c), rho the solver's running geometric mean of the residual
+ * reduction per V-cycle (measured on the device; 1 until a cycle has run).
+ * A correction can only pay where the cycles it saves cost more than the
+ * inference.  qd_stats.net_cycles_needed / net_cycles_taken report, over the
+ * corrected solves, the cycles their guesses needed and those they took. */
 int qd_solver_warm_start_gate(qd_solver *s, double ratio);
+/* The measured rule's cost of one correction in V-cycles (>= 0; 0 gives
+ * the rule "when one V-cycle would not reach the threshold"); selects the
+ * measured rule. */
+int qd_solver_warm_start_cost(qd_solver *s, double cycles);
 
 /* training steps taken, and the loss of the last step */
 int qd_unet_stats(qd_unet *u, long long *train_steps, float *last_loss);

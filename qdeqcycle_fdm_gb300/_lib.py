@@ -81,6 +81,7 @@ EXPORTS = [
     ("qd_unet_train_step_host", C.c_int, [C.c_void_p, _fp, _fp, C.c_float, _fp]),
     ("qd_solver_warm_start", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_float]),
     ("qd_solver_warm_start_gate", C.c_int, [C.c_void_p, C.c_double]),
+    ("qd_solver_warm_start_cost", C.c_int, [C.c_void_p, C.c_double]),
     ("qd_unet_stats", C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), _fp]),
     ("qd_unet_time", C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp]),
 ]
@@ -101,7 +102,8 @@ class Rk43Params(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("solves", C.c_longlong), ("vcycles", C.c_longlong), ("attempts", C.c_longlong),
                 ("steps", C.c_longlong), ("newton_iters", C.c_longlong),
-                ("kernel_launches", C.c_longlong), ("net_solves", C.c_longlong)]
+                ("kernel_launches", C.c_longlong), ("net_solves", C.c_longlong),
+                ("net_cycles_needed", C.c_double), ("net_cycles_taken", C.c_double)]
 
 
 class Tuning(C.Structure):

@@ -259,8 +259,9 @@ int qd_solver_create_mapped(int ni, int nk, double dh, const double *mu_equi, co
     *out = nullptr;
     QD_TRY(check_opts(opt));
     qd_solver *s = new qd_solver();
-    s->net_ratio = 0.0;   // the measured one-cycle gate
     memset((void *)s, 0, sizeof(*s));
+    s->net_cost = kNetCostCycles;   // the measured gate: run the network where a guess
+    s->net_ratio = -kNetCostCycles; // needs more than 1 + cost V-cycles
     s->ni = ni; s->nk = nk; s->nx = ni + 2; s->nz = nk + 2; s->dh = dh;
     s->opt = *opt;
     int rc = QD_OK;
@@ -335,6 +336,8 @@ int qd_get_stats(qd_solver *s, qd_stats *st) {
     // host-issued kernels plus the kernels the solve graphs ran on the device
     st->steps = s->steps; st->kernel_launches = s->launches + (long long)ss.kernels;
     st->net_solves = (long long)ss.net_solves;
+    st->net_cycles_needed = ss.net_cycles_needed;
+    st->net_cycles_taken = ss.net_cycles_taken;
     std::vector<int> it(s->nz);
     QD_CUDA(cudaMemcpy(it.data(), s->F.iters, s->nz * sizeof(int), cudaMemcpyDeviceToHost));
     long long sum = 0;

@@ -418,6 +418,10 @@ struct TileGeom {
 
 static constexpr int kBoxW = 64;       // default k_up boxes: one pass of 32 lanes per row
 static constexpr int kDownBoxW = 64;   // default k_down boxes (qd_autotune may pick others)
+// k_down's default box width: 64 columns, 128 on levels of 2049 columns or
+// more, where the halo's share matters more than a wave's fill (measured at
+// 4097^2: 203 us per launch with 128-column boxes, 207 with 64, 213 with 96)
+static int down_box_default(int K) { return K >= 2049 ? 128 : kDownBoxW; }
 static constexpr int kWaveCtas = 150;
 
 static size_t two_cta_smem() { return std::min<size_t>(smem_limit(), 112 * 1024); }
@@ -520,7 +524,7 @@ static int launch_down(qd_solver *s, Level<T> *Ls, int l, int S, int zero_u, boo
     const LvArgs<T> g = lv(s, Ls, l), c = lv(s, Ls, l + 1);
     // the residual goes into f, or into the dinv slot on the FP64 level 0
     const bool has_f = g.f != nullptr;
-    const TileGeom t = pick_down<T>(c.N, c.K, g.N, g.K, S, has_f, s->box_down ? s->box_down : kDownBoxW);
+    const TileGeom t = pick_down<T>(c.N, c.K, g.N, g.K, S, has_f, s->box_down ? s->box_down : down_box_default(g.K));
     const int BH = t.BH, W = t.W, CH = t.TH, CW = t.TW, ntj = t.ntj, ntk = t.ntk;
     const size_t smem = t.smem;
     if (BH > 256 || W > 256 || smem > smem_limit()) {
@@ -834,10 +838,11 @@ static int time_kernel_t(qd_solver *s, Level<T> *Ls, int which, int reps) {
     for (int i = 0; i < reps; i++) {
         switch (which) {
             case QD_KERNEL_DOWN0: {
-                // as in a cycle: level-0 u (the FP64 solution, or the FP32
-                // correction) in, the smoothed field into the scratch array
+                // as in a cycle: the FP64 solution in (the mixed solver's
+                // FP32 correction starts from zero and loads no u), the
+                // smoothed field into the scratch array
                 bool in_r = false;
-                QD_TRY(launch_down<T>(s, Ls, 0, S, 0, &in_r));
+                QD_TRY(launch_down<T>(s, Ls, 0, S, MODE_UP == 2 ? 1 : 0, &in_r));
                 break;
             }
             case QD_KERNEL_UP0: {

@@ -154,6 +154,29 @@ __device__ void tile_halfsweep(const LvArgs<T> &g, const STile<T> &t, int color)
     }
 }
 
+// The first (red) half-sweep from a zero field: every neighbour is zero, so
+// the update is u = dinv (0 - h2 f) -- the same value the general update
+// gives (all four products are zero), with no neighbour or face-modulus
+// loads.  Only the field's sign of zero can differ (-0 here where f = 0).
+template <typename T>
+__device__ void tile_first_halfsweep_from_zero(const LvArgs<T> &g, const STile<T> &t) {
+    const int cmax = min(t.LC - 2, g.K - 2 - t.kL0);
+    for (int r = TWARP; r < t.LR; r += TNWARP) {
+        const int j = t.jL0 + r;
+        const int rn = (j == 0) ? r + 1 : r - 1;
+        const int rs = (j == g.N - 1) ? r - 1 : r + 1;
+        if (rn < 0 || rn >= t.LR || rs < 0 || rs >= t.LR) continue;
+        const int p = (j + t.kL0) & 1;
+        const int sr = r * t.W;
+        for (int c = p + 2 * TLANE; c <= cmax; c += 64) {
+            if (c < 1) continue;
+            const int idx = sr + c;
+            const T f = t.f ? t.f[idx] : (T)0;
+            t.u[idx] = t.dv[idx] * ((T)0 - g.h2 * f);
+        }
+    }
+}
+
 // residual at local (r, c) of global row j (interior column, neighbours in tile)
 template <typename T>
 __device__ __forceinline__ T tile_residual(const LvArgs<T> &g, const STile<T> &t, int r, int c, int j) {
@@ -205,7 +228,10 @@ __global__ void __launch_bounds__(NT, 2)
     STile<T> t = carve<T>(smem, jL0, kL0, LR, LC, maps.BH, maps.W, has_f);
     if (!tile_load(g, maps, t, zero_u != 0, src_r != 0, &bar, status)) return;
     for (int s = 0; s < S; s++) {
-        tile_halfsweep(g, t, s & 1);
+        if (s == 0 && zero_u)
+            tile_first_halfsweep_from_zero(g, t);
+        else
+            tile_halfsweep(g, t, s & 1);
         __syncthreads();
     }
     T *res = t.f ? t.f : t.dv;
@@ -307,7 +333,10 @@ __global__ void __launch_bounds__(NT, 2)
         __syncthreads();
     }
     for (int s = 0; s < S; s++) {
-        tile_halfsweep(g, t, s & 1);
+        if (s == 0 && zero_u && !prolong)
+            tile_first_halfsweep_from_zero(g, t);
+        else
+            tile_halfsweep(g, t, s & 1);
         __syncthreads();
     }
     const int ka = max(1, k0), kb = min(g.K - 2, k1 - 1);

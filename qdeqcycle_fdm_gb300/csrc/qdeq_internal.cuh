@@ -88,6 +88,11 @@ enum : unsigned int { ST_NEWTON_NAN = 1u, ST_NEWTON_CAP = 2u, ST_NEWTON_BRACKET 
 // set by a multigrid tile kernel whose TMA staging did not complete
 static constexpr unsigned int ST_TMA_TIMEOUT = 8u;
 
+// The learned correction's default cost in V-cycles for the measured gate:
+// one inference on the level-1 grid of a 1025^2 solver (181 us) against one
+// V-cycle there with its FP64 residual (about 100 us) is about two cycles.
+static constexpr double kNetCostCycles = 2.0;
+
 // state of the device-driven multigrid loop (mg_graph.cu)
 struct SolveState {
     double thr, delta, r0;
@@ -100,6 +105,9 @@ struct SolveState {
     unsigned long long net_solves;        // solves whose guess the network corrected
     double log_rho;                       // running mean of log(||r|| after / before a V-cycle)
     unsigned long long rho_samples;       // cycles in that mean
+    // the corrected solves' V-cycles: those their guesses needed (estimated
+    // from the measured reduction per cycle) and those they took
+    double net_cycles_needed, net_cycles_taken;
 };
 
 // ---- programmatic dependent launch ----------------------------------------
@@ -136,10 +144,12 @@ static inline cudaError_t launch_pdl(bool pdl, void (*kern)(KArgs...), dim3 grid
 // graph's loop condition from it.
 // phase 0: a solve's only first decision; 1: the first decision of a solve
 // whose guess the network corrects when ||r|| of the guess exceeds
-// net_ratio x the threshold (st->net); net_ratio 0: by more than one
-// V-cycle's measured reduction, i.e. when one cycle would not reach the
-// threshold (ratio 1 / rho, rho = exp(log_rho), while no cycle has been
-// measured ratio 1); 2: the decision after that correction (the same solve)
+// ratio x the threshold (st->net): net_ratio >= 1 that fixed ratio;
+// net_ratio <= 0 the measured rule, ratio rho^-(1 + c) with c = -net_ratio
+// the network's cost in V-cycles and rho = exp(log_rho) the measured
+// reduction per cycle -- the guess would need more than 1 + c cycles
+// (ratio 1 while no cycle has been measured); 2: the decision after that
+// correction (the same solve)
 __device__ inline int solve_begin_dev(const double *scal, SolveState *st, int rel, double tol, int n_kernels,
                                       int phase, double net_ratio = 1.0) {
     const double r0 = rel ? sqrt(scal[1]) : 0.0;
@@ -163,8 +173,11 @@ __device__ inline int solve_begin_dev(const double *scal, SolveState *st, int re
     st->go = go;
     if (phase == 0) st->net = 0;
     else if (phase == 1) {
-        const double ratio = net_ratio > 0.0 ? net_ratio : (st->rho_samples ? exp(-st->log_rho) : 1.0);
+        const double ratio =
+            net_ratio > 0.0 ? net_ratio : (st->rho_samples ? exp(-(1.0 - net_ratio) * st->log_rho) : 1.0);
         st->net = go && !(delta <= ratio * thr);
+        if (st->net && st->rho_samples && st->log_rho < 0.0)
+            st->net_cycles_needed += ceil(log(delta / thr) / -st->log_rho);
     }
     return go;
 }
@@ -193,6 +206,7 @@ __device__ inline int solve_check_dev(const double *scal, SolveState *st, int ma
         st->flag |= 2;
         go = 0;
     }
+    if (!go && st->net) st->net_cycles_taken += st->cycles;
     st->go = go;
     return go;
 }
@@ -262,7 +276,9 @@ struct qd_solver {
     void *d_tail_img[2];   // coarse-tail coefficient images, FP32 [0] and FP64 [1]
     void *unet;            // attached warm-start network (unet.cu), or null
     bool net_paused;       // solves leave the attached network out (the autotuner's timing)
-    double net_ratio;      // the network corrects guesses with ||r|| > net_ratio x threshold
+    double net_ratio;      // the network's gate: >= 1 a fixed ratio of ||r|| to the threshold;
+                           // <= 0 the measured rule with a cost of -net_ratio V-cycles
+    double net_cost;       // the measured rule's cost (V-cycles)
     void *history;         // ring of earlier solutions for the initial guess (history.cu), or null
     void *snapshot;        // the snapshot writer in flight (io.cu), or null
     int tail_l0;           // first level of the coarse tail

@@ -1321,12 +1321,24 @@ int qd_solver_warm_start(qd_solver *s, qd_unet *u, int mode, float lr) {
     return QD_OK;
 }
 
+// s->net_ratio: >= 1 a fixed ratio; <= 0 the measured rule with a cost of
+// -net_ratio V-cycles (solve_begin_dev)
 int qd_solver_warm_start_gate(qd_solver *s, double ratio) {
     if (!s || !(ratio == 0.0 || ratio >= 1.0) || !isfinite(ratio)) {
         set_error("qd_solver_warm_start_gate: ratio must be 0 or finite and >= 1");
         return QD_ERR_ARG;
     }
-    s->net_ratio = ratio;
+    s->net_ratio = ratio == 0.0 ? -s->net_cost : ratio;
+    return QD_OK;
+}
+
+int qd_solver_warm_start_cost(qd_solver *s, double cycles) {
+    if (!s || !(cycles >= 0.0) || !isfinite(cycles)) {
+        set_error("qd_solver_warm_start_cost: the cost must be finite and >= 0 V-cycles");
+        return QD_ERR_ARG;
+    }
+    s->net_cost = cycles;
+    if (s->net_ratio <= 0.0) s->net_ratio = -cycles;
     return QD_OK;
 }
 

@@ -83,9 +83,16 @@ class UNet:
     def set_gate(solver, ratio: float) -> None:
         """Prediction mode's gate: the network corrects a solve's guess only
         when the guess's residual exceeds ratio x the solve's threshold;
-        ratio 0 (the default): when one V-cycle, at the solver's measured
-        reduction per cycle, would not reach the threshold."""
+        ratio 0 (the default): when the guess would need more than 1 + cost
+        V-cycles at the solver's measured reduction per cycle (set_cost,
+        default 2)."""
         check(solver.L.qd_solver_warm_start_gate(solver.h, float(ratio)))
+
+    @staticmethod
+    def set_cost(solver, cycles: float) -> None:
+        """The measured gate's cost of one correction in V-cycles (default
+        2): the network runs where a guess needs more than 1 + cost cycles."""
+        check(solver.L.qd_solver_warm_start_cost(solver.h, float(cycles)))
 
     def time(self, what: str = "forward", reps: int = 10):
         """(microseconds per run, tensor-core FLOPs per run) of one inference

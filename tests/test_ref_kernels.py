@@ -107,3 +107,40 @@ def test_live_reference_kernels_vs_oracle_and_library(gpu_lib, oracle_lib):
     cyc, rn, _ = s.ode_solve()
     assert cyc == cyc_ref
     assert rel(s.download_u()[1:-1, 1:-1], ref_mg) < 1e-11
+
+
+@pytest.mark.gpu
+def test_reference_gpu_path_under_the_oracle_rk43(gpu_lib, oracle_lib):
+    """The reference's GPU path as the bench's reference arm times it: the
+    oracle's RK43 loop with every elliptic solve done by the reference's own
+    kernels under its host sequencing (oracle/refgpu.c).  Three accepted
+    steps on a 65^2 problem against the same loop solving on the CPU with
+    the same schedule (6 levels V(32,32), relative 1e-10): same V-cycle
+    counts, states to 1e-9 (the kernels contract multiply-adds, the oracle
+    does not)."""
+    if not oracle.refgpu_available():
+        pytest.skip("oracle/_ref/ref_kernels.cubin not built (needs the reference sources)")
+    from qdeqcycle_fdm_gb300 import config, problem
+    cfg = config.small(65, mu_profile="layered", layer_depth_km=20.0)
+    prob = problem.build_problem(cfg, homogenize=lambda ni, nk, mu: oracle.set_medium(ni, nk, mu)[1])
+    runs = []
+    for gpu in (False, True):
+        sim = oracle.Simulation(prob, 6, 32, 32, 32, 1, 1e-10, 0)
+        rg = None
+        if gpu:
+            rg = oracle.RefGpuMultigrid(prob, rel=1, tol=1e-10)
+            rg.attach(sim)
+        sim.start()
+        for _ in range(3):
+            assert sim.step() == 0
+        runs.append(sim.state())
+        if rg is not None:
+            st = rg.stats()
+            assert st["solves"] == runs[-1]["solves"] and st["vcycles"] == runs[-1]["vcycles"]
+            rg.close()
+    cpu, gpu = runs
+    k = slice(1, prob.nk + 1)
+    assert gpu["vcycles"] == cpu["vcycles"]
+    assert rel(gpu["U"], cpu["U"]) < 1e-9
+    assert rel(gpu["V"][k], cpu["V"][k]) < 1e-9
+    assert abs(gpu["t"] - cpu["t"]) <= 1e-12 * cpu["t"]

@@ -126,6 +126,7 @@ def test_warm_start_coupled_to_the_solver():
     w0 = sim.state(with_u=False)
     steps, loss = net.stats()
     net.attach(sim.solver, warmstart.MODE_PREDICT)
+    warmstart.UNet.set_cost(sim.solver, 0.0)     # every guess one cycle or more from the threshold
     sim.step(K)
     w1 = sim.state(with_u=False)
     sim.close()
@@ -168,7 +169,11 @@ def test_prediction_runs_only_where_the_guess_misses():
         with pytest.raises(QdError):
             warmstart.UNet.set_gate(sim.solver, bad)
     warmstart.UNet.set_gate(sim.solver, 30.0)
-    warmstart.UNet.set_gate(sim.solver, 0.0)      # back to the measured one-cycle gate
+    warmstart.UNet.set_gate(sim.solver, 0.0)      # back to the measured rule ...
+    warmstart.UNet.set_cost(sim.solver, 0.0)      # ... at zero cost: any guess a cycle or more out
+    for bad in (-1.0, float("nan"), float("inf")):
+        with pytest.raises(QdError):
+            warmstart.UNet.set_cost(sim.solver, bad)
     sim.start()
     sim.step(2)
     s = sim.solver
@@ -229,11 +234,12 @@ def test_warm_start_on_a_coarse_grid(n, level):
     """A 33 x 33 network on the solver's level-1 grid (65 x 65 solver) or
     level-2 grid (129 x 129): its inputs are every other or every fourth
     level-0 node and its prediction is interpolated bilinearly.  It trains
-    on the solver's own solves, the run still follows the plain run (the
-    multigrid solves to its tolerance from the corrected guess), and the
-    prediction does not cost V-cycles: at most 1 % more than the plain run
-    (measured: 3.41 vs 3.73 per solve on the level-1 grid, 3.78 vs 3.79 on
-    the level-2 grid)."""
+    on the solver's own solves and the run still follows the plain run (the
+    multigrid solves to its tolerance from the corrected guess).  On the
+    level-1 grid the trained network must save V-cycles -- at least 5 %
+    (measured: 3.41 vs 3.73 per solve), so the test fails when it gains
+    nothing; on the level-2 grid (every fourth node) it saves none (3.78 vs
+    3.79), and the test holds it only to costing none (at most 1 % more)."""
     import dataclasses
     from qdeqcycle_fdm_gb300 import api, config, problem
     cfg = config.small(n)
@@ -261,6 +267,7 @@ def test_warm_start_on_a_coarse_grid(n, level):
     w0 = sim.state(with_u=False)
     steps, loss = net.stats()
     net.attach(sim.solver, warmstart.MODE_PREDICT)
+    warmstart.UNet.set_cost(sim.solver, 0.0)
     sim.step(K)
     w1 = sim.state(with_u=False)
     sim.close()
@@ -272,4 +279,12 @@ def test_warm_start_on_a_coarse_grid(n, level):
     assert w1["net_solves"] > w0["net_solves"]
     for k in ("Slip", "psi"):
         assert rel(w1[k], p1[k]) < 1e-5, (k, rel(w1[k], p1[k]))
-    assert c_ws <= 1.01 * c_plain, (c_ws, c_plain)
+    if level == 1:
+        assert c_ws <= 0.95 * c_plain, (c_ws, c_plain)
+        # the solver's own account of the corrected solves agrees: fewer
+        # cycles taken than their guesses needed
+        taken = w1["net_cycles_taken"] - w0["net_cycles_taken"]
+        needed = w1["net_cycles_needed"] - w0["net_cycles_needed"]
+        assert taken < needed, (taken, needed)
+    else:
+        assert c_ws <= 1.01 * c_plain, (c_ws, c_plain)
