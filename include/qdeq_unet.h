@@ -78,7 +78,12 @@ int qd_solver_warm_start(qd_solver *s, qd_unet *u, int mode, float lr);
  * reduction per V-cycle (measured on the device; 1 until a cycle has run).
  * A correction can only pay where the cycles it saves cost more than the
  * inference.  qd_stats.net_cycles_needed / net_cycles_taken report, over the
- * corrected solves, the cycles their guesses needed and those they took. */
+ * corrected solves, the cycles their guesses needed and those they took.
+ * Under the measured rule the RK43 driver also stands the network by for
+ * the next attempt when no solve of an attempt had a guess that needed it:
+ * those solves run the solve graph without the network's conditional node
+ * (it would have been left out of all of them), and the first guess that
+ * needs it brings the network's graph back for the attempt after. */
 int qd_solver_warm_start_gate(qd_solver *s, double ratio);
 /* The measured rule's cost of one correction in V-cycles (>= 0; 0 gives
  * the rule "when one V-cycle would not reach the threshold"); selects the

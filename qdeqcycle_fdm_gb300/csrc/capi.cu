@@ -159,6 +159,7 @@ static int step_begin(qd_solver *s) {
 static int attempt_enqueue(qd_solver *s) {
     const double *c = rk_c();
     s->attempts++;
+    QD_CUDA(cudaMemsetAsync(&s->d_solve->need_max, 0, sizeof(double), s->stream));
     if (s->t + s->dt > s->P.tmax) s->dt = s->P.tmax - s->t;
     for (int st = 2; st <= 6; st++) QD_TRY(stage(s, st, c[st]));
     QD_TRY(launch_error(s));
@@ -178,6 +179,7 @@ static int attempt_finish(qd_solver *s, int attemptCount, double *totErr, int *r
     // and makes that solve fail too
     QD_TRY(status_flag_error(*s->h_status));
     QD_TRY(solve_flag_error(*s->h_solve));
+    warm_start_standby_update(s, s->h_solve->need_max);
     *totErr = s->h_scal[2];
     *retry = 0;
     if (*totErr < s->P.totTol) return QD_OK;
@@ -390,6 +392,7 @@ int qd_download_u(qd_solver *s, double *U) {
 
 int qd_ode_solve(qd_solver *s, int *cycles, double *rnorm, double *r0norm) {
     if (!s) return QD_ERR_ARG;
+    s->net_standby = false;   // the standby is the RK loop's, decided per attempt
     return mg_solve(s, cycles, rnorm, r0norm);
 }
 

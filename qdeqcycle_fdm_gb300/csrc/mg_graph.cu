@@ -70,12 +70,26 @@ static bool same_opts(const qd_mg_options &a, const qd_mg_options &b) {
            a.surface_prolong == b.surface_prolong && a.coarse_solve == b.coarse_solve;
 }
 
-void solve_graph_free(qd_solver *s) {
-    SolveGraph *g = static_cast<SolveGraph *>(s->solve_graph);
+// The solver's instantiated solve graphs: [0] without the network's
+// correction, [1] with it (a predicting solver switches between them when
+// the warm start stands by, see warm_start_standby_update)
+struct SolveGraphs {
+    SolveGraph *g[2] = {nullptr, nullptr};
+};
+
+static void graph_free(SolveGraph *g) {
     if (!g) return;
     if (g->exec) cudaGraphExecDestroy(g->exec);
     if (g->graph) cudaGraphDestroy(g->graph);
     delete g;
+}
+
+void solve_graph_free(qd_solver *s) {
+    SolveGraphs *gs = static_cast<SolveGraphs *>(s->solve_graph);
+    if (!gs) return;
+    graph_free(gs->g[0]);
+    graph_free(gs->g[1]);
+    delete gs;
     s->solve_graph = nullptr;
 }
 
@@ -279,18 +293,23 @@ static int solve_eager(qd_solver *s) {
 // Enqueue one solve on the solver's stream (no host synchronisation).
 int mg_solve_async(qd_solver *s) {
     if (eager_solve()) return solve_eager(s);
-    SolveGraph *sg = static_cast<SolveGraph *>(s->solve_graph);
-    if (sg && (!same_opts(sg->opt, s->opt) || sg->net != warm_start_predicting(s) ||
-               sg->net_ratio != s->net_ratio)) {
-        solve_graph_free(s);
+    SolveGraphs *gs = static_cast<SolveGraphs *>(s->solve_graph);
+    if (!gs) {
+        gs = new SolveGraphs();
+        s->solve_graph = gs;
+    }
+    const int key = warm_start_predicting(s) ? 1 : 0;
+    SolveGraph *&sg = gs->g[key];
+    if (sg && (!same_opts(sg->opt, s->opt) || sg->net_ratio != s->net_ratio)) {
+        graph_free(sg);
         sg = nullptr;
     }
     if (!sg) {
         sg = new SolveGraph();
-        s->solve_graph = sg;
         const int rc = build(s, sg);
         if (rc != QD_OK) {
-            solve_graph_free(s);
+            graph_free(sg);
+            sg = nullptr;
             return rc;
         }
     }

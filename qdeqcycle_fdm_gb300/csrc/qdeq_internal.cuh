@@ -108,6 +108,10 @@ struct SolveState {
     // the corrected solves' V-cycles: those their guesses needed (estimated
     // from the measured reduction per cycle) and those they took
     double net_cycles_needed, net_cycles_taken;
+    // the most V-cycles any solve's first guess needed since the host last
+    // cleared it (1e30 while no cycle has been measured): the host's
+    // warm-start standby reads it once per RK attempt
+    double need_max;
 };
 
 // ---- programmatic dependent launch ----------------------------------------
@@ -171,6 +175,10 @@ __device__ inline int solve_begin_dev(const double *scal, SolveState *st, int re
         go = 0;
     }
     st->go = go;
+    if (go && phase != 2) {
+        const double need = (st->rho_samples && st->log_rho < 0.0) ? ceil(log(delta / thr) / -st->log_rho) : 1e30;
+        st->need_max = fmax(st->need_max, need);
+    }
     if (phase == 0) st->net = 0;
     else if (phase == 1) {
         const double ratio =
@@ -276,6 +284,7 @@ struct qd_solver {
     void *d_tail_img[2];   // coarse-tail coefficient images, FP32 [0] and FP64 [1]
     void *unet;            // attached warm-start network (unet.cu), or null
     bool net_paused;       // solves leave the attached network out (the autotuner's timing)
+    bool net_standby;      // ... and while no guess of the last RK attempt needed the network
     double net_ratio;      // the network's gate: >= 1 a fixed ratio of ||r|| to the threshold;
                            // <= 0 the measured rule with a cost of -net_ratio V-cycles
     double net_cost;       // the measured rule's cost (V-cycles)
@@ -334,6 +343,8 @@ int mg_solve_async(qd_solver *s);
 int solve_state_read(qd_solver *s, SolveState *out);
 int solve_state_clear_flag(qd_solver *s);
 void solve_graph_free(qd_solver *s);
+// unet.cu: the warm start's standby decision from an RK attempt's need_max
+void warm_start_standby_update(qd_solver *s, double need_max);
 // fault.cu
 int fault_alloc(qd_solver *s);
 void fault_free(qd_solver *s);

@@ -1112,7 +1112,19 @@ int warm_start_after_boundary(qd_solver *s) {
 
 bool warm_start_predicting(qd_solver *s) {
     const qd_unet *u = static_cast<const qd_unet *>(s->unet);
-    return u && u->mode == 2 && !s->net_paused;
+    return u && u->mode == 2 && !s->net_paused && !s->net_standby;
+}
+
+// The host's side of the measured gate, once per RK attempt: when no solve
+// of the attempt just finished had a first guess that needed more than
+// 1 + cost V-cycles, the next attempt's solves run the graph without the
+// network's conditional correction (the device gate would have left the
+// network out of all of them anyway, and the conditional node itself costs
+// time); as soon as one does, the network's graph comes back.  Only with the
+// measured rule and in prediction mode.
+void warm_start_standby_update(qd_solver *s, double need_max) {
+    const qd_unet *u = static_cast<const qd_unet *>(s->unet);
+    s->net_standby = u && u->mode == 2 && s->net_ratio <= 0.0 && !(need_max > 1.0 + s->net_cost);
 }
 
 // features, the forward pass and u0 = u, u += prediction (k_apply); all on
@@ -1313,6 +1325,7 @@ int qd_solver_warm_start(qd_solver *s, qd_unet *u, int mode, float lr) {
     if (!u->d_u_start) QD_CUDA(cudaMalloc(&u->d_u_start, sizeof(double) * (size_t)s->dims[0].N * s->dims[0].P));
     if (s->unet != u) QD_CUDA(cudaMemset(u->d_prev, 0, sizeof(float) * (size_t)u->g[0].P));   // a new run
     solve_graph_free(s);     // the solve graph holds the attached network's kernels
+    s->net_standby = false;
     u->stream = s->stream;   // the net runs on the solver's stream while attached
     u->stride = stride;
     u->mode = mode;
