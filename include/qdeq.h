@@ -287,13 +287,14 @@ int qd_rk43_resume(qd_solver *s, const qd_rk43_params *p, const double *Slip,
                    double errA1, int it);
 /* Batched ensemble: advance n independent, started solvers (any grids and
  * parameters, each with its own adaptive dt) by nsteps accepted steps each,
- * interleaving their GPU work: every instance's attempt (stages 2-6 and the
- * error estimate) is queued on its own stream before the host waits on any,
- * so the kernels of small instances fill the GPU together.  Each instance
- * follows exactly the operations qd_rk43_step would run on it.  An instance
- * at tmax or maxNumSteps stops; steps_done (n entries, may be NULL) gets the
- * steps each took.  No counterpart in the reference, which runs one
- * simulation per process. */
+ * interleaving their GPU work on their own streams.  Every instance runs its
+ * own sequence of attempts and commits; the host serves whichever
+ * instance's queued work has finished (an event per instance, polled), so
+ * no instance waits for the others' steps and the kernels of many instances
+ * fill the GPU together.  Each instance follows exactly the operations
+ * qd_rk43_step would run on it.  An instance at tmax or maxNumSteps stops;
+ * steps_done (n entries, may be NULL) gets the steps each took.  No
+ * counterpart in the reference, which runs one simulation per process. */
 int qd_ensemble_step(qd_solver **s, int n, int nsteps, int *steps_done);
 /* State read-back (any pointer may be NULL): Slip, psi, V (= f1.V_f),
  * Ts, dpsi (= f1.dpsi). */
