@@ -123,6 +123,10 @@ def parse():
     p.add_argument("--history", type=int, default=4,
                    help="stored solutions of the solution-history guess (0: start every solve "
                         "from the previous solution, as the reference)")
+    p.add_argument("--newton-start", type=int, default=1, choices=[0, 1],
+                   help="Newton start of the fast solvers (1: a binary32 solve of the log form, then the "
+                        "reference's FP64 iteration; 0: the reference's x = 0); the plain FP64 drop-in and "
+                        "the FP64 reference of the error measurement keep 0")
     p.add_argument("--config2-wall-s", type=float, default=240.0,
                    help="--config config2: seconds of stepping from steady sliding")
     p.add_argument("--error-steps", type=int, default=10,
@@ -337,6 +341,7 @@ def run_ours(args):
         tprob = problem.build_problem(tcfg)
         tsim = api.Simulation(tprob, mg)
         tsim.solver.set_solution_history(H)
+        tsim.solver.set_newton_start(args.newton_start)
         net = warmstart.UNet(unet_n(tprob.nk), unet_n(tprob.ni), seed=args.seed)
         net.attach(tsim.solver, warmstart.MODE_TRAIN, args.lr)
         tsim.start()
@@ -355,10 +360,12 @@ def run_ours(args):
         return net, {"train_samples": n, "last_loss": loss, "train_instance_seed": tcfg.seed,
                      "train_years": st["t"] / YEAR_S, "train_steps": st["it"], "train_wall_s": wall}
 
-    def resumed(mg, history=0, net=None, start=None, params=None):
-        """A solver restarted from a checkpoint (the window's by default)."""
+    def resumed(mg, history=0, net=None, start=None, params=None, newton=None):
+        """A solver restarted from a checkpoint (the window's by default);
+        newton: the Newton start (default --newton-start)."""
         sim = api.Simulation(prob, mg)
         sim.solver.set_solution_history(history)
+        sim.solver.set_newton_start(args.newton_start if newton is None else newton)
         if net is not None:
             net.attach(sim.solver, warmstart.MODE_PREDICT)
             warmstart.UNet.set_gate(sim.solver, args.net_gate)
@@ -367,7 +374,7 @@ def run_ours(args):
         sim.resume(ck if start is None else start, params=params)
         return sim
 
-    def timed_run(mg, host_io=False, net=None, history=0, tune=False):
+    def timed_run(mg, host_io=False, net=None, history=0, tune=False, newton=None):
         """Restart from the window checkpoint, W untimed warm-up steps, then
         K steps each bracketed by CUDA events on the solver's stream (L2
         flushed before each); with `history` >= 2 every stage solve starts
@@ -376,7 +383,7 @@ def run_ours(args):
         after the warm-up steps (outside the timed region).  host_io: every
         step goes through the C ABI with host buffers -- state and u uploaded
         from pinned memory before, read back after (the e2e measurement)."""
-        sim = resumed(mg, history, net)
+        sim = resumed(mg, history, net, newton=newton)
         sim.step(args.warmup)
         tuning = sim.solver.autotune(3) if tune else None
         stream = torch.cuda.ExternalStream(sim.solver.stream_ptr())
@@ -424,6 +431,7 @@ def run_ours(args):
                      "t0": s0["t"], "t_end": s1["t"], "it0": s0["it"], "it1": s1["it"],
                      "launches": s1["kernel_launches"] - s0["kernel_launches"],
                      "vcycles": s1["vcycles"] - s0["vcycles"], "solves": s1["solves"] - s0["solves"],
+                     "newton": (s1["newton_iters"] - s0["newton_iters"]) / max(1, (s1["solves"] - s0["solves"]) * prob.nk),
                      "net_solves": s1["net_solves"] - s0["net_solves"],
                      "net_needed": s1["net_cycles_needed"] - s0["net_cycles_needed"],
                      "net_taken": s1["net_cycles_taken"] - s0["net_cycles_taken"],
@@ -440,6 +448,7 @@ def run_ours(args):
         return {"value": job_value(run), "ms_per_step": reduce_max(run["ms"]) / args.steps,
                 "vcycles_per_solve": run["vcycles"] / max(1, run["solves"]),
                 "solves_per_step": run["solves"] / args.steps, "sim_years_timed": run["yrs"],
+                "newton_iters_per_node_solve": run["newton"],
                 "span_s": [run["t0"], run["t_end"]]}
 
     def ensemble_run(ksteps=8, full=False):
@@ -463,6 +472,7 @@ def run_ours(args):
             sims = [api.Simulation(p, c.mg) for p, c in zip(probs, cfgs)]
             for x in sims:
                 x.solver.set_solution_history(H)
+                x.solver.set_newton_start(args.newton_start)
                 x.start()
             if mode == "batched":
                 api.ensemble_step(sims, 3)
@@ -557,7 +567,7 @@ def run_ours(args):
             simh, fh = timed_run(fp64s_cfg, history=H)
             simh.close()
             extra["fp64_history"] = summary(fh)
-        sim64, plain = timed_run(fp64_cfg)
+        sim64, plain = timed_run(fp64_cfg, newton=0)
         sim64.close()
         sim64s, plain_s = timed_run(fp64s_cfg)
         sim64s.close()
@@ -578,7 +588,7 @@ def run_ours(args):
         runs = {}
         for name, mg, hist, nn in (("exact", tight, 0, None), ("fp64_1e-9", fp64s_cfg, 0, None),
                                    ("headline", mixed_cfg, H, net)):
-            s = resumed(mg, hist, nn, params=params)
+            s = resumed(mg, hist, nn, params=params, newton=0 if name == "exact" else None)
             s.step(nsteps)
             runs[name] = s.state()
             if nn is not None:
@@ -777,10 +787,13 @@ def run_ours(args):
                        "span_s": [head["t0"], head["t_end"]],
                        "mg": f"{cfg.mg.n_levels} levels V({sched[0]},{sched[1]}), "
                              f"rel {cfg.mg.tol:g}, {mode}, exact coarsest solve, surface-row prolongation",
+                       "newton_start": ("binary32 log-form solve, then the reference's FP64 iteration"
+                                        if args.newton_start else "the reference's x = 0"),
                        "parallelism": f"replicas x{world}", "l2": "flushed before every timed step"},
             "sim_years_timed": head["yrs"], "t_start_s": head["t0"], "t_end_s": head["t_end"],
             "vcycles_per_solve": head["vcycles"] / max(1, head["solves"]),
             "solves_per_step": head["solves"] / args.steps,
+            "newton_iters_per_node_solve": head["newton"],
             "network_corrected_solves": head["net_solves"] / max(1, head["solves"]) if learned else None,
             "network_gate": (f"measured: corrects guesses that would need more than {1 + args.net_cost:g} V-cycles"
                              if args.net_gate == 0.0 else f"fixed: ||r|| > {args.net_gate:g} x threshold")
@@ -794,8 +807,9 @@ def run_ours(args):
             "plain_fp64": None if plain is None else {
                 "value": plain_value, "ms_per_step": plain["ms"] / args.steps,
                 "vcycles_per_solve": plain["vcycles"] / max(1, plain["solves"]),
+                "newton_iters_per_node_solve": plain["newton"],
                 "mg": "the reference's algorithm: prolongation without the surface row, coarsest-level sweeps, "
-                      "previous-solution start"},
+                      "previous-solution start, Newton from x = 0"},
             "speedup_vs_plain_fp64": value / world / plain_value if plain_value else None,
             "gpu_launches": head["launches"],
             "roofline": roofline, "clocks": clk, "e2e": e2e, "cpu_baseline": cpu,
@@ -858,6 +872,7 @@ def run_config2(args):
     k = slice(1, prob.nk + 1)
     sim = api.Simulation(prob, cfg.mg)
     sim.solver.set_solution_history(args.history)
+    sim.solver.set_newton_start(args.newton_start)
     sim.start()
     stream = torch.cuda.ExternalStream(sim.solver.stream_ptr())
     s0 = sim.state(with_u=False)
@@ -907,6 +922,7 @@ def run_config2(args):
     for name, mg, hist in (("exact", tight, 0), ("fp64_1e-9", fp64, 0), ("mixed", cfg.mg, args.history)):
         x = api.Simulation(prob, mg)
         x.solver.set_solution_history(hist)
+        x.solver.set_newton_start(args.newton_start if name == "mixed" else 0)
         x.resume(ck, U=U, params=params)
         x.step(5)
         out[name] = x.state()

@@ -205,10 +205,16 @@ int qd_mg_time_kernel(qd_solver *s, int kernel, int reps, double *us);
 int qd_probe_bounded_wait(qd_solver *s, int polls);
 
 /* The binary64 -> binary32 rounding (to nearest, ties to even) that the
- * mixed-precision residual kernel performs on the device's integer pipes,
+ * learned warm start's input kernels perform on the device's integer pipes,
  * applied to n host values (a device round trip), so that tests can hold it
  * to IEEE conversion on the host.  No counterpart in the reference. */
 int qd_convert_f64_to_f32(const double *in, float *out, int n);
+
+/* The binary64 -> double-float split (x = hi + lo, two binary32 values,
+ * to within 2^-47 |x|) that the mixed-precision residual kernel performs on
+ * the device's integer pipes, applied to n host values (a device round
+ * trip), for tests.  No counterpart in the reference. */
+int qd_split_f64(const double *in, float *hi, float *lo, int n);
 
 /* The level-0 residual norm ||0 - A u||2 that qd_mg_residual_norm returns,
  * for a caller that cannot allocate device memory: a host framework that
@@ -287,14 +293,13 @@ int qd_rk43_resume(qd_solver *s, const qd_rk43_params *p, const double *Slip,
                    double errA1, int it);
 /* Batched ensemble: advance n independent, started solvers (any grids and
  * parameters, each with its own adaptive dt) by nsteps accepted steps each,
- * interleaving their GPU work on their own streams.  Every instance runs its
- * own sequence of attempts and commits; the host serves whichever
- * instance's queued work has finished (an event per instance, polled), so
- * no instance waits for the others' steps and the kernels of many instances
- * fill the GPU together.  Each instance follows exactly the operations
- * qd_rk43_step would run on it.  An instance at tmax or maxNumSteps stops;
- * steps_done (n entries, may be NULL) gets the steps each took.  No
- * counterpart in the reference, which runs one simulation per process. */
+ * interleaving their GPU work: every instance's attempt (stages 2-6 and the
+ * error estimate) is queued on its own stream before the host waits on any,
+ * so the kernels of small instances fill the GPU together.  Each instance
+ * follows exactly the operations qd_rk43_step would run on it.  An instance
+ * at tmax or maxNumSteps stops; steps_done (n entries, may be NULL) gets the
+ * steps each took.  No counterpart in the reference, which runs one
+ * simulation per process. */
 int qd_ensemble_step(qd_solver **s, int n, int nsteps, int *steps_done);
 /* State read-back (any pointer may be NULL): Slip, psi, V (= f1.V_f),
  * Ts, dpsi (= f1.dpsi). */
@@ -346,6 +351,16 @@ int qd_set_tiles(qd_solver *s, int box_up, int box_down);
  * replaced (qd_upload_u, qd_rk43_set_state); a new run (qd_rk43_start) and
  * qd_checkpoint_load clear them, and a checkpoint file does not hold them. */
 int qd_set_solution_history(qd_solver *s, int m);
+/* Start of the Newton solve for slip rate where the seed is the
+ * reference's zero (every RK stage, fault.cpp:180-228 with
+ * odeSolver.cpp:1484-1488).  mode 0 (the default): x = 0, the reference's
+ * iterates.  mode 1: x from a binary32 Newton solve of the log form of the
+ * same equation, then the same FP64 iteration and stopping rule, which end
+ * at the same root (to the rule's 1e-10) in two or three FP64 steps where
+ * the reference's start takes up to eleven near a rupture front.  The
+ * iteration count the solver reports is then that of the FP64 steps.  No
+ * counterpart in the reference. */
+int qd_set_newton_start(qd_solver *s, int mode);
 /* The last fit: coef[0..6] the coefficients of the earlier solutions
  * (newest first), coef[7] the fit's boundary misfit over the change from
  * the latest solution's boundary data (1: no gain); *nd coefficients are

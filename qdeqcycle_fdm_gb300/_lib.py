@@ -42,6 +42,7 @@ EXPORTS = [
     ("qd_mg_residual_norm", C.c_int, [C.c_void_p, _dp]),
     ("qd_mg_time_kernel", C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp]),
     ("qd_convert_f64_to_f32", C.c_int, [_dp, _fp, C.c_int]),
+    ("qd_split_f64", C.c_int, [_dp, _fp, _fp, C.c_int]),
     ("qd_residual_norm_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                            C.c_int, C.c_double, C.c_void_p, _dp]),
     ("qd_fault_setup", C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp, C.c_double,
@@ -61,6 +62,7 @@ EXPORTS = [
     ("qd_rk43_set_state", C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp, C.c_double, C.c_double,
                                     C.c_double, C.c_double, C.c_int]),
     ("qd_set_solution_history", C.c_int, [C.c_void_p, C.c_int]),
+    ("qd_set_newton_start", C.c_int, [C.c_void_p, C.c_int]),
     ("qd_autotune", C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     ("qd_set_tiles", C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     ("qd_solution_history_fit", C.c_int, [C.c_void_p, _dp, _ip]),

@@ -233,6 +233,12 @@ class Solver:
         the previous solution as the reference)."""
         check(self.L.qd_set_solution_history(self.h, int(m)))
 
+    def set_newton_start(self, mode):
+        """Start of the Newton solve for slip rate: 0 the reference's x = 0
+        (the default), 1 a binary32 solve of the equation's log form; the
+        same FP64 iteration then ends at the same root in fewer steps."""
+        check(self.L.qd_set_newton_start(self.h, int(mode)))
+
     def autotune(self, reps=3):
         """Time the candidate smoother schedules and tile box widths on this
         solver's problem (the last stored solve replayed from the solution

@@ -10,7 +10,6 @@
 #include <stdarg.h>
 #include <string.h>
 
-#include <thread>
 #include <vector>
 
 #include "qdeq_internal.cuh"
@@ -113,8 +112,8 @@ static int reset_status(qd_solver *s) {
 // enqueued on the solver's stream without waiting
 static int stage(qd_solver *s, int st, double ratio) {
     QD_TRY(warm_start_before_boundary(s));     // no-ops without an attached network
-    QD_TRY(launch_stage_boundary(s, st, ratio, nullptr, nullptr));
-    QD_TRY(history_guess(s, warm_start_bc_buffer(s)));   // no-op unless enabled
+    QD_TRY(launch_stage_boundary(s, st, ratio, true));   // + the history fit when enabled
+    QD_TRY(history_apply(s, warm_start_bc_buffer(s)));   // no-op unless enabled
     QD_TRY(warm_start_after_boundary(s));
     QD_TRY(mg_solve_async(s));
     QD_TRY(warm_start_after_solve(s));
@@ -429,6 +428,15 @@ int qd_convert_f64_to_f32(const double *in, float *out, int n) {
     return convert_f64_f32(in, out, n);
 }
 
+int qd_split_f64(const double *in, float *hi, float *lo, int n) {
+    if (!in || !hi || !lo || n < 0) {
+        set_error("qd_split_f64: bad arguments");
+        return QD_ERR_ARG;
+    }
+    if (n == 0) return QD_OK;
+    return convert_f64_f32(in, hi, n, lo);
+}
+
 int qd_mg_time_kernel(qd_solver *s, int kernel, int reps, double *us) {
     if (!s || !us) {
         set_error("qd_mg_time_kernel: bad arguments");
@@ -479,7 +487,7 @@ int qd_set_boundary(qd_solver *s, const double *slip, double t_elapsed, double r
     const double t0 = s->t, dt0 = s->dt;
     s->t = t_elapsed;
     s->dt = dt;
-    int rc = launch_stage_boundary(s, 1, ratio, nullptr, nullptr);
+    int rc = launch_stage_boundary(s, 1, ratio, false);
     s->t = t0;
     s->dt = dt0;
     QD_TRY(rc);
@@ -590,79 +598,46 @@ int qd_ensemble_step(qd_solver **ss, int n, int nsteps, int *steps_done) {
             if (ss[j] == ss[i]) { set_error("qd_ensemble_step: solver %d listed twice", i); return QD_ERR_ARG; }
         if (steps_done) steps_done[i] = 0;
     }
-    // Each instance runs its own sequence of steps as a small state machine
-    // and the host serves whichever instance's GPU work has finished (an
-    // event per instance, polled): no instance waits for the others' steps,
-    // and every instance performs exactly the operations qd_rk43_step would.
-    enum Phase { IDLE, ATTEMPT, COMMIT, DONE };
-    struct Inst {
-        Phase ph = IDLE;
-        int att = 0, done = 0;
-        double err = 0.0;
-        cudaEvent_t ev = nullptr;
-    };
-    std::vector<Inst> in(n);
-    int rc = QD_OK;
-    for (int i = 0; i < n && rc == QD_OK; i++)
-        if (cudaEventCreateWithFlags(&in[i].ev, cudaEventDisableTiming) != cudaSuccess) {
-            set_error("qd_ensemble_step: event creation failed");
-            rc = QD_ERR_CUDA;
+    std::vector<char> act(n), trying(n);
+    std::vector<int> att(n);
+    std::vector<double> err(n);
+    for (int k = 0; k < nsteps; k++) {
+        int nact = 0;
+        for (int i = 0; i < n; i++) {
+            act[i] = can_step(ss[i]);
+            if (!act[i]) continue;
+            nact++;
+            QD_TRY(step_begin(ss[i]));
+            trying[i] = 1;
+            att[i] = 0;
         }
-    auto start_step = [&](int i) -> int {
-        Inst &x = in[i];
-        if (x.done >= nsteps || !can_step(ss[i])) {
-            x.ph = DONE;
-            return QD_OK;
-        }
-        QD_TRY(step_begin(ss[i]));
-        x.att = 1;
-        QD_TRY(attempt_enqueue(ss[i]));
-        QD_CUDA(cudaEventRecord(x.ev, ss[i]->stream));
-        x.ph = ATTEMPT;
-        return QD_OK;
-    };
-    for (int i = 0; i < n && rc == QD_OK; i++) rc = start_step(i);
-    int left = 0;
-    for (int i = 0; i < n; i++) left += in[i].ph != DONE;
-    while (rc == QD_OK && left > 0) {
-        bool progressed = false;
-        for (int i = 0; i < n && rc == QD_OK; i++) {
-            Inst &x = in[i];
-            if (x.ph == DONE) continue;
-            const cudaError_t q = cudaEventQuery(x.ev);
-            if (q == cudaErrorNotReady) continue;
-            if (q != cudaSuccess) {
-                set_error("qd_ensemble_step: %s", cudaGetErrorString(q));
-                rc = QD_ERR_CUDA;
-                break;
-            }
-            progressed = true;
-            if (x.ph == ATTEMPT) {
-                int retry = 0;
-                rc = attempt_finish(ss[i], x.att, &x.err, &retry);
-                if (rc != QD_OK) break;
-                if (retry) {
-                    x.att++;
-                    rc = attempt_enqueue(ss[i]);
-                } else {
-                    rc = commit_enqueue(ss[i]);
-                    x.ph = COMMIT;
+        if (!nact) break;
+        for (int left = nact; left > 0;) {
+            // every instance still trying enqueues its attempt before any waits
+            for (int i = 0; i < n; i++)
+                if (act[i] && trying[i]) {
+                    att[i]++;
+                    QD_TRY(attempt_enqueue(ss[i]));
                 }
-                if (rc == QD_OK && cudaEventRecord(x.ev, ss[i]->stream) != cudaSuccess) rc = QD_ERR_CUDA;
-            } else {   // COMMIT
-                rc = commit_finish(ss[i], x.err);
-                if (rc != QD_OK) break;
-                x.done++;
-                if (steps_done) steps_done[i] = x.done;
-                rc = start_step(i);
-                if (x.ph == DONE) left--;
-            }
+            for (int i = 0; i < n; i++)
+                if (act[i] && trying[i]) {
+                    int retry = 0;
+                    QD_TRY(attempt_finish(ss[i], att[i], &err[i], &retry));
+                    if (!retry) {
+                        trying[i] = 0;
+                        left--;
+                    }
+                }
         }
-        if (!progressed && rc == QD_OK) std::this_thread::yield();
+        for (int i = 0; i < n; i++)
+            if (act[i]) QD_TRY(commit_enqueue(ss[i]));
+        for (int i = 0; i < n; i++)
+            if (act[i]) {
+                QD_TRY(commit_finish(ss[i], err[i]));
+                if (steps_done) steps_done[i]++;
+            }
     }
-    for (int i = 0; i < n; i++)
-        if (in[i].ev) cudaEventDestroy(in[i].ev);
-    return rc;
+    return QD_OK;
 }
 
 int qd_rk43_step(qd_solver *s, int nsteps, int *steps_done) {
@@ -708,6 +683,15 @@ int qd_rk43_set_state(qd_solver *s, const double *Slip, const double *psi, const
     QD_CUDA(cudaStreamSynchronize(s->stream));
     s->t = t; s->dt = dt; s->errA[0] = errA0; s->errA[1] = errA1; s->it = it;
     s->started = 1;
+    return QD_OK;
+}
+
+int qd_set_newton_start(qd_solver *s, int mode) {
+    if (!s || (mode != 0 && mode != 1)) {
+        set_error("qd_set_newton_start: mode must be 0 or 1");
+        return QD_ERR_ARG;
+    }
+    s->newton_start = mode;
     return QD_OK;
 }
 

@@ -4,7 +4,7 @@
 // node; nodes are independent (fault.cpp:139-232, odeSolver.cpp:1150-1238).
 #include <math.h>
 
-#include "qdeq_internal.cuh"
+#include "hist_fit.cuh"
 
 namespace qd {
 
@@ -53,12 +53,14 @@ struct FaultArgs {
     double *u0;  // level-0 displacement (compact, pitched)
     FaultState F;
     DevStatus *status;
+    int start32;    // Newton start: 0 the reference's x = 0, 1 newton_start32
 };
 
 static FaultArgs fargs(qd_solver *s) {
     FaultArgs a;
     a.nk = s->nk; a.K = s->dims[0].K; a.P = s->dims[0].P; a.dh = s->dh;
     a.u0 = s->L64[0].u; a.F = s->F; a.status = s->d_status;
+    a.start32 = s->newton_start;
     return a;
 }
 
@@ -81,29 +83,95 @@ __device__ __forceinline__ double log_sinh(double y) {
     return y > 20.0 ? y - 0.69314718055994531 + log1p(-exp(-2.0 * y)) : log(sinh(y));
 }
 
+// A single-precision start for the Newton iteration below (the solver's
+// Newton start mode 1).  With y = |x|, Y = |fb|/fa and r = Y - y the
+// equation is  (A/fa) sinh y = r  on 0 < y < Y, carried through ln(A/fa)
+// (A = 2 eta V0 e^{-psi/a} leaves binary32's range).  Each step is Newton on
+// the form that is nearly linear where the step is taken: the equation as
+// it stands, (A/fa) sinh y - r, where (A/fa) cosh y < 1 (the linear term
+// dominates its slope), and its log form  ln(A/fa) + ln sinh y - ln r
+// elsewhere (the exponential dominates: there the reference's iteration
+// from x = 0 walks down the exponential one unit of x per step, up to 11
+// steps near a rupture front).  Both are increasing in y; a step that
+// leaves the shrinking sign bracket bisects it.  The start is the least of
+// Y and ln(2|fb|/A + 1), both upper bounds of the root (sinh y >= (e^y -
+// 1)/2); at most 12 steps, to a relative step of 1e-6.  In binary32 on the
+// FP32 pipe this costs little against one FP64 step (GB300's FP64 pipe
+// issues about one instruction per SM clock).  The inputs are rounded on
+// the integer pipes (d2f_rne).  Returns x = sign(fb) y, or 0 (the
+// reference's seed) when fb = 0 or nothing finite came out.
+__device__ double newton_start32(double Ts, double Tn, double tau0, double a, double eta, double psi,
+                                 double V0) {
+    const float fb = d2f_rne(Ts + tau0), af = d2f_rne(a);
+    const float fa = af * fabsf(d2f_rne(Tn)), afb = fabsf(fb);
+    const float lnA = logf(2.f * d2f_rne(eta) * d2f_rne(V0)) - d2f_rne(psi) / af;
+    const float lnAf = lnA - logf(fa);                          // ln(A / fa)
+    const float Y = afb / fa;
+    if (!(Y > 0.f) || !isfinite(Y) || !isfinite(lnAf)) return 0.0;
+    const float t = 0.6931472f + logf(afb) - lnA;              // ln(2|fb|/A)
+    float y = fminf(Y, t > 15.f ? t : log1pf(expf(t)));
+    float ylo = 0.f, yhi = Y;
+    for (int it = 0; it < 12; it++) {
+        float ls, lc;                                           // ln sinh y, ln cosh y
+        if (y > 15.f) {
+            ls = lc = y - 0.6931472f;
+        } else {
+            ls = logf(sinhf(y));
+            lc = logf(coshf(y));
+        }
+        const float q = expf(fminf(lnAf + lc, 80.f));          // (A/fa) cosh y
+        const float r = Y - y;
+        float yn;
+        if (q < 1.f || !(r > 0.f)) {
+            const float g = expf(fminf(lnAf + ls, 80.f)) - r;
+            if (g > 0.f) yhi = fminf(yhi, y); else ylo = fmaxf(ylo, y);
+            yn = y - g / (q + 1.f);
+        } else {
+            const float G = lnAf + ls - logf(r);
+            if (G > 0.f) yhi = fminf(yhi, y); else ylo = fmaxf(ylo, y);
+            yn = y - G / (1.f / tanhf(y) + 1.f / r);
+        }
+        if (!(yn >= ylo && yn <= yhi)) yn = 0.5f * (ylo + yhi);
+        const bool done = fabsf(yn - y) <= 1e-6f * y;
+        y = yn;
+        if (done) break;
+    }
+    if (!(y > 0.f) || !isfinite(y)) return 0.0;
+    const double x = f2d_exact(y);
+    return fb > 0.f ? x : -x;
+}
+
 // NRsearch (fault.cpp:180-228) for one node, safeguarded.  Unknown
 // x = asinh(V e^{psi/a} / 2V0); residual g(x) = A sinh x + fa x - fb with
 // A = 2 eta V0 e^{-psi/a} > 0, fa = a |sigma_n| > 0, so g is increasing and
 // the root lies in the bracket between 0 and fb/fa.
 // Phase 1 is the reference's Newton step and stopping rule; from the
-// reference's seed (x = 0) its iterates never leave the bracket, so they are
+// reference's seed (x = 0) its iterates never leave the bracket (by more
+// than a few ulps, where an end of the bracket is the root), so they are
 // the reference's.  If a step leaves the bracket or overflows (the reference
 // then produces NaN and exits), phase 2 takes over: Newton on
 // G(y) = ln(A sinh y) - ln(|fb| - fa y), y = |x|, which is nearly linear
 // where sinh is exponential, with bisection whenever a step leaves the
-// shrinking bracket.
+// shrinking bracket.  start32: with the reference's zero seed, start from
+// newton_start32 instead (clamped into the bracket); the iteration and its
+// stopping rule are the same, so it ends at the same root in fewer FP64
+// steps (iters counts the FP64 steps).
 __device__ double newton_v(double Ts, double Tn, double tau0, double a, double eta, double psi,
-                           double V0, double Vseed, int *iters, unsigned int *flags) {
-    // the seed's x; a zero seed (the reference's, every stage after the
-    // first) gives x = +0 without the exponential and asinh while e^{psi/a}
-    // is finite, the same value the full expression gives
+                           double V0, double Vseed, int *iters, unsigned int *flags, bool start32 = false) {
     const double pa = psi / a;
-    double x = (Vseed == 0.0 && pa < 709.0) ? 0.0 : asinh(0.5 * Vseed / V0 * exp(pa));
     const double fa = a * fabs(Tn);
     const double fb = Ts + tau0;
     const double A = 2.0 * eta * V0 * exp(-pa);
     double lo, hi;
     if (fb >= 0.0) { lo = 0.0; hi = fb / fa; } else { lo = fb / fa; hi = 0.0; }
+    // the seed's x; a zero seed (the reference's, every stage after the
+    // first) gives x = +0 without the exponential and asinh while e^{psi/a}
+    // is finite, the same value the full expression gives
+    double x;
+    if (start32 && Vseed == 0.0)
+        x = fmin(fmax(newton_start32(Ts, Tn, tau0, a, eta, psi, V0), lo), hi);
+    else
+        x = (Vseed == 0.0 && pa < 709.0) ? 0.0 : asinh(0.5 * Vseed / V0 * exp(pa));
     if (!(x >= lo && x <= hi)) x = 0.5 * (lo + hi);
     const int itmax = 200;
     int it = 0;
@@ -119,7 +187,12 @@ __device__ double newton_v(double Ts, double Tn, double tau0, double a, double e
         if (!isnan(fy)) {
             if (fy > 0.0) hi = fmin(hi, x); else lo = fmax(lo, x);
         }
-        if (!(xn >= lo && xn <= hi) || isinf(fy) || isnan(fy)) {
+        // a step may end a few ulps past a bracket end that sits on the
+        // root (the linear term dominating, or the bracket closed to an
+        // ulp): that is where the reference's step ends too, not a step
+        // out of the bracket
+        const double slack = 4.0 * 2.220446049250313e-16 * fmax(fabs(lo), fabs(hi));
+        if (!(xn >= lo - slack && xn <= hi + slack) || isinf(fy) || isnan(fy)) {
             phase2 = true;
             *flags |= ST_NEWTON_BRACKET;
             break;
@@ -183,15 +256,10 @@ __device__ __forceinline__ void report(DevStatus *st, unsigned int flags, int no
 // kernels
 // ---------------------------------------------------------------------------
 
-// Stage combination k_s = y + dt sum_j a_sj f_j (odeSolver.cpp:1491-1561),
-// the Newton seed of the stage (f_s.V_f, zeroed by the reference, :1484-1488,
-// :1610) and setBoundary's two Dirichlet columns (:1162-1172).
-// stage 1 copies y (the start and the post-accept refresh, :1430,1606-1614).
-__global__ void k_stage_boundary(FaultArgs A, int stage, double t, double dt, double ratio) {
-    pdl_trigger();
-    pdl_wait();
-    const int k = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    if (k > A.nk) return;
+// one fault node of k_stage_boundary: the stage's k_s, its Newton seed and
+// the two Dirichlet values of row k-1 (also returned in g0, g1)
+__device__ __forceinline__ void stage_boundary_node(const FaultArgs &A, int stage, double t, double dt,
+                                                    double ratio, int k, double *g0, double *g1) {
     const FaultState &F = A.F;
     double ks = F.Slip[k], kp = F.psi[k];
     if (stage > 1) {
@@ -207,15 +275,49 @@ __global__ void k_stage_boundary(FaultArgs A, int stage, double t, double dt, do
     F.kslip[stage][k] = ks;
     F.kpsi[stage][k] = kp;
     double *row = A.u0 + (long)(k - 1) * A.P;
-    row[0] = 0.5 * ks;
-    row[A.K - 1] = 0.50 * F.Vini * (t + ratio * dt) + F.SlipShift[k];
+    *g0 = 0.5 * ks;
+    *g1 = 0.50 * F.Vini * (t + ratio * dt) + F.SlipShift[k];
+    row[0] = *g0;
+    row[A.K - 1] = *g1;
 }
 
-// Blocks past the fault nodes' copy the solved u into a history slot: the
-// Newton chains leave the SMs nearly idle, so the copy rides along instead
-// of taking a launch of its own.  Rows are dealt round-robin to the copy
-// blocks, 16-byte pairs across the block's threads, four pairs in flight
-// per thread.  The pitch P is even, so every pair is 16-byte aligned.
+// Stage combination k_s = y + dt sum_j a_sj f_j (odeSolver.cpp:1491-1561),
+// the Newton seed of the stage (f_s.V_f, zeroed by the reference, :1484-1488,
+// :1610) and setBoundary's two Dirichlet columns (:1162-1172).
+// stage 1 copies y (the start and the post-accept refresh, :1430,1606-1614).
+// With ND > 0 the same launch also fits the new boundary data by the
+// solution history's (hist_fit.cuh): each thread adds its node's two
+// boundary values to the normal equations and the last block solves them,
+// so the guess needs no launch of its own for the fit.
+template <int ND>
+__global__ void __launch_bounds__(FIT_THREADS)
+    k_stage_boundary(FaultArgs A, int stage, double t, double dt, double ratio, FitArgs fit) {
+    pdl_trigger();
+    pdl_wait();
+    const int k = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if constexpr (ND > 0) {
+        FitAcc<ND> acc;
+        acc.zero();
+        if (k <= A.nk) {
+            double g0, g1;
+            stage_boundary_node(A, stage, t, dt, ratio, k, &g0, &g1);
+            acc.add(fit, k - 1, g0);
+            acc.add(fit, fit.N + k - 1, g1);
+        }
+        fit_reduce_solve<ND>(fit, acc);
+    } else if (k <= A.nk) {
+        double g0, g1;
+        stage_boundary_node(A, stage, t, dt, ratio, k, &g0, &g1);
+    }
+}
+
+// Blocks past the fault nodes' copy the solved u into a history slot as
+// double-float pairs (d_split), and its boundary columns in FP64: the Newton
+// chains leave the SMs nearly idle, so the copy rides along instead of
+// taking a launch of its own.  Rows are dealt round-robin to the copy
+// blocks, 16-byte pairs of nodes across the block's threads, four pairs in
+// flight per thread.  The pitch P is even, so every pair is 16-byte aligned
+// in both fields.
 __device__ __forceinline__ void copy_rows(const CopyJob &J, int blk, int nblk) {
     constexpr int U = 4;
     const int step = 2 * (int)blockDim.x;
@@ -232,7 +334,8 @@ __device__ __forceinline__ void copy_rows(const CopyJob &J, int blk, int nblk) {
             for (int i = 0; i < U; i++) {
                 const int c = c0 + i * step;
                 if (c >= J.P) break;
-                *reinterpret_cast<double2 *>(J.dst + r0 + c) = v[i];
+                const float2 a = d_split(v[i].x), b = d_split(v[i].y);
+                *reinterpret_cast<float4 *>(J.dst + r0 + c) = make_float4(a.x, a.y, b.x, b.y);
                 if (c == 0) J.bc[row] = v[i].x;
                 if (c == J.K - 1) J.bc[J.N + row] = v[i].x;
                 if (c + 1 == J.K - 1) J.bc[J.N + row] = v[i].y;
@@ -261,7 +364,7 @@ __global__ void k_fault_stage(FaultArgs A, int stage, CopyJob job, int fault_blo
     unsigned int flags = 0;
     int it = 0;
     const double V = newton_v(Ts, Tn, F.have_tau0 ? F.tau0[k] : 0.0, F.a[k], F.eta[k], psi, F.V0,
-                              F.fV[stage][k], &it, &flags);
+                              F.fV[stage][k], &it, &flags, A.start32 != 0);
     F.fV[stage][k] = V;
     F.fdpsi[stage][k] = aging(psi, F.b[k], V, F.f0, F.V0, F.L);
     F.iters[k] += it;
@@ -282,7 +385,7 @@ __global__ void k_newton(FaultArgs A, const double *Ts, const double *psi, doubl
     unsigned int flags = 0;
     int it = 0;
     V[k] = newton_v(Ts[k], F.Tn0[k], F.have_tau0 ? F.tau0[k] : 0.0, F.a[k], F.eta[k], psi[k], F.V0,
-                    V[k], &it, &flags);
+                    V[k], &it, &flags, A.start32 != 0);
     iters[k] = it;
     report(A.status, flags, k);
 }
@@ -382,9 +485,23 @@ void fault_free(qd_solver *s) {
 // error estimate) are launched with programmatic stream serialization: each
 // waits for its predecessor (pdl_wait) before touching its data, and the
 // launch latency between them overlaps the predecessor's tail.
-int launch_stage_boundary(qd_solver *s, int stage, double ratio, const double *, const double *) {
-    QD_CUDA(launch_pdl(true, k_stage_boundary, dim3(nblk(s->nk, 128)), dim3(128), 0, s->stream, fargs(s), stage,
-                       s->t, s->dt, ratio));
+int launch_stage_boundary(qd_solver *s, int stage, double ratio, bool fit) {
+    FitArgs fa{};
+    const int nd = fit ? history_fit_args(s, &fa) : 0;
+    const dim3 grid(nblk(s->nk, FIT_THREADS)), block(FIT_THREADS);
+    switch (nd) {
+#define QD_SB_CASE(n)                                                                                    \
+    case n:                                                                                              \
+        QD_CUDA(launch_pdl(true, k_stage_boundary<n>, grid, block, 0, s->stream, fargs(s), stage, s->t, s->dt, \
+                           ratio, fa));                                                                  \
+        break;
+        QD_SB_CASE(0) QD_SB_CASE(1) QD_SB_CASE(2) QD_SB_CASE(3) QD_SB_CASE(4) QD_SB_CASE(5) QD_SB_CASE(6)
+        QD_SB_CASE(7)
+#undef QD_SB_CASE
+        default:
+            set_error("stage boundary: %d fit unknowns", nd);
+            return QD_ERR_STATE;
+    }
     QD_LAUNCH_CHECK(s);
     return QD_OK;
 }

@@ -180,44 +180,111 @@ __global__ void __launch_bounds__(BX * BY) k_residual(View<T> v, T *r, double *p
     }
 }
 
-// FP64 residual of the level-0 field, written as the FP32 right-hand side
-// of the correction equation, and ||r||^2 into *out (mixed precision).
+// The level-0 residual of the mixed-precision solver, written as the FP32
+// right-hand side of the correction equation, and ||r||^2 into *out.
 //
-// GB300 issues about two FP64 instructions per SM clock, which bounds this
-// kernel, so it spends five of them per node: the stored diagonal replaces
-// three additions; without a right-hand side the 1/h^2 scale is applied in
-// FP32 after the conversion; the FP64 -> FP32 conversion runs on the
-// integer pipes (d2f_rne); the norm sums the squares of the FP32 residual
-// the correction equation receives, in FP32 over a warp (128 nodes) and in
-// FP64 above that -- a relative error near 1e-7 in the norm, which only the
-// stopping test reads.  The last block to
-// finish adds the per-block partials in a fixed order (the sum is
-// deterministic) and re-arms the counter for the next launch.
-static constexpr int RES_RPT = 4;
+// GB300 issues about one FP64 fused multiply-add per SM clock, so a
+// residual in FP64 arithmetic (five per node) is bound by that pipe at a
+// quarter of the bandwidth the kernel's bytes allow.  This kernel reads the
+// same bytes -- u in FP64 and the moduli cx, cz and diag, stored at set-up
+// as double-float pairs (d_split, 8 bytes a value like their FP64 copies)
+// -- and evaluates
+//   lap = cW uW + cE uE + cN uN + cS uS - diag uC
+// in double-float arithmetic on the FP32 and integer pipes: each u is split
+// into hi + lo on the integer pipes, each product is the exact FP32 product
+// of the hi parts (the rounding error recovered by an FMA) plus the two
+// cross terms, and the five hi products are summed exactly with Knuth's
+// two-sum, the rounding errors and cross terms collected in FP32.  The
+// error of lap is a few units of 2^-46 of sum |c u| (2^-53 for the FP64
+// evaluation).  At a 1e-9 relative tolerance on a 1025^2 grid that is about
+// 1 % of the tolerance's norm, spread as rounding noise uncorrelated with
+// the residual, so the norm the stopping test reads moves by about 1e-4 of
+// itself; the right-hand sides of the cycles, far above the tolerance, keep
+// FP32's precision.  r = -lap / h^2.
+//
+// Layout: tiles of 30 columns x BY * RES_DF_RPT rows.  A warp covers 32
+// consecutive columns of which the middle 30 are its output (the outer two
+// lanes supply the west and east neighbours through shuffles), and each
+// thread walks RES_DF_RPT consecutive rows of its column with its u values
+// split once and kept in registers.  A grid of RES_DF_CTAS_PER_SM blocks per
+// SM strides over the tiles, so that the block-wide reduction at the end
+// (whose barrier idles a block's early warps) comes once per block instead
+// of once per tile.  The norm sums the squares of the FP32 residual in FP32
+// over a warp and in FP64 above that -- a relative error near 1e-7 in the
+// norm, which only the stopping test reads.  The last block to finish adds
+// the per-block partials in a fixed order (the sum is deterministic) and
+// re-arms the counter for the next launch.
+static constexpr int RES_RPT = 4;          // rows per thread of the FP64 reductions (k_mr_dots)
+static constexpr int RES_DF_COLS = 30;     // output columns per warp
+static constexpr int RES_DF_RPT = 4;       // rows per thread
+static constexpr int RES_DF_CTAS_PER_SM = 3;
 
-template <bool HAS_F>
-__global__ void __launch_bounds__(BX * BY)
-    k_residual64_to32(View<double> v, const double *__restrict__ diag, float *f32, double *partial,
-                      unsigned *count, double *out, Decide dc) {
+__global__ void __launch_bounds__(BX * BY, RES_DF_CTAS_PER_SM)
+    k_residual_df(View<double> v, const float2 *__restrict__ cx2, const float2 *__restrict__ cz2,
+                  const float2 *__restrict__ dg2, float *f32, double *partial, unsigned *count, double *out,
+                  Decide dc) {
     pdl_trigger();
     pdl_wait();   // launched with programmatic serialization: the previous kernel's data first
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j0 = blockIdx.y * (BY * RES_RPT) + threadIdx.y;
+    constexpr int R = RES_DF_RPT;
+    const int lane = threadIdx.x;
+    const int N = v.N, K = v.K, P = v.P;
+    const int ntx = (K - 2 + RES_DF_COLS - 1) / RES_DF_COLS, nty = (N + BY * R - 1) / (BY * R);
     const float nih2 = -(float)v.inv_h2;
     float sq = 0.f;   // squares of the FP32 residual, summed in FP32 within a warp
-    if (k >= 1 && k <= v.K - 2) {
-        const double *__restrict__ u = v.u;
+    for (int tile = blockIdx.x; tile < ntx * nty; tile += gridDim.x) {
+        const int ty = tile / ntx, tx = tile - ty * ntx;
+        const int k = tx * RES_DF_COLS + lane;                 // lanes 0 and 31: neighbours only
+        const int j0 = (ty * BY + threadIdx.y) * R;
+        if (j0 >= N) continue;                                  // uniform over the warp
+        const bool out_col = lane >= 1 && lane <= RES_DF_COLS && k <= K - 2;
+        // every load first, at clamped (always valid) indices, so that they
+        // are all in flight together: u at rows j0-1 .. j0+R of this column
+        // (mirrored at both ends; rows past the last are clamped, no output
+        // reads them), the moduli of rows j0 .. j0+R-1 at the output column
+        const int ku = min(k, K - 1), kc = max(1, min(k, K - 2));
+        double uv[R + 2];
+        float2 cWv[R], cEv[R], cNv[R + 1], dgv[R];
 #pragma unroll
-        for (int i = 0; i < RES_RPT; i++) {
-            const int j = j0 + i * BY;
-            if (j < v.N) {
-                const long c = (long)j * v.P + k;
-                const long up = (j == 0) ? v.P : -(long)v.P;
-                const long dn = (j == v.N - 1) ? -(long)v.P : v.P;
-                const double lap = v.cx[c - 1] * u[c - 1] + v.cx[c] * u[c + 1] + v.cz[c] * u[c + up] +
-                                   v.cz[c + v.P] * u[c + dn] - diag[c] * u[c];
-                const float r = HAS_F ? d2f_rne(v.f[c] - lap * v.inv_h2) : d2f_rne(lap) * nih2;
-                f32[c] = r;
+        for (int i = 0; i < R + 2; i++) {
+            int j = j0 - 1 + i;
+            j = j < 0 ? 1 : (j > N - 1 ? 2 * (N - 1) - j : j);
+            j = max(0, min(j, N - 1));
+            uv[i] = __ldg(v.u + (long)j * P + ku);
+        }
+#pragma unroll
+        for (int i = 0; i <= R; i++) {
+            const long c = (long)min(j0 + i, N) * P + kc;   // cz has N + 1 rows
+            cNv[i] = __ldg(cz2 + c);
+            if (i < R) {
+                const long cc = (long)min(j0 + i, N - 1) * P + kc;
+                cWv[i] = __ldg(cx2 + cc - 1);
+                cEv[i] = __ldg(cx2 + cc);
+                dgv[i] = __ldg(dg2 + cc);
+            }
+        }
+        float uh[R + 2], ul[R + 2];
+#pragma unroll
+        for (int i = 0; i < R + 2; i++) {
+            const float2 x = d_split(uv[i]);
+            uh[i] = x.x;
+            ul[i] = x.y;
+        }
+#pragma unroll
+        for (int i = 0; i < R; i++) {
+            const int j = j0 + i;
+            const float wh = __shfl_up_sync(0xffffffffu, uh[i + 1], 1);
+            const float wl = __shfl_up_sync(0xffffffffu, ul[i + 1], 1);
+            const float eh = __shfl_down_sync(0xffffffffu, uh[i + 1], 1);
+            const float el = __shfl_down_sync(0xffffffffu, ul[i + 1], 1);
+            if (out_col && j < N) {
+                float s, lo;
+                df_first(cWv[i].x, cWv[i].y, wh, wl, s, lo);
+                df_acc(cEv[i].x, cEv[i].y, eh, el, s, lo);
+                df_acc(cNv[i].x, cNv[i].y, uh[i], ul[i], s, lo);
+                df_acc(cNv[i + 1].x, cNv[i + 1].y, uh[i + 2], ul[i + 2], s, lo);
+                df_acc(-dgv[i].x, -dgv[i].y, uh[i + 1], ul[i + 1], s, lo);
+                const float r = __fadd_rn(s, lo) * nih2;
+                f32[(long)j * P + k] = r;
                 sq = fmaf(r, r, sq);
             }
         }
@@ -276,6 +343,18 @@ __global__ void __launch_bounds__(BX * BY)
         const int go = solve_check_dev(out, dc.st, dc.max_cycles, dc.n_kernels);
         if (dc.in_graph) cudaGraphSetConditional(dc.h, go ? 1u : 0u);
     }
+}
+
+// the double-float moduli of level 0 (d_split of cx, cz and diag)
+__global__ void k_split_moduli(int N, int P, const double *cx, const double *cz, const double *diag, float2 *cx2,
+                               float2 *cz2, float2 *dg2) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long n = (long)N * P;
+    if (i < n) {
+        cx2[i] = d_split(cx[i]);
+        dg2[i] = d_split(diag[i]);
+    }
+    if (i < n + P) cz2[i] = d_split(cz[i]);
 }
 
 // residual norm^2 of the zero-interior guess: only the columns next to the
@@ -342,6 +421,11 @@ int mg_alloc(qd_solver *s, const double *mu_equi_host, const double *jrow_host) 
         s->dims[l].inv_h2 = 1.0 / (h * h);
     }
     s->nlev = nl;
+    {
+        int dev = 0;
+        QD_CUDA(cudaGetDevice(&dev));
+        QD_CUDA(cudaDeviceGetAttribute(&s->n_sm, cudaDevAttrMultiProcessorCount, dev));
+    }
     int rc = QD_OK;
     for (int l = 0; l < nl; l++) {
         const size_t n = (size_t)s->dims[l].N * s->dims[l].P;
@@ -361,6 +445,16 @@ int mg_alloc(qd_solver *s, const double *mu_equi_host, const double *jrow_host) 
         s->L32[l].dinv = dalloc<float>(n, &rc);
         if (rc != QD_OK) {
             set_error("device allocation failed on level %d", l);
+            return rc;
+        }
+    }
+    if (s->opt.precision == QD_PREC_MIXED) {
+        const size_t n = (size_t)s->dims[0].N * s->dims[0].P;
+        s->res_cx = dalloc<float2>(n, &rc);
+        s->res_cz = dalloc<float2>(n + s->dims[0].P, &rc);
+        s->res_dg = dalloc<float2>(n, &rc);
+        if (rc != QD_OK) {
+            set_error("device allocation failed (level-0 double-float moduli)");
             return rc;
         }
     }
@@ -393,6 +487,14 @@ int mg_alloc(qd_solver *s, const double *mu_equi_host, const double *jrow_host) 
         k_build_dinv<<<grd, blk, 0, s->stream>>>(d.N, d.K, d.P, s->L64[l].cx, s->L64[l].cz,
                                                  s->L64[l].dinv, s->L32[l].cx, s->L32[l].cz,
                                                  s->L32[l].dinv, s->L64[l].diag);
+        QD_LAUNCH_CHECK(s);
+    }
+    if (s->res_cx) {
+        const LevelDims &d = s->dims[0];
+        const long n = (long)(d.N + 1) * d.P;
+        k_split_moduli<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(d.N, d.P, s->L64[0].cx, s->L64[0].cz,
+                                                                           s->L64[0].diag, s->res_cx, s->res_cz,
+                                                                           s->res_dg);
         QD_LAUNCH_CHECK(s);
     }
     QD_CUDA(cudaStreamSynchronize(s->stream));
@@ -480,6 +582,10 @@ void mg_free(qd_solver *s) {
         s->L64[l] = Level<double>();
         s->L32[l] = Level<float>();
     }
+    cudaFree(s->res_cx);
+    cudaFree(s->res_cz);
+    cudaFree(s->res_dg);
+    s->res_cx = s->res_cz = s->res_dg = nullptr;
     cudaFree(s->d_partial);
     cudaFree(s->d_count);
     s->d_count = nullptr;
@@ -605,36 +711,36 @@ int mr_step(qd_solver *s, const double *u0) {
     return QD_OK;
 }
 
-// ||r||^2 of level 0 into d_scal[slot]; for mixed precision also writes the
-// FP32 correction right-hand side.
-// the mixed solver's level-0 residual with a decision fused into its last
-// block (norm into d_scal[0], ||r0||^2 into d_scal[1] for mode 1)
-int level0_norm_decide(qd_solver *s, const Decide &dc) {
+// the mixed solver's level-0 residual (k_residual_df) into the FP32
+// right-hand side, ||r||^2 into d_scal[slot] and the decision dc
+static int residual_df(qd_solver *s, const Decide &dc, int slot, bool pdl) {
+    if (!s->res_cx) {
+        set_error("level-0 residual: the double-float moduli exist only in mixed precision");
+        return QD_ERR_STATE;
+    }
     View<double> v = make_view(s, s->L64, 0);
-    dim3 blk(BX, BY), grd(cdiv(v.K, BX), cdiv(v.N, BY * RES_RPT));
-    if (v.f)
-        QD_CUDA(launch_pdl(true, k_residual64_to32<true>, grd, blk, 0, s->stream, v, (const double *)s->L64[0].diag,
-                           s->L32[0].f, s->d_partial, s->d_count, s->d_scal, dc));
-    else
-        QD_CUDA(launch_pdl(true, k_residual64_to32<false>, grd, blk, 0, s->stream, v,
-                           (const double *)s->L64[0].diag, s->L32[0].f, s->d_partial, s->d_count, s->d_scal, dc));
+    const int tiles = cdiv(v.K - 2, RES_DF_COLS) * cdiv(v.N, BY * RES_DF_RPT);
+    dim3 blk(BX, BY), grd(std::min(tiles, RES_DF_CTAS_PER_SM * s->n_sm));
+    QD_CUDA(launch_pdl(pdl, k_residual_df, grd, blk, 0, s->stream, v, (const float2 *)s->res_cx,
+                       (const float2 *)s->res_cz, (const float2 *)s->res_dg, s->L32[0].f, s->d_partial, s->d_count,
+                       s->d_scal + slot, dc));
     QD_LAUNCH_CHECK(s);
     return QD_OK;
 }
 
+// the mixed solver's level-0 residual with a decision fused into its last
+// block (norm into d_scal[0], ||r0||^2 into d_scal[1] for mode 1)
+int level0_norm_decide(qd_solver *s, const Decide &dc) {
+    QD_TRY(residual_df(s, dc, 0, true));
+    return QD_OK;
+}
+
+// ||r||^2 of level 0 into d_scal[slot]: in FP64 (to32 = 0), or the mixed
+// solver's residual, which also writes the FP32 correction right-hand side
 int level0_norm(qd_solver *s, int to32, int slot) {
     View<double> v = make_view(s, s->L64, 0);
     if (to32) {
-        dim3 blk(BX, BY), grd(cdiv(v.K, BX), cdiv(v.N, BY * RES_RPT));
-        if (v.f)
-            k_residual64_to32<true><<<grd, blk, 0, s->stream>>>(v, s->L64[0].diag, s->L32[0].f,
-                                                                 s->d_partial, s->d_count,
-                                                                 s->d_scal + slot, Decide{});
-        else
-            k_residual64_to32<false><<<grd, blk, 0, s->stream>>>(v, s->L64[0].diag, s->L32[0].f,
-                                                                  s->d_partial, s->d_count,
-                                                                  s->d_scal + slot, Decide{});
-        QD_LAUNCH_CHECK(s);
+        QD_TRY(residual_df(s, Decide{}, slot, false));
         return QD_OK;
     }
     dim3 blk(BX, BY), grd(cdiv(v.K, BX), cdiv(v.N, BY));
@@ -685,24 +791,34 @@ int mg_residual_norm(qd_solver *s, double *rnorm) {
     return QD_OK;
 }
 
-__global__ void k_d2f(const double *in, float *out, int n) {
+__global__ void k_d2f(const double *in, float *out, int n, float *lo) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = d2f_rne(in[i]);
+    if (i >= n) return;
+    if (lo) {
+        const float2 x = d_split(in[i]);
+        out[i] = x.x;
+        lo[i] = x.y;
+    } else {
+        out[i] = d2f_rne(in[i]);
+    }
 }
 
-// d2f_rne over a host array (a device round trip), for its test
-int convert_f64_f32(const double *in, float *out, int n) {
+// d2f_rne (lo null) or d_split over a host array (a device round trip), for
+// their tests
+int convert_f64_f32(const double *in, float *out, int n, float *lo) {
     double *din = nullptr;
-    float *dout = nullptr;
+    float *dout = nullptr, *dlo = nullptr;
     int rc = QD_OK;
     if (cudaMalloc(&din, sizeof(double) * (size_t)n) != cudaSuccess ||
         cudaMalloc(&dout, sizeof(float) * (size_t)n) != cudaSuccess ||
+        (lo && cudaMalloc(&dlo, sizeof(float) * (size_t)n) != cudaSuccess) ||
         cudaMemcpy(din, in, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice) != cudaSuccess) {
         rc = QD_ERR_CUDA;
     } else {
-        k_d2f<<<cdiv(n, 256), 256>>>(din, dout, n);
+        k_d2f<<<cdiv(n, 256), 256>>>(din, dout, n, dlo);
         if (cudaGetLastError() != cudaSuccess ||
-            cudaMemcpy(out, dout, sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost) != cudaSuccess)
+            cudaMemcpy(out, dout, sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost) != cudaSuccess ||
+            (lo && cudaMemcpy(lo, dlo, sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost) != cudaSuccess))
             rc = QD_ERR_CUDA;
     }
     if (rc != QD_OK) {
@@ -711,6 +827,7 @@ int convert_f64_f32(const double *in, float *out, int n) {
     }
     cudaFree(din);
     cudaFree(dout);
+    cudaFree(dlo);
     return rc;
 }
 

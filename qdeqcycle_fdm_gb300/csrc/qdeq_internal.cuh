@@ -231,8 +231,8 @@ struct Decide {
 };
 
 // binary64 -> binary32 with round-to-nearest-even, on the integer pipes.
-// GB300's FP64 pipe also executes the hardware F2F conversion, and that pipe
-// bounds the mixed-precision residual kernel; this routine follows the IEEE
+// GB300's FP64 pipe, which issues about one instruction per SM clock, also
+// executes the hardware F2F conversion; this routine follows the IEEE
 // 754 definition directly: keep the top 23 of the 52 fraction bits, round on
 // the 29 dropped bits (ties to even) and let a carry out of the fraction
 // bump the exponent (which also rounds the largest values to infinity as
@@ -264,6 +264,63 @@ __device__ __forceinline__ float d2f_rne(double x) {
     return __uint_as_float(sign | q);
 }
 
+// binary64 x -> a pair of binary32 (hi, lo) with x = hi + lo to within
+// 2^-48 |x| (the double-float representation of Dekker, "A floating-point
+// technique for extending the available precision", 1971), in about 16
+// integer and FP32 instructions (GB300's FP64 pipe, which executes the
+// hardware conversion, issues about one instruction per SM clock).  With x =
+// +-1.f 2^(e-1023): hi keeps the sign, the exponent and the top 23 of the 52
+// fraction bits (truncated), built from the high word rebiased and the top
+// three bits of the low word; the 29 bits below are an integer m, and lo =
+// m 2^(e-1075) is m converted to binary32 (rounded to 24 bits) times that
+// power of two, exact; |lo| < ulp(hi).  |x| < 2^-74 (zeros included) gives
+// (+-0, 0): an absolute error under 2^-74, far below any displacement the
+// solver resolves; |x| >= 2^128 gives (+-inf, 0); NaN gives (NaN, 0).
+__device__ __forceinline__ float2 d_split(double x) {
+    const unsigned hw = (unsigned)__double2hiint(x), lw = (unsigned)__double2loint(x);
+    const unsigned sign = hw & 0x80000000u, mag = hw & 0x7FFFFFFFu;   // exponent and top 20 fraction bits
+    if (mag < (949u << 20)) return make_float2(__uint_as_float(sign), 0.f);
+    if (mag >= (1151u << 20)) {
+        const bool nan = mag > 0x7FF00000u || (mag == 0x7FF00000u && lw != 0u);
+        return make_float2(__uint_as_float(sign | 0x7F800000u | (nan ? 0x00400000u : 0u)), 0.f);
+    }
+    const float hi = __uint_as_float(sign | ((mag - (896u << 20)) << 3) | (lw >> 29));
+    const float scale = __uint_as_float(sign | (((mag >> 20) - 948u) << 23));   // +-2^(e-1075)
+    return make_float2(hi, __uint2float_rn(lw & 0x1FFFFFFFu) * scale);
+}
+
+// s + lo += (ch + cl)(uh + ul): the hi product exactly (p + e) into the
+// running sum by two-sum, everything smaller into lo.  The _rn intrinsics
+// keep the compiler from contracting the product into the sum.
+// s + lo = (ch + cl)(uh + ul): the first term of a df_acc sum
+__device__ __forceinline__ void df_first(float ch, float cl, float uh, float ul, float &s, float &lo) {
+    s = __fmul_rn(ch, uh);
+    lo = fmaf(ch, ul, fmaf(cl, uh, fmaf(ch, uh, -s)));
+}
+
+__device__ __forceinline__ void df_acc(float ch, float cl, float uh, float ul, float &s, float &lo) {
+    const float p = __fmul_rn(ch, uh);
+    const float e = fmaf(ch, uh, -p);
+    const float t = fmaf(ch, ul, fmaf(cl, uh, e));
+    const float sn = __fadd_rn(s, p);
+    const float bb = __fsub_rn(sn, s);
+    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(sn, bb)), __fsub_rn(p, bb));
+    s = sn;
+    lo = __fadd_rn(lo, __fadd_rn(err, t));
+}
+
+// binary32 -> binary64 exactly, on the integer pipes (GB300's FP64 pipe
+// executes the hardware conversion): sign, exponent rebiased by 1023 - 127,
+// the 23 fraction bits at the top of the 52.  Subnormal inputs give +-0: in
+// the double-float sums here they can only be rounding debris far below the
+// values' resolution.  Infinities and NaN carry over.
+__device__ __forceinline__ double f2d_exact(float x) {
+    const unsigned b = __float_as_uint(x), sign = b & 0x80000000u, e = (b >> 23) & 0xFFu, m = b & 0x7FFFFFu;
+    if (e == 0u) return __hiloint2double((int)sign, 0);
+    const unsigned ex = e == 0xFFu ? 0x7FFu : e + (1023u - 127u);
+    return __hiloint2double((int)(sign | (ex << 20) | (m >> 3)), (int)(m << 29));
+}
+
 }  // namespace qd
 
 struct qd_solver {
@@ -271,12 +328,16 @@ struct qd_solver {
     double dh;
     qd_mg_options opt;
     int nlev;
+    int n_sm;              // the device's SM count
     qd::LevelDims dims[QD_MAXLEV];
     qd::Level<double> L64[QD_MAXLEV];
     qd::Level<float> L32[QD_MAXLEV];
     cudaStream_t stream;
     double *d_partial;     // per-block reduction partials
     unsigned *d_count;     // blocks done, for reductions finished by their last block
+    // level-0 cx, cz and diag as double-float pairs (d_split), for the
+    // mixed-precision residual; null in FP64 solvers
+    float2 *res_cx, *res_cz, *res_dg;
     double *d_ainv64;      // dense inverse of the coarsest-level operator (or null)
     float *d_ainv32;
     int n_cint;            // its order: coarsest N * (K-2) interior unknowns
@@ -288,6 +349,7 @@ struct qd_solver {
     double net_ratio;      // the network's gate: >= 1 a fixed ratio of ||r|| to the threshold;
                            // <= 0 the measured rule with a cost of -net_ratio V-cycles
     double net_cost;       // the measured rule's cost (V-cycles)
+    int newton_start;      // the Newton solve's start: 0 the reference's x = 0, 1 a binary32 solve
     void *history;         // ring of earlier solutions for the initial guess (history.cu), or null
     void *snapshot;        // the snapshot writer in flight (io.cu), or null
     int tail_l0;           // first level of the coarse tail
@@ -335,7 +397,7 @@ int level0_norm_decide(qd_solver *s, const Decide &dc);
 // u = u0 + alpha (u - u0) with the alpha that minimises the energy norm of
 // the level-0 error (the guess u0's correction u - u0 scaled optimally)
 int mr_step(qd_solver *s, const double *u0);
-int convert_f64_f32(const double *in, float *out, int n);
+int convert_f64_f32(const double *in, float *out, int n, float *lo = nullptr);
 int r0_norm(qd_solver *s, int slot);
 void tail_image_free(qd_solver *s);
 // mg_graph.cu
@@ -348,13 +410,14 @@ void warm_start_standby_update(qd_solver *s, double need_max);
 // fault.cu
 int fault_alloc(qd_solver *s);
 void fault_free(qd_solver *s);
-int launch_stage_boundary(qd_solver *s, int stage, double ratio, const double *slip_dev,
-                          const double *psi_dev);
+// fit: also fit the new boundary data by the solution history's (when the
+// next solve will start from a history guess), for history_apply
+int launch_stage_boundary(qd_solver *s, int stage, double ratio, bool fit);
 // a copy of the solved level-0 u into a slot of the solution history
 // (history_push_job), run by extra CTAs of the fault-stage kernel
 struct CopyJob {
     const double *src = nullptr;   // null: no copy
-    double *dst = nullptr;         // N x P field
+    float2 *dst = nullptr;         // N x P field as double-float pairs (d_split)
     double *bc = nullptr;          // its boundary columns, [fault rows, far rows]
     int N = 0, K = 0, P = 0;
 };
@@ -385,7 +448,9 @@ void warm_start_detach(qd_solver *s);
 double *warm_start_bc_buffer(qd_solver *s);
 // history.cu: initial guess from the solution history
 int history_set(qd_solver *s, int m);
-int history_guess(qd_solver *s, double *implied_bc);
+// the guess in u's interior from the fit launch_stage_boundary made
+// (no-op without one)
+int history_apply(qd_solver *s, double *implied_bc);
 // after a stage solve: the store of the solution into the ring as a copy
 // job for the next kernel that takes one (the ring's slot is claimed now);
 // job->src stays null without a history

@@ -220,6 +220,86 @@ def test_newton_safeguard_recovers_where_reference_overflows():
     assert np.all(np.isfinite(V[k])) and np.max(np.abs(g)) < 1e-9 * 60.0
 
 
+def test_newton_binary32_start_reaches_the_reference_root():
+    """Newton start mode 1 (a binary32 solve of the log form, then the same
+    FP64 iteration and stopping rule): over states from steady sliding to
+    seismic slip rates, the slip rate equals the oracle's (the reference's
+    iteration from x = 0) to 1e-12, in at most 3 FP64 steps where the
+    reference's start takes up to 11; fb = 0 gives V = 0; the case where
+    the reference's first step overflows is solved too."""
+    cfg, prob = make_problem(65)
+    s = api.Solver(prob.ni, prob.nk, prob.dh, prob.mu_equi, prob.mu_node, cfg.mg)
+    s.fault_setup(prob)
+    s.set_newton_start(1)
+    k = slice(1, prob.nk + 1)
+    rng = np.random.default_rng(9)
+    for trial in range(4):
+        psi = prob.psi.copy()
+        psi[k] = rng.uniform(0.45, 0.85, prob.nk)
+        fb = rng.uniform(-5.0, 40.0, prob.nz)
+        fb[prob.nk // 2] = 0.0
+        Ts = fb - prob.tau0
+        seed = np.zeros(prob.nz)
+        V, it, rc = s.nrsearch(Ts, psi, seed)
+        assert rc == 0
+        oV, oit, st = oracle.nrsearch(prob.nk, Ts, prob.Tau_n0, prob.a, prob.eta, psi, prob.V0, seed,
+                                      tau0=prob.tau0)
+        assert st == 0
+        nz = oV[k] != 0.0
+        assert np.max(np.abs(V[k][nz] - oV[k][nz]) / np.abs(oV[k][nz])) < 1e-12
+        assert V[prob.nk // 2] == 0.0 and oV[prob.nk // 2] == 0.0
+        assert it[k].max() <= 3 and oit[k].max() >= 7, (it[k].max(), oit[k].max())
+    p = prob
+    p.a[:] = 0.005
+    p.Tau_n0[:] = -10.0
+    p.eta[:] = 4.0
+    s2 = api.Solver(p.ni, p.nk, p.dh, p.mu_equi, p.mu_node, cfg.mg)
+    s2.fault_setup(p, with_tau0=False)
+    s2.set_newton_start(1)
+    Ts = np.full(p.nz, 60.0)
+    psi = np.full(p.nz, 0.7)
+    V, it, rc = s2.nrsearch(Ts, psi, np.zeros(p.nz))
+    assert rc == 0
+    x = np.arcsinh(V[k] / (2 * p.V0) * np.exp(psi[k] / p.a[k]))
+    g = p.eta[k] * V[k] + p.a[k] * 10.0 * x - Ts[k]
+    assert np.all(np.isfinite(V[k])) and np.max(np.abs(g)) < 1e-9 * 60.0
+    with pytest.raises(Exception):
+        s.set_newton_start(2)
+
+
+def test_newton_binary32_start_keeps_the_rk_steps():
+    """100 fixed RK43 steps (the 100-step bar's set-up) with Newton start
+    mode 1 against the oracle (the reference's start) to the bar's
+    tolerances, with fewer FP64 Newton steps than mode 0."""
+    cfg, prob = make_problem(65)
+    prob.ini_dt = prob.mindt = prob.maxdt = 3e5
+    mg = config.MGConfig(n_levels=cfg.mg.n_levels, nu_pre=2, nu_post=2, nu_coarse=32, tol_mode=1,
+                         tol=1e-13, max_cycles=400, surface_prolong=1)
+    cpu = oracle.Simulation(prob, mg.n_levels, mg.nu_pre, mg.nu_post, mg.nu_coarse, mg.tol_mode,
+                            mg.tol, mg.max_cycles, surface_prolong=1)
+    cpu.start()
+    for _ in range(100):
+        cpu.step()
+    c = cpu.state()
+    iters = []
+    k = slice(1, prob.nk + 1)
+    for mode in (0, 1):
+        gpu = api.Simulation(prob, mg)
+        gpu.solver.set_newton_start(mode)
+        gpu.start()
+        gpu.step(100)
+        g = gpu.state()
+        gpu.close()
+        assert g["it"] == 100
+        assert rel(g["t"], c["t"]) < 1e-12
+        assert rel(g["Slip"][k], c["Slip"][k]) < 1e-8
+        assert rel(g["psi"][k], c["psi"][k]) < 1e-8
+        assert np.max(np.abs(g["V"][k] - c["V"][k]) / c["V"][k]) < 1e-10
+        assert rel(g["U"], c["U"]) < 1e-10
+        iters.append(g["newton_iters"])
+    assert iters[1] < iters[0], iters
+
+
 @pytest.mark.parametrize("surface", [0, 1])
 def test_rk43_100_steps_match_oracle(surface):
     """100 accepted RK43 steps of the interseismic period, GPU vs oracle.
@@ -331,3 +411,66 @@ def test_f64_to_f32_rounding_matches_ieee():
     nan = np.isnan(ref)
     assert np.array_equal(np.isnan(out), nan)
     assert np.array_equal(out[~nan].view(np.uint32), ref[~nan].view(np.uint32))
+
+
+def test_double_float_split_matches_its_definition():
+    """The mixed residual's split x = hi + lo (d_split), on the integer and
+    FP32 pipes: hi is x truncated to binary32's 24 significant bits, lo the
+    remainder rounded to nearest binary32, bit for bit against the same on
+    the host, so |hi + lo - x| <= 2^-48 |x|; |x| < 2^-74 and zeros give
+    (+-0, 0), |x| >= 2^128 +-inf, NaN stays NaN."""
+    import ctypes as C
+    from qdeqcycle_fdm_gb300 import _lib
+    rng = np.random.default_rng(11)
+    x = rng.uniform(-1, 1, 40000) * 10.0 ** rng.uniform(-30, 38, 40000)
+    x = np.concatenate([x, [0.0, -0.0, 1.0, -1.0, 2.0 ** -74, -(2.0 ** -74), np.nextafter(2.0 ** -74, 0),
+                            1e-40, 1e39, -1e39, np.inf, -np.inf, np.nan, 1.0 + 2.0 ** -52, 3.0 - 2.0 ** -51,
+                            np.nextafter(2.0 ** 128, 0), 2.0 ** 128]])
+    x = np.ascontiguousarray(x)
+    hi = np.empty(x.size, dtype=np.float32)
+    lo = np.empty(x.size, dtype=np.float32)
+    L = _lib.load()
+    fp = C.POINTER(C.c_float)
+    rc = L.qd_split_f64(x.ctypes.data_as(C.POINTER(C.c_double)), hi.ctypes.data_as(fp), lo.ctypes.data_as(fp),
+                        x.size)
+    assert rc == 0, L.qd_last_error().decode()
+    low29 = np.uint64((1 << 29) - 1)
+    with np.errstate(over="ignore", invalid="ignore"):
+        ok = np.isfinite(x) & (np.abs(x) >= 2.0 ** -74) & (np.abs(x) < 2.0 ** 128)
+        hi_ref = (x.view(np.uint64) & ~low29).view(np.float64)
+        lo_ref = np.where(ok, x - hi_ref, 0.0).astype(np.float32)
+        assert np.array_equal(hi[ok].view(np.uint32), hi_ref[ok].astype(np.float32).view(np.uint32))
+        assert np.array_equal(lo[ok], lo_ref[ok])      # by value: a zero lo may carry x's sign
+        err = np.abs(hi[ok].astype(np.float64) + lo[ok].astype(np.float64) - x[ok])
+        assert np.all(err <= 2.0 ** -48 * np.abs(x[ok]))
+    tiny = np.abs(x) < 2.0 ** -74
+    assert np.all(hi[tiny] == 0.0) and np.all(lo[tiny] == 0.0)
+    assert np.array_equal(np.signbit(hi[tiny]), np.signbit(x[tiny]))
+    over = np.isinf(x) | (np.isfinite(x) & (np.abs(x) >= 2.0 ** 128))
+    assert np.all(np.isinf(hi[over])) and np.array_equal(np.sign(hi[over]), np.sign(x[over]))
+    assert np.all(lo[over] == 0.0)
+    assert np.isnan(hi[np.isnan(x)]).all() and np.all(lo[np.isnan(x)] == 0.0)
+
+
+def test_mixed_residual_matches_fp64_residual():
+    """The mixed solver's level-0 residual, evaluated in double-float
+    arithmetic on the FP32 and integer pipes, reports the norm that the
+    oracle's FP64 residual of the same u gives to 1e-4 (measured: 4e-6):
+    after a solve to 1e-10 of ||r0|| (random boundary data, the finest
+    tolerance the tests use) and after one to 1e-3."""
+    cfg, prob = make_problem(257, mu_profile="layered", layer_depth_km=8.0)
+    mg = oracle.Multigrid(prob.ni, prob.nk, prob.dh, prob.mu_equi, 6, 2, 2, 32)
+    U = random_U(prob, 5)
+    for tol in (1e-10, 1e-3):
+        s = api.Solver(prob.ni, prob.nk, prob.dh, prob.mu_equi, prob.mu_node,
+                       config.MGConfig(n_levels=6, nu_pre=2, nu_post=2, nu_coarse=32, tol_mode=1, tol=tol,
+                                       max_cycles=100, precision=1, surface_prolong=1, coarse_solve=1))
+        s.upload_u(U)
+        cyc, rn, r0 = s.ode_solve()
+        got = compact(s.download_u()).copy()
+        s.close()
+        r = np.zeros_like(got)
+        mg.residual(r, got, np.zeros_like(got), 0)
+        rn64 = mg.norm2(r)
+        assert abs(rn - rn64) <= 1e-4 * rn64, (tol, rn, rn64)
+        assert rn <= tol * r0
