@@ -58,7 +58,7 @@ YEAR_S = 365.25 * 86400.0
 # flushed before the kernel: the V-cycle kernels of the mixed solver at
 # 1025^2 and the U-Net's first 16 -> 16 channel convolution on the network's
 # grid, keyed by the network's nodes per side
-TRAFFIC = {"up0": 31.19e6, "down0": 17.35e6, "residual": 33.74e6}
+TRAFFIC = {"up0": 31.19e6, "down0": 17.35e6, "residual": 33.90e6}
 TRAFFIC_CONV16 = {513: 8.62e6, 1025: 34.03e6}
 METRIC = "simulated yr/hr at 1025² (learned+mixed vs plain FP64 MG, 1e-9 rel residual)"
 WINDOW = "config1_1025_rupture3"
@@ -127,6 +127,10 @@ def parse():
                    help="Newton start of the fast solvers (1: a binary32 solve of the log form, then the "
                         "reference's FP64 iteration; 0: the reference's x = 0); the plain FP64 drop-in and "
                         "the FP64 reference of the error measurement keep 0")
+    p.add_argument("--tail-sweeps", type=int, default=1,
+                   help="pre- and post-sweeps on the coarse tail's levels (<= 65 rows) of the fast solvers "
+                        "(0: the fine levels' schedule); the plain FP64 drop-in and the FP64 reference of "
+                        "the error measurement keep 0")
     p.add_argument("--config2-wall-s", type=float, default=240.0,
                    help="--config config2: seconds of stepping from steady sliding")
     p.add_argument("--error-steps", type=int, default=10,
@@ -342,6 +346,7 @@ def run_ours(args):
         tsim = api.Simulation(tprob, mg)
         tsim.solver.set_solution_history(H)
         tsim.solver.set_newton_start(args.newton_start)
+        tsim.solver.set_tail_sweeps(args.tail_sweeps)
         net = warmstart.UNet(unet_n(tprob.nk), unet_n(tprob.ni), seed=args.seed)
         net.attach(tsim.solver, warmstart.MODE_TRAIN, args.lr)
         tsim.start()
@@ -360,12 +365,14 @@ def run_ours(args):
         return net, {"train_samples": n, "last_loss": loss, "train_instance_seed": tcfg.seed,
                      "train_years": st["t"] / YEAR_S, "train_steps": st["it"], "train_wall_s": wall}
 
-    def resumed(mg, history=0, net=None, start=None, params=None, newton=None):
+    def resumed(mg, history=0, net=None, start=None, params=None, newton=None, tail=None):
         """A solver restarted from a checkpoint (the window's by default);
-        newton: the Newton start (default --newton-start)."""
+        newton: the Newton start (default --newton-start), tail: the coarse
+        tail's sweeps (default --tail-sweeps)."""
         sim = api.Simulation(prob, mg)
         sim.solver.set_solution_history(history)
         sim.solver.set_newton_start(args.newton_start if newton is None else newton)
+        sim.solver.set_tail_sweeps(args.tail_sweeps if tail is None else tail)
         if net is not None:
             net.attach(sim.solver, warmstart.MODE_PREDICT)
             warmstart.UNet.set_gate(sim.solver, args.net_gate)
@@ -374,7 +381,7 @@ def run_ours(args):
         sim.resume(ck if start is None else start, params=params)
         return sim
 
-    def timed_run(mg, host_io=False, net=None, history=0, tune=False, newton=None):
+    def timed_run(mg, host_io=False, net=None, history=0, tune=False, newton=None, tail=None):
         """Restart from the window checkpoint, W untimed warm-up steps, then
         K steps each bracketed by CUDA events on the solver's stream (L2
         flushed before each); with `history` >= 2 every stage solve starts
@@ -383,7 +390,7 @@ def run_ours(args):
         after the warm-up steps (outside the timed region).  host_io: every
         step goes through the C ABI with host buffers -- state and u uploaded
         from pinned memory before, read back after (the e2e measurement)."""
-        sim = resumed(mg, history, net, newton=newton)
+        sim = resumed(mg, history, net, newton=newton, tail=tail)
         sim.step(args.warmup)
         tuning = sim.solver.autotune(3) if tune else None
         stream = torch.cuda.ExternalStream(sim.solver.stream_ptr())
@@ -473,6 +480,7 @@ def run_ours(args):
             for x in sims:
                 x.solver.set_solution_history(H)
                 x.solver.set_newton_start(args.newton_start)
+                x.solver.set_tail_sweeps(args.tail_sweeps)
                 x.start()
             if mode == "batched":
                 api.ensemble_step(sims, 3)
@@ -567,7 +575,7 @@ def run_ours(args):
             simh, fh = timed_run(fp64s_cfg, history=H)
             simh.close()
             extra["fp64_history"] = summary(fh)
-        sim64, plain = timed_run(fp64_cfg, newton=0)
+        sim64, plain = timed_run(fp64_cfg, newton=0, tail=0)
         sim64.close()
         sim64s, plain_s = timed_run(fp64s_cfg)
         sim64s.close()
@@ -588,7 +596,8 @@ def run_ours(args):
         runs = {}
         for name, mg, hist, nn in (("exact", tight, 0, None), ("fp64_1e-9", fp64s_cfg, 0, None),
                                    ("headline", mixed_cfg, H, net)):
-            s = resumed(mg, hist, nn, params=params, newton=0 if name == "exact" else None)
+            s = resumed(mg, hist, nn, params=params, newton=0 if name == "exact" else None,
+                        tail=0 if name == "exact" else None)
             s.step(nsteps)
             runs[name] = s.state()
             if nn is not None:
@@ -682,7 +691,8 @@ def run_ours(args):
     #   up0      prolongation 8 B + nu_post sweeps x 20 B + u64 += e 16 B per
     #            level-0 node, + 4 B per level-1 node
     #            (nu_pre, nu_post: the schedule the run used, tuned or not)
-    #   residual FP64 u, cx, cz, diag read + FP32 rhs written: 36 B per node
+    #   residual FP64 u and the moduli cx, cz, diag (double-float pairs)
+    #            read + FP32 rhs written: 36 B per node
     #   conv16   16 BF16 channels read and written: 64 B per padded pixel of
     #            the network's grid
     # Launches per step: one of each cycle kernel per V-cycle, the residual
@@ -707,7 +717,7 @@ def run_ours(args):
     algo = {**algo_bytes(cfg.ni, cfg.nk), "conv16": 64.0 * pad_px}
     names = {"up0": f"k_up<float,2> level 0 (prolongation + {nu_post} sweep(s) + u64 += e)",
              "down0": f"k_down<float> level 0 ({nu_pre} sweep(s) + residual + restriction)",
-             "residual": "k_residual64_to32 (FP64 residual -> FP32 rhs + norm)",
+             "residual": "k_residual_df (level-0 residual in double-float -> FP32 rhs + norm)",
              "tail": "k_tail<float> (levels <= 65 rows, one CTA)",
              "conv16": f"k_conv_rows<16,16> (U-Net 3x3 convolution, {unet_n(cfg.nk)}x{unet_n(cfg.ni)} grid, tcgen05)"}
     REPS = 50
@@ -742,10 +752,6 @@ def run_ours(args):
                 "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
                 "grid": "1025x1025 (L2-resident between launches: effective rate)",
                 "kernels": kern}
-    if dom == "residual":
-        # the FP64 residual is kept in FP64 on purpose; on GB300 its limit is
-        # the FP64 pipe (ncu capture of the V-cycle kernels at 1025^2)
-        roofline["limiter"] = "FP64 pipe, 77 % busy in the ncu capture (6 FP64 operations per node)"
     if not args.no_hbm:
         roofline["hbm_4097"] = hbm_kernels(api, config, problem, mixed_cfg, algo_bytes, names, peak, REPS)
 
@@ -789,6 +795,8 @@ def run_ours(args):
                              f"rel {cfg.mg.tol:g}, {mode}, exact coarsest solve, surface-row prolongation",
                        "newton_start": ("binary32 log-form solve, then the reference's FP64 iteration"
                                         if args.newton_start else "the reference's x = 0"),
+                       "tail_sweeps": (f"V({args.tail_sweeps},{args.tail_sweeps}) on the levels of <= 65 rows"
+                                       if args.tail_sweeps else "the fine schedule on every level"),
                        "parallelism": f"replicas x{world}", "l2": "flushed before every timed step"},
             "sim_years_timed": head["yrs"], "t_start_s": head["t0"], "t_end_s": head["t_end"],
             "vcycles_per_solve": head["vcycles"] / max(1, head["solves"]),
@@ -809,7 +817,7 @@ def run_ours(args):
                 "vcycles_per_solve": plain["vcycles"] / max(1, plain["solves"]),
                 "newton_iters_per_node_solve": plain["newton"],
                 "mg": "the reference's algorithm: prolongation without the surface row, coarsest-level sweeps, "
-                      "previous-solution start, Newton from x = 0"},
+                      "previous-solution start, Newton from x = 0, the fine schedule on every level"},
             "speedup_vs_plain_fp64": value / world / plain_value if plain_value else None,
             "gpu_launches": head["launches"],
             "roofline": roofline, "clocks": clk, "e2e": e2e, "cpu_baseline": cpu,
@@ -873,6 +881,7 @@ def run_config2(args):
     sim = api.Simulation(prob, cfg.mg)
     sim.solver.set_solution_history(args.history)
     sim.solver.set_newton_start(args.newton_start)
+    sim.solver.set_tail_sweeps(args.tail_sweeps)
     sim.start()
     stream = torch.cuda.ExternalStream(sim.solver.stream_ptr())
     s0 = sim.state(with_u=False)
@@ -923,6 +932,7 @@ def run_config2(args):
         x = api.Simulation(prob, mg)
         x.solver.set_solution_history(hist)
         x.solver.set_newton_start(args.newton_start if name == "mixed" else 0)
+        x.solver.set_tail_sweeps(args.tail_sweeps if name == "mixed" else 0)
         x.resume(ck, U=U, params=params)
         x.step(5)
         out[name] = x.state()
@@ -978,7 +988,7 @@ def run_hbm_only(args):
         return {"up0": (24.0 + 20.0 * mixed.nu_post) * n0 + 4.0 * n1,
                 "down0": (16.0 + 20.0 * mixed.nu_pre) * n0 + 4.0 * n1, "residual": 36.0 * n0}
     names = {"down0": "k_down<float> level 0", "up0": "k_up<float,2> level 0",
-             "residual": "k_residual64_to32"}
+             "residual": "k_residual_df"}
     peak = _peaks().get("hbm_gbs", 6800.0)
     print(json.dumps(hbm_kernels(api, config, problem, mixed, algo_bytes, names, peak, args.hbm_reps)), flush=True)
     return 0

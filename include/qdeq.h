@@ -47,7 +47,8 @@ extern "C" {
 /* precision of the multigrid cycles */
 #define QD_PREC_FP64 0          /* FP64 V-cycles (the drop-in)               */
 #define QD_PREC_MIXED 1         /* FP32 V-cycles inside FP64 iterative
-                                   refinement; FP64 residual and update      */
+                                   refinement: FP64 u and update, residual
+                                   in double-float (48-bit) arithmetic       */
 
 /* Ceiling on the V-cycles of one solve run as a CUDA graph when max_cycles
  * is <= 0: the graph's loop is decided on the device, where no host check
@@ -361,6 +362,14 @@ int qd_set_solution_history(qd_solver *s, int m);
  * iteration count the solver reports is then that of the FP64 steps.  No
  * counterpart in the reference. */
 int qd_set_newton_start(qd_solver *s, int mode);
+/* Red-black sweeps before and after the coarse-grid correction on the
+ * levels the single-CTA coarse tail runs (those of at most 65 rows): n >= 1
+ * sets both to n; 0 (the default) keeps the fine levels' nu_pre and
+ * nu_post, the reference's schedule.  On those levels a V-cycle is bound by
+ * one SM's barriers, and with the exact coarsest solve fewer sweeps there
+ * leave the cycle's reduction nearly unchanged.  No counterpart in the
+ * reference. */
+int qd_set_tail_sweeps(qd_solver *s, int n);
 /* The last fit: coef[0..6] the coefficients of the earlier solutions
  * (newest first), coef[7] the fit's boundary misfit over the change from
  * the latest solution's boundary data (1: no gain); *nd coefficients are

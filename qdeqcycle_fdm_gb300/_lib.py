@@ -63,6 +63,7 @@ EXPORTS = [
                                     C.c_double, C.c_double, C.c_int]),
     ("qd_set_solution_history", C.c_int, [C.c_void_p, C.c_int]),
     ("qd_set_newton_start", C.c_int, [C.c_void_p, C.c_int]),
+    ("qd_set_tail_sweeps", C.c_int, [C.c_void_p, C.c_int]),
     ("qd_autotune", C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     ("qd_set_tiles", C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     ("qd_solution_history_fit", C.c_int, [C.c_void_p, _dp, _ip]),

@@ -239,6 +239,11 @@ class Solver:
         same FP64 iteration then ends at the same root in fewer steps."""
         check(self.L.qd_set_newton_start(self.h, int(mode)))
 
+    def set_tail_sweeps(self, n):
+        """Pre- and post-sweeps on the coarse tail's levels (<= 65 rows);
+        0: the fine levels' schedule (the default)."""
+        check(self.L.qd_set_tail_sweeps(self.h, int(n)))
+
     def autotune(self, reps=3):
         """Time the candidate smoother schedules and tile box widths on this
         solver's problem (the last stored solve replayed from the solution

@@ -686,6 +686,15 @@ int qd_rk43_set_state(qd_solver *s, const double *Slip, const double *psi, const
     return QD_OK;
 }
 
+int qd_set_tail_sweeps(qd_solver *s, int n) {
+    if (!s || n < 0 || n > 64) {
+        set_error("qd_set_tail_sweeps: n must be 0..64");
+        return QD_ERR_ARG;
+    }
+    s->tail_sweeps = n;
+    return QD_OK;
+}
+
 int qd_set_newton_start(qd_solver *s, int mode) {
     if (!s || (mode != 0 && mode != 1)) {
         set_error("qd_set_newton_start: mode must be 0 or 1");

@@ -161,7 +161,13 @@ __device__ double newton_v(double Ts, double Tn, double tau0, double a, double e
     const double pa = psi / a;
     const double fa = a * fabs(Tn);
     const double fb = Ts + tau0;
-    const double A = 2.0 * eta * V0 * exp(-pa);
+    // A = 2 eta V0 e^{-pa}, formed where it is used: with the binary32
+    // start, |x| > 20 (nearly every node) needs only eta V0 e^{|x| - pa}
+    double A = -1.0;
+    auto coefA = [&]() {
+        if (A < 0.0) A = 2.0 * eta * V0 * exp(-pa);
+        return A;
+    };
     double lo, hi;
     if (fb >= 0.0) { lo = 0.0; hi = fb / fa; } else { lo = fb / fa; hi = 0.0; }
     // the seed's x; a zero seed (the reference's, every stage after the
@@ -177,11 +183,21 @@ __device__ double newton_v(double Ts, double Tn, double tau0, double a, double e
     int it = 0;
     bool done = false, phase2 = false;
     while (it < itmax) {
-        // sinh(0) = 0 and cosh(0) = 1 exactly: the first step from the
-        // reference's zero seed needs neither function
-        const bool x0 = x == 0.0;
-        const double fy = A * (x0 ? 0.0 : sinh(x)) + fa * x - fb;
-        const double df = A * (x0 ? 1.0 : cosh(x)) + fa;
+        double as, ac;   // A sinh x, A cosh x
+        if (start32 && fabs(x) > 20.0) {
+            // e^{-2|x|} < 2^-57: sinh |x| = cosh |x| = e^{|x|}/2 to within
+            // the rounding, one exponential instead of three
+            ac = eta * V0 * exp(fabs(x) - pa);
+            as = x > 0.0 ? ac : -ac;
+        } else {
+            // sinh(0) = 0 and cosh(0) = 1 exactly: the first step from the
+            // reference's zero seed needs neither function
+            const bool x0 = x == 0.0;
+            as = coefA() * (x0 ? 0.0 : sinh(x));
+            ac = coefA() * (x0 ? 1.0 : cosh(x));
+        }
+        const double fy = as + fa * x - fb;
+        const double df = ac + fa;
         const double d = -fy / (df + 1e-100);
         const double xn = x + d;
         if (!isnan(fy)) {
@@ -197,16 +213,18 @@ __device__ double newton_v(double Ts, double Tn, double tau0, double a, double e
             *flags |= ST_NEWTON_BRACKET;
             break;
         }
-        const double err = fabs(d) / (fabs(x) + 1e-100);
+        // the reference's test |d| / |x| < 1e-10; with the binary32 start
+        // the same test without the division
+        const bool conv = start32 ? fabs(d) < 1e-10 * (fabs(x) + 1e-100) : fabs(d) / (fabs(x) + 1e-100) < 1e-10;
         it++;
         x = xn;
-        if (err < 1e-10) { done = true; break; }
+        if (conv) { done = true; break; }
     }
     if (phase2) {
         const double sg = fb >= 0.0 ? 1.0 : -1.0, afb = fabs(fb);
         double ylo = sg > 0.0 ? lo : -hi, yhi = sg > 0.0 ? hi : -lo;
         double y = fmin(fmax(sg * x, ylo), yhi);
-        const double lnA = log(A);
+        const double lnA = log(coefA());
         while (it < itmax) {
             double yn;
             const double rem = afb - fa * y;
@@ -228,8 +246,14 @@ __device__ double newton_v(double Ts, double Tn, double tau0, double a, double e
     }
     if (!done) *flags |= ST_NEWTON_CAP;
     *iters = it;
-    double V = 2.0 * V0 * exp(-psi / a);
-    V = V * sinh(x);
+    double V;
+    if (start32 && fabs(x) > 20.0) {
+        V = V0 * exp(fabs(x) - pa);
+        if (x < 0.0) V = -V;
+    } else {
+        V = 2.0 * V0 * exp(-psi / a);
+        V = V * sinh(x);
+    }
     if (isnan(V)) *flags |= ST_NEWTON_NAN;
     return V;
 }

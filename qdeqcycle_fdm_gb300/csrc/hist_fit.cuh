@@ -109,8 +109,13 @@ __device__ void fit_reduce_solve(const FitArgs &F, FitAcc<ND> &acc) {
         *F.count = 0;                               // ready for the next fit
     }
 
-    // unit-diagonal scaling, 1e-12 ridge, Cholesky
-    double G[ND][ND], b[ND], sc[ND], L[ND][ND], y[ND], c[ND];
+    // unit-diagonal scaling, 1e-12 ridge, Cholesky.  This is one thread's
+    // chain of FP64 instructions on a pipe that issues about one per SM
+    // clock, so it avoids FP64 divisions and square roots: the scales are
+    // binary32 reciprocal square roots (any scale serves; these make the
+    // diagonal 1 to within 1e-7), and each pivot's reciprocal square root r
+    // gives both L_jj = p r and the divisions by L_jj as products.
+    double G[ND][ND], b[ND], sc[ND], L[ND][ND], rinv[ND], y[ND], c[ND];
     int q = 0;
     for (int k = 0; k < ND; k++)
         for (int l = k; l < ND; l++) {
@@ -120,28 +125,32 @@ __device__ void fit_reduce_solve(const FitArgs &F, FitAcc<ND> &acc) {
     for (int k = 0; k < ND; k++) b[k] = sums[NT + k];
     const double tt = sums[NA - 1];
     bool ok = true;
-    for (int k = 0; k < ND; k++) sc[k] = G[k][k] > 0.0 ? 1.0 / sqrt(G[k][k]) : 0.0;
+    for (int k = 0; k < ND; k++) {
+        const float g = d2f_rne(G[k][k]);
+        sc[k] = (g > 0.f && g < 3.0e38f) ? f2d_exact(rsqrtf(g)) : 0.0;
+    }
     for (int j = 0; j < ND && ok; j++) {
         double sjj = (sc[j] > 0.0 ? G[j][j] * sc[j] * sc[j] : 1.0) + 1e-12;
         for (int k = 0; k < j; k++) sjj -= L[j][k] * L[j][k];
         if (!(sjj > 0.0)) { ok = false; break; }
-        L[j][j] = sqrt(sjj);
+        rinv[j] = rsqrt(sjj);
+        L[j][j] = sjj * rinv[j];
         for (int i = j + 1; i < ND; i++) {
             double sij = G[i][j] * sc[i] * sc[j];
             for (int k = 0; k < j; k++) sij -= L[i][k] * L[j][k];
-            L[i][j] = sij / L[j][j];
+            L[i][j] = sij * rinv[j];
         }
     }
     if (ok) {
         for (int i = 0; i < ND; i++) {
             double r = b[i] * sc[i];
             for (int k = 0; k < i; k++) r -= L[i][k] * y[k];
-            y[i] = r / L[i][i];
+            y[i] = r * rinv[i];
         }
         for (int i = ND - 1; i >= 0; i--) {
             double r = y[i];
             for (int k = i + 1; k < ND; k++) r -= L[k][i] * c[k];
-            c[i] = r / L[i][i];
+            c[i] = r * rinv[i];
         }
         for (int i = 0; i < ND; i++) {
             c[i] *= sc[i];

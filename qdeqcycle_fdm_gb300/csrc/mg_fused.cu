@@ -721,7 +721,9 @@ static int launch_tail(qd_solver *s, Level<T> *Ls, int lt) {
     const int nl = s->nlev;
     TailArgs<T> ta;
     for (int l = 0; l < nl; l++) ta.L[l] = lv(s, Ls, l);
-    ta.p.l0 = lt; ta.p.nlev = nl; ta.p.nu_pre = s->opt.nu_pre; ta.p.nu_post = s->opt.nu_post;
+    ta.p.l0 = lt; ta.p.nlev = nl;
+    ta.p.nu_pre = s->tail_sweeps > 0 ? s->tail_sweeps : s->opt.nu_pre;
+    ta.p.nu_post = s->tail_sweeps > 0 ? s->tail_sweeps : s->opt.nu_post;
     ta.p.nu_coarse = s->opt.nu_coarse; ta.p.surface = s->opt.surface_prolong;
     ta.p.coarse_solve = s->opt.coarse_solve;
     ta.p.nint = s->n_cint;

@@ -14,7 +14,7 @@
 //   WHILE      body: one V-cycle -> ||r|| -> k_solve_check: next decision
 //
 // In mixed precision the prologue and the body's check are folded into the
-// last block of the FP64 residual's reduction (one kernel each).
+// last block of the level-0 residual's reduction (one kernel each).
 //
 // The loop condition is a graph conditional handle that the check kernels
 // set on the device (cudaGraphSetConditional), so no host round trip
@@ -41,6 +41,7 @@ struct SolveGraph {
     qd_mg_options opt;
     bool net = false;   // built with the network's conditional correction
     double net_ratio = 0.0;
+    int tail_sweeps = 0;
 };
 
 // n_kernels: kernels of the prologue, this one included; in_graph: set the
@@ -118,7 +119,7 @@ static int capture_cycle(qd_solver *s, cudaGraphConditionalHandle h, int in_grap
         dc.in_graph = in_graph;
         dc.h = h;
         dc.st = s->d_solve;
-        QD_TRY(level0_norm_decide(s, dc));   // FP64 residual -> FP32 rhs, norm, decision
+        QD_TRY(level0_norm_decide(s, dc));   // level-0 residual -> FP32 rhs, norm, decision
         *fused = true;
     } else {
         int nb = 0;
@@ -247,6 +248,7 @@ static int build(qd_solver *s, SolveGraph *sg) {
     QD_TRY(end_capture(s, nullptr, rc));
     QD_CUDA(cudaGraphInstantiate(&sg->exec, sg->graph, 0));
     sg->opt = s->opt;
+    sg->tail_sweeps = s->tail_sweeps;
     return QD_OK;
 }
 
@@ -300,7 +302,7 @@ int mg_solve_async(qd_solver *s) {
     }
     const int key = warm_start_predicting(s) ? 1 : 0;
     SolveGraph *&sg = gs->g[key];
-    if (sg && (!same_opts(sg->opt, s->opt) || sg->net_ratio != s->net_ratio)) {
+    if (sg && (!same_opts(sg->opt, s->opt) || sg->net_ratio != s->net_ratio || sg->tail_sweeps != s->tail_sweeps)) {
         graph_free(sg);
         sg = nullptr;
     }

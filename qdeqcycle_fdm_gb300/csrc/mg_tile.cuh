@@ -342,7 +342,9 @@ __global__ void __launch_bounds__(NT, 2)
     const int ka = max(1, k0), kb = min(g.K - 2, k1 - 1);
     if (MODE == 2) {
         // u64 += e: the loads of two rows x two columns go out before any
-        // store, so each warp waits on memory once per four nodes
+        // store, so each warp waits on memory once per four nodes; e is
+        // widened on the integer pipes (f2d_exact), leaving the FP64 pipe
+        // one addition per node
         for (int jb = j0 + TWARP; jb < j1; jb += 2 * TNWARP) {
             double a[2][2];
 #pragma unroll
@@ -358,13 +360,13 @@ __global__ void __launch_bounds__(NT, 2)
                 for (int h = 0; h < 2; h++) {
                     const int j = jb + q * TNWARP, k = ka + TLANE + 32 * h;
                     if (j < j1 && k <= kb)
-                        u64[(long)j * P64 + k] = a[q][h] + (double)t.u[(j - jL0) * t.W + (k - kL0)];
+                        u64[(long)j * P64 + k] = a[q][h] + f2d_exact(t.u[(j - jL0) * t.W + (k - kL0)]);
                 }
             for (int q = 0; q < 2; q++) {   // columns past 64 (wide tiles only)
                 const int j = jb + q * TNWARP;
                 if (j >= j1) break;
                 for (int k = ka + TLANE + 64; k <= kb; k += 32)
-                    u64[(long)j * P64 + k] += (double)t.u[(j - jL0) * t.W + (k - kL0)];
+                    u64[(long)j * P64 + k] += f2d_exact(t.u[(j - jL0) * t.W + (k - kL0)]);
             }
         }
         return;

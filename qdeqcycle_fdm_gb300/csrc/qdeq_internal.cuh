@@ -90,7 +90,7 @@ static constexpr unsigned int ST_TMA_TIMEOUT = 8u;
 
 // The learned correction's default cost in V-cycles for the measured gate:
 // one inference on the level-1 grid of a 1025^2 solver (181 us) against one
-// V-cycle there with its FP64 residual (about 100 us) is about two cycles.
+// V-cycle there with its level-0 residual (about 100 us) is about two cycles.
 static constexpr double kNetCostCycles = 2.0;
 
 // state of the device-driven multigrid loop (mg_graph.cu)
@@ -219,7 +219,7 @@ __device__ inline int solve_check_dev(const double *scal, SolveState *st, int ma
     return go;
 }
 
-// a decision fused into the last block of the level-0 FP64 residual
+// a decision fused into the last block of the level-0 residual's
 // reduction (mixed precision): mode 1 also computes ||r0||^2 and takes the
 // first decision (phase as for solve_begin_dev; phase 1 also sets h_net to
 // the decision), mode 2 the decision after a cycle; mode 0 none
@@ -353,6 +353,7 @@ struct qd_solver {
     void *history;         // ring of earlier solutions for the initial guess (history.cu), or null
     void *snapshot;        // the snapshot writer in flight (io.cu), or null
     int tail_l0;           // first level of the coarse tail
+    int tail_sweeps;       // pre- and post-sweeps on the tail's levels (0: the fine levels' nu_pre, nu_post)
     int box_up, box_down;  // staged tile box widths of k_up / k_down (0: the default 64)
     void *solve_graph;     // the instantiated multigrid graph (mg_graph.cu)
     qd::SolveState *d_solve, *h_solve;
@@ -391,7 +392,8 @@ int tiles_set(qd_solver *s, int box_up, int box_down);
 int time_kernel(qd_solver *s, int which, int reps, double *us);
 // a bounded mbarrier wait that nothing completes (gives up after `polls`)
 int wait_probe(qd_solver *s, unsigned polls);
-// mg.cu: level-0 norms into d_scal[slot] (to32: FP64 residual -> FP32 rhs)
+// mg.cu: level-0 norms into d_scal[slot] (to32: the mixed solver's
+// double-float residual -> FP32 rhs)
 int level0_norm(qd_solver *s, int to32, int slot);
 int level0_norm_decide(qd_solver *s, const Decide &dc);
 // u = u0 + alpha (u - u0) with the alpha that minimises the energy norm of

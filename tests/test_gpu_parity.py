@@ -135,6 +135,37 @@ def test_mixed_solve_with_exact_coarse_solve():
     assert rel(res[(1, 1)][1], res[(0, 0)][1]) < 1e-8
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_tail_sweeps_reach_the_same_solution(precision):
+    """One pre- and one post-sweep on the coarse tail's levels (65 rows and
+    below; qd_set_tail_sweeps) instead of V(2,2) there: the solve still
+    meets 1e-10 of ||r0|| with at most one V-cycle more, and its u agrees
+    with the default schedule's and with the oracle's solve to what that
+    tolerance lets through."""
+    cfg, prob = make_problem(257, mu_profile="layered", layer_depth_km=8.0)
+    mg_cfg = config.MGConfig(n_levels=6, nu_pre=2, nu_post=2, nu_coarse=32, tol_mode=1, tol=1e-10,
+                             max_cycles=100, precision=precision, surface_prolong=1, coarse_solve=1)
+    U = random_U(prob, 6)
+    res = {}
+    for tail in (0, 1):
+        s = api.Solver(prob.ni, prob.nk, prob.dh, prob.mu_equi, prob.mu_node, mg_cfg)
+        s.set_tail_sweeps(tail)
+        s.upload_u(U)
+        cyc, rn, r0 = s.ode_solve()
+        assert rn <= 1e-10 * r0
+        res[tail] = (cyc, compact(s.download_u()))
+        if tail == 1:
+            with pytest.raises(Exception):
+                s.set_tail_sweeps(-1)
+        s.close()
+    assert res[1][0] <= res[0][0] + 1, (res[0][0], res[1][0])
+    assert rel(res[1][1], res[0][1]) < 1e-8
+    mg = oracle.Multigrid(prob.ni, prob.nk, prob.dh, prob.mu_equi, 6, 2, 2, 32)
+    u = compact(U).copy()
+    mg.solve(u, tol_mode=1, tol=1e-12, max_cycles=200)
+    assert rel(res[1][1], u) < 1e-8
+
+
 def test_reference_schedule_solve_matches_oracle():
     """The reference's own schedule: 6 levels, V(32,32), absolute 1e-9."""
     cfg, prob = make_problem(129, mu_profile="layered", layer_depth_km=20.0)
