@@ -131,6 +131,9 @@ def parse():
                    help="pre- and post-sweeps on the coarse tail's levels (<= 65 rows) of the fast solvers "
                         "(0: the fine levels' schedule); the plain FP64 drop-in and the FP64 reference of "
                         "the error measurement keep 0")
+    p.add_argument("--smooth-ratio", type=float, default=2.5,
+                   help="mixed-precision solvers: a level-0 smoothing pass instead of a V-cycle after a cycle "
+                        "that left ||r|| within this ratio of the threshold (0: off)")
     p.add_argument("--config2-wall-s", type=float, default=240.0,
                    help="--config config2: seconds of stepping from steady sliding")
     p.add_argument("--error-steps", type=int, default=10,
@@ -347,6 +350,7 @@ def run_ours(args):
         tsim.solver.set_solution_history(H)
         tsim.solver.set_newton_start(args.newton_start)
         tsim.solver.set_tail_sweeps(args.tail_sweeps)
+        tsim.solver.set_smooth_correction(args.smooth_ratio)
         net = warmstart.UNet(unet_n(tprob.nk), unet_n(tprob.ni), seed=args.seed)
         net.attach(tsim.solver, warmstart.MODE_TRAIN, args.lr)
         tsim.start()
@@ -373,6 +377,8 @@ def run_ours(args):
         sim.solver.set_solution_history(history)
         sim.solver.set_newton_start(args.newton_start if newton is None else newton)
         sim.solver.set_tail_sweeps(args.tail_sweeps if tail is None else tail)
+        if mg.precision == 1:
+            sim.solver.set_smooth_correction(args.smooth_ratio)
         if net is not None:
             net.attach(sim.solver, warmstart.MODE_PREDICT)
             warmstart.UNet.set_gate(sim.solver, args.net_gate)
@@ -438,6 +444,7 @@ def run_ours(args):
                      "t0": s0["t"], "t_end": s1["t"], "it0": s0["it"], "it1": s1["it"],
                      "launches": s1["kernel_launches"] - s0["kernel_launches"],
                      "vcycles": s1["vcycles"] - s0["vcycles"], "solves": s1["solves"] - s0["solves"],
+                     "smooths": s1["smooth_corrections"] - s0["smooth_corrections"],
                      "newton": (s1["newton_iters"] - s0["newton_iters"]) / max(1, (s1["solves"] - s0["solves"]) * prob.nk),
                      "net_solves": s1["net_solves"] - s0["net_solves"],
                      "net_needed": s1["net_cycles_needed"] - s0["net_cycles_needed"],
@@ -454,6 +461,7 @@ def run_ours(args):
     def summary(run):
         return {"value": job_value(run), "ms_per_step": reduce_max(run["ms"]) / args.steps,
                 "vcycles_per_solve": run["vcycles"] / max(1, run["solves"]),
+                "smoothing_passes_per_solve": run["smooths"] / max(1, run["solves"]),
                 "solves_per_step": run["solves"] / args.steps, "sim_years_timed": run["yrs"],
                 "newton_iters_per_node_solve": run["newton"],
                 "span_s": [run["t0"], run["t_end"]]}
@@ -481,6 +489,7 @@ def run_ours(args):
                 x.solver.set_solution_history(H)
                 x.solver.set_newton_start(args.newton_start)
                 x.solver.set_tail_sweeps(args.tail_sweeps)
+                x.solver.set_smooth_correction(args.smooth_ratio)
                 x.start()
             if mode == "batched":
                 api.ensemble_step(sims, 3)
@@ -534,6 +543,7 @@ def run_ours(args):
                               "window": args.window, "steps": args.steps, "warmup": args.warmup,
                               "ms_per_step": run["ms"] / args.steps,
                               "vcycles_per_solve": run["vcycles"] / max(1, run["solves"]),
+                              "smoothing_passes_per_solve": run["smooths"] / max(1, run["solves"]),
                               "solves_per_step": run["solves"] / args.steps,
                               "network_corrected_solves": run["net_solves"] / max(1, run["solves"]),
                               "autotune": run["autotune"]}),
@@ -656,6 +666,8 @@ def run_ours(args):
         nst = s1["it"] - s0["it"]
         return {"value": yrs / (ms / 3.6e6), "sim_years": yrs, "steps": nst, "ms": ms, "ms_per_step": ms / nst,
                 "host_wall_s": wall, "vcycles_per_solve": (s1["vcycles"] - s0["vcycles"]) / max(1, s1["solves"] - s0["solves"]),
+                "smoothing_passes_per_solve": (s1["smooth_corrections"] - s0["smooth_corrections"])
+                / max(1, s1["solves"] - s0["solves"]),
                 "solves_per_step": (s1["solves"] - s0["solves"]) / nst,
                 "network_corrected_solves": (s1["net_solves"] - s0["net_solves"]) / max(1, s1["solves"] - s0["solves"]),
                 "network_cycles_needed_taken": [s1["net_cycles_needed"] - s0["net_cycles_needed"],
@@ -800,6 +812,7 @@ def run_ours(args):
                        "parallelism": f"replicas x{world}", "l2": "flushed before every timed step"},
             "sim_years_timed": head["yrs"], "t_start_s": head["t0"], "t_end_s": head["t_end"],
             "vcycles_per_solve": head["vcycles"] / max(1, head["solves"]),
+            "smoothing_passes_per_solve": head["smooths"] / max(1, head["solves"]),
             "solves_per_step": head["solves"] / args.steps,
             "newton_iters_per_node_solve": head["newton"],
             "network_corrected_solves": head["net_solves"] / max(1, head["solves"]) if learned else None,
@@ -882,6 +895,7 @@ def run_config2(args):
     sim.solver.set_solution_history(args.history)
     sim.solver.set_newton_start(args.newton_start)
     sim.solver.set_tail_sweeps(args.tail_sweeps)
+    sim.solver.set_smooth_correction(args.smooth_ratio)
     sim.start()
     stream = torch.cuda.ExternalStream(sim.solver.stream_ptr())
     s0 = sim.state(with_u=False)
@@ -920,6 +934,8 @@ def run_config2(args):
     sim.close()
     run = {"sim_years": yrs, "steps": nst, "ms": ms, "ms_per_step": ms / max(1, nst),
            "value": yrs / (ms / 3.6e6), "vcycles_per_solve": (s1["vcycles"] - s0["vcycles"]) / max(1, s1["solves"] - s0["solves"]),
+           "smoothing_passes_per_solve": (s1["smooth_corrections"] - s0["smooth_corrections"])
+           / max(1, s1["solves"] - s0["solves"]),
            "ruptures_seen": ruptures, "max_V": vmax, "t_end_yr": s1["t"] / YEAR_S, "dt_end_s": s1["dt"]}
 
     # error against FP64 on identical fixed steps from the state reached
@@ -933,6 +949,8 @@ def run_config2(args):
         x.solver.set_solution_history(hist)
         x.solver.set_newton_start(args.newton_start if name == "mixed" else 0)
         x.solver.set_tail_sweeps(args.tail_sweeps if name == "mixed" else 0)
+        if name == "mixed":
+            x.solver.set_smooth_correction(args.smooth_ratio)
         x.resume(ck, U=U, params=params)
         x.step(5)
         out[name] = x.state()

@@ -110,6 +110,8 @@ typedef struct qd_stats {
                                 guesses would have needed (from the
                                 measured reduction per cycle) ...          */
     double net_cycles_taken;  /* ... and the V-cycles they took            */
+    long long smooth_corrections; /* level-0 smoothing passes that replaced
+                                a V-cycle (qd_set_smooth_correction)       */
 } qd_stats;
 
 const char *qd_version(void);
@@ -370,6 +372,17 @@ int qd_set_newton_start(qd_solver *s, int mode);
  * leave the cycle's reduction nearly unchanged.  No counterpart in the
  * reference. */
 int qd_set_tail_sweeps(qd_solver *s, int n);
+/* Mixed precision only: after a V-cycle that leaves ||r|| above the
+ * threshold by at most `ratio`, the next correction of the solve is a
+ * level-0 smoothing pass (four red-black sweeps on the correction equation
+ * from zero, one kernel) instead of a V-cycle; at most one such pass in a
+ * row, and the solve still stops only at the same tolerance.  A V-cycle
+ * leaves a residual whose norm is mostly rough components, which the pass
+ * removes: at 1025^2 it cuts ||r|| to about a third, so ratios up to about
+ * 2.5 finish the solve with it.  ratio 0 (the default): off.  Counted in
+ * qd_stats.smooth_corrections, not in vcycles.  No counterpart in the
+ * reference. */
+int qd_set_smooth_correction(qd_solver *s, double ratio);
 /* The last fit: coef[0..6] the coefficients of the earlier solutions
  * (newest first), coef[7] the fit's boundary misfit over the change from
  * the latest solution's boundary data (1: no gain); *nd coefficients are

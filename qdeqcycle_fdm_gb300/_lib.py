@@ -64,6 +64,7 @@ EXPORTS = [
     ("qd_set_solution_history", C.c_int, [C.c_void_p, C.c_int]),
     ("qd_set_newton_start", C.c_int, [C.c_void_p, C.c_int]),
     ("qd_set_tail_sweeps", C.c_int, [C.c_void_p, C.c_int]),
+    ("qd_set_smooth_correction", C.c_int, [C.c_void_p, C.c_double]),
     ("qd_autotune", C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     ("qd_set_tiles", C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     ("qd_solution_history_fit", C.c_int, [C.c_void_p, _dp, _ip]),
@@ -106,7 +107,8 @@ class Stats(C.Structure):
     _fields_ = [("solves", C.c_longlong), ("vcycles", C.c_longlong), ("attempts", C.c_longlong),
                 ("steps", C.c_longlong), ("newton_iters", C.c_longlong),
                 ("kernel_launches", C.c_longlong), ("net_solves", C.c_longlong),
-                ("net_cycles_needed", C.c_double), ("net_cycles_taken", C.c_double)]
+                ("net_cycles_needed", C.c_double), ("net_cycles_taken", C.c_double),
+                ("smooth_corrections", C.c_longlong)]
 
 
 class Tuning(C.Structure):

@@ -244,6 +244,12 @@ class Solver:
         0: the fine levels' schedule (the default)."""
         check(self.L.qd_set_tail_sweeps(self.h, int(n)))
 
+    def set_smooth_correction(self, ratio):
+        """Mixed precision: a level-0 smoothing pass instead of a V-cycle
+        after a cycle that left ||r|| within `ratio` of the threshold (0:
+        off, the default)."""
+        check(self.L.qd_set_smooth_correction(self.h, float(ratio)))
+
     def autotune(self, reps=3):
         """Time the candidate smoother schedules and tile box widths on this
         solver's problem (the last stored solve replayed from the solution

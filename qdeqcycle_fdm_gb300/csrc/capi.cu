@@ -340,6 +340,7 @@ int qd_get_stats(qd_solver *s, qd_stats *st) {
     st->net_solves = (long long)ss.net_solves;
     st->net_cycles_needed = ss.net_cycles_needed;
     st->net_cycles_taken = ss.net_cycles_taken;
+    st->smooth_corrections = (long long)ss.total_smooths;
     std::vector<int> it(s->nz);
     QD_CUDA(cudaMemcpy(it.data(), s->F.iters, s->nz * sizeof(int), cudaMemcpyDeviceToHost));
     long long sum = 0;
@@ -692,6 +693,19 @@ int qd_set_tail_sweeps(qd_solver *s, int n) {
         return QD_ERR_ARG;
     }
     s->tail_sweeps = n;
+    return QD_OK;
+}
+
+int qd_set_smooth_correction(qd_solver *s, double ratio) {
+    if (!s || !(ratio == 0.0 || (ratio > 1.0 && ratio <= 1e6))) {
+        set_error("qd_set_smooth_correction: ratio must be 0 or in (1, 1e6]");
+        return QD_ERR_ARG;
+    }
+    if (ratio > 0.0 && s->opt.precision != QD_PREC_MIXED) {
+        set_error("qd_set_smooth_correction: the smoothing pass needs mixed precision");
+        return QD_ERR_ARG;
+    }
+    s->smooth_ratio = ratio;
     return QD_OK;
 }
 

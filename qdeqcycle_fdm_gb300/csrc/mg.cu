@@ -340,8 +340,11 @@ __global__ void __launch_bounds__(BX * BY, RES_DF_CTAS_PER_SM)
             }
         }
     } else if (dc.mode == 2 && tid == 0) {
-        const int go = solve_check_dev(out, dc.st, dc.max_cycles, dc.n_kernels);
-        if (dc.in_graph) cudaGraphSetConditional(dc.h, go ? 1u : 0u);
+        const int go = solve_check_dev(out, dc.st, dc.max_cycles, dc.n_kernels, dc.smooth_ratio, dc.n_kernels_smooth);
+        if (dc.in_graph) {
+            cudaGraphSetConditional(dc.h, go ? 1u : 0u);
+            if (dc.smooth_ratio > 1.0) cudaGraphSetConditional(dc.h_smooth, dc.st->smooth ? 1u : 0u);
+        }
     }
 }
 

@@ -829,6 +829,15 @@ int vcycle64_norm(qd_solver *s, int *nblocks) { return vcycle_fused<double, 1>(s
 
 int vcycle32_into64(qd_solver *s) { return vcycle_fused<float, 2>(s, s->L32, 1, nullptr); }
 
+// The level-0 smoothing pass of the mixed solver (the correction after a
+// V-cycle that left the residual near the threshold): SMAX half-sweeps on
+// A e = r from e = 0, then u64 += e -- the level-0 k_up of a cycle without
+// the prolongation, one launch.
+int smooth32_into64(qd_solver *s) {
+    bool in_r = false;
+    return launch_up<float, 2>(s, s->L32, 0, SMAX, 0, 1, &in_r, false, s->L64[0].u, s->dims[0].P);
+}
+
 // One kernel of the V-cycle the solver's precision runs, launched `reps`
 // times back to back on the solver's stream between two events: the
 // per-launch time of a kernel that otherwise runs inside the solve graph.

@@ -42,6 +42,7 @@ struct SolveGraph {
     bool net = false;   // built with the network's conditional correction
     double net_ratio = 0.0;
     int tail_sweeps = 0;
+    double smooth_ratio = 0.0;
 };
 
 // n_kernels: kernels of the prologue, this one included; in_graph: set the
@@ -104,22 +105,40 @@ static int cycle_cap(const qd_solver *s, int in_graph) {
     return in_graph ? QD_SOLVE_GRAPH_MAX_CYCLES : 0;
 }
 
-// the body of one loop iteration: a V-cycle and the norm of the new
-// residual; in mixed precision the norm's last block also takes the loop's
-// decision (*fused set), otherwise k_solve_check follows
+// the mixed solver's check after a correction: the level-0 residual ->
+// FP32 rhs, its norm and the loop's decision in the residual's last block
+// (and, with the smoothing pass enabled, whether the next correction is
+// one: h_smooth); n_cycle / n_smooth: the kernels of a V-cycle iteration
+// and of a smoothing iteration before the check
+static int mixed_check(qd_solver *s, cudaGraphConditionalHandle h, cudaGraphConditionalHandle h_smooth,
+                       int in_graph, int n_cycle, int n_smooth) {
+    Decide dc{};
+    dc.mode = 2;
+    dc.max_cycles = cycle_cap(s, in_graph);
+    dc.n_kernels = n_cycle + 1;
+    dc.n_kernels_smooth = n_smooth + 1;
+    dc.smooth_ratio = s->smooth_ratio;
+    dc.in_graph = in_graph;
+    dc.h = h;
+    dc.h_smooth = h_smooth;
+    dc.st = s->d_solve;
+    return level0_norm_decide(s, dc);
+}
+
+// the body of one loop iteration: a V-cycle (or, smooth, the mixed
+// solver's level-0 smoothing pass) and the norm of the new residual; in
+// mixed precision the norm's last block also takes the loop's decision
+// (*fused set), otherwise k_solve_check follows
 static int capture_cycle(qd_solver *s, cudaGraphConditionalHandle h, int in_graph, long long launches0,
-                         bool *fused) {
+                         bool *fused, bool smooth = false) {
     *fused = false;
     if (s->opt.precision == QD_PREC_MIXED) {
-        QD_TRY(vcycle32_into64(s));          // FP32 cycle on A e = r, then u += e
-        Decide dc{};
-        dc.mode = 2;
-        dc.max_cycles = cycle_cap(s, in_graph);
-        dc.n_kernels = (int)(s->launches - launches0) + 1;
-        dc.in_graph = in_graph;
-        dc.h = h;
-        dc.st = s->d_solve;
-        QD_TRY(level0_norm_decide(s, dc));   // level-0 residual -> FP32 rhs, norm, decision
+        if (smooth)
+            QD_TRY(smooth32_into64(s));      // level-0 sweeps on A e = r from zero, then u += e
+        else
+            QD_TRY(vcycle32_into64(s));      // FP32 cycle on A e = r, then u += e
+        const int n = (int)(s->launches - launches0);
+        QD_TRY(mixed_check(s, h, 0, in_graph, n, n));
         *fused = true;
     } else {
         int nb = 0;
@@ -235,20 +254,51 @@ static int build(qd_solver *s, SolveGraph *sg) {
     cudaGraphNode_t loop;
     QD_CUDA(cudaGraphAddNode(&loop, sg->graph, leaf ? &leaf : nullptr, nullptr, leaf ? 1 : 0, &cp));
     cudaGraph_t body = cp.conditional.phGraph_out[0];
-    QD_CUDA(cudaStreamBeginCaptureToGraph(s->stream, body, nullptr, nullptr, 0,
-                                          cudaStreamCaptureModeRelaxed));
-    bool fused = false;
-    rc = capture_cycle(s, h, 1, launches0, &fused);
-    if (rc == QD_OK && !fused) {
-        const int n = (int)(s->launches - launches0) + 1;
-        k_solve_check<<<1, 1, 0, s->stream>>>(h, s->d_scal, s->d_solve, cycle_cap(s, 1), n, 1);
-        if (cudaPeekAtLastError() != cudaSuccess) rc = QD_ERR_CUDA;
+    if (s->opt.precision == QD_PREC_MIXED && s->smooth_ratio > 1.0) {
+        // body: IF the check chose the smoothing pass THEN that pass ELSE a
+        // V-cycle; then the check (residual, norm, both decisions)
+        cudaGraphConditionalHandle h_smooth;
+        QD_CUDA(cudaGraphConditionalHandleCreate(&h_smooth, sg->graph, 0, cudaGraphCondAssignDefault));
+        cudaGraphNodeParams ep = {};
+        ep.type = cudaGraphNodeTypeConditional;
+        ep.conditional.handle = h_smooth;
+        ep.conditional.type = cudaGraphCondTypeIf;
+        ep.conditional.size = 2;
+        cudaGraphNode_t branch;
+        QD_CUDA(cudaGraphAddNode(&branch, body, nullptr, nullptr, 0, &ep));
+        QD_CUDA(cudaStreamBeginCaptureToGraph(s->stream, ep.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                              cudaStreamCaptureModeRelaxed));
+        rc = smooth32_into64(s);
+        const int n_smooth = (int)(s->launches - launches0);
+        s->launches = launches0;
+        QD_TRY(end_capture(s, nullptr, rc));
+        QD_CUDA(cudaStreamBeginCaptureToGraph(s->stream, ep.conditional.phGraph_out[1], nullptr, nullptr, 0,
+                                              cudaStreamCaptureModeRelaxed));
+        rc = vcycle32_into64(s);
+        const int n_cycle = (int)(s->launches - launches0);
+        s->launches = launches0;
+        QD_TRY(end_capture(s, nullptr, rc));
+        QD_CUDA(cudaStreamBeginCaptureToGraph(s->stream, body, &branch, nullptr, 1, cudaStreamCaptureModeRelaxed));
+        rc = mixed_check(s, h, h_smooth, 1, n_cycle, n_smooth);
+        s->launches = launches0;
+        QD_TRY(end_capture(s, nullptr, rc));
+    } else {
+        QD_CUDA(cudaStreamBeginCaptureToGraph(s->stream, body, nullptr, nullptr, 0,
+                                              cudaStreamCaptureModeRelaxed));
+        bool fused = false;
+        rc = capture_cycle(s, h, 1, launches0, &fused);
+        if (rc == QD_OK && !fused) {
+            const int n = (int)(s->launches - launches0) + 1;
+            k_solve_check<<<1, 1, 0, s->stream>>>(h, s->d_scal, s->d_solve, cycle_cap(s, 1), n, 1);
+            if (cudaPeekAtLastError() != cudaSuccess) rc = QD_ERR_CUDA;
+        }
+        s->launches = launches0;
+        QD_TRY(end_capture(s, nullptr, rc));
     }
-    s->launches = launches0;
-    QD_TRY(end_capture(s, nullptr, rc));
     QD_CUDA(cudaGraphInstantiate(&sg->exec, sg->graph, 0));
     sg->opt = s->opt;
     sg->tail_sweeps = s->tail_sweeps;
+    sg->smooth_ratio = s->smooth_ratio;
     return QD_OK;
 }
 
@@ -282,7 +332,7 @@ static int solve_eager(qd_solver *s) {
         QD_TRY(solve_state_read(s, &st));
         if (!st.go) return QD_OK;
         bool fused = false;
-        QD_TRY(capture_cycle(s, 0, 0, launches0, &fused));
+        QD_TRY(capture_cycle(s, 0, 0, launches0, &fused, st.smooth != 0));
         if (!fused) {
             k_solve_check<<<1, 1, 0, s->stream>>>(0, s->d_scal, s->d_solve, cycle_cap(s, 0),
                                                   (int)(s->launches - launches0) + 1, 0);
@@ -302,7 +352,8 @@ int mg_solve_async(qd_solver *s) {
     }
     const int key = warm_start_predicting(s) ? 1 : 0;
     SolveGraph *&sg = gs->g[key];
-    if (sg && (!same_opts(sg->opt, s->opt) || sg->net_ratio != s->net_ratio || sg->tail_sweeps != s->tail_sweeps)) {
+    if (sg && (!same_opts(sg->opt, s->opt) || sg->net_ratio != s->net_ratio || sg->tail_sweeps != s->tail_sweeps ||
+               sg->smooth_ratio != s->smooth_ratio)) {
         graph_free(sg);
         sg = nullptr;
     }

@@ -112,6 +112,11 @@ struct SolveState {
     // cleared it (1e30 while no cycle has been measured): the host's
     // warm-start standby reads it once per RK attempt
     double need_max;
+    // the next correction is a level-0 smoothing pass instead of a V-cycle
+    // (set by the check after a V-cycle that left ||r|| within the solver's
+    // smoothing ratio of the threshold), and how many such passes ran
+    int smooth;
+    unsigned long long total_smooths;
 };
 
 // ---- programmatic dependent launch ----------------------------------------
@@ -163,6 +168,7 @@ __device__ inline int solve_begin_dev(const double *scal, SolveState *st, int re
     st->thr = thr;
     st->delta = delta;
     st->cycles = 0;
+    st->smooth = 0;
     if (phase == 2) st->net_solves++;
     else st->total_solves++;
     st->kernels += (unsigned long long)n_kernels;
@@ -190,12 +196,22 @@ __device__ inline int solve_begin_dev(const double *scal, SolveState *st, int re
     return go;
 }
 
-__device__ inline int solve_check_dev(const double *scal, SolveState *st, int max_cycles, int n_kernels) {
+// After a correction: the running reduction per V-cycle (V-cycles only),
+// the loop's next decision and, with smooth_ratio > 1 (mixed precision),
+// whether the next correction is a level-0 smoothing pass: once per solve,
+// after a V-cycle that left ||r|| within smooth_ratio of the threshold
+// (there the residual is mostly the rough part a smoothing pass removes;
+// measured at 1025^2: one pass of four sweeps cuts ||r|| to about 1/3).
+// cycles counts both kinds against the cap; n_kernels and n_kernels_smooth
+// are the kernels of the two kinds of iteration.
+__device__ inline int solve_check_dev(const double *scal, SolveState *st, int max_cycles, int n_kernels,
+                                      double smooth_ratio = 0.0, int n_kernels_smooth = 0) {
     const double delta = sqrt(scal[0]);
+    const bool was_smooth = st->smooth != 0;
     // the cycle's reduction factor, into the running mean of its log
     // (weight 1/8 after the first eight; factors clamped to [1e-6, 1])
     const double red = delta / st->delta;
-    if (st->delta > 0.0 && isfinite(red)) {
+    if (!was_smooth && st->delta > 0.0 && isfinite(red)) {
         const double l = log(fmin(fmax(red, 1e-6), 1.0));
         const double w = st->rho_samples < 8 ? 1.0 / (double)(st->rho_samples + 1) : 0.125;
         st->log_rho += w * (l - st->log_rho);
@@ -203,8 +219,13 @@ __device__ inline int solve_check_dev(const double *scal, SolveState *st, int ma
     }
     st->delta = delta;
     st->cycles++;
-    st->total_cycles++;
-    st->kernels += (unsigned long long)n_kernels;
+    if (was_smooth) {
+        st->total_smooths++;
+        st->kernels += (unsigned long long)n_kernels_smooth;
+    } else {
+        st->total_cycles++;
+        st->kernels += (unsigned long long)n_kernels;
+    }
     int go = !(delta <= st->thr);
     if (go && !isfinite(delta)) {
         st->flag |= 1;
@@ -215,6 +236,7 @@ __device__ inline int solve_check_dev(const double *scal, SolveState *st, int ma
         go = 0;
     }
     if (!go && st->net) st->net_cycles_taken += st->cycles;
+    st->smooth = go && !was_smooth && smooth_ratio > 1.0 && delta <= smooth_ratio * st->thr;
     st->go = go;
     return go;
 }
@@ -228,6 +250,11 @@ struct Decide {
     double tol, net_ratio;
     cudaGraphConditionalHandle h, h_net;
     SolveState *st;
+    // mode 2: the level-0 smoothing pass (smooth_ratio > 1: enabled; its
+    // condition goes to h_smooth in a graph; n_kernels_smooth as n_kernels)
+    double smooth_ratio;
+    int n_kernels_smooth;
+    cudaGraphConditionalHandle h_smooth;
 };
 
 // binary64 -> binary32 with round-to-nearest-even, on the integer pipes.
@@ -354,6 +381,8 @@ struct qd_solver {
     void *snapshot;        // the snapshot writer in flight (io.cu), or null
     int tail_l0;           // first level of the coarse tail
     int tail_sweeps;       // pre- and post-sweeps on the tail's levels (0: the fine levels' nu_pre, nu_post)
+    double smooth_ratio;   // mixed precision: a level-0 smoothing pass instead of a second V-cycle
+                           // within this ratio of the threshold (0: off)
     int box_up, box_down;  // staged tile box widths of k_up / k_down (0: the default 64)
     void *solve_graph;     // the instantiated multigrid graph (mg_graph.cu)
     qd::SolveState *d_solve, *h_solve;
@@ -386,6 +415,7 @@ int build_coarse_inverse(qd_solver *s);
 // mg_fused.cu
 int vcycle64_norm(qd_solver *s, int *nblocks);
 int vcycle32_into64(qd_solver *s);
+int smooth32_into64(qd_solver *s);
 void tma_cache_free(qd_solver *s);
 int tail_image_build(qd_solver *s);
 int tiles_set(qd_solver *s, int box_up, int box_down);

@@ -166,6 +166,43 @@ def test_tail_sweeps_reach_the_same_solution(precision):
     assert rel(res[1][1], u) < 1e-8
 
 
+def test_smoothing_pass_reaches_the_same_solution():
+    """Mixed precision with the level-0 smoothing pass
+    (qd_set_smooth_correction; ratio 1e6 alternates passes and V-cycles):
+    solves from rough data meet 1e-10 of ||r0|| (the tolerance is checked
+    after every correction), the smoothing passes are counted apart from the
+    V-cycles, no two come in a row, and u agrees with the oracle's solution
+    to what the tolerance lets through.  The FP64 solver refuses the pass."""
+    cfg, prob = make_problem(257, mu_profile="layered", layer_depth_km=8.0)
+    mg_cfg = config.MGConfig(n_levels=6, nu_pre=2, nu_post=2, nu_coarse=32, tol_mode=1, tol=1e-10,
+                             max_cycles=100, precision=1, surface_prolong=1, coarse_solve=1)
+    mg = oracle.Multigrid(prob.ni, prob.nk, prob.dh, prob.mu_equi, 6, 2, 2, 32)
+    smooths = 0
+    for seed in range(6):
+        U = random_U(prob, 20 + seed)
+        u = compact(U).copy()
+        mg.solve(u, tol_mode=1, tol=1e-12, max_cycles=200)
+        s = api.Solver(prob.ni, prob.nk, prob.dh, prob.mu_equi, prob.mu_node, mg_cfg)
+        s.set_smooth_correction(1e6 if seed % 2 else 3.0)
+        s.upload_u(U)
+        cyc, rn, r0 = s.ode_solve()
+        st = s.stats()
+        assert rn <= 1e-10 * r0
+        assert cyc == st["vcycles"] + st["smooth_corrections"]
+        assert st["smooth_corrections"] <= st["vcycles"]
+        smooths += st["smooth_corrections"]
+        assert rel(compact(s.download_u()), u) < 1e-8
+        with pytest.raises(Exception):
+            s.set_smooth_correction(0.5)
+        s.close()
+    assert smooths > 0
+    s64 = api.Solver(prob.ni, prob.nk, prob.dh, prob.mu_equi, prob.mu_node,
+                     config.MGConfig(**{**mg_cfg.__dict__, "precision": 0}))
+    with pytest.raises(Exception):
+        s64.set_smooth_correction(2.5)
+    s64.close()
+
+
 def test_reference_schedule_solve_matches_oracle():
     """The reference's own schedule: 6 levels, V(32,32), absolute 1e-9."""
     cfg, prob = make_problem(129, mu_profile="layered", layer_depth_km=20.0)
