@@ -546,6 +546,7 @@ def run_ours(args):
                               "smoothing_passes_per_solve": run["smooths"] / max(1, run["solves"]),
                               "solves_per_step": run["solves"] / args.steps,
                               "network_corrected_solves": run["net_solves"] / max(1, run["solves"]),
+                              "launches_per_step": run["launches"] / args.steps,
                               "autotune": run["autotune"]}),
                   flush=True)
         if net is not None:
