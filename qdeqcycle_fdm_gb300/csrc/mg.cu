@@ -225,6 +225,10 @@ __global__ void __launch_bounds__(BX * BY, RES_DF_CTAS_PER_SM)
                   Decide dc) {
     pdl_trigger();
     pdl_wait();   // launched with programmatic serialization: the previous kernel's data first
+    // the graph's first check, after a prologue that found the guess
+    // converged: skipped (every block reads the flag before the last block
+    // of this launch could write it)
+    if (dc.gate && !__ldcg(dc.gate)) return;
     constexpr int R = RES_DF_RPT;
     const int lane = threadIdx.x;
     const int N = v.N, K = v.K, P = v.P;
@@ -333,7 +337,8 @@ __global__ void __launch_bounds__(BX * BY, RES_DF_CTAS_PER_SM)
         }
         if (tid == 0) {
             if (dc.rel) out[1] = r0;
-            const int go = solve_begin_dev(out, dc.st, dc.rel, dc.tol, dc.n_kernels, dc.phase, dc.net_ratio);
+            const int go = solve_begin_dev(out, dc.st, dc.rel, dc.tol, dc.n_kernels, dc.phase, dc.net_ratio,
+                                           dc.n_kernels_gated);
             if (dc.in_graph) {
                 cudaGraphSetConditional(dc.h, go ? 1u : 0u);
                 if (dc.phase == 1) cudaGraphSetConditional(dc.h_net, dc.st->net ? 1u : 0u);

@@ -87,6 +87,7 @@ struct TailArgs {
     LvArgs<T> L[QD_MAXLEV];
     const T *img;                  // the packed image in global memory
     unsigned *status;
+    const int *gate;               // non-null: skip the launch when *gate is 0
     TailLevels p;
 };
 
@@ -184,6 +185,7 @@ template <typename T, bool ALLS>
 __global__ void __launch_bounds__(NT_TAIL) k_tail(TailArgs<T> a) {
     pdl_trigger();
     pdl_wait();   // launched with programmatic serialization: the previous kernel's data first
+    if (a.gate && !__ldcg(a.gate)) return;   // a solve that needs no cycle: this one is skipped
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bar;
     __shared__ TV<T> V[QD_MAXLEV];   // per-level views, read by every thread
@@ -535,7 +537,7 @@ static int launch_down(qd_solver *s, Level<T> *Ls, int l, int S, int zero_u, boo
     QD_TRY(tile_maps<T>(s, Ls, l, W, BH, &maps));
     QD_TRY(set_smem(k_down<T>, smem));
     QD_CUDA(launch_pdl(true, k_down<T>, dim3(ntk, ntj), dim3(NT), smem, s->stream, g, c, *maps, CH, CW, ntj, ntk,
-                       S, zero_u, (int)*in_r, field(Ls, l, !*in_r), &s->d_status->flags));
+                       S, zero_u, (int)*in_r, field(Ls, l, !*in_r), &s->d_status->flags, s->cycle_gate));
     QD_LAUNCH_CHECK(s);
     *in_r = !*in_r;
     return QD_OK;
@@ -568,7 +570,7 @@ static int launch_up(qd_solver *s, Level<T> *Ls, int l, int S, int prolong, int 
     const T *cu = (l + 1 < s->nlev) ? field(Ls, l + 1, coarse_in_r) : nullptr;
     QD_CUDA(launch_pdl(true, k_up<T, MODE>, dim3(ntk, ntj), dim3(NT), smem, s->stream, g, c, *maps, TH, TW, ntj,
                        ntk, S, prolong, s->opt.surface_prolong, zero_u, (int)*in_r, field(Ls, l, !*in_r), cu,
-                       s->d_partial, u64, P64, &s->d_status->flags));
+                       s->d_partial, u64, P64, &s->d_status->flags, s->cycle_gate));
     QD_LAUNCH_CHECK(s);
     if (MODE != 2) *in_r = !*in_r;
     if (nblocks) *nblocks = ntj * ntk;
@@ -729,6 +731,7 @@ static int launch_tail(qd_solver *s, Level<T> *Ls, int lt) {
     ta.p.nint = s->n_cint;
     ta.img = static_cast<const T *>(s->d_tail_img[sizeof(T) == 8]);
     ta.status = &s->d_status->flags;
+    ta.gate = s->cycle_gate;
     if (!ta.img || s->tail_l0 != lt) {
         set_error("coarse tail image missing");
         return QD_ERR_ARG;

@@ -111,8 +111,9 @@ static int cycle_cap(const qd_solver *s, int in_graph) {
 // one: h_smooth); n_cycle / n_smooth: the kernels of a V-cycle iteration
 // and of a smoothing iteration before the check
 static int mixed_check(qd_solver *s, cudaGraphConditionalHandle h, cudaGraphConditionalHandle h_smooth,
-                       int in_graph, int n_cycle, int n_smooth) {
+                       int in_graph, int n_cycle, int n_smooth, const int *gate = nullptr) {
     Decide dc{};
+    dc.gate = gate;
     dc.mode = 2;
     dc.max_cycles = cycle_cap(s, in_graph);
     dc.n_kernels = n_cycle + 1;
@@ -159,7 +160,7 @@ static int capture_cycle(qd_solver *s, cudaGraphConditionalHandle h, int in_grap
 // k_solve_begin.  n_kernels counts the prologue's kernels and `extra`
 // kernels launched before it; phase as for solve_begin_dev.
 static int prologue(qd_solver *s, cudaGraphConditionalHandle h, cudaGraphConditionalHandle h_net, int in_graph,
-                    long long launches0, int extra, int phase) {
+                    long long launches0, int extra, int phase, int n_gated = 0) {
     const int rel = s->opt.tol_mode == QD_TOL_REL;
     if (s->opt.precision == QD_PREC_MIXED) {
         Decide dc{};
@@ -167,6 +168,7 @@ static int prologue(qd_solver *s, cudaGraphConditionalHandle h, cudaGraphConditi
         dc.rel = rel;
         dc.tol = s->opt.tol;
         dc.n_kernels = (int)(s->launches - launches0) + 1 + extra;
+        dc.n_kernels_gated = n_gated;
         dc.in_graph = in_graph;
         dc.phase = phase;
         dc.net_ratio = s->net_ratio;
@@ -186,10 +188,11 @@ static int prologue(qd_solver *s, cudaGraphConditionalHandle h, cudaGraphConditi
 
 // the network's correction of the guess and the prologue again (the body
 // of the graph's IF node, or its eager form)
-static int corrected_prologue(qd_solver *s, cudaGraphConditionalHandle h, int in_graph, long long launches0) {
+static int corrected_prologue(qd_solver *s, cudaGraphConditionalHandle h, int in_graph, long long launches0,
+                              int n_gated = 0) {
     int nk = 0;
     QD_TRY(warm_start_predict(s, &nk));
-    return prologue(s, h, 0, in_graph, launches0, nk, 2);
+    return prologue(s, h, 0, in_graph, launches0, nk, 2, n_gated);
 }
 
 static int end_capture(qd_solver *s, cudaGraph_t *g, int rc) {
@@ -201,33 +204,73 @@ static int end_capture(qd_solver *s, cudaGraph_t *g, int rc) {
     return QD_OK;
 }
 
+// the node of a captured chain in g that nothing depends on
+static int chain_leaf(cudaGraph_t g, cudaGraphNode_t *leaf) {
+    size_t n = 0;
+    QD_CUDA(cudaGraphGetNodes(g, nullptr, &n));
+    std::vector<cudaGraphNode_t> nodes(n);
+    QD_CUDA(cudaGraphGetNodes(g, nodes.data(), &n));
+    *leaf = nullptr;
+    for (auto nd : nodes) {
+        size_t nout = 0;
+        QD_CUDA(cudaGraphNodeGetDependentNodes(nd, nullptr, nullptr, &nout));
+        if (nout == 0) *leaf = nd;
+    }
+    return QD_OK;
+}
+
+// The kernels of one mixed-precision V-cycle (captured into a throwaway
+// graph and counted).
+static int count_cycle_kernels(qd_solver *s, int *n) {
+    const long long l0 = s->launches;
+    cudaGraph_t tmp = nullptr;
+    QD_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeRelaxed));
+    const int rc = vcycle32_into64(s);
+    *n = (int)(s->launches - l0);
+    s->launches = l0;
+    QD_TRY(end_capture(s, &tmp, rc));
+    if (tmp) cudaGraphDestroy(tmp);
+    return QD_OK;
+}
+
+// One solve graph:
+//   prologue -> [IF net: correction, prologue] -> loop
+// In FP64 the loop is a WHILE node whose body is a V-cycle and the check.
+// A conditional node costs about as much as two empty kernel launches each
+// time it is evaluated (measured on GB300: a WHILE node of one iteration
+// around an empty kernel about 10 us, an untaken IF node about 12 us), and
+// with the history guess nearly every mixed-precision solve takes exactly
+// one V-cycle.  So in mixed precision the first V-cycle and its check
+// follow the prologue as plain nodes, their kernels skipping themselves
+// when the prologue found the guess converged (they read SolveState.go),
+// and only the corrections after the first run in the WHILE node -- each a
+// V-cycle, or with the smoothing pass enabled an IF/ELSE node choosing the
+// pass or a V-cycle, then the check.
 static int build(qd_solver *s, SolveGraph *sg) {
     QD_CUDA(cudaGraphCreate(&sg->graph, 0));
-    cudaGraphConditionalHandle h, h_net = 0;
+    cudaGraphConditionalHandle h, h_net = 0, h_smooth = 0;
     QD_CUDA(cudaGraphConditionalHandleCreate(&h, sg->graph, 0, cudaGraphCondAssignDefault));
     sg->net = warm_start_predicting(s);
     sg->net_ratio = s->net_ratio;
     if (sg->net) QD_CUDA(cudaGraphConditionalHandleCreate(&h_net, sg->graph, 0, cudaGraphCondAssignDefault));
+    const bool mixed = s->opt.precision == QD_PREC_MIXED;
+    const bool smooth = mixed && s->smooth_ratio > 1.0;
+    if (smooth) QD_CUDA(cudaGraphConditionalHandleCreate(&h_smooth, sg->graph, 0, cudaGraphCondAssignDefault));
+    int n_cycle = 0;
+    if (mixed) QD_TRY(count_cycle_kernels(s, &n_cycle));
+    const int n_gated = mixed ? n_cycle + 1 : 0;
     // prologue, captured into the top-level graph
     // captured launches are counted on the device each time they run, so the
     // host counter is restored after each capture
     const long long launches0 = s->launches;
     QD_CUDA(cudaStreamBeginCaptureToGraph(s->stream, sg->graph, nullptr, nullptr, 0,
                                           cudaStreamCaptureModeRelaxed));
-    int rc = prologue(s, h, h_net, 1, launches0, 0, sg->net ? 1 : 0);
+    int rc = prologue(s, h, h_net, 1, launches0, 0, sg->net ? 1 : 0, n_gated);
     s->launches = launches0;
     QD_TRY(end_capture(s, nullptr, rc));
     // the prologue is a chain: its one leaf is the next node's dependency
-    size_t n = 0;
-    QD_CUDA(cudaGraphGetNodes(sg->graph, nullptr, &n));
-    std::vector<cudaGraphNode_t> nodes(n);
-    QD_CUDA(cudaGraphGetNodes(sg->graph, nodes.data(), &n));
     cudaGraphNode_t leaf = nullptr;
-    for (auto nd : nodes) {
-        size_t nout = 0;
-        QD_CUDA(cudaGraphNodeGetDependentNodes(nd, nullptr, nullptr, &nout));
-        if (nout == 0) leaf = nd;
-    }
+    QD_TRY(chain_leaf(sg->graph, &leaf));
     if (sg->net) {
         // IF the guess misses the tolerance by more than the gate: the
         // network's correction and the prologue on the corrected guess
@@ -241,10 +284,26 @@ static int build(qd_solver *s, SolveGraph *sg) {
         QD_CUDA(cudaGraphAddNode(&gate, sg->graph, leaf ? &leaf : nullptr, nullptr, leaf ? 1 : 0, &ip));
         QD_CUDA(cudaStreamBeginCaptureToGraph(s->stream, ip.conditional.phGraph_out[0], nullptr, nullptr, 0,
                                               cudaStreamCaptureModeRelaxed));
-        rc = corrected_prologue(s, h, 1, launches0);
+        rc = corrected_prologue(s, h, 1, launches0, n_gated);
         s->launches = launches0;
         QD_TRY(end_capture(s, nullptr, rc));
         leaf = gate;
+    }
+    if (mixed) {
+        // the first V-cycle and its check, skipped by their kernels when
+        // the prologue found the guess converged (SolveState.go = 0, and
+        // the prologue then set the loop's condition to 0)
+        QD_CUDA(cudaStreamBeginCaptureToGraph(s->stream, sg->graph, leaf ? &leaf : nullptr, nullptr, leaf ? 1 : 0,
+                                              cudaStreamCaptureModeRelaxed));
+        s->cycle_gate = &s->d_solve->go;
+        rc = vcycle32_into64(s);
+        if (rc == QD_OK) rc = mixed_check(s, h, h_smooth, 1, n_cycle, 1, &s->d_solve->go);
+        s->cycle_gate = nullptr;
+        s->launches = launches0;
+        QD_TRY(end_capture(s, nullptr, rc));
+        cudaGraphNode_t last = nullptr;
+        QD_TRY(chain_leaf(sg->graph, &last));
+        leaf = last;
     }
     cudaGraphNodeParams cp = {};
     cp.type = cudaGraphNodeTypeConditional;
@@ -254,11 +313,9 @@ static int build(qd_solver *s, SolveGraph *sg) {
     cudaGraphNode_t loop;
     QD_CUDA(cudaGraphAddNode(&loop, sg->graph, leaf ? &leaf : nullptr, nullptr, leaf ? 1 : 0, &cp));
     cudaGraph_t body = cp.conditional.phGraph_out[0];
-    if (s->opt.precision == QD_PREC_MIXED && s->smooth_ratio > 1.0) {
+    if (smooth) {
         // body: IF the check chose the smoothing pass THEN that pass ELSE a
         // V-cycle; then the check (residual, norm, both decisions)
-        cudaGraphConditionalHandle h_smooth;
-        QD_CUDA(cudaGraphConditionalHandleCreate(&h_smooth, sg->graph, 0, cudaGraphCondAssignDefault));
         cudaGraphNodeParams ep = {};
         ep.type = cudaGraphNodeTypeConditional;
         ep.conditional.handle = h_smooth;
@@ -275,7 +332,6 @@ static int build(qd_solver *s, SolveGraph *sg) {
         QD_CUDA(cudaStreamBeginCaptureToGraph(s->stream, ep.conditional.phGraph_out[1], nullptr, nullptr, 0,
                                               cudaStreamCaptureModeRelaxed));
         rc = vcycle32_into64(s);
-        const int n_cycle = (int)(s->launches - launches0);
         s->launches = launches0;
         QD_TRY(end_capture(s, nullptr, rc));
         QD_CUDA(cudaStreamBeginCaptureToGraph(s->stream, body, &branch, nullptr, 1, cudaStreamCaptureModeRelaxed));

@@ -160,7 +160,7 @@ static inline cudaError_t launch_pdl(bool pdl, void (*kern)(KArgs...), dim3 grid
 // (ratio 1 while no cycle has been measured); 2: the decision after that
 // correction (the same solve)
 __device__ inline int solve_begin_dev(const double *scal, SolveState *st, int rel, double tol, int n_kernels,
-                                      int phase, double net_ratio = 1.0) {
+                                      int phase, double net_ratio = 1.0, int n_kernels_gated = 0) {
     const double r0 = rel ? sqrt(scal[1]) : 0.0;
     const double thr = rel ? (r0 > 0.0 ? tol * r0 : tol) : tol;
     const double delta = sqrt(scal[0]);
@@ -181,6 +181,7 @@ __device__ inline int solve_begin_dev(const double *scal, SolveState *st, int re
         go = 0;
     }
     st->go = go;
+    if (!go) st->kernels += (unsigned long long)n_kernels_gated;
     if (go && phase != 2) {
         const double need = (st->rho_samples && st->log_rho < 0.0) ? ceil(log(delta / thr) / -st->log_rho) : 1e30;
         st->need_max = fmax(st->need_max, need);
@@ -255,6 +256,11 @@ struct Decide {
     double smooth_ratio;
     int n_kernels_smooth;
     cudaGraphConditionalHandle h_smooth;
+    // mode 2: non-null, the check is skipped when *gate is 0 (the graph's
+    // first V-cycle, after a prologue that found the guess converged);
+    // mode 1: the kernels so skipped, counted as launched
+    const int *gate;
+    int n_kernels_gated;
 };
 
 // binary64 -> binary32 with round-to-nearest-even, on the integer pipes.
@@ -383,6 +389,8 @@ struct qd_solver {
     int tail_sweeps;       // pre- and post-sweeps on the tail's levels (0: the fine levels' nu_pre, nu_post)
     double smooth_ratio;   // mixed precision: a level-0 smoothing pass instead of a second V-cycle
                            // within this ratio of the threshold (0: off)
+    const int *cycle_gate; // while capturing a solve graph's first V-cycle: the device flag
+                           // (SolveState.go) its kernels check to skip themselves; else null
     int box_up, box_down;  // staged tile box widths of k_up / k_down (0: the default 64)
     void *solve_graph;     // the instantiated multigrid graph (mg_graph.cu)
     qd::SolveState *d_solve, *h_solve;
