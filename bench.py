@@ -422,12 +422,9 @@ def run_ours(args):
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
             if host_io:
-                sim.solver.rk43_set_state(hv["Slip"], hv["psi"], hv["V"], hv["dpsi"], st["t"], st["dt"],
-                                          st["errA"][0], st["errA"][1], st["it"])
-                sim.solver.upload_u(hU)
-                sim.solver.rk43_step(1)
-                st = sim.solver.rk43_state(out=hv)
-                sim.solver.download_u(out=hU)
+                # the state and u in pinned host buffers, uploaded, stepped and
+                # read back by one C-ABI call (qd_rk43_step_host)
+                sim.solver.rk43_step_host(1, st, hU)
             else:
                 sim.step(1)
             e1.record(stream)

@@ -281,6 +281,19 @@ int qd_cal_dpsi(qd_solver *s, const double *psi, const double *V, double *dpsi);
 int qd_rk43_start(qd_solver *s, const qd_rk43_params *p, const double *Slip,
                   const double *psi);
 int qd_rk43_step(qd_solver *s, int nsteps, int *steps_done);
+/* qd_rk43_step on a state that lives on the host, the way the reference's
+ * RK43 holds it: Slip, psi, V (= f1.V_f), dpsi (= f1.dpsi) (nz arrays) and
+ * the ghosted nz x nx field U are uploaded, nsteps steps are taken, and all
+ * five, with Ts (nz, may be NULL), are written back; state4 holds
+ * {t, dt, errA0, errA1} and *it the accepted step count, read and updated.
+ * The same as qd_rk43_set_state, qd_upload_u, qd_rk43_step,
+ * qd_rk43_get_state and qd_download_u in turn, with the transfers queued
+ * behind one another and one host wait instead of five (pinned host
+ * buffers let the copies run asynchronously).  No counterpart in the
+ * reference. */
+int qd_rk43_step_host(qd_solver *s, int nsteps, double *Slip, double *psi, double *V,
+                      double *dpsi, double *Ts, double *U, double *state4, int *it,
+                      int *steps_done);
 /* Restart from the fault state alone (a compact checkpoint: Slip and psi,
  * nz arrays, and the loop's scalars t, dt, errA0, errA1 and the accepted
  * step count it): the state an accepted step leaves behind is Slip, psi,

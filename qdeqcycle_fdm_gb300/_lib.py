@@ -62,6 +62,7 @@ EXPORTS = [
     ("qd_rk43_set_state", C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp, C.c_double, C.c_double,
                                     C.c_double, C.c_double, C.c_int]),
     ("qd_set_solution_history", C.c_int, [C.c_void_p, C.c_int]),
+    ("qd_rk43_step_host", C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _ip, _ip]),
     ("qd_set_newton_start", C.c_int, [C.c_void_p, C.c_int]),
     ("qd_set_tail_sweeps", C.c_int, [C.c_void_p, C.c_int]),
     ("qd_set_smooth_correction", C.c_int, [C.c_void_p, C.c_double]),

@@ -227,6 +227,19 @@ class Solver:
         check(self.L.qd_rk43_set_state(self.h, _p(Slip), _p(psi), _p(V), _p(dpsi), t, dt, errA0,
                                        errA1, it))
 
+    def rk43_step_host(self, n, st, U):
+        """qd_rk43_step_host: n steps on a host-held state.  st: a dict of
+        nz float64 arrays Slip, psi, V, dpsi, Ts and the scalars t, dt,
+        errA, it (as rk43_state returns), updated in place; U: the ghosted
+        nz x nx float64 field, updated in place.  Returns the steps taken."""
+        d4 = np.array([st["t"], st["dt"], st["errA"][0], st["errA"][1]])
+        it = C.c_int(int(st["it"]))
+        done = C.c_int(0)
+        check(self.L.qd_rk43_step_host(self.h, int(n), _p(st["Slip"]), _p(st["psi"]), _p(st["V"]), _p(st["dpsi"]),
+                                       _p(st["Ts"]), _p(U), _p(d4), C.byref(it), C.byref(done)))
+        st.update(t=d4[0], dt=d4[1], errA=(d4[2], d4[3]), it=it.value)
+        return done.value
+
     def set_solution_history(self, m):
         """Start each stage solve from the least-squares combination of the
         last m solutions that best matches the new boundary data (m < 2: off,

@@ -304,6 +304,8 @@ int qd_solver_destroy(qd_solver *s) {
     warm_start_detach(s);            // the network outlives the solver
     history_free(s);
     snapshot_free(s);                // waits for a snapshot still being written
+    cudaFree(s->io_dev);
+    cudaFreeHost(s->io_host);
     mg_free(s);
     fault_free(s);
     solve_graph_free(s);
@@ -355,39 +357,93 @@ int qd_set_medium(int ni, int nk, const double *mu_node, double *mu_equi) {
     return set_medium_gpu(ni, nk, mu_node, mu_equi);
 }
 
+}  // extern "C"
+
+namespace qd {
+
+// Host transfers of u and of the fault state go through staging buffers,
+// one contiguous copy each way: a 2-D copy of the pitched field moves one
+// row per DMA descriptor, and five 8-KB vector copies cost five API calls;
+// a kernel then places the data.  At 1025^2 an upload of u took 72 us as a
+// 2-D copy against 54 us for the same bytes in one copy.
+static int io_staging(qd_solver *s) {
+    if (s->io_dev) return QD_OK;
+    const size_t nd = (size_t)s->nz * s->nx + 5 * (size_t)s->nz;
+    if (cudaMalloc(&s->io_dev, nd * sizeof(double)) != cudaSuccess ||
+        cudaMallocHost(&s->io_host, 5 * (size_t)s->nz * sizeof(double)) != cudaSuccess) {
+        (void)cudaGetLastError();
+        cudaFree(s->io_dev);
+        s->io_dev = nullptr;
+        set_error("transfer staging: out of memory");
+        return QD_ERR_NOMEM;
+    }
+    return QD_OK;
+}
+
+// the interior of the ghosted nz x nx array G (rows 1..nk, columns 1..ni,
+// :669-677) into the pitched level-0 field
+__global__ void k_u_from_ghosted(const double *G, double *u, int N, int K, int P, int nx) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (k < K) u[(long)j * P + k] = G[(long)(j + 1) * nx + k + 1];
+}
+
+// the pitched level-0 field into the ghosted array with extend_crew's ghost
+// values (odeSolver.cpp:612-650): ghost columns 2 U[1] - U[2] and
+// 2 U[ni] - U[ni-1] on every row, then ghost rows 0 and nk+1 copies of rows
+// 2 and nk-1 (ghost columns included).  2a is exact, so the expression rounds
+// as the host's does.
+__global__ void k_u_to_ghosted(const double *u, double *G, int ni, int nk, int P) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y;
+    const int nx = ni + 2;
+    if (c >= nx) return;
+    const int rr = r == 0 ? 2 : (r == nk + 1 ? nk - 1 : r);     // the row the value comes from
+    const double *row = u + (long)(rr - 1) * P - 1;               // row[c]: ghosted column c
+    double v;
+    if (c == 0) v = 2.0 * row[1] - row[2];
+    else if (c == ni + 1) v = 2.0 * row[ni] - row[ni - 1];
+    else v = row[c];
+    G[(long)r * nx + c] = v;
+}
+
+// up to five nz-vectors gathered into (get) or scattered from (put) the
+// packed staging vector
+struct Vec5 {
+    double *p[5];
+};
+__global__ void k_vec5(Vec5 v, double *packed, int nz, int put) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, q = blockIdx.y;
+    if (i >= nz || !v.p[q]) return;
+    if (put) v.p[q][i] = packed[(long)q * nz + i];
+    else packed[(long)q * nz + i] = v.p[q][i];
+}
+
+}  // namespace qd
+
+extern "C" {
+
 int qd_upload_u(qd_solver *s, const double *U) {
     if (!s || !U) return QD_ERR_ARG;
+    QD_TRY(io_staging(s));
     const LevelDims &d = s->dims[0];
-    // interior of the ghosted array: rows 1..nk, columns 1..ni (:669-677)
-    QD_CUDA(cudaMemcpy2DAsync(s->L64[0].u, d.P * sizeof(double), U + s->nx + 1,
-                              s->nx * sizeof(double), d.K * sizeof(double), d.N,
-                              cudaMemcpyHostToDevice, s->stream));
+    QD_CUDA(cudaMemcpyAsync(s->io_dev, U, sizeof(double) * (size_t)s->nz * s->nx, cudaMemcpyHostToDevice,
+                            s->stream));
+    k_u_from_ghosted<<<dim3((d.K + 255) / 256, d.N), 256, 0, s->stream>>>(s->io_dev, s->L64[0].u, d.N, d.K, d.P,
+                                                                          s->nx);
+    QD_LAUNCH_CHECK(s);
     QD_CUDA(cudaStreamSynchronize(s->stream));
     return QD_OK;
 }
 
-// extend_crew (odeSolver.cpp:612-650) on the host array
-static void extend_crew_host(int ni, int nk, double *U) {
-    const int nx = ni + 2, nz = nk + 2;
-    for (int k = 0; k < nz; k++) {
-        double *row = U + (long)k * nx;
-        row[0] = 2.0 * row[1] - row[2];
-        row[ni + 1] = 2.0 * row[ni] - row[ni - 1];
-    }
-    for (int i = 0; i < nx; i++) {
-        U[i] = U[i + 2L * nx];
-        U[i + (long)(nk + 1) * nx] = U[i + (long)(nk - 1) * nx];
-    }
-}
-
 int qd_download_u(qd_solver *s, double *U) {
     if (!s || !U) return QD_ERR_ARG;
+    QD_TRY(io_staging(s));
     const LevelDims &d = s->dims[0];
-    QD_CUDA(cudaMemcpy2DAsync(U + s->nx + 1, s->nx * sizeof(double), s->L64[0].u,
-                              d.P * sizeof(double), d.K * sizeof(double), d.N,
-                              cudaMemcpyDeviceToHost, s->stream));
+    k_u_to_ghosted<<<dim3((s->nx + 255) / 256, s->nz), 256, 0, s->stream>>>(s->L64[0].u, s->io_dev, s->ni, s->nk,
+                                                                             d.P);
+    QD_LAUNCH_CHECK(s);
+    QD_CUDA(cudaMemcpyAsync(U, s->io_dev, sizeof(double) * (size_t)s->nz * s->nx, cudaMemcpyDeviceToHost,
+                            s->stream));
     QD_CUDA(cudaStreamSynchronize(s->stream));
-    extend_crew_host(s->ni, s->nk, U);
     return QD_OK;
 }
 
@@ -655,14 +711,71 @@ int qd_rk43_step(qd_solver *s, int nsteps, int *steps_done) {
     return rc;
 }
 
+int qd_rk43_step_host(qd_solver *s, int nsteps, double *Slip, double *psi, double *V, double *dpsi, double *Ts,
+                      double *U, double *state4, int *it, int *steps_done) {
+    if (!s || nsteps < 0 || !Slip || !psi || !V || !dpsi || !U || !state4 || !it) return QD_ERR_ARG;
+    if (!s->fault_ready) { set_error("qd_rk43_step_host: no fault set up"); return QD_ERR_STATE; }
+    QD_TRY(io_staging(s));
+    QD_CUDA(cudaStreamSynchronize(s->stream));      // the pinned staging is free
+    const LevelDims &d = s->dims[0];
+    const size_t n = s->nz * sizeof(double);
+    double *packed = s->io_dev + (size_t)s->nz * s->nx;
+    // in: the state vectors packed into one copy, u in one copy, both placed by kernels
+    const double *src[4] = {Slip, psi, V, dpsi};
+    for (int q = 0; q < 4; q++) memcpy(s->io_host + (size_t)q * s->nz, src[q], n);
+    QD_CUDA(cudaMemcpyAsync(packed, s->io_host, 4 * n, cudaMemcpyHostToDevice, s->stream));
+    Vec5 vin = {{s->F.Slip, s->F.psi, s->F.fV[1], s->F.fdpsi[1], nullptr}};
+    k_vec5<<<dim3((s->nz + 255) / 256, 5), 256, 0, s->stream>>>(vin, packed, s->nz, 1);
+    QD_LAUNCH_CHECK(s);
+    QD_CUDA(cudaMemcpyAsync(s->io_dev, U, sizeof(double) * (size_t)s->nz * s->nx, cudaMemcpyHostToDevice,
+                            s->stream));
+    k_u_from_ghosted<<<dim3((d.K + 255) / 256, d.N), 256, 0, s->stream>>>(s->io_dev, s->L64[0].u, d.N, d.K, d.P,
+                                                                          s->nx);
+    QD_LAUNCH_CHECK(s);
+    s->t = state4[0]; s->dt = state4[1]; s->errA[0] = state4[2]; s->errA[1] = state4[3]; s->it = *it;
+    s->started = 1;
+    int done = 0;
+    int rc = QD_OK;
+    while (done < nsteps && s->it < s->P.maxNumSteps && s->t < s->P.tmax) {   // :1462
+        rc = rk_step(s);
+        if (rc != QD_OK) break;
+        done++;
+    }
+    if (steps_done) *steps_done = done;
+    if (rc != QD_OK) return rc;
+    // out: the state vectors gathered into one copy, u with its ghost values in one copy
+    Vec5 vout = {{s->F.Slip, s->F.psi, s->F.fV[1], s->F.fdpsi[1], Ts ? s->F.Ts : nullptr}};
+    k_vec5<<<dim3((s->nz + 255) / 256, 5), 256, 0, s->stream>>>(vout, packed, s->nz, 0);
+    QD_LAUNCH_CHECK(s);
+    QD_CUDA(cudaMemcpyAsync(s->io_host, packed, (Ts ? 5 : 4) * n, cudaMemcpyDeviceToHost, s->stream));
+    k_u_to_ghosted<<<dim3((s->nx + 255) / 256, s->nz), 256, 0, s->stream>>>(s->L64[0].u, s->io_dev, s->ni, s->nk,
+                                                                             d.P);
+    QD_LAUNCH_CHECK(s);
+    QD_CUDA(cudaMemcpyAsync(U, s->io_dev, sizeof(double) * (size_t)s->nz * s->nx, cudaMemcpyDeviceToHost,
+                            s->stream));
+    QD_CUDA(cudaStreamSynchronize(s->stream));
+    double *dst[5] = {Slip, psi, V, dpsi, Ts};
+    for (int q = 0; q < 5; q++)
+        if (dst[q]) memcpy(dst[q], s->io_host + (size_t)q * s->nz, n);
+    state4[0] = s->t; state4[1] = s->dt; state4[2] = s->errA[0]; state4[3] = s->errA[1];
+    *it = s->it;
+    return QD_OK;
+}
+
 int qd_rk43_get_state(qd_solver *s, double *Slip, double *psi, double *V, double *Ts, double *dpsi) {
     if (!s) return QD_ERR_ARG;
-    const size_t n = s->nz * sizeof(double);
-    const double *src[5] = {s->F.Slip, s->F.psi, s->F.fV[1], s->F.Ts, s->F.fdpsi[1]};
+    QD_TRY(io_staging(s));
     double *dst[5] = {Slip, psi, V, Ts, dpsi};
-    for (int i = 0; i < 5; i++)
-        if (dst[i]) QD_CUDA(cudaMemcpyAsync(dst[i], src[i], n, cudaMemcpyDeviceToHost, s->stream));
+    Vec5 v;
+    const double *src[5] = {s->F.Slip, s->F.psi, s->F.fV[1], s->F.Ts, s->F.fdpsi[1]};
+    for (int q = 0; q < 5; q++) v.p[q] = dst[q] ? const_cast<double *>(src[q]) : nullptr;
+    double *packed = s->io_dev + (size_t)s->nz * s->nx;
+    k_vec5<<<dim3((s->nz + 255) / 256, 5), 256, 0, s->stream>>>(v, packed, s->nz, 0);
+    QD_LAUNCH_CHECK(s);
+    QD_CUDA(cudaMemcpyAsync(s->io_host, packed, 5 * s->nz * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
     QD_CUDA(cudaStreamSynchronize(s->stream));
+    for (int q = 0; q < 5; q++)
+        if (dst[q]) memcpy(dst[q], s->io_host + (size_t)q * s->nz, s->nz * sizeof(double));
     return QD_OK;
 }
 
@@ -676,11 +789,17 @@ int qd_rk43_get_scalars(qd_solver *s, double *d4, int *it) {
 int qd_rk43_set_state(qd_solver *s, const double *Slip, const double *psi, const double *V,
                       const double *dpsi, double t, double dt, double errA0, double errA1, int it) {
     if (!s || !Slip || !psi || !V || !dpsi) return QD_ERR_ARG;
+    QD_TRY(io_staging(s));
+    // the pinned staging may still feed an earlier transfer on the stream
+    QD_CUDA(cudaStreamSynchronize(s->stream));
     const size_t n = s->nz * sizeof(double);
-    QD_CUDA(cudaMemcpyAsync(s->F.Slip, Slip, n, cudaMemcpyHostToDevice, s->stream));
-    QD_CUDA(cudaMemcpyAsync(s->F.psi, psi, n, cudaMemcpyHostToDevice, s->stream));
-    QD_CUDA(cudaMemcpyAsync(s->F.fV[1], V, n, cudaMemcpyHostToDevice, s->stream));
-    QD_CUDA(cudaMemcpyAsync(s->F.fdpsi[1], dpsi, n, cudaMemcpyHostToDevice, s->stream));
+    const double *src[4] = {Slip, psi, V, dpsi};
+    for (int q = 0; q < 4; q++) memcpy(s->io_host + (size_t)q * s->nz, src[q], n);
+    double *packed = s->io_dev + (size_t)s->nz * s->nx;
+    QD_CUDA(cudaMemcpyAsync(packed, s->io_host, 4 * n, cudaMemcpyHostToDevice, s->stream));
+    Vec5 v = {{s->F.Slip, s->F.psi, s->F.fV[1], s->F.fdpsi[1], nullptr}};
+    k_vec5<<<dim3((s->nz + 255) / 256, 5), 256, 0, s->stream>>>(v, packed, s->nz, 1);
+    QD_LAUNCH_CHECK(s);
     QD_CUDA(cudaStreamSynchronize(s->stream));
     s->t = t; s->dt = dt; s->errA[0] = errA0; s->errA[1] = errA1; s->it = it;
     s->started = 1;

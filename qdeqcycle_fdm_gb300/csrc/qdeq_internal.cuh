@@ -385,6 +385,9 @@ struct qd_solver {
     int newton_start;      // the Newton solve's start: 0 the reference's x = 0, 1 a binary32 solve
     void *history;         // ring of earlier solutions for the initial guess (history.cu), or null
     void *snapshot;        // the snapshot writer in flight (io.cu), or null
+    // staging of the host transfers (allocated on first use): the ghosted
+    // nz x nx field and five nz-vectors on the device, five nz-vectors pinned
+    double *io_dev, *io_host;
     int tail_l0;           // first level of the coarse tail
     int tail_sweeps;       // pre- and post-sweeps on the tail's levels (0: the fine levels' nu_pre, nu_post)
     double smooth_ratio;   // mixed precision: a level-0 smoothing pass instead of a second V-cycle

@@ -432,6 +432,39 @@ def test_rk43_adaptive_steps_match_oracle():
     assert rel(g["Slip"][k], c["Slip"][k]) < 1e-8
 
 
+def test_host_buffer_step_equals_the_device_step():
+    """qd_rk43_step_host (the state and the ghosted u on the host, uploaded,
+    stepped, read back in one call) gives the same bits as qd_rk43_step on
+    the device-resident state followed by the state and u read-backs, and
+    its u carries extend_crew's ghost values."""
+    cfg, prob = make_problem(65)
+    outs = []
+    for host in (False, True):
+        sim = api.Simulation(prob, cfg.mg)
+        sim.solver.set_solution_history(3)
+        sim.start()
+        sim.step(3)
+        st = sim.solver.rk43_state()
+        U = sim.solver.download_u()
+        if host:
+            for _ in range(4):
+                assert sim.solver.rk43_step_host(1, st, U) == 1
+        else:
+            sim.step(4)
+            st = sim.solver.rk43_state()
+            U = sim.solver.download_u()
+        outs.append((st, U))
+        sim.close()
+    (a, Ua), (b, Ub) = outs
+    for key in ("Slip", "psi", "V", "dpsi", "Ts"):
+        assert np.array_equal(a[key], b[key]), key
+    assert a["t"] == b["t"] and a["dt"] == b["dt"] and a["it"] == b["it"]
+    assert np.array_equal(Ua, Ub)
+    Ue = Ub.copy()
+    oracle.extend_crew(prob.ni, prob.nk, Ue)
+    assert np.array_equal(Ue, Ub)
+
+
 def test_gpu_runs_are_bitwise_reproducible():
     cfg, prob = make_problem(33)
     outs = []
