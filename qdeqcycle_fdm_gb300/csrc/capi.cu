@@ -149,9 +149,14 @@ static const double *rk_c() {
     return t.c;
 }
 
+// The solve's failure flags are not cleared between steps: every flag is a
+// failure the step reports, after which the run restarts (qd_rk43_start and
+// qd_rk43_resume clear them), so a flag the commit's refresh solve raised
+// stays set until the next attempt's check or the call's last check reads
+// it.
 static int step_begin(qd_solver *s) {
     s->it = s->it + 1;
-    return solve_state_clear_flag(s);
+    return QD_OK;
 }
 
 // stages 2..6 and the error estimate of one attempt, and the copies of the
@@ -195,16 +200,19 @@ static int commit_enqueue(qd_solver *s) {
     return stage(s, 1, 0.0);                                      // :1615-1619
 }
 
-static int commit_finish(qd_solver *s, double totErr) {
+// the host's side of a commit; check: wait for the refresh and read the
+// failure flags now (otherwise the next attempt's check, or the last check
+// of the call, reads them: one host wait fewer per step)
+static int commit_finish(qd_solver *s, double totErr, bool check) {
     const double newDeltaT = (totErr != 0.0) ? step_size(s->it, s->dt, s->P, totErr, s->errA) : s->dt;
     s->errA[1] = s->errA[0];
     s->errA[0] = totErr;
     s->dt = newDeltaT;
     s->steps++;
-    return check_status(s);
+    return check ? check_status(s) : QD_OK;
 }
 
-static int rk_step(qd_solver *s) {
+static int rk_step(qd_solver *s, bool check) {
     QD_TRY(step_begin(s));
     double totErr = 0.0;
     int retry = 1;
@@ -213,7 +221,7 @@ static int rk_step(qd_solver *s) {
         QD_TRY(attempt_finish(s, attemptCount, &totErr, &retry));
     }
     QD_TRY(commit_enqueue(s));
-    return commit_finish(s, totErr);
+    return commit_finish(s, totErr, check);
 }
 
 static bool can_step(const qd_solver *s) { return s->it < s->P.maxNumSteps && s->t < s->P.tmax; }
@@ -690,10 +698,11 @@ int qd_ensemble_step(qd_solver **ss, int n, int nsteps, int *steps_done) {
             if (act[i]) QD_TRY(commit_enqueue(ss[i]));
         for (int i = 0; i < n; i++)
             if (act[i]) {
-                QD_TRY(commit_finish(ss[i], err[i]));
+                QD_TRY(commit_finish(ss[i], err[i], false));
                 if (steps_done) steps_done[i]++;
             }
     }
+    for (int i = 0; i < n; i++) QD_TRY(check_status(ss[i]));   // the last refresh solves' flags
     return QD_OK;
 }
 
@@ -703,10 +712,11 @@ int qd_rk43_step(qd_solver *s, int nsteps, int *steps_done) {
     int done = 0;
     int rc = QD_OK;
     while (done < nsteps && s->it < s->P.maxNumSteps && s->t < s->P.tmax) {   // :1462
-        rc = rk_step(s);
+        rc = rk_step(s, false);
         if (rc != QD_OK) break;
         done++;
     }
+    if (rc == QD_OK && done > 0) rc = check_status(s);   // the last refresh solve's flags
     if (steps_done) *steps_done = done;
     return rc;
 }
@@ -737,12 +747,15 @@ int qd_rk43_step_host(qd_solver *s, int nsteps, double *Slip, double *psi, doubl
     int done = 0;
     int rc = QD_OK;
     while (done < nsteps && s->it < s->P.maxNumSteps && s->t < s->P.tmax) {   // :1462
-        rc = rk_step(s);
+        rc = rk_step(s, false);
         if (rc != QD_OK) break;
         done++;
     }
     if (steps_done) *steps_done = done;
     if (rc != QD_OK) return rc;
+    // the last refresh solve's flags, read with the results
+    QD_CUDA(cudaMemcpyAsync(s->h_status, s->d_status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s->stream));
+    QD_CUDA(cudaMemcpyAsync(s->h_solve, s->d_solve, sizeof(SolveState), cudaMemcpyDeviceToHost, s->stream));
     // out: the state vectors gathered into one copy, u with its ghost values in one copy
     Vec5 vout = {{s->F.Slip, s->F.psi, s->F.fV[1], s->F.fdpsi[1], Ts ? s->F.Ts : nullptr}};
     k_vec5<<<dim3((s->nz + 255) / 256, 5), 256, 0, s->stream>>>(vout, packed, s->nz, 0);
@@ -759,6 +772,10 @@ int qd_rk43_step_host(qd_solver *s, int nsteps, double *Slip, double *psi, doubl
         if (dst[q]) memcpy(dst[q], s->io_host + (size_t)q * s->nz, n);
     state4[0] = s->t; state4[1] = s->dt; state4[2] = s->errA[0]; state4[3] = s->errA[1];
     *it = s->it;
+    if (done > 0) {
+        QD_TRY(status_flag_error(*s->h_status));
+        QD_TRY(solve_flag_error(*s->h_solve));
+    }
     return QD_OK;
 }
 

@@ -1,6 +1,9 @@
 """The headline solver -- the learned correction on the solution-history
-guess, FP32 V-cycles inside FP64 iterative refinement -- against the CPU
-oracle's FP64 RK43 loop on identical fixed steps, through a rupture.
+guess, FP32 V-cycles inside FP64 iterative refinement with the
+double-float residual, the binary32 Newton start, V(1,1) on the coarse
+tail and the level-0 smoothing pass -- against the CPU oracle's FP64 RK43
+loop (the reference's Newton start and schedule) on identical fixed steps,
+through a rupture.
 
 A 257 x 257 problem with config 1's physics (layered medium, +-5 % a-b
 perturbation) runs on the GPU from steady sliding into its first rupture
@@ -44,6 +47,11 @@ def test_learned_mixed_steps_through_a_rupture_match_fp64_oracle(gpu_lib, oracle
     # into the first rupture, training the network on the way
     sim = api.Simulation(prob, mg)
     sim.solver.set_solution_history(4)
+    # the bench's headline settings: binary32 Newton start, V(1,1) on the
+    # coarse tail's levels, the level-0 smoothing pass
+    sim.solver.set_newton_start(1)
+    sim.solver.set_tail_sweeps(1)
+    sim.solver.set_smooth_correction(2.5)
     net = warmstart.UNet((n - 1) // 2 + 1, (n - 1) // 2 + 1, seed=3)
     net.attach(sim.solver, warmstart.MODE_TRAIN, 1e-3)
     sim.start()

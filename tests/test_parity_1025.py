@@ -120,17 +120,22 @@ def test_headline_solve_1025_against_fp64_oracle(prob):
     mg = config.MGConfig(n_levels=8, nu_pre=2, nu_post=2, nu_coarse=32, tol_mode=1, tol=1e-9, max_cycles=200,
                          precision=1, surface_prolong=1, coarse_solve=1)
     U = random_U(p, 23)
-    s = api.Solver(p.ni, p.nk, p.dh, p.mu_equi, p.mu_node, mg)
-    s.upload_u(U)
-    cyc, rn, r0 = s.ode_solve()
-    assert rn <= 1e-9 * r0
-    got = compact(s.download_u())
     m = oracle.Multigrid(p.ni, p.nk, p.dh, p.mu_equi, 8, 2, 2, 32, surface_prolong=1, coarse_solve=1)
     u = compact(U).copy()
     ocyc, orn, or0 = m.solve(u, tol_mode=1, tol=1e-13, max_cycles=200)
-    assert rel(r0, or0) < 1e-12
-    assert rel(got, u) < 1e-8
-    s.close()
+    # the plain mixed solver, and with the bench's V(1,1) on the coarse
+    # tail and the level-0 smoothing pass
+    for tail, ratio in ((0, 0.0), (1, 2.5)):
+        s = api.Solver(p.ni, p.nk, p.dh, p.mu_equi, p.mu_node, mg)
+        s.set_tail_sweeps(tail)
+        s.set_smooth_correction(ratio)
+        s.upload_u(U)
+        cyc, rn, r0 = s.ode_solve()
+        assert rn <= 1e-9 * r0
+        got = compact(s.download_u())
+        assert rel(r0, or0) < 1e-12
+        assert rel(got, u) < 1e-8
+        s.close()
 
 
 def _errors(g, c, p):
@@ -174,6 +179,11 @@ def test_headline_rk_steps_1025_from_rupture_checkpoint(prob):
                           precision=1, surface_prolong=1, coarse_solve=1)
     gpu = api.Simulation(p, gmg)
     gpu.solver.set_solution_history(4)
+    # the bench's headline settings: binary32 Newton start, V(1,1) on the
+    # coarse tail's levels, the level-0 smoothing pass
+    gpu.solver.set_newton_start(1)
+    gpu.solver.set_tail_sweeps(1)
+    gpu.solver.set_smooth_correction(2.5)
     gpu.resume(ck, params=params)
     gpu.step(nsteps)
     g = gpu.state()
