@@ -1153,6 +1153,11 @@ int warm_start_predict(qd_solver *s, int *kernels) {
 int warm_start_after_solve(qd_solver *s) {
     qd_unet *u = static_cast<qd_unet *>(s->unet);
     if (!u || !u->mode) return QD_OK;
+    // on standby no solve of the attempt runs the network, so its next
+    // input is not formed; the first solve after the standby reads the last
+    // change formed before it (a stale input only weakens that prediction,
+    // whose correction is still scaled by the energy-optimal step)
+    if (u->mode == 2 && s->net_standby) return QD_OK;
     const LevelDims &d = s->dims[0];
     const UGrid &g = u->g[0];
     QD_CUDA(launch_pdl(true, k_target, dim3(cdv(g.P, 256)), dim3(256), 0, s->stream, (const double *)s->L64[0].u,
