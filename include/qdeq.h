@@ -233,8 +233,7 @@ int qd_split_f64(const double *in, float *hi, float *lo, int n);
  * doubles (517 KB) that every GPU using this library keeps until the
  * process exits; grids of more than 4097 rows or 4097 columns are rejected with
  * QD_ERR_ARG.  The first call on each device looks up that array's device
- * address, so make it before any stream capture.  All calls share the
- * array: calls that overlap on the GPU (two streams, two host threads)
+ * address and keeps it.  All calls share the array: calls that overlap on the GPU (two streams, two host threads)
  * race and must be serialised by the caller.  This entry point has no
  * counterpart in the reference. */
 int qd_residual_norm_noalloc(const double *u, const double *cx, const double *cz, int nk, int ni,
