@@ -791,7 +791,7 @@ def run_ours(args):
         if tn:
             guess += f", autotuned tiles ({tn['box_down']}/{tn['box_up']}-column boxes)"
         else:
-            guess += ", default 64-column tiles"
+            guess += ", default tiles (96-column k_down and 64-column k_up boxes at level 0)"
         mode = (f"learned warm start on the {guess} + FP32 cycles in FP64 refinement" if learned
                 else f"{guess} + FP32 cycles in FP64 refinement")
         line = {

@@ -109,13 +109,16 @@ int autotune(qd_solver *s, int reps, qd_tuning *out) {
     cands.push_back(initial);
     const int sched[][2] = {{1, 1}, {2, 2}, {3, 3}, {4, 4}, {1, 2}, {2, 1}, {2, 3}, {3, 2}};
     const int boxes[] = {64, 96, 128};
+    int def_up = 0, def_down = 0;
+    tiles_default_level0(s, &def_up, &def_down);
+    const int eff_up = initial.box_up ? initial.box_up : def_up;
+    const int eff_down = initial.box_down ? initial.box_down : def_down;
     for (const auto &sc : sched)
         for (int bu : boxes)
             for (int bd : boxes) {
                 const Candidate c{sc[0], sc[1], bu, bd};
                 const bool same = c.nu_pre == initial.nu_pre && c.nu_post == initial.nu_post &&
-                                  (c.box_up == initial.box_up || (initial.box_up == 0 && bu == 64)) &&
-                                  (c.box_down == initial.box_down || (initial.box_down == 0 && bd == 64));
+                                  bu == eff_up && bd == eff_down;
                 if (!same) cands.push_back(c);
             }
 

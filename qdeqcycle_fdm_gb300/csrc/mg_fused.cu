@@ -422,8 +422,14 @@ static constexpr int kBoxW = 64;       // default k_up boxes: one pass of 32 lan
 static constexpr int kDownBoxW = 64;   // default k_down boxes (qd_autotune may pick others)
 // k_down's default box width: 64 columns, 128 on levels of 2049 columns or
 // more, where the halo's share matters more than a wave's fill (measured at
-// 4097^2: 203 us per launch with 128-column boxes, 207 with 64, 213 with 96)
-static int down_box_default(int K) { return K >= 2049 ? 128 : kDownBoxW; }
+// 4097^2: 203 us per launch with 128-column boxes, 207 with 64, 213 with 96),
+// and 96 on FP32 levels of 1025 to 2048 columns (at 1025^2 in the rupture
+// window: 16.7 us per launch against 19.1 with 64 and 20.2 with 80)
+template <typename T>
+static int down_box_default(int K) {
+    if (K >= 2049) return 128;
+    return (sizeof(T) == 4 && K >= 1025) ? 96 : kDownBoxW;
+}
 static constexpr int kWaveCtas = 150;
 
 static size_t two_cta_smem() { return std::min<size_t>(smem_limit(), 112 * 1024); }
@@ -526,7 +532,7 @@ static int launch_down(qd_solver *s, Level<T> *Ls, int l, int S, int zero_u, boo
     const LvArgs<T> g = lv(s, Ls, l), c = lv(s, Ls, l + 1);
     // the residual goes into f, or into the dinv slot on the FP64 level 0
     const bool has_f = g.f != nullptr;
-    const TileGeom t = pick_down<T>(c.N, c.K, g.N, g.K, S, has_f, s->box_down ? s->box_down : down_box_default(g.K));
+    const TileGeom t = pick_down<T>(c.N, c.K, g.N, g.K, S, has_f, s->box_down ? s->box_down : down_box_default<T>(g.K));
     const int BH = t.BH, W = t.W, CH = t.TH, CW = t.TW, ntj = t.ntj, ntk = t.ntk;
     const size_t smem = t.smem;
     if (BH > 256 || W > 256 || smem > smem_limit()) {
@@ -635,6 +641,14 @@ int tiles_set(qd_solver *s, int box_up, int box_down) {
     s->box_down = box_down;
     solve_graph_free(s);
     return QD_OK;
+}
+
+// the box widths the level-0 tile kernels use when none is set (the level-0
+// V-cycle runs in FP32 in mixed precision)
+void tiles_default_level0(const qd_solver *s, int *box_up, int *box_down) {
+    const int K = s->dims[0].K;
+    *box_up = kBoxW;
+    *box_down = s->opt.precision == QD_PREC_MIXED ? down_box_default<float>(K) : down_box_default<double>(K);
 }
 
 int encode_tiled_3d(CUtensorMap *map, const void *base, int dtype, int esz, long d0, long d1, long d2,

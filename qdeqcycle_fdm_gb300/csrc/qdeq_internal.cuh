@@ -430,6 +430,7 @@ int smooth32_into64(qd_solver *s);
 void tma_cache_free(qd_solver *s);
 int tail_image_build(qd_solver *s);
 int tiles_set(qd_solver *s, int box_up, int box_down);
+void tiles_default_level0(const qd_solver *s, int *box_up, int *box_down);
 int time_kernel(qd_solver *s, int which, int reps, double *us);
 // a bounded mbarrier wait that nothing completes (gives up after `polls`)
 int wait_probe(qd_solver *s, unsigned polls);
