@@ -444,6 +444,7 @@ def run_ours(args):
                      "smooths": s1["smooth_corrections"] - s0["smooth_corrections"],
                      "newton": (s1["newton_iters"] - s0["newton_iters"]) / max(1, (s1["solves"] - s0["solves"]) * prob.nk),
                      "net_solves": s1["net_solves"] - s0["net_solves"],
+                     "net_armed": s1["net_armed_solves"] - s0["net_armed_solves"],
                      "net_needed": s1["net_cycles_needed"] - s0["net_cycles_needed"],
                      "net_taken": s1["net_cycles_taken"] - s0["net_cycles_taken"],
                      "attempts": s1["attempts"] - s0["attempts"], "autotune": tuning}
@@ -668,6 +669,8 @@ def run_ours(args):
                 / max(1, s1["solves"] - s0["solves"]),
                 "solves_per_step": (s1["solves"] - s0["solves"]) / nst,
                 "network_corrected_solves": (s1["net_solves"] - s0["net_solves"]) / max(1, s1["solves"] - s0["solves"]),
+                "network_armed_solves": (s1["net_armed_solves"] - s0["net_armed_solves"])
+                / max(1, s1["solves"] - s0["solves"]),
                 "network_cycles_needed_taken": [s1["net_cycles_needed"] - s0["net_cycles_needed"],
                                                 s1["net_cycles_taken"] - s0["net_cycles_taken"]],
                 "ruptures_seen": ruptures}
@@ -814,6 +817,7 @@ def run_ours(args):
             "solves_per_step": head["solves"] / args.steps,
             "newton_iters_per_node_solve": head["newton"],
             "network_corrected_solves": head["net_solves"] / max(1, head["solves"]) if learned else None,
+            "network_armed_solves": head["net_armed"] / max(1, head["solves"]) if learned else None,
             "network_gate": (f"measured: corrects guesses that would need more than {1 + args.net_cost:g} V-cycles"
                              if args.net_gate == 0.0 else f"fixed: ||r|| > {args.net_gate:g} x threshold")
             if learned else None,

@@ -112,6 +112,9 @@ typedef struct qd_stats {
     double net_cycles_taken;  /* ... and the V-cycles they took            */
     long long smooth_corrections; /* level-0 smoothing passes that replaced
                                 a V-cycle (qd_set_smooth_correction)       */
+    long long net_armed_solves; /* solves that carried the attached
+                                network's conditional correction (not on
+                                standby), whether or not it ran            */
 } qd_stats;
 
 const char *qd_version(void);

@@ -109,7 +109,7 @@ class Stats(C.Structure):
                 ("steps", C.c_longlong), ("newton_iters", C.c_longlong),
                 ("kernel_launches", C.c_longlong), ("net_solves", C.c_longlong),
                 ("net_cycles_needed", C.c_double), ("net_cycles_taken", C.c_double),
-                ("smooth_corrections", C.c_longlong)]
+                ("smooth_corrections", C.c_longlong), ("net_armed_solves", C.c_longlong)]
 
 
 class Tuning(C.Structure):

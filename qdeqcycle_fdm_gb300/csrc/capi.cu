@@ -351,6 +351,7 @@ int qd_get_stats(qd_solver *s, qd_stats *st) {
     st->net_cycles_needed = ss.net_cycles_needed;
     st->net_cycles_taken = ss.net_cycles_taken;
     st->smooth_corrections = (long long)ss.total_smooths;
+    st->net_armed_solves = s->net_armed_solves;
     std::vector<int> it(s->nz);
     QD_CUDA(cudaMemcpy(it.data(), s->F.iters, s->nz * sizeof(int), cudaMemcpyDeviceToHost));
     long long sum = 0;

@@ -401,6 +401,7 @@ static int solve_eager(qd_solver *s) {
 
 // Enqueue one solve on the solver's stream (no host synchronisation).
 int mg_solve_async(qd_solver *s) {
+    if (warm_start_predicting(s)) s->net_armed_solves++;
     if (eager_solve()) return solve_eager(s);
     SolveGraphs *gs = static_cast<SolveGraphs *>(s->solve_graph);
     if (!gs) {

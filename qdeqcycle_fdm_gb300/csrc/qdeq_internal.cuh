@@ -411,6 +411,7 @@ struct qd_solver {
     int started;
     // counters
     long long solves, vcycles, attempts, steps, newton_iters, launches;
+    long long net_armed_solves;   // solves enqueued with the network's conditional correction
 };
 
 namespace qd {

@@ -1178,10 +1178,12 @@ int warm_start_after_solve(qd_solver *s) {
 
 // where the solution-history guess leaves the boundary data its combination
 // implies, so that the network's boundary-change inputs describe what the
-// guess still misses (null when no network is in use)
+// guess still misses (null when no network is in use, and on standby, when
+// no solve of the attempt can run the network)
 double *warm_start_bc_buffer(qd_solver *s) {
     qd_unet *u = static_cast<qd_unet *>(s->unet);
-    return (u && u->mode) ? u->d_bc_old : nullptr;
+    if (!u || !u->mode || (u->mode == 2 && s->net_standby)) return nullptr;
+    return u->d_bc_old;
 }
 
 void warm_start_detach(qd_solver *s) {

@@ -142,6 +142,9 @@ def test_warm_start_coupled_to_the_solver():
     # from the previous solution nearly every stage solve misses the
     # tolerance, so the network corrects nearly every guess
     assert w1["net_solves"] - w0["net_solves"] >= 0.5 * (w1["solves"] - w0["solves"])
+    # a corrected solve carried the network's node (was not on standby)
+    assert w1["net_armed_solves"] - w0["net_armed_solves"] >= w1["net_solves"] - w0["net_solves"]
+    assert p1["net_armed_solves"] == 0
 
 
 def test_prediction_runs_only_where_the_guess_misses():
