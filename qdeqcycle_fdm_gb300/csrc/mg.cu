@@ -298,13 +298,35 @@ __global__ void __launch_bounds__(BX * BY, RES_DF_CTAS_PER_SM)
     __shared__ double wsum[BX * BY / 32];
     __shared__ bool last;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const unsigned nblk = gridDim.x;   // a one-dimensional grid
+    // mode 1 with the relative tolerance: ||r0||^2 of the zero-interior
+    // guess (as k_r0: only the columns next to the Dirichlet data see a
+    // residual), its rows dealt round-robin to the blocks, each block's
+    // first warp summing its few rows into partial[nblk + block]
+    const bool r0_rows = dc.mode == 1 && dc.rel;
+    double r0b = 0.0;
+    if (r0_rows && tid < 32) {
+        for (int j = tid * (int)nblk + (int)blockIdx.x; j < v.N; j += 32 * (int)nblk) {
+            const long row = (long)j * v.P;
+            if (v.K - 2 == 1) {
+                const double r = -(v.cx[row] * v.u[row] + v.cx[row + 1] * v.u[row + 2]) * v.inv_h2;
+                r0b += r * r;
+            } else if (v.K - 2 > 1) {
+                const double r1 = -v.cx[row] * v.u[row] * v.inv_h2;
+                const double r2 = -v.cx[row + v.K - 2] * v.u[row + v.K - 1] * v.inv_h2;
+                r0b += r1 * r1 + r2 * r2;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) r0b += __shfl_down_sync(0xffffffffu, r0b, o);
+    }
     if ((tid & 31) == 0) wsum[tid >> 5] = (double)sq;
     __syncthreads();
-    const unsigned nblk = gridDim.x * gridDim.y;
     if (tid == 0) {
         double b = 0.0;
         for (int w = 0; w < BX * BY / 32; w++) b += wsum[w];
-        partial[blockIdx.y * gridDim.x + blockIdx.x] = b;
+        partial[blockIdx.x] = b;
+        if (r0_rows) partial[nblk + blockIdx.x] = r0b;
         __threadfence();
         last = atomicAdd(count, 1u) == nblk - 1;
     }
@@ -319,20 +341,11 @@ __global__ void __launch_bounds__(BX * BY, RES_DF_CTAS_PER_SM)
         *count = 0;
     }
     if (dc.mode == 1) {
-        // ||r0||^2 of the zero-interior guess (as k_r0), then the first decision
+        // the blocks' ||r0||^2 parts, summed in a fixed order, then the
+        // first decision
         double r0 = 0.0;
         if (dc.rel) {
-            for (int j = tid; j < v.N; j += blockDim.x * blockDim.y) {
-                const long row = (long)j * v.P;
-                if (v.K - 2 == 1) {
-                    const double r = -(v.cx[row] * v.u[row] + v.cx[row + 1] * v.u[row + 2]) * v.inv_h2;
-                    r0 += r * r;
-                } else if (v.K - 2 > 1) {
-                    const double r1 = -v.cx[row] * v.u[row] * v.inv_h2;
-                    const double r2 = -v.cx[row + v.K - 2] * v.u[row + v.K - 1] * v.inv_h2;
-                    r0 += r1 * r1 + r2 * r2;
-                }
-            }
+            for (unsigned i = tid; i < nblk; i += blockDim.x * blockDim.y) r0 += __ldcg(partial + nblk + i);
             r0 = block_sum(r0);
         }
         if (tid == 0) {
@@ -729,6 +742,10 @@ static int residual_df(qd_solver *s, const Decide &dc, int slot, bool pdl) {
     View<double> v = make_view(s, s->L64, 0);
     const int tiles = cdiv(v.K - 2, RES_DF_COLS) * cdiv(v.N, BY * RES_DF_RPT);
     dim3 blk(BX, BY), grd(std::min(tiles, RES_DF_CTAS_PER_SM * s->n_sm));
+    if (2 * (long)grd.x > s->n_partial) {   // the squares' and ||r0||'s block sums
+        set_error("level-0 residual: %u blocks exceed the partial buffer", grd.x);
+        return QD_ERR_ARG;
+    }
     QD_CUDA(launch_pdl(pdl, k_residual_df, grd, blk, 0, s->stream, v, (const float2 *)s->res_cx,
                        (const float2 *)s->res_cz, (const float2 *)s->res_dg, s->L32[0].f, s->d_partial, s->d_count,
                        s->d_scal + slot, dc));

@@ -159,6 +159,12 @@ static inline cudaError_t launch_pdl(bool pdl, void (*kern)(KArgs...), dim3 grid
 // reduction per cycle -- the guess would need more than 1 + c cycles
 // (ratio 1 while no cycle has been measured); 2: the decision after that
 // correction (the same solve)
+// V-cycles that take ||r|| = delta below thr at the mean reduction
+// exp(log_rho) < 1 per cycle (an estimate, in binary32)
+__device__ inline double cycles_needed(double delta, double thr, double log_rho) {
+    return (double)ceilf(logf((float)delta / (float)thr) / -(float)log_rho);
+}
+
 __device__ inline int solve_begin_dev(const double *scal, SolveState *st, int rel, double tol, int n_kernels,
                                       int phase, double net_ratio = 1.0, int n_kernels_gated = 0) {
     const double r0 = rel ? sqrt(scal[1]) : 0.0;
@@ -182,17 +188,21 @@ __device__ inline int solve_begin_dev(const double *scal, SolveState *st, int re
     }
     st->go = go;
     if (!go) st->kernels += (unsigned long long)n_kernels_gated;
+    // the estimates below (cycles a guess needs, the network's gate) take
+    // their logarithms and exponentials in binary32: one thread's chain of
+    // FP64 transcendentals is microseconds on GB300's FP64 pipe
     if (go && phase != 2) {
-        const double need = (st->rho_samples && st->log_rho < 0.0) ? ceil(log(delta / thr) / -st->log_rho) : 1e30;
+        const double need = (st->rho_samples && st->log_rho < 0.0) ? cycles_needed(delta, thr, st->log_rho) : 1e30;
         st->need_max = fmax(st->need_max, need);
     }
     if (phase == 0) st->net = 0;
     else if (phase == 1) {
         const double ratio =
-            net_ratio > 0.0 ? net_ratio : (st->rho_samples ? exp(-(1.0 - net_ratio) * st->log_rho) : 1.0);
+            net_ratio > 0.0 ? net_ratio
+                            : (st->rho_samples ? (double)expf(-(float)((1.0 - net_ratio) * st->log_rho)) : 1.0);
         st->net = go && !(delta <= ratio * thr);
         if (st->net && st->rho_samples && st->log_rho < 0.0)
-            st->net_cycles_needed += ceil(log(delta / thr) / -st->log_rho);
+            st->net_cycles_needed += cycles_needed(delta, thr, st->log_rho);
     }
     return go;
 }
@@ -211,9 +221,9 @@ __device__ inline int solve_check_dev(const double *scal, SolveState *st, int ma
     const bool was_smooth = st->smooth != 0;
     // the cycle's reduction factor, into the running mean of its log
     // (weight 1/8 after the first eight; factors clamped to [1e-6, 1])
-    const double red = delta / st->delta;
+    const float red = (float)delta / (float)st->delta;   // an estimate: binary32
     if (!was_smooth && st->delta > 0.0 && isfinite(red)) {
-        const double l = log(fmin(fmax(red, 1e-6), 1.0));
+        const double l = (double)logf(fminf(fmaxf(red, 1e-6f), 1.0f));
         const double w = st->rho_samples < 8 ? 1.0 / (double)(st->rho_samples + 1) : 0.125;
         st->log_rho += w * (l - st->log_rho);
         st->rho_samples++;
