@@ -70,6 +70,44 @@ __device__ static double block_sum(double v) {
     return v;  // valid in thread 0
 }
 
+// block_sum in binary32 (valid in thread 0)
+__device__ static float block_sum_f(float v) {
+    __shared__ float sh[32];
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int nthr = blockDim.x * blockDim.y;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((tid & 31) == 0) sh[tid >> 5] = v;
+    __syncthreads();
+    if (tid < 32) {
+        v = (tid < (nthr + 31) / 32) ? sh[tid] : 0.f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    }
+    __syncthreads();
+    return v;
+}
+
+// block_sum of double-float pairs (valid in thread 0)
+__device__ static float2 block_sum_df(float2 v) {
+    __shared__ float2 sh[32];
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int nthr = blockDim.x * blockDim.y;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v = df_add(v, make_float2(__shfl_down_sync(0xffffffffu, v.x, o), __shfl_down_sync(0xffffffffu, v.y, o)));
+    if ((tid & 31) == 0) sh[tid >> 5] = v;
+    __syncthreads();
+    if (tid < 32) {
+        v = (tid < (nthr + 31) / 32) ? sh[tid] : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            v = df_add(v, make_float2(__shfl_down_sync(0xffffffffu, v.x, o), __shfl_down_sync(0xffffffffu, v.y, o)));
+    }
+    __syncthreads();
+    return v;
+}
+
 __global__ void k_final_sum(const double *partial, int n, double *out) {
     double v = 0.0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) v += partial[i];
@@ -295,70 +333,83 @@ __global__ void __launch_bounds__(BX * BY, RES_DF_CTAS_PER_SM)
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
-    __shared__ double wsum[BX * BY / 32];
+    // The reductions from here on run in binary32, as the squares within
+    // each warp did: the norm is good to about 1e-6 of itself either way
+    // (only the stopping test reads it), and a chain of dependent FP64
+    // additions costs about 130 clocks an addition on GB300's FP64 pipe
+    // against 4 in binary32.  The block sums go to `partial` as floats.
+    __shared__ float wsum[BX * BY / 32];
     __shared__ bool last;
+    float *pf = reinterpret_cast<float *>(partial);
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
     const unsigned nblk = gridDim.x;   // a one-dimensional grid
     // mode 1 with the relative tolerance: ||r0||^2 of the zero-interior
     // guess (as k_r0: only the columns next to the Dirichlet data see a
-    // residual), its rows dealt round-robin to the blocks, each block's
-    // first warp summing its few rows into partial[nblk + block]
+    // residual), its rows dealt round-robin to the blocks, each row in FP64
+    // and the sums as double-float pairs (||r0|| sets the threshold and is
+    // reported, so it keeps FP64's precision), each block's first warp
+    // summing its few rows into pf[nblk + 2 block ..]
     const bool r0_rows = dc.mode == 1 && dc.rel;
-    double r0b = 0.0;
+    float2 r0b = make_float2(0.f, 0.f);
     if (r0_rows && tid < 32) {
+        double acc = 0.0;
         for (int j = tid * (int)nblk + (int)blockIdx.x; j < v.N; j += 32 * (int)nblk) {
             const long row = (long)j * v.P;
             if (v.K - 2 == 1) {
                 const double r = -(v.cx[row] * v.u[row] + v.cx[row + 1] * v.u[row + 2]) * v.inv_h2;
-                r0b += r * r;
+                acc += r * r;
             } else if (v.K - 2 > 1) {
                 const double r1 = -v.cx[row] * v.u[row] * v.inv_h2;
                 const double r2 = -v.cx[row + v.K - 2] * v.u[row + v.K - 1] * v.inv_h2;
-                r0b += r1 * r1 + r2 * r2;
+                acc += r1 * r1 + r2 * r2;
             }
         }
+        r0b = df_of(acc);
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) r0b += __shfl_down_sync(0xffffffffu, r0b, o);
+        for (int o = 16; o > 0; o >>= 1)
+            r0b = df_add(r0b, make_float2(__shfl_xor_sync(0xffffffffu, r0b.x, o), __shfl_xor_sync(0xffffffffu, r0b.y, o)));
     }
-    if ((tid & 31) == 0) wsum[tid >> 5] = (double)sq;
+    if ((tid & 31) == 0) wsum[tid >> 5] = sq;
     __syncthreads();
     if (tid == 0) {
-        double b = 0.0;
+        float b = 0.f;
         for (int w = 0; w < BX * BY / 32; w++) b += wsum[w];
-        partial[blockIdx.x] = b;
-        if (r0_rows) partial[nblk + blockIdx.x] = r0b;
+        pf[blockIdx.x] = b;
+        if (r0_rows) {
+            pf[nblk + 2 * blockIdx.x] = r0b.x;
+            pf[nblk + 2 * blockIdx.x + 1] = r0b.y;
+        }
         __threadfence();
         last = atomicAdd(count, 1u) == nblk - 1;
     }
     __syncthreads();
     if (!last) return;
     __threadfence();
-    double t = 0.0;
-    for (unsigned i = tid; i < nblk; i += blockDim.x * blockDim.y) t += __ldcg(partial + i);
-    t = block_sum(t);
-    if (tid == 0) {
-        *out = t;
-        *count = 0;
+    // the last block: the block sums in a fixed order (deterministic)
+    float t = 0.f;
+    for (unsigned i = tid; i < nblk; i += blockDim.x * blockDim.y) t += __ldcg(pf + i);
+    t = block_sum_f(t);
+    float2 r0 = make_float2(0.f, 0.f);
+    if (r0_rows) {
+        for (unsigned i = tid; i < nblk; i += blockDim.x * blockDim.y)
+            r0 = df_add(r0, make_float2(__ldcg(pf + nblk + 2 * i), __ldcg(pf + nblk + 2 * i + 1)));
+        r0 = block_sum_df(r0);
     }
+    if (tid != 0) return;
+    *out = f2d_exact(t);
+    *count = 0;
+    const double delta = f2d_exact(sqrtf(t));
     if (dc.mode == 1) {
-        // the blocks' ||r0||^2 parts, summed in a fixed order, then the
-        // first decision
-        double r0 = 0.0;
-        if (dc.rel) {
-            for (unsigned i = tid; i < nblk; i += blockDim.x * blockDim.y) r0 += __ldcg(partial + nblk + i);
-            r0 = block_sum(r0);
+        const double r0sq = f2d_exact(r0.x) + f2d_exact(r0.y);
+        if (dc.rel) out[1] = r0sq;
+        const int go = solve_begin_dev(delta, sqrt_refined(r0sq), dc.st, dc.rel, dc.tol, dc.n_kernels, dc.phase,
+                                       dc.net_ratio, dc.n_kernels_gated);
+        if (dc.in_graph) {
+            cudaGraphSetConditional(dc.h, go ? 1u : 0u);
+            if (dc.phase == 1) cudaGraphSetConditional(dc.h_net, dc.st->net ? 1u : 0u);
         }
-        if (tid == 0) {
-            if (dc.rel) out[1] = r0;
-            const int go = solve_begin_dev(out, dc.st, dc.rel, dc.tol, dc.n_kernels, dc.phase, dc.net_ratio,
-                                           dc.n_kernels_gated);
-            if (dc.in_graph) {
-                cudaGraphSetConditional(dc.h, go ? 1u : 0u);
-                if (dc.phase == 1) cudaGraphSetConditional(dc.h_net, dc.st->net ? 1u : 0u);
-            }
-        }
-    } else if (dc.mode == 2 && tid == 0) {
-        const int go = solve_check_dev(out, dc.st, dc.max_cycles, dc.n_kernels, dc.smooth_ratio, dc.n_kernels_smooth);
+    } else if (dc.mode == 2) {
+        const int go = solve_check_dev(delta, dc.st, dc.max_cycles, dc.n_kernels, dc.smooth_ratio, dc.n_kernels_smooth);
         if (dc.in_graph) {
             cudaGraphSetConditional(dc.h, go ? 1u : 0u);
             if (dc.smooth_ratio > 1.0) cudaGraphSetConditional(dc.h_smooth, dc.st->smooth ? 1u : 0u);

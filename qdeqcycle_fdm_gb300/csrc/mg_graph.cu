@@ -51,7 +51,7 @@ struct SolveGraph {
 __global__ void k_solve_begin(cudaGraphConditionalHandle h, cudaGraphConditionalHandle h_net, const double *scal,
                               SolveState *st, int rel, double tol, int n_kernels, int in_graph, int phase,
                               double net_ratio) {
-    const int go = solve_begin_dev(scal, st, rel, tol, n_kernels, phase, net_ratio);
+    const int go = solve_begin_dev(sqrt(scal[0]), rel ? sqrt(scal[1]) : 0.0, st, rel, tol, n_kernels, phase, net_ratio);
     if (in_graph) {
         cudaGraphSetConditional(h, go ? 1u : 0u);
         if (phase == 1) cudaGraphSetConditional(h_net, st->net ? 1u : 0u);
@@ -61,7 +61,7 @@ __global__ void k_solve_begin(cudaGraphConditionalHandle h, cudaGraphConditional
 // n_kernels: kernels of one loop iteration, this one included
 __global__ void k_solve_check(cudaGraphConditionalHandle h, const double *scal, SolveState *st,
                               int max_cycles, int n_kernels, int in_graph) {
-    const int go = solve_check_dev(scal, st, max_cycles, n_kernels);
+    const int go = solve_check_dev(sqrt(scal[0]), st, max_cycles, n_kernels);
     if (in_graph) cudaGraphSetConditional(h, go ? 1u : 0u);
 }
 

@@ -165,11 +165,12 @@ __device__ inline double cycles_needed(double delta, double thr, double log_rho)
     return (double)ceilf(logf((float)delta / (float)thr) / -(float)log_rho);
 }
 
-__device__ inline int solve_begin_dev(const double *scal, SolveState *st, int rel, double tol, int n_kernels,
+// delta = ||r|| of the guess, r0 = ||r0|| (read with the relative
+// tolerance only)
+__device__ inline int solve_begin_dev(double delta, double r0, SolveState *st, int rel, double tol, int n_kernels,
                                       int phase, double net_ratio = 1.0, int n_kernels_gated = 0) {
-    const double r0 = rel ? sqrt(scal[1]) : 0.0;
+    if (!rel) r0 = 0.0;
     const double thr = rel ? (r0 > 0.0 ? tol * r0 : tol) : tol;
-    const double delta = sqrt(scal[0]);
     st->r0 = r0;
     st->thr = thr;
     st->delta = delta;
@@ -215,9 +216,8 @@ __device__ inline int solve_begin_dev(const double *scal, SolveState *st, int re
 // measured at 1025^2: one pass of four sweeps cuts ||r|| to about 1/3).
 // cycles counts both kinds against the cap; n_kernels and n_kernels_smooth
 // are the kernels of the two kinds of iteration.
-__device__ inline int solve_check_dev(const double *scal, SolveState *st, int max_cycles, int n_kernels,
+__device__ inline int solve_check_dev(double delta, SolveState *st, int max_cycles, int n_kernels,
                                       double smooth_ratio = 0.0, int n_kernels_smooth = 0) {
-    const double delta = sqrt(scal[0]);
     const bool was_smooth = st->smooth != 0;
     // the cycle's reduction factor, into the running mean of its log
     // (weight 1/8 after the first eight; factors clamped to [1e-6, 1])
@@ -364,6 +364,39 @@ __device__ __forceinline__ double f2d_exact(float x) {
     return __hiloint2double((int)(sign | (ex << 20) | (m >> 3)), (int)(m << 29));
 }
 
+// x as a double-float pair hi + lo (hi = x rounded to binary32, lo = the
+// rest rounded to binary32: x to about 2^-48 of itself within binary32's
+// range), without the FP64 pipe's conversion
+__device__ __forceinline__ float2 df_of(double x) {
+    const float hi = d2f_rne(x);
+    return make_float2(hi, d2f_rne(x - f2d_exact(hi)));
+}
+
+// a + b for double-float pairs: Knuth's two-sum of the high parts, the low
+// parts and the rounding error summed, then renormalised (about 2^-44 of
+// the sum for sums of like-signed terms)
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
+    const float s = __fadd_rn(a.x, b.x);
+    const float bb = __fsub_rn(s, a.x);
+    const float e = __fadd_rn(__fsub_rn(a.x, __fsub_rn(s, bb)), __fsub_rn(b.x, bb));
+    const float t = __fadd_rn(e, __fadd_rn(a.y, b.y));
+    const float hi = __fadd_rn(s, t);
+    return make_float2(hi, __fsub_rn(t, __fsub_rn(hi, s)));
+}
+
+// sqrt(x) in FP64 from a binary32 reciprocal square root and one Newton
+// step (Heron's correction y + (x - y^2) r / 2): within a few units of
+// 2^-52 of sqrt(x), with a shorter chain of dependent FP64 instructions
+// than the library's sqrt; outside binary32's range, and for 0, negative
+// or non-finite x, the library's sqrt
+__device__ __forceinline__ double sqrt_refined(double x) {
+    const float xf = d2f_rne(x);
+    if (!(xf > 0.f) || isinf(xf) || !isfinite(x)) return sqrt(x);
+    const double r = f2d_exact(rsqrtf(xf));
+    const double y = x * r;
+    return fma(0.5 * r, fma(-y, y, x), y);
+}
+
 }  // namespace qd
 
 struct qd_solver {
@@ -404,7 +437,7 @@ struct qd_solver {
                            // within this ratio of the threshold (0: off)
     const int *cycle_gate; // while capturing a solve graph's first V-cycle: the device flag
                            // (SolveState.go) its kernels check to skip themselves; else null
-    int box_up, box_down;  // staged tile box widths of k_up / k_down (0: the default 64)
+    int box_up, box_down;  // staged tile box widths of k_up / k_down (0: the defaults)
     void *solve_graph;     // the instantiated multigrid graph (mg_graph.cu)
     qd::SolveState *d_solve, *h_solve;
     int n_partial;
