@@ -155,9 +155,16 @@ __device__ double newton_start32(double Ts, double Tn, double tau0, double a, do
 // shrinking bracket.  start32: with the reference's zero seed, start from
 // newton_start32 instead (clamped into the bracket); the iteration and its
 // stopping rule are the same, so it ends at the same root in fewer FP64
-// steps (iters counts the FP64 steps).
-__device__ double newton_v(double Ts, double Tn, double tau0, double a, double eta, double psi,
-                           double V0, double Vseed, int *iters, unsigned int *flags, bool start32 = false) {
+// steps (iters counts the FP64 steps).  Each dependent FP64 instruction
+// waits about 130 clocks for the one before it on GB300, so this path also
+// shortens the chain: e^{|x| - pa} is carried from step to step by the
+// step's small factor (exp_small) instead of a new exponential, the
+// division of the step is div_refined, and the aging law's exponential
+// (*ag = e^{ag_arg}, when ag is not null) is taken beside the first
+// exponential, where the two chains overlap.
+__device__ __forceinline__ double newton_v(double Ts, double Tn, double tau0, double a, double eta, double psi,
+                           double V0, double Vseed, int *iters, unsigned int *flags, bool start32 = false,
+                           double ag_arg = 0.0, double *ag = nullptr) {
     const double pa = psi / a;
     const double fa = a * fabs(Tn);
     const double fb = Ts + tau0;
@@ -179,6 +186,13 @@ __device__ double newton_v(double Ts, double Tn, double tau0, double a, double e
     else
         x = (Vseed == 0.0 && pa < 709.0) ? 0.0 : asinh(0.5 * Vseed / V0 * exp(pa));
     if (!(x >= lo && x <= hi)) x = 0.5 * (lo + hi);
+    // e^{|x| - pa} for the current x while |x| > 20 (binary32 start), else < 0
+    double E = -1.0;
+    if (start32 && fabs(x) > 20.0) {
+        E = exp(fabs(x) - pa);
+        if (ag) *ag = exp(ag_arg);
+        ag = nullptr;
+    }
     const int itmax = 200;
     int it = 0;
     bool done = false, phase2 = false;
@@ -187,7 +201,8 @@ __device__ double newton_v(double Ts, double Tn, double tau0, double a, double e
         if (start32 && fabs(x) > 20.0) {
             // e^{-2|x|} < 2^-57: sinh |x| = cosh |x| = e^{|x|}/2 to within
             // the rounding, one exponential instead of three
-            ac = eta * V0 * exp(fabs(x) - pa);
+            if (E < 0.0) E = exp(fabs(x) - pa);
+            ac = eta * V0 * E;
             as = x > 0.0 ? ac : -ac;
         } else {
             // sinh(0) = 0 and cosh(0) = 1 exactly: the first step from the
@@ -198,7 +213,7 @@ __device__ double newton_v(double Ts, double Tn, double tau0, double a, double e
         }
         const double fy = as + fa * x - fb;
         const double df = ac + fa;
-        const double d = -fy / (df + 1e-100);
+        const double d = start32 ? -div_refined(fy, df + 1e-100) : -fy / (df + 1e-100);
         const double xn = x + d;
         if (!isnan(fy)) {
             if (fy > 0.0) hi = fmin(hi, x); else lo = fmax(lo, x);
@@ -217,6 +232,10 @@ __device__ double newton_v(double Ts, double Tn, double tau0, double a, double e
         // the same test without the division
         const bool conv = start32 ? fabs(d) < 1e-10 * (fabs(x) + 1e-100) : fabs(d) / (fabs(x) + 1e-100) < 1e-10;
         it++;
+        if (E >= 0.0) {
+            const double dd = fabs(xn) - fabs(x);
+            E = (fabs(xn) > 20.0 && fabs(dd) <= 1e-3) ? E * exp_small(dd) : -1.0;
+        }
         x = xn;
         if (conv) { done = true; break; }
     }
@@ -243,12 +262,14 @@ __device__ double newton_v(double Ts, double Tn, double tau0, double a, double e
             if (err < 1e-10) { done = true; break; }
         }
         x = sg * y;
+        E = -1.0;
     }
     if (!done) *flags |= ST_NEWTON_CAP;
     *iters = it;
+    if (ag) *ag = exp(ag_arg);
     double V;
     if (start32 && fabs(x) > 20.0) {
-        V = V0 * exp(fabs(x) - pa);
+        V = V0 * (E >= 0.0 ? E : exp(fabs(x) - pa));
         if (x < 0.0) V = -V;
     } else {
         V = 2.0 * V0 * exp(-psi / a);
@@ -258,13 +279,17 @@ __device__ double newton_v(double Ts, double Tn, double tau0, double a, double e
     return V;
 }
 
-// cal_dpsi (odeSolver.cpp:1196-1204)
-__device__ __forceinline__ double aging(double psi, double b, double V, double f0, double V0,
-                                        double L) {
-    const double A = exp((f0 - psi) / b);
+// cal_dpsi (odeSolver.cpp:1196-1204); aging_from takes its exponential
+// A = e^{(f0 - psi)/b} already formed
+__device__ __forceinline__ double aging_from(double A, double b, double V, double V0, double L) {
     double d = 0.0;
     if (!isinf(A) && b > 1e-3) d = (b * V0 / L) * (A - V / V0);
     return d;
+}
+
+__device__ __forceinline__ double aging(double psi, double b, double V, double f0, double V0,
+                                        double L) {
+    return aging_from(exp((f0 - psi) / b), b, V, V0, L);
 }
 
 __device__ __forceinline__ void report(DevStatus *st, unsigned int flags, int node) {
@@ -385,12 +410,14 @@ __global__ void k_fault_stage(FaultArgs A, int stage, CopyJob job, int fault_blo
     F.Ts[k] = Ts;
     F.Tn[k] = Tn;
     const double psi = F.kpsi[stage][k];
+    const double bk = F.b[k];
     unsigned int flags = 0;
     int it = 0;
+    double agA = 0.0;   // the aging law's exponential, formed inside the Newton solve
     const double V = newton_v(Ts, Tn, F.have_tau0 ? F.tau0[k] : 0.0, F.a[k], F.eta[k], psi, F.V0,
-                              F.fV[stage][k], &it, &flags, A.start32 != 0);
+                              F.fV[stage][k], &it, &flags, A.start32 != 0, (F.f0 - psi) / bk, &agA);
     F.fV[stage][k] = V;
-    F.fdpsi[stage][k] = aging(psi, F.b[k], V, F.f0, F.V0, F.L);
+    F.fdpsi[stage][k] = aging_from(agA, bk, V, F.V0, F.L);
     F.iters[k] += it;
     report(A.status, flags, k);
 }

@@ -384,6 +384,35 @@ __device__ __forceinline__ float2 df_add(float2 a, float2 b) {
     return make_float2(hi, __fsub_rn(t, __fsub_rn(hi, s)));
 }
 
+// 1/sqrt(x) in FP64 from a binary32 reciprocal square root and one Newton
+// step r (3 - x r^2) / 2: within about 1e-14 of itself, four dependent FP64
+// instructions; outside binary32's range, and for 0, negative or
+// non-finite x, the library's rsqrt
+__device__ __forceinline__ double rsqrt_refined(double x) {
+    const float xf = d2f_rne(x);
+    if (!(xf > 0.f) || isinf(xf) || !isfinite(x)) return rsqrt(x);
+    const double r = f2d_exact(rsqrtf(xf));
+    return r * fma(-0.5 * x * r, r, 1.5);
+}
+
+// a / b in FP64 from a binary32 reciprocal and two Newton corrections
+// (the reciprocal's, then the quotient's): within about an ulp of a / b in
+// five dependent FP64 instructions; where b is 0, not finite or outside
+// binary32's range, the library's division
+__device__ __forceinline__ double div_refined(double a, double b) {
+    const float bf = d2f_rne(b);
+    if (!(fabsf(bf) > 0.f) || isinf(bf) || !isfinite(b)) return a / b;
+    double r = f2d_exact(__frcp_rn(bf));
+    r = fma(r, fma(-b, r, 1.0), r);
+    const double q = a * r;
+    return fma(r, fma(-b, q, a), q);
+}
+
+// e^d for |d| <= 1e-3 by its Taylor series to d^6 (error below 2e-25)
+__device__ __forceinline__ double exp_small(double d) {
+    return 1.0 + d * (1.0 + d * (1.0 / 2.0 + d * (1.0 / 6.0 + d * (1.0 / 24.0 + d * (1.0 / 120.0 + d * (1.0 / 720.0))))));
+}
+
 // sqrt(x) in FP64 from a binary32 reciprocal square root and one Newton
 // step (Heron's correction y + (x - y^2) r / 2): within a few units of
 // 2^-52 of sqrt(x), with a shorter chain of dependent FP64 instructions
