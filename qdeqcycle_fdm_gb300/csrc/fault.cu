@@ -447,13 +447,17 @@ __global__ void k_dpsi(FaultArgs A, const double *psi, const double *V, double *
     dpsi[k] = aging(psi[k], A.F.b[k], V[k], A.F.f0, A.F.V0, A.F.L);
 }
 
-// y3 / y4 (odeSolver.cpp:1569-1593) and computeError (:1211-1238); one block.
-__global__ void k_error(FaultArgs A, double dt, double *out) {
+// y3 / y4 (odeSolver.cpp:1569-1593) and computeError (:1211-1238).  One
+// fault node per thread in 32-thread blocks: the nodes' FP64 work spread
+// over nk/32 SMs (GB300's FP64 pipe takes about 20 clocks a warp
+// instruction per SM); each block's sums into partial[2 block ..], the last
+// block to finish adds them in a fixed order (deterministic) and re-arms
+// the counter.  inv_sqrt_n = 1/sqrt(nk).
+__global__ void k_error(FaultArgs A, double dt, double *partial, unsigned *count, double inv_sqrt_n, double *out) {
     pdl_wait();
-    __shared__ double s1[1024], s2[1024];
     const FaultState &F = A.F;
     double e1 = 0.0, e2 = 0.0;
-    for (int k = threadIdx.x + 1; k <= A.nk; k += blockDim.x) {
+    if (const int k = blockIdx.x * blockDim.x + threadIdx.x + 1; k <= A.nk) {
         double y3s = F.Slip[k] + c_rk.hb[1] * dt * F.fV[1][k];
         double y4s = F.Slip[k] + c_rk.b[1] * dt * F.fV[1][k];
         double y3p = F.psi[k] + c_rk.hb[1] * dt * F.fdpsi[1][k];
@@ -466,22 +470,37 @@ __global__ void k_error(FaultArgs A, double dt, double *out) {
         }
         F.y3s[k] = y3s; F.y3p[k] = y3p; F.y4s[k] = y4s; F.y4p[k] = y4p;
         const double t1 = y3s - y4s, t2 = y3p - y4p;
-        e1 += t1 * t1;
-        e2 += t2 * t2;
+        e1 = t1 * t1;
+        e2 = t2 * t2;
     }
-    s1[threadIdx.x] = e1;
-    s2[threadIdx.x] = e2;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        e1 += __shfl_down_sync(0xffffffffu, e1, o);
+        e2 += __shfl_down_sync(0xffffffffu, e2, o);
+    }
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        partial[2 * blockIdx.x] = e1;
+        partial[2 * blockIdx.x + 1] = e2;
+        __threadfence();
+        last = atomicAdd(count, 1u) == gridDim.x - 1;
+    }
     __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if (threadIdx.x < w) {
-            s1[threadIdx.x] += s1[threadIdx.x + w];
-            s2[threadIdx.x] += s2[threadIdx.x + w];
-        }
-        __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double s1 = 0.0, s2 = 0.0;
+    for (unsigned b = threadIdx.x; b < gridDim.x; b += 32) {
+        s1 += __ldcg(partial + 2 * b);
+        s2 += __ldcg(partial + 2 * b + 1);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        s1 += __shfl_down_sync(0xffffffffu, s1, o);
+        s2 += __shfl_down_sync(0xffffffffu, s2, o);
     }
     if (threadIdx.x == 0) {
-        const double sn = sqrt((double)A.nk);
-        *out = sqrt(s1[0]) / (sn * 1.0) + sqrt(s2[0]) / (sn * 1.0);
+        *count = 0;
+        *out = sqrt_refined(s1) * inv_sqrt_n + sqrt_refined(s2) * inv_sqrt_n;
     }
 }
 
@@ -575,7 +594,13 @@ int launch_fault(qd_solver *s, int stage, const CopyJob &job) {
 }
 
 int launch_error(qd_solver *s) {
-    QD_CUDA(launch_pdl(true, k_error, dim3(1), dim3(1024), 0, s->stream, fargs(s), s->dt, s->d_scal + 2));
+    const int nb = nblk(s->nk, 32);
+    if (2 * nb > s->n_partial) {
+        set_error("error estimate: %d blocks exceed the partial buffer", nb);
+        return QD_ERR_ARG;
+    }
+    QD_CUDA(launch_pdl(true, k_error, dim3(nb), dim3(32), 0, s->stream, fargs(s), s->dt, s->d_partial, s->d_count,
+                       1.0 / sqrt((double)s->nk), s->d_scal + 2));
     QD_LAUNCH_CHECK(s);
     return QD_OK;
 }
