@@ -167,7 +167,11 @@ static int attempt_enqueue(qd_solver *s) {
     QD_CUDA(cudaMemsetAsync(&s->d_solve->need_max, 0, sizeof(double), s->stream));
     if (s->t + s->dt > s->P.tmax) s->dt = s->P.tmax - s->t;
     for (int st = 2; st <= 6; st++) QD_TRY(stage(s, st, c[st]));
-    QD_TRY(launch_error(s));
+    // the attempt's report: written by the error kernel into the pinned
+    // host copies where the device can address them, else three copies
+    const bool mapped = s->dh_scal && s->dh_solve && s->dh_status;
+    QD_TRY(launch_error(s, mapped));
+    if (mapped) return QD_OK;
     QD_CUDA(cudaMemcpyAsync(s->h_scal + 2, s->d_scal + 2, sizeof(double), cudaMemcpyDeviceToHost,
                             s->stream));
     QD_CUDA(cudaMemcpyAsync(s->h_solve, s->d_solve, sizeof(SolveState), cudaMemcpyDeviceToHost, s->stream));
@@ -286,6 +290,19 @@ int qd_solver_create_mapped(int ni, int nk, double dh, const double *mu_equi, co
         set_error("qd_solver_create: CUDA set-up failed: %s", cudaGetErrorString(cudaGetLastError()));
         qd_solver_destroy(s);
         return QD_ERR_CUDA;
+    }
+    {   // device addresses of the pinned host copies (the error kernel's
+        // attempt report); none where the device cannot address them
+        void *a = nullptr, *b = nullptr, *c = nullptr;
+        if (cudaHostGetDevicePointer(&a, s->h_scal, 0) == cudaSuccess &&
+            cudaHostGetDevicePointer(&b, s->h_solve, 0) == cudaSuccess &&
+            cudaHostGetDevicePointer(&c, s->h_status, 0) == cudaSuccess) {
+            s->dh_scal = static_cast<double *>(a);
+            s->dh_solve = static_cast<SolveState *>(b);
+            s->dh_status = static_cast<DevStatus *>(c);
+        } else {
+            (void)cudaGetLastError();
+        }
     }
     rc = mg_alloc(s, mu_equi, jrow);
     if (rc == QD_OK) rc = fault_alloc(s);

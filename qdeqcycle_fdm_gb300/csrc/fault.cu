@@ -452,8 +452,20 @@ __global__ void k_dpsi(FaultArgs A, const double *psi, const double *V, double *
 // over nk/32 SMs (GB300's FP64 pipe takes about 20 clocks a warp
 // instruction per SM); each block's sums into partial[2 block ..], the last
 // block to finish adds them in a fixed order (deterministic) and re-arms
-// the counter.  inv_sqrt_n = 1/sqrt(nk).
-__global__ void k_error(FaultArgs A, double dt, double *partial, unsigned *count, double inv_sqrt_n, double *out) {
+// the counter.  inv_sqrt_n = 1/sqrt(nk).  With rep.err set, the last block
+// also writes the attempt's report into pinned host memory (the device
+// addresses of the solver's host copies): the error, the solve state and
+// the status the host reads after its one wait of the attempt.
+struct AttemptReport {
+    double *err;                 // null: no report
+    SolveState *st;
+    DevStatus *status;
+    const SolveState *d_st;
+    const DevStatus *d_status;
+};
+
+__global__ void k_error(FaultArgs A, double dt, double *partial, unsigned *count, double inv_sqrt_n, double *out,
+                        AttemptReport rep) {
     pdl_wait();
     const FaultState &F = A.F;
     double e1 = 0.0, e2 = 0.0;
@@ -500,7 +512,14 @@ __global__ void k_error(FaultArgs A, double dt, double *partial, unsigned *count
     }
     if (threadIdx.x == 0) {
         *count = 0;
-        *out = sqrt_refined(s1) * inv_sqrt_n + sqrt_refined(s2) * inv_sqrt_n;
+        const double e = sqrt_refined(s1) * inv_sqrt_n + sqrt_refined(s2) * inv_sqrt_n;
+        *out = e;
+        if (rep.err) {
+            *rep.err = e;
+            *rep.st = *rep.d_st;
+            *rep.status = *rep.d_status;
+            __threadfence_system();
+        }
     }
 }
 
@@ -593,14 +612,26 @@ int launch_fault(qd_solver *s, int stage, const CopyJob &job) {
     return QD_OK;
 }
 
-int launch_error(qd_solver *s) {
+int launch_error(qd_solver *s, bool report) {
     const int nb = nblk(s->nk, 32);
     if (2 * nb > s->n_partial) {
         set_error("error estimate: %d blocks exceed the partial buffer", nb);
         return QD_ERR_ARG;
     }
+    AttemptReport rep{};
+    if (report) {
+        if (!s->dh_scal || !s->dh_solve || !s->dh_status) {
+            set_error("error estimate: the pinned host copies are not addressable by the device");
+            return QD_ERR_STATE;
+        }
+        rep.err = s->dh_scal + 2;
+        rep.st = s->dh_solve;
+        rep.status = s->dh_status;
+        rep.d_st = s->d_solve;
+        rep.d_status = s->d_status;
+    }
     QD_CUDA(launch_pdl(true, k_error, dim3(nb), dim3(32), 0, s->stream, fargs(s), s->dt, s->d_partial, s->d_count,
-                       1.0 / sqrt((double)s->nk), s->d_scal + 2));
+                       1.0 / sqrt((double)s->nk), s->d_scal + 2, rep));
     QD_LAUNCH_CHECK(s);
     return QD_OK;
 }

@@ -469,6 +469,11 @@ struct qd_solver {
     int box_up, box_down;  // staged tile box widths of k_up / k_down (0: the defaults)
     void *solve_graph;     // the instantiated multigrid graph (mg_graph.cu)
     qd::SolveState *d_solve, *h_solve;
+    // device addresses of the pinned h_scal, h_solve and h_status (null when
+    // the device cannot address them): the error kernel's attempt report
+    double *dh_scal;
+    qd::SolveState *dh_solve;
+    qd::DevStatus *dh_status;
     int n_partial;
     double *d_scal;        // device scalars: [0] ||r||^2, [1] ||r0||^2, [2] totErr, [3] the step of mr_step
     double *h_scal;        // pinned mirror
@@ -541,7 +546,10 @@ struct CopyJob {
 // the stage's stress, Newton and aging law (k_fault_stage); with job.src
 // set the same launch also stores u into the solution history
 int launch_fault(qd_solver *s, int stage, const CopyJob &job);
-int launch_error(qd_solver *s);
+// the error estimate; with report set, its last block also writes the
+// attempt's report (the error, the solve state, the status) straight into
+// the solver's pinned host copies, in place of three copies after it
+int launch_error(qd_solver *s, bool report);
 int launch_commit(qd_solver *s);
 int launch_stress(qd_solver *s);
 int launch_newton(qd_solver *s, const double *Ts, const double *psi, double *V, int *iters);
