@@ -110,9 +110,9 @@ static int reset_status(qd_solver *s) {
 
 // one stage: boundary data, elliptic solve, stress/Newton/aging law, all
 // enqueued on the solver's stream without waiting
-static int stage(qd_solver *s, int st, double ratio) {
+static int stage(qd_solver *s, int st, double ratio, bool commit = false) {
     QD_TRY(warm_start_before_boundary(s));     // no-ops without an attached network
-    QD_TRY(launch_stage_boundary(s, st, ratio, true));   // + the history fit when enabled
+    QD_TRY(launch_stage_boundary(s, st, ratio, true, commit));   // + the history fit when enabled
     QD_TRY(history_apply(s, warm_start_bc_buffer(s)));   // no-op unless enabled
     QD_TRY(warm_start_after_boundary(s));
     QD_TRY(mg_solve_async(s));
@@ -164,7 +164,6 @@ static int step_begin(qd_solver *s) {
 static int attempt_enqueue(qd_solver *s) {
     const double *c = rk_c();
     s->attempts++;
-    QD_CUDA(cudaMemsetAsync(&s->d_solve->need_max, 0, sizeof(double), s->stream));
     if (s->t + s->dt > s->P.tmax) s->dt = s->P.tmax - s->t;
     for (int st = 2; st <= 6; st++) QD_TRY(stage(s, st, c[st]));
     // the attempt's report: written by the error kernel into the pinned
@@ -200,8 +199,7 @@ static int attempt_finish(qd_solver *s, int attemptCount, double *totErr, int *r
 
 static int commit_enqueue(qd_solver *s) {
     s->t = s->t + s->dt;
-    QD_TRY(launch_commit(s));
-    return stage(s, 1, 0.0);                                      // :1615-1619
+    return stage(s, 1, 0.0, true);   // the commit (:1606-1614) in the refresh stage's launch (:1615-1619)
 }
 
 // the host's side of a commit; check: wait for the refresh and read the

@@ -337,13 +337,26 @@ __device__ __forceinline__ void stage_boundary_node(const FaultArgs &A, int stag
 // With ND > 0 the same launch also fits the new boundary data by the
 // solution history's (hist_fit.cuh): each thread adds its node's two
 // boundary values to the normal equations and the last block solves them,
-// so the guess needs no launch of its own for the fit.
+// so the guess needs no launch of its own for the fit.  commit: first the
+// accepted step's commit of each node (y <- y4, f_1 zeroed; odeSolver.cpp:
+// 1606-1614), which the refresh stage 1 then copies; zero, when not null, is
+// set to 0 by one thread (the solve state's need_max at an attempt's first
+// stage).
 template <int ND>
 __global__ void __launch_bounds__(FIT_THREADS)
-    k_stage_boundary(FaultArgs A, int stage, double t, double dt, double ratio, FitArgs fit) {
+    k_stage_boundary(FaultArgs A, int stage, double t, double dt, double ratio, FitArgs fit, int commit,
+                     double *zero) {
     pdl_trigger();
     pdl_wait();
     const int k = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (zero && blockIdx.x == 0 && threadIdx.x == 0) *zero = 0.0;
+    if (commit && k <= A.nk) {
+        const FaultState &F = A.F;
+        F.Slip[k] = F.y4s[k];
+        F.psi[k] = F.y4p[k];
+        F.fV[1][k] = 0.0;
+        F.fdpsi[1][k] = 0.0;
+    }
     if constexpr (ND > 0) {
         FitAcc<ND> acc;
         acc.zero();
@@ -523,17 +536,6 @@ __global__ void k_error(FaultArgs A, double dt, double *partial, unsigned *count
     }
 }
 
-// accepted step: y <- y4, f1 zeroed (odeSolver.cpp:1606-1614)
-__global__ void k_commit(FaultArgs A) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    if (k > A.nk) return;
-    const FaultState &F = A.F;
-    F.Slip[k] = F.y4s[k];
-    F.psi[k] = F.y4p[k];
-    F.fV[1][k] = 0.0;
-    F.fdpsi[1][k] = 0.0;
-}
-
 // ---------------------------------------------------------------------------
 // host wrappers
 // ---------------------------------------------------------------------------
@@ -574,15 +576,17 @@ void fault_free(qd_solver *s) {
 // error estimate) are launched with programmatic stream serialization: each
 // waits for its predecessor (pdl_wait) before touching its data, and the
 // launch latency between them overlaps the predecessor's tail.
-int launch_stage_boundary(qd_solver *s, int stage, double ratio, bool fit) {
+int launch_stage_boundary(qd_solver *s, int stage, double ratio, bool fit, bool commit) {
     FitArgs fa{};
     const int nd = fit ? history_fit_args(s, &fa) : 0;
+    // an RK attempt's first stage: the attempt's need_max starts from 0
+    double *zero = (stage == 2 && fit) ? &s->d_solve->need_max : nullptr;
     const dim3 grid(nblk(s->nk, FIT_THREADS)), block(FIT_THREADS);
     switch (nd) {
 #define QD_SB_CASE(n)                                                                                    \
     case n:                                                                                              \
         QD_CUDA(launch_pdl(true, k_stage_boundary<n>, grid, block, 0, s->stream, fargs(s), stage, s->t, s->dt, \
-                           ratio, fa));                                                                  \
+                           ratio, fa, commit ? 1 : 0, zero));                                            \
         break;
         QD_SB_CASE(0) QD_SB_CASE(1) QD_SB_CASE(2) QD_SB_CASE(3) QD_SB_CASE(4) QD_SB_CASE(5) QD_SB_CASE(6)
         QD_SB_CASE(7)
@@ -636,11 +640,6 @@ int launch_error(qd_solver *s, bool report) {
     return QD_OK;
 }
 
-int launch_commit(qd_solver *s) {
-    k_commit<<<nblk(s->nk, 128), 128, 0, s->stream>>>(fargs(s));
-    QD_LAUNCH_CHECK(s);
-    return QD_OK;
-}
 
 int launch_stress(qd_solver *s) {
     k_stress<<<nblk(s->nk, 128), 128, 0, s->stream>>>(fargs(s));

@@ -534,7 +534,8 @@ int fault_alloc(qd_solver *s);
 void fault_free(qd_solver *s);
 // fit: also fit the new boundary data by the solution history's (when the
 // next solve will start from a history guess), for history_apply
-int launch_stage_boundary(qd_solver *s, int stage, double ratio, bool fit);
+// commit: the accepted step's commit first (stage 1's refresh)
+int launch_stage_boundary(qd_solver *s, int stage, double ratio, bool fit, bool commit = false);
 // a copy of the solved level-0 u into a slot of the solution history
 // (history_push_job), run by extra CTAs of the fault-stage kernel
 struct CopyJob {
@@ -550,7 +551,6 @@ int launch_fault(qd_solver *s, int stage, const CopyJob &job);
 // attempt's report (the error, the solve state, the status) straight into
 // the solver's pinned host copies, in place of three copies after it
 int launch_error(qd_solver *s, bool report);
-int launch_commit(qd_solver *s);
 int launch_stress(qd_solver *s);
 int launch_newton(qd_solver *s, const double *Ts, const double *psi, double *V, int *iters);
 int launch_dpsi(qd_solver *s, const double *psi, const double *V, double *dpsi);
