@@ -247,8 +247,8 @@ __global__ void __launch_bounds__(BX * BY) k_residual(View<T> v, T *r, double *p
 // split once and kept in registers.  A grid of RES_DF_CTAS_PER_SM blocks per
 // SM strides over the tiles, so that the block-wide reduction at the end
 // (whose barrier idles a block's early warps) comes once per block instead
-// of once per tile.  The norm sums the squares of the FP32 residual in FP32
-// over a warp and in FP64 above that -- a relative error near 1e-7 in the
+// of once per tile.  The norm sums the squares of the FP32 residual in
+// FP32 throughout (residual_df_finish) -- a relative error near 1e-6 in the
 // norm, which only the stopping test reads.  The last block to finish adds
 // the per-block partials in a fixed order (the sum is deterministic) and
 // re-arms the counter for the next launch.
