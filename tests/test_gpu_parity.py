@@ -6,7 +6,7 @@ Tolerances (FP64):
     operation as the reference's source reads);
   * converged solves, stress, slip rate: 1e-10 relative;
   * after 100 accepted RK43 steps: u, tau, V to 1e-10 and slip, psi to 1e-8
-    relative (the spec parity bar).
+    relative (the drop-in's parity bar).
 """
 import numpy as np
 import pytest

@@ -1,7 +1,7 @@
 """The grid stretched in depth (config 2): the metric form of the operator.
 
 The reference's grid is uniform (coord.cpp:18,27); a stretched grid is this
-project's own discretisation, so the oracle is the judge: the CPU oracle
+project's own discretisation, so the oracle is the only reference: the CPU oracle
 applies the metric J = dz/dzeta as x-face moduli mu J and z-face moduli
 mu / J on the uniform computational grid.  Here:
   * with J = 1 the metric code path reproduces the uniform oracle bit for bit;
